@@ -1,0 +1,791 @@
+// axg_evolve.cu -- leapfrog kernels of the lattice hot path (evolve.f90:238-339).
+//
+// Three arithmetic paths:
+//  * FP64-plain (drop-in for evolve_phi / evolve_phidot): a pointwise drift
+//    kernel and a 7-point stencil kick kernel, FP64, every operation written
+//    with non-contractible IEEE intrinsics in the reference's order so the
+//    result is bit-identical to the CPU restatement.
+//  * FP64-fused and FP32-mixed: one pass per step computing the kick and the
+//    following drift.  phi and u_ij ping-pong between two buffers; the stencil
+//    fields (phi, u) of each z-plane are staged in shared memory by TMA
+//    (cp.async.bulk.tensor) into a ring of mbarrier-tracked stages while the
+//    pointwise fields (phi', u', Kahan compensations) stream through registers.
+//    A CTA owns a TX x TY column of the lattice and marches through zc planes.
+//    Halos: y rows and x columns are separate TMA boxes at wrapped coordinates
+//    (periodic lattice), x boxes 16 bytes wide so their x coordinate is always
+//    16-byte aligned.
+#include <cudaTypedefs.h>
+
+#include "axg_detmath.h"
+#include "axg_internal.h"
+
+namespace {
+
+constexpr int kStages = 4;            // TMA ring depth (z-1, z, z+1, prefetch)
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz: mbarrier wait limit
+
+// ------------------------------------------------------------------------
+// FP64-plain kernels (evolve.f90:259-281 and 283-339)
+// ------------------------------------------------------------------------
+struct KickCoeffs {
+  double f1, f2, f3, fs;  // fact1, fact2, fact3, source factor
+  double A, B, C, D;      // dV/dphi* = (A|phi|^2+B) phi + C + D conj(phi)
+  double d;               // 2 dspa (grav_waves.f90:331)
+};
+
+__global__ void k_drift_fp64(double2 *__restrict__ phi, const double2 *__restrict__ phid,
+                             double *__restrict__ u, const double *__restrict__ ud, int64_t n3,
+                             double h, int uij) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    double2 a = phi[s];
+    const double2 b = phid[s];
+    a.x = AXD_ADD(a.x, AXD_MUL(h, b.x));
+    a.y = AXD_ADD(a.y, AXD_MUL(h, b.y));
+    phi[s] = a;
+    if (uij) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const int64_t i = c * n3 + s;
+        u[i] = AXD_ADD(u[i], AXD_MUL(h, ud[i]));
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+__global__ void __launch_bounds__(256) k_kick_fp64(const double2 *__restrict__ phi,
+                                                   double2 *__restrict__ phid,
+                                                   const double *__restrict__ u,
+                                                   double *__restrict__ ud, int n, KickCoeffs k,
+                                                   int uij) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+  const int iz = blockIdx.z;
+  if (ix >= n || iy >= n) return;
+  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int ix1 = wrapi(ix - 1, n), ix2 = wrapi(ix + 1, n);
+  const int iy1 = wrapi(iy - 1, n), iy2 = wrapi(iy + 1, n);
+  const int iz1 = wrapi(iz - 1, n), iz2 = wrapi(iz + 1, n);
+  const int64_t c = iz * n2 + (int64_t)iy * n + ix;
+  const int64_t sx1 = iz * n2 + (int64_t)iy * n + ix1, sx2 = iz * n2 + (int64_t)iy * n + ix2;
+  const int64_t sy1 = iz * n2 + (int64_t)iy1 * n + ix, sy2 = iz * n2 + (int64_t)iy2 * n + ix;
+  const int64_t sz1 = iz1 * n2 + (int64_t)iy * n + ix, sz2 = iz2 * n2 + (int64_t)iy * n + ix;
+  const double2 pc = phi[c], px1 = phi[sx1], px2 = phi[sx2], py1 = phi[sy1], py2 = phi[sy2],
+                pz1 = phi[sz1], pz2 = phi[sz2];
+  // dlap (evolve.f90:325-328), left to right
+  double lr = AXD_ADD(px1.x, px2.x);
+  lr = AXD_ADD(lr, py1.x);
+  lr = AXD_ADD(lr, py2.x);
+  lr = AXD_ADD(lr, pz1.x);
+  lr = AXD_ADD(lr, pz2.x);
+  lr = AXD_SUB(lr, AXD_MUL(6.0, pc.x));
+  double li = AXD_ADD(px1.y, px2.y);
+  li = AXD_ADD(li, py1.y);
+  li = AXD_ADD(li, py2.y);
+  li = AXD_ADD(li, pz1.y);
+  li = AXD_ADD(li, pz2.y);
+  li = AXD_SUB(li, AXD_MUL(6.0, pc.y));
+  // dVdphi (potential.f90:43-60)
+  const double s2 = AXD_ADD(AXD_MUL(pc.x, pc.x), AXD_MUL(pc.y, pc.y));
+  const double g = AXD_ADD(AXD_MUL(k.A, s2), k.B);
+  double vr = AXD_MUL(g, pc.x), vi = AXD_MUL(g, pc.y);
+  if (k.D != 0.0) {
+    vr = AXD_ADD(vr, AXD_MUL(k.D, pc.x));
+    vi = AXD_SUB(vi, AXD_MUL(k.D, pc.y));
+  }
+  vr = AXD_ADD(vr, k.C);
+  // data2 = fact1*data2 + fact2*dlap + fact3*ddv (evolve.f90:330)
+  const double2 pd = phid[c];
+  double pr = AXD_ADD(AXD_MUL(k.f1, pd.x), AXD_MUL(k.f2, lr));
+  pr = AXD_ADD(pr, AXD_MUL(k.f3, vr));
+  double pi_ = AXD_ADD(AXD_MUL(k.f1, pd.y), AXD_MUL(k.f2, li));
+  pi_ = AXD_ADD(pi_, AXD_MUL(k.f3, vi));
+  phid[c] = make_double2(pr, pi_);
+  if (uij) {
+    double dr[3], di[3];
+    dr[0] = AXD_DIV(AXD_SUB(px2.x, px1.x), k.d);
+    di[0] = AXD_DIV(AXD_SUB(px2.y, px1.y), k.d);
+    dr[1] = AXD_DIV(AXD_SUB(py2.x, py1.x), k.d);
+    di[1] = AXD_DIV(AXD_SUB(py2.y, py1.y), k.d);
+    dr[2] = AXD_DIV(AXD_SUB(pz2.x, pz1.x), k.d);
+    di[2] = AXD_DIV(AXD_SUB(pz2.y, pz1.y), k.d);
+    int comp = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int j = 0; j <= i; ++j, ++comp) {
+        const double *uc = u + comp * n3;
+        double src = AXD_ADD(AXD_MUL(dr[i], dr[j]), AXD_MUL(di[i], di[j]));
+        src = AXD_MUL(2.0, src);
+        double lu = AXD_ADD(uc[sx1], uc[sx2]);
+        lu = AXD_ADD(lu, uc[sy1]);
+        lu = AXD_ADD(lu, uc[sy2]);
+        lu = AXD_ADD(lu, uc[sz1]);
+        lu = AXD_ADD(lu, uc[sz2]);
+        lu = AXD_SUB(lu, AXD_MUL(6.0, uc[c]));
+        double v = AXD_ADD(AXD_MUL(k.f1, ud[comp * n3 + c]), AXD_MUL(k.f2, lu));
+        v = AXD_ADD(v, AXD_MUL(k.fs, src));
+        ud[comp * n3 + c] = v;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// FP32 Kahan drift (first half drift of the fused scheme)
+// ------------------------------------------------------------------------
+__device__ __forceinline__ void kahan_add(float &x, float &c, float inc) {
+  const float y = inc - c;
+  const float t = x + y;
+  c = (t - x) - y;
+  x = t;
+}
+
+__global__ void k_drift_fp32(float2 *__restrict__ phi, const float2 *__restrict__ phid,
+                             float2 *__restrict__ cphi, float *__restrict__ u,
+                             const float *__restrict__ ud, float *__restrict__ cu, int64_t n3,
+                             float h, int uij) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    float2 a = phi[s], c = cphi[s];
+    const float2 b = phid[s];
+    kahan_add(a.x, c.x, h * b.x);
+    kahan_add(a.y, c.y, h * b.y);
+    phi[s] = a;
+    cphi[s] = c;
+    if (uij) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const int64_t i = k * n3 + s;
+        float x = u[i], cc = cu[i];
+        kahan_add(x, cc, h * ud[i]);
+        u[i] = x;
+        cu[i] = cc;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// TMA / mbarrier primitives (inline PTX)
+// ------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after kWaitCycles and reports failure.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+}
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1,
+                                            int c2, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1,
+                                            int c2, int c3, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+
+// ------------------------------------------------------------------------
+// fused kernel: one stage of shared memory holds one z-plane of the stencil
+// fields of a TX x TY column with its halos.
+// ------------------------------------------------------------------------
+template <typename R>
+struct V2;
+template <>
+struct V2<float> {
+  using T = float2;
+};
+template <>
+struct V2<double> {
+  using T = double2;
+};
+
+constexpr int align128(int b) { return (b + 127) / 128 * 128; }
+
+template <typename R, int TX, int TY, bool UIJ>
+struct StageLayout {
+  using V = typename V2<R>::T;
+  static constexpr int PHW = sizeof(R) == 4 ? 2 : 1;  // phi halo width (16 B rule for FP32)
+  static constexpr int UHW = 16 / (int)sizeof(R);     // u halo width (16 B)
+  static constexpr int phi_main = 0;
+  static constexpr int phi_main_sz = align128((TY + 2) * TX * (int)sizeof(V));
+  static constexpr int phi_hl = phi_main + phi_main_sz;
+  static constexpr int phi_h_sz = align128(TY * PHW * (int)sizeof(V));
+  static constexpr int phi_hr = phi_hl + phi_h_sz;
+  static constexpr int u_top = phi_hr + phi_h_sz;
+  static constexpr int u_row_sz = UIJ ? align128(6 * TX * (int)sizeof(R)) : 0;
+  static constexpr int u_body = u_top + u_row_sz;
+  static constexpr int u_body_sz = UIJ ? align128(6 * TY * TX * (int)sizeof(R)) : 0;
+  static constexpr int u_bot = u_body + u_body_sz;
+  static constexpr int u_hl = u_bot + u_row_sz;
+  static constexpr int u_h_sz = UIJ ? align128(6 * TY * UHW * (int)sizeof(R)) : 0;
+  static constexpr int u_hr = u_hl + u_h_sz;
+  static constexpr int bytes = u_hr + u_h_sz;
+  // bytes actually delivered by the TMA boxes of one stage
+  static constexpr int tx_bytes =
+      (TY + 2) * TX * (int)sizeof(V) + 2 * TY * PHW * (int)sizeof(V) +
+      (UIJ ? (2 * 6 * TX + 6 * TY * TX + 2 * 6 * TY * UHW) * (int)sizeof(R) : 0);
+};
+
+template <typename R>
+struct FusedParams {
+  typename V2<R>::T *phi_out;
+  typename V2<R>::T *phid;
+  typename V2<R>::T *cphi;  // FP32 only
+  R *u_out;
+  R *ud;
+  R *cu;  // FP32 only
+  int64_t n3;
+  int n, zc;
+  R f1, f2, f3, fsc, dtd, A, B, C, D;
+  double d;  // 2 dspa (FP64 path keeps the reference's division)
+  int *err;
+};
+
+template <typename R>
+__device__ __forceinline__ void tma_phi(uint32_t dst, const CUtensorMap *m, int x, int y, int z,
+                                        uint32_t bar) {
+  if constexpr (sizeof(R) == 4)
+    tma_load_3d(dst, m, x, y, z, bar);  // 8-byte elements holding (re, im) float pairs
+  else
+    tma_load_4d(dst, m, 0, x, y, z, bar);  // (re|im, x, y, z) doubles
+}
+
+template <typename R, int TX, int TY, bool UIJ>
+__global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 : 1))
+    k_fused(const __grid_constant__ CUtensorMap tm_prow, const __grid_constant__ CUtensorMap tm_pbody,
+            const __grid_constant__ CUtensorMap tm_phalo, const __grid_constant__ CUtensorMap tm_urow,
+            const __grid_constant__ CUtensorMap tm_ubody, const __grid_constant__ CUtensorMap tm_uhalo,
+            const FusedParams<R> P) {
+  using L = StageLayout<R, TX, TY, UIJ>;
+  using V = typename V2<R>::T;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * L::bytes);
+
+  const int n = P.n, zc = P.zc;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int ncx = n / TX;
+  const int x0 = (blockIdx.x % ncx) * TX, y0 = (blockIdx.x / ncx) * TY, z0 = blockIdx.y * zc;
+  const int nplanes = zc + 2;
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    fence_barrier_init();
+    fence_proxy_async();
+  }
+  __syncthreads();
+
+  auto issue = [&](int p) {
+    int z = z0 - 1 + p;
+    z = z < 0 ? z + n : (z >= n ? z - n : z);
+    const int s = p % kStages;
+    unsigned char *st = smem + s * L::bytes;
+    const uint32_t bar = smem_u32(&bars[s]);
+    mbar_expect_tx(bar, (uint32_t)L::tx_bytes);
+    const int ym = y0 == 0 ? n - 1 : y0 - 1;
+    const int yp = y0 + TY == n ? 0 : y0 + TY;
+    const int xpl = x0 - L::PHW < 0 ? x0 - L::PHW + n : x0 - L::PHW;
+    const int xr = x0 + TX == n ? 0 : x0 + TX;
+    tma_phi<R>(smem_u32(st + L::phi_main), &tm_prow, x0, ym, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_main + TX * (int)sizeof(V)), &tm_pbody, x0, y0, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_main + (TY + 1) * TX * (int)sizeof(V)), &tm_prow, x0, yp, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_hl), &tm_phalo, xpl, y0, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_hr), &tm_phalo, xr, y0, z, bar);
+    if constexpr (UIJ) {
+      const int xul = x0 - L::UHW < 0 ? x0 - L::UHW + n : x0 - L::UHW;
+      tma_load_4d(smem_u32(st + L::u_top), &tm_urow, x0, ym, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_body), &tm_ubody, x0, y0, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_bot), &tm_urow, x0, yp, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_hl), &tm_uhalo, xul, y0, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_hr), &tm_uhalo, xr, y0, z, 0, bar);
+    }
+  };
+
+  if (tid == 0) {
+    const int first = nplanes < kStages ? nplanes : kStages;
+    for (int p = 0; p < first; ++p) issue(p);
+  }
+  bool ok = mbar_wait_bounded(smem_u32(&bars[0]), 0);
+  ok = ok && mbar_wait_bounded(smem_u32(&bars[1]), 0);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) atomicCAS(P.err, 0, AXG_KERR_MBAR_TIMEOUT);
+    return;
+  }
+
+  const int64_t n2 = (int64_t)n * n;
+  for (int k = 0; k < zc; ++k) {
+    const int p = k + 1;
+    const int z = z0 + k;
+    const int64_t s = z * n2 + (int64_t)(y0 + ty) * n + (x0 + tx);
+    // pointwise fields of this plane (issued before the stage wait)
+    const V pd = P.phid[s];
+    V cp;
+    if constexpr (sizeof(R) == 4) cp = P.cphi[s];
+    R udv[UIJ ? 6 : 1], cuv[UIJ ? 6 : 1];
+    if constexpr (UIJ) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        udv[c] = P.ud[c * P.n3 + s];
+        if constexpr (sizeof(R) == 4) cuv[c] = P.cu[c * P.n3 + s];
+      }
+    }
+    const int snext = (p + 1) % kStages;
+    ok = mbar_wait_bounded(smem_u32(&bars[snext]), (uint32_t)(((p + 1) / kStages) & 1));
+
+    if (ok) {
+      const unsigned char *sp = smem + ((p - 1) % kStages) * L::bytes;
+      const unsigned char *sc = smem + (p % kStages) * L::bytes;
+      const unsigned char *sn = smem + snext * L::bytes;
+      const V *pm = reinterpret_cast<const V *>(sc + L::phi_main);
+      const V *phl = reinterpret_cast<const V *>(sc + L::phi_hl);
+      const V *phr = reinterpret_cast<const V *>(sc + L::phi_hr);
+      const V c0 = pm[(ty + 1) * TX + tx];
+      const V xm = tx > 0 ? pm[(ty + 1) * TX + tx - 1] : phl[ty * L::PHW + L::PHW - 1];
+      const V xp = tx < TX - 1 ? pm[(ty + 1) * TX + tx + 1] : phr[ty * L::PHW];
+      const V ym = pm[ty * TX + tx];
+      const V yp = pm[(ty + 2) * TX + tx];
+      const V zm = reinterpret_cast<const V *>(sp + L::phi_main)[(ty + 1) * TX + tx];
+      const V zp = reinterpret_cast<const V *>(sn + L::phi_main)[(ty + 1) * TX + tx];
+
+      if constexpr (sizeof(R) == 4) {
+        // ---- FP32-mixed: difference-form Laplacian, Kahan drift ----
+        const float lr = ((xm.x - c0.x) + (xp.x - c0.x)) + ((ym.x - c0.x) + (yp.x - c0.x)) +
+                         ((zm.x - c0.x) + (zp.x - c0.x));
+        const float li = ((xm.y - c0.y) + (xp.y - c0.y)) + ((ym.y - c0.y) + (yp.y - c0.y)) +
+                         ((zm.y - c0.y) + (zp.y - c0.y));
+        const float s2 = c0.x * c0.x + c0.y * c0.y;
+        const float g = P.A * s2 + P.B;
+        const float vr = g * c0.x + P.D * c0.x + P.C;
+        const float vi = g * c0.y - P.D * c0.y;
+        V pdn;
+        pdn.x = P.f1 * pd.x + P.f2 * lr + P.f3 * vr;
+        pdn.y = P.f1 * pd.y + P.f2 * li + P.f3 * vi;
+        V pn = c0;
+        kahan_add(pn.x, cp.x, P.dtd * pdn.x);
+        kahan_add(pn.y, cp.y, P.dtd * pdn.y);
+        P.phid[s] = pdn;
+        P.cphi[s] = cp;
+        P.phi_out[s] = pn;
+        if constexpr (UIJ) {
+          const float gxr = xp.x - xm.x, gxi = xp.y - xm.y;
+          const float gyr = yp.x - ym.x, gyi = yp.y - ym.y;
+          const float gzr = zp.x - zm.x, gzi = zp.y - zm.y;
+          float S[6];
+          S[0] = gxr * gxr + gxi * gxi;
+          S[1] = gyr * gxr + gyi * gxi;
+          S[2] = gyr * gyr + gyi * gyi;
+          S[3] = gzr * gxr + gzi * gxi;
+          S[4] = gzr * gyr + gzi * gyi;
+          S[5] = gzr * gzr + gzi * gzi;
+          const float *ub = reinterpret_cast<const float *>(sc + L::u_body);
+          const float *ut = reinterpret_cast<const float *>(sc + L::u_top);
+          const float *ubt = reinterpret_cast<const float *>(sc + L::u_bot);
+          const float *uhl = reinterpret_cast<const float *>(sc + L::u_hl);
+          const float *uhr = reinterpret_cast<const float *>(sc + L::u_hr);
+          const float *ubp = reinterpret_cast<const float *>(sp + L::u_body);
+          const float *ubn = reinterpret_cast<const float *>(sn + L::u_body);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            const int o = (c * TY + ty) * TX + tx;
+            const float uc = ub[o];
+            const float uxm = tx > 0 ? ub[o - 1] : uhl[(c * TY + ty) * L::UHW + L::UHW - 1];
+            const float uxp = tx < TX - 1 ? ub[o + 1] : uhr[(c * TY + ty) * L::UHW];
+            const float uym = ty > 0 ? ub[o - TX] : ut[c * TX + tx];
+            const float uyp = ty < TY - 1 ? ub[o + TX] : ubt[c * TX + tx];
+            const float uzm = ubp[o], uzp = ubn[o];
+            const float lu = ((uxm - uc) + (uxp - uc)) + ((uym - uc) + (uyp - uc)) +
+                             ((uzm - uc) + (uzp - uc));
+            const float udn = P.f1 * udv[c] + P.f2 * lu + P.fsc * S[c];
+            float un = uc, cc = cuv[c];
+            kahan_add(un, cc, P.dtd * udn);
+            P.ud[c * P.n3 + s] = udn;
+            P.cu[c * P.n3 + s] = cc;
+            P.u_out[c * P.n3 + s] = un;
+          }
+        }
+      } else {
+        // ---- FP64-fused: same operations and order as the plain kernels ----
+        double lr = AXD_ADD(xm.x, xp.x);
+        lr = AXD_ADD(lr, ym.x);
+        lr = AXD_ADD(lr, yp.x);
+        lr = AXD_ADD(lr, zm.x);
+        lr = AXD_ADD(lr, zp.x);
+        lr = AXD_SUB(lr, AXD_MUL(6.0, c0.x));
+        double li = AXD_ADD(xm.y, xp.y);
+        li = AXD_ADD(li, ym.y);
+        li = AXD_ADD(li, yp.y);
+        li = AXD_ADD(li, zm.y);
+        li = AXD_ADD(li, zp.y);
+        li = AXD_SUB(li, AXD_MUL(6.0, c0.y));
+        const double s2 = AXD_ADD(AXD_MUL(c0.x, c0.x), AXD_MUL(c0.y, c0.y));
+        const double g = AXD_ADD(AXD_MUL(P.A, s2), P.B);
+        double vr = AXD_MUL(g, c0.x), vi = AXD_MUL(g, c0.y);
+        if (P.D != 0.0) {
+          vr = AXD_ADD(vr, AXD_MUL(P.D, c0.x));
+          vi = AXD_SUB(vi, AXD_MUL(P.D, c0.y));
+        }
+        vr = AXD_ADD(vr, P.C);
+        double pr = AXD_ADD(AXD_MUL(P.f1, pd.x), AXD_MUL(P.f2, lr));
+        pr = AXD_ADD(pr, AXD_MUL(P.f3, vr));
+        double pi_ = AXD_ADD(AXD_MUL(P.f1, pd.y), AXD_MUL(P.f2, li));
+        pi_ = AXD_ADD(pi_, AXD_MUL(P.f3, vi));
+        P.phid[s] = make_double2(pr, pi_);
+        P.phi_out[s] =
+            make_double2(AXD_ADD(c0.x, AXD_MUL(P.dtd, pr)), AXD_ADD(c0.y, AXD_MUL(P.dtd, pi_)));
+        if constexpr (UIJ) {
+          double dr[3], di[3];
+          dr[0] = AXD_DIV(AXD_SUB(xp.x, xm.x), P.d);
+          di[0] = AXD_DIV(AXD_SUB(xp.y, xm.y), P.d);
+          dr[1] = AXD_DIV(AXD_SUB(yp.x, ym.x), P.d);
+          di[1] = AXD_DIV(AXD_SUB(yp.y, ym.y), P.d);
+          dr[2] = AXD_DIV(AXD_SUB(zp.x, zm.x), P.d);
+          di[2] = AXD_DIV(AXD_SUB(zp.y, zm.y), P.d);
+          const double *ub = reinterpret_cast<const double *>(sc + L::u_body);
+          const double *ut = reinterpret_cast<const double *>(sc + L::u_top);
+          const double *ubt = reinterpret_cast<const double *>(sc + L::u_bot);
+          const double *uhl = reinterpret_cast<const double *>(sc + L::u_hl);
+          const double *uhr = reinterpret_cast<const double *>(sc + L::u_hr);
+          const double *ubp = reinterpret_cast<const double *>(sp + L::u_body);
+          const double *ubn = reinterpret_cast<const double *>(sn + L::u_body);
+          int c = 0;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+#pragma unroll
+            for (int j = 0; j <= i; ++j, ++c) {
+              const int o = (c * TY + ty) * TX + tx;
+              const double uc = ub[o];
+              const double uxm = tx > 0 ? ub[o - 1] : uhl[(c * TY + ty) * L::UHW + L::UHW - 1];
+              const double uxp = tx < TX - 1 ? ub[o + 1] : uhr[(c * TY + ty) * L::UHW];
+              const double uym = ty > 0 ? ub[o - TX] : ut[c * TX + tx];
+              const double uyp = ty < TY - 1 ? ub[o + TX] : ubt[c * TX + tx];
+              const double uzm = ubp[o], uzp = ubn[o];
+              double src = AXD_ADD(AXD_MUL(dr[i], dr[j]), AXD_MUL(di[i], di[j]));
+              src = AXD_MUL(2.0, src);
+              double lu = AXD_ADD(uxm, uxp);
+              lu = AXD_ADD(lu, uym);
+              lu = AXD_ADD(lu, uyp);
+              lu = AXD_ADD(lu, uzm);
+              lu = AXD_ADD(lu, uzp);
+              lu = AXD_SUB(lu, AXD_MUL(6.0, uc));
+              double v = AXD_ADD(AXD_MUL(P.f1, udv[c]), AXD_MUL(P.f2, lu));
+              v = AXD_ADD(v, AXD_MUL(P.fsc, src));
+              P.ud[c * P.n3 + s] = v;
+              P.u_out[c * P.n3 + s] = AXD_ADD(uc, AXD_MUL(P.dtd, v));
+            }
+          }
+        }
+      }
+    }
+    // all threads are done with stage (p-1); refill it with plane p-1+kStages
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicCAS(P.err, 0, AXG_KERR_MBAR_TIMEOUT);
+      return;
+    }
+    if (tid == 0 && p - 1 + kStages < nplanes) {
+      fence_proxy_async();
+      issue(p - 1 + kStages);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// tile table (autotuner search space) and host-side launch
+// ------------------------------------------------------------------------
+const axg_tile_cfg kTiles[] = {
+    {32, 16, 32}, {32, 8, 32}, {32, 16, 64}, {32, 8, 64}, {32, 16, 16}, {32, 8, 16}, {32, 4, 32},
+};
+constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+int encode(axg_ctx *ctx, CUtensorMap *m, CUtensorMapDataType dt, int rank, void *base,
+           const cuuint64_t *dims, const cuuint64_t *strides, const cuuint32_t *box) {
+  auto fn = encode_fn();
+  if (!fn) return axg_set_error(ctx, AXG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  CUresult r = fn(m, dt, (cuuint32_t)rank, base, dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return axg_set_error(ctx, AXG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return AXG_OK;
+}
+
+int build_tmaps(axg_ctx *ctx, int cfg) {
+  if (ctx->tm.valid && ctx->tm.cfg == cfg) return AXG_OK;
+  const axg_tile_cfg t = kTiles[cfg];
+  const cuuint64_t n = (cuuint64_t)ctx->n;
+  const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
+  const bool uij = ctx->p.gw_mode == AXG_GW_UIJ;
+  const int rs = fp32 ? 4 : 8;  // bytes of one real
+  for (int b = 0; b < 2; ++b) {
+    if (fp32) {
+      cuuint64_t dims[3] = {n, n, n};
+      cuuint64_t str[2] = {n * 8, n * n * 8};
+      cuuint32_t row[3] = {(cuuint32_t)t.tx, 1, 1}, body[3] = {(cuuint32_t)t.tx, (cuuint32_t)t.ty, 1},
+                 halo[3] = {2, (cuuint32_t)t.ty, 1};
+      AXG_TRY(encode(ctx, &ctx->tm.phi_row[b], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, ctx->phi[b], dims, str, row));
+      AXG_TRY(encode(ctx, &ctx->tm.phi_body[b], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, ctx->phi[b], dims, str, body));
+      AXG_TRY(encode(ctx, &ctx->tm.phi_halo[b], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, ctx->phi[b], dims, str, halo));
+    } else {
+      cuuint64_t dims[4] = {2, n, n, n};
+      cuuint64_t str[3] = {16, n * 16, n * n * 16};
+      cuuint32_t row[4] = {2, (cuuint32_t)t.tx, 1, 1}, body[4] = {2, (cuuint32_t)t.tx, (cuuint32_t)t.ty, 1},
+                 halo[4] = {2, 1, (cuuint32_t)t.ty, 1};
+      AXG_TRY(encode(ctx, &ctx->tm.phi_row[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, ctx->phi[b], dims, str, row));
+      AXG_TRY(encode(ctx, &ctx->tm.phi_body[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, ctx->phi[b], dims, str, body));
+      AXG_TRY(encode(ctx, &ctx->tm.phi_halo[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, ctx->phi[b], dims, str, halo));
+    }
+    if (uij) {
+      const CUtensorMapDataType dt = fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+      cuuint64_t dims[4] = {n, n, n, 6};
+      cuuint64_t str[3] = {n * rs, n * n * rs, n * n * n * rs};
+      const cuuint32_t uhw = 16 / rs;
+      cuuint32_t row[4] = {(cuuint32_t)t.tx, 1, 1, 6}, body[4] = {(cuuint32_t)t.tx, (cuuint32_t)t.ty, 1, 6},
+                 halo[4] = {uhw, (cuuint32_t)t.ty, 1, 6};
+      AXG_TRY(encode(ctx, &ctx->tm.u_row[b], dt, 4, ctx->u[b], dims, str, row));
+      AXG_TRY(encode(ctx, &ctx->tm.u_body[b], dt, 4, ctx->u[b], dims, str, body));
+      AXG_TRY(encode(ctx, &ctx->tm.u_halo[b], dt, 4, ctx->u[b], dims, str, halo));
+    } else {
+      // unused placeholders (kernel never dereferences them without UIJ)
+      ctx->tm.u_row[b] = ctx->tm.phi_row[b];
+      ctx->tm.u_body[b] = ctx->tm.phi_body[b];
+      ctx->tm.u_halo[b] = ctx->tm.phi_halo[b];
+    }
+  }
+  ctx->tm.valid = true;
+  ctx->tm.cfg = cfg;
+  return AXG_OK;
+}
+
+template <typename R, int TX, int TY, bool UIJ>
+int launch_fused_t(axg_ctx *ctx, const FusedParams<R> &P, const char *name) {
+  using L = StageLayout<R, TX, TY, UIJ>;
+  const int smem = kStages * L::bytes + kStages * 8 + 128;
+  static bool attr_set = false;
+  if (!attr_set) {
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_fused<R, TX, TY, UIJ>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr_set = true;
+  }
+  const int b = ctx->cur;
+  dim3 grid((unsigned)((ctx->n / TX) * (ctx->n / TY)), (unsigned)(ctx->n / P.zc));
+  dim3 block(TX, TY);
+  AXG_LAUNCH(ctx, name, (k_fused<R, TX, TY, UIJ>), grid, block, smem, ctx->tm.phi_row[b],
+             ctx->tm.phi_body[b], ctx->tm.phi_halo[b], ctx->tm.u_row[b], ctx->tm.u_body[b],
+             ctx->tm.u_halo[b], P);
+  return AXG_OK;
+}
+
+template <typename R, bool UIJ>
+int launch_fused_cfg(axg_ctx *ctx, const FusedParams<R> &P, int cfg, const char *name) {
+  const axg_tile_cfg t = kTiles[cfg];
+  if (t.tx == 32 && t.ty == 16) return launch_fused_t<R, 32, 16, UIJ>(ctx, P, name);
+  if (t.tx == 32 && t.ty == 8) return launch_fused_t<R, 32, 8, UIJ>(ctx, P, name);
+  if (t.tx == 32 && t.ty == 4) return launch_fused_t<R, 32, 4, UIJ>(ctx, P, name);
+  return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "tile configuration");
+}
+
+}  // namespace
+
+// --------------------------------------------------------------------------
+int axg_evo_tile_count() { return kNumTiles; }
+axg_tile_cfg axg_evo_tile(int i) { return kTiles[i]; }
+
+int axg_evo_tile_supported(const axg_ctx *ctx, int i) {
+  if (i < 0 || i >= kNumTiles) return 0;
+  const axg_tile_cfg t = kTiles[i];
+  const int64_t n = ctx->n;
+  if (n % t.tx || n % t.ty || n % t.zc) return 0;
+  if (n < 2 * t.ty || n < 4) return 0;
+  // shared memory budget per CTA (227 KB)
+  const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
+  const bool uij = ctx->p.gw_mode == AXG_GW_UIJ;
+  const int rs = fp32 ? 4 : 8, vs = 2 * rs;
+  const int phw = fp32 ? 2 : 1, uhw = 16 / rs;
+  auto a = [](int b) { return (b + 127) / 128 * 128; };
+  int st = a((t.ty + 2) * t.tx * vs) + 2 * a(t.ty * phw * vs);
+  if (uij) st += 2 * a(6 * t.tx * rs) + a(6 * t.ty * t.tx * rs) + 2 * a(6 * t.ty * uhw * rs);
+  if (kStages * st + kStages * 8 + 128 > 227 * 1024) return 0;
+  return 1;
+}
+
+int axg_evo_default_tile(const axg_ctx *ctx) {
+  // preferred order; first supported wins
+  const int pref_fp32[] = {0, 1, 2, 3, 4, 5, 6};
+  const int pref_fp64[] = {1, 3, 5, 0, 2, 4, 6};
+  const int *pref = ctx->p.precision == AXG_PREC_FP32_MIXED ? pref_fp32 : pref_fp64;
+  for (int i = 0; i < kNumTiles; ++i)
+    if (axg_evo_tile_supported(ctx, pref[i])) return pref[i];
+  return -1;
+}
+
+int axg_evo_drift(axg_ctx *ctx, double h) {
+  const int uij = ctx->p.gw_mode == AXG_GW_UIJ;
+  const int64_t n3 = ctx->n3;
+  int blocks = (int)((n3 + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  const int b = ctx->cur;
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
+    AXG_LAUNCH(ctx, "drift_fp32_kahan", k_drift_fp32, blocks, 256, 0, (float2 *)ctx->phi[b],
+               (const float2 *)ctx->phid, (float2 *)ctx->cphi, (float *)ctx->u[b],
+               (const float *)ctx->ud, (float *)ctx->cu, n3, (float)h, uij);
+  } else {
+    AXG_LAUNCH(ctx, "drift_fp64", k_drift_fp64, blocks, 256, 0, (double2 *)ctx->phi[b],
+               (const double2 *)ctx->phid, (double *)ctx->u[b], (const double *)ctx->ud, n3, h,
+               uij);
+  }
+  return AXG_OK;
+}
+
+int axg_evo_kick_plain(axg_ctx *ctx, double t, double dt) {
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+    return axg_set_error(ctx, AXG_ERR_STATE, "separate kick is the FP64 path; FP32 runs fused");
+  double f[4], pot[4];
+  axg_kick_coeffs(&ctx->p, t, dt, f, pot);
+  KickCoeffs k{f[0], f[1], f[2], f[3], pot[0], pot[1], pot[2], pot[3], ctx->p.dspa * 2};
+  const int n = (int)ctx->n;
+  dim3 block(32, 8);
+  dim3 grid((n + 31) / 32, (n + 7) / 8, n);
+  const int b = ctx->cur;
+  AXG_LAUNCH(ctx, "kick_fp64_plain", k_kick_fp64, grid, block, 0, (const double2 *)ctx->phi[b],
+             (double2 *)ctx->phid, (const double *)ctx->u[b], (double *)ctx->ud, n, k,
+             ctx->p.gw_mode == AXG_GW_UIJ ? 1 : 0);
+  return AXG_OK;
+}
+
+int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd) {
+  if (ctx->p.precision == AXG_PREC_FP64_PLAIN)
+    return axg_set_error(ctx, AXG_ERR_STATE, "fused step requested on the FP64-plain path");
+  int cfg = ctx->tile_cfg >= 0 ? ctx->tile_cfg : axg_evo_default_tile(ctx);
+  if (cfg < 0 || !axg_evo_tile_supported(ctx, cfg))
+    return axg_set_error(ctx, AXG_ERR_UNSUPPORTED,
+                         "lattice size has no supported fused tile (N must be a multiple of 32)");
+  AXG_TRY(build_tmaps(ctx, cfg));
+  double f[4], pot[4];
+  axg_kick_coeffs(&ctx->p, t, dt, f, pot);
+  const bool uij = ctx->p.gw_mode == AXG_GW_UIJ;
+  const int b = ctx->cur, o = 1 - b;
+  const axg_tile_cfg tc = kTiles[cfg];
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
+    FusedParams<float> P;
+    P.phi_out = (float2 *)ctx->phi[o];
+    P.phid = (float2 *)ctx->phid;
+    P.cphi = (float2 *)ctx->cphi;
+    P.u_out = (float *)ctx->u[o];
+    P.ud = (float *)ctx->ud;
+    P.cu = (float *)ctx->cu;
+    P.n3 = ctx->n3;
+    P.n = (int)ctx->n;
+    P.zc = tc.zc;
+    P.f1 = (float)f[0];
+    P.f2 = (float)f[1];
+    P.f3 = (float)f[2];
+    // source with raw differences: fs * 2 * (d_i d_j) / (2 dx)^2
+    P.fsc = (float)(f[3] * 2.0 / ((2.0 * ctx->p.dspa) * (2.0 * ctx->p.dspa)));
+    P.dtd = (float)dtd;
+    P.A = (float)pot[0];
+    P.B = (float)pot[1];
+    P.C = (float)pot[2];
+    P.D = (float)pot[3];
+    P.d = 2.0 * ctx->p.dspa;
+    P.err = ctx->d_err;
+    if (uij) AXG_TRY((launch_fused_cfg<float, true>(ctx, P, cfg, "fused_kd_fp32_uij")));
+    else AXG_TRY((launch_fused_cfg<float, false>(ctx, P, cfg, "fused_kd_fp32_phi")));
+  } else {
+    FusedParams<double> P;
+    P.phi_out = (double2 *)ctx->phi[o];
+    P.phid = (double2 *)ctx->phid;
+    P.cphi = nullptr;
+    P.u_out = (double *)ctx->u[o];
+    P.ud = (double *)ctx->ud;
+    P.cu = nullptr;
+    P.n3 = ctx->n3;
+    P.n = (int)ctx->n;
+    P.zc = tc.zc;
+    P.f1 = f[0];
+    P.f2 = f[1];
+    P.f3 = f[2];
+    P.fsc = f[3];
+    P.dtd = dtd;
+    P.A = pot[0];
+    P.B = pot[1];
+    P.C = pot[2];
+    P.D = pot[3];
+    P.d = 2.0 * ctx->p.dspa;
+    P.err = ctx->d_err;
+    if (uij) AXG_TRY((launch_fused_cfg<double, true>(ctx, P, cfg, "fused_kd_fp64_uij")));
+    else AXG_TRY((launch_fused_cfg<double, false>(ctx, P, cfg, "fused_kd_fp64_phi")));
+  }
+  ctx->cur = o;
+  return AXG_OK;
+}
+
+int axg_evo_check_error(axg_ctx *ctx) {
+  int h = 0;
+  AXG_CUDA_TRY(ctx, cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h == AXG_KERR_MBAR_TIMEOUT) {
+    int z = 0;
+    cudaMemcpy(ctx->d_err, &z, sizeof(int), cudaMemcpyHostToDevice);
+    return axg_set_error(ctx, AXG_ERR_TIMEOUT, "fused kernel: TMA stage wait timed out");
+  }
+  if (h != 0) {
+    int z = 0;
+    cudaMemcpy(ctx->d_err, &z, sizeof(int), cudaMemcpyHostToDevice);
+    return axg_set_error(ctx, AXG_ERR_CUDA, "kernel reported error " + std::to_string(h));
+  }
+  return AXG_OK;
+}

@@ -1,0 +1,201 @@
+// axg_internal.h -- context and shared helpers of libaxgpu (GB300, sm_103a).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/axgpu.h"
+
+// Error codes written by kernels into ctx->d_err (first writer wins).
+#define AXG_KERR_MBAR_TIMEOUT 1
+#define AXG_KERR_BOUNDS 2
+
+// Fused-kernel tile configurations known to the autotuner.
+struct axg_tile_cfg {
+  int tx, ty, zc;
+};
+
+struct axg_kernel_stat {
+  std::string name;
+  int64_t launches = 0;
+  double total_ms = 0.0;
+};
+
+struct axg_tmaps {
+  bool valid = false;
+  int cfg = -1;
+  CUtensorMap phi_row[2], phi_body[2], phi_halo[2];
+  CUtensorMap u_row[2], u_body[2], u_halo[2];
+};
+
+struct axg_ctx {
+  axg_params p{};
+  int64_t n = 0, n3 = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+
+  // evolution state; phi[cur] / u[cur] are current (fused paths ping-pong)
+  void *phi[2] = {nullptr, nullptr};
+  void *phid = nullptr;
+  void *cphi = nullptr;  // Kahan compensation of the phi drift (FP32 path)
+  void *u[2] = {nullptr, nullptr};
+  void *ud = nullptr;
+  void *cu = nullptr;  // Kahan compensation of the u drift (FP32 path)
+  int cur = 0;
+  size_t elem = 8;  // bytes of one real of the field storage
+
+  // Green's-function GW state (grav_waves.f90)
+  double2 *acc = nullptr;  // [4][n3]
+  double *gsrc = nullptr;  // [6][n3] real sources S_ij
+  double2 *gsrcF = nullptr;  // [6][n*n*(n/2+1)]
+  cufftHandle plan_gsrc = 0;
+  bool plan_gsrc_ok = false;
+
+  // defects
+  int8_t *flags = nullptr;  // per cell, bits 1/2/4
+  double *phase = nullptr;  // per site phase scratch
+  bool flags_valid = false;
+  // fit results of the last id_defects
+  double *d_strings = nullptr;
+  double *d_walls = nullptr;
+  int64_t cap_strings = 0, cap_walls = 0;
+  int64_t last_ns = 0, last_nw = 0, last_nm = 0;
+
+  // spectra
+  double *spec_mat = nullptr;  // mat_spec [num_cov][501]
+  double *spec_largeq0 = nullptr, *spec_dq = nullptr;  // per ij
+  std::vector<double> h_mat_spec, h_largeq, h_dq, h_wav;
+  std::vector<double> last_power;
+  double2 *spec_buf = nullptr;  // (N/deg)^3 complex
+  cufftHandle plan_spec = 0;
+  bool plan_spec_ok = false;
+  int64_t ns_spec = 0;
+
+  // GW spectra of u_ij (R2C of 12 fields)
+  cufftHandle plan_u = 0;
+  bool plan_u_ok = false;
+  void *ubuf = nullptr;  // real inputs / complex outputs workspace
+
+  // reductions
+  double *d_red = nullptr;  // small FP64 reduction buffer
+  unsigned long long *d_cnt = nullptr;  // small counter buffer
+  int *d_err = nullptr;
+  size_t red_cap = 0;
+
+  // tensor maps for the fused kernel
+  axg_tmaps tm;
+  int tile_cfg = -1;  // chosen tile configuration (-1: default)
+
+  // timing
+  cudaEvent_t user_ev[8] = {};
+  bool ktiming = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<cudaEvent_t> ev_pool;
+  std::map<std::string, int> kid;
+  std::vector<axg_kernel_stat> kstats;
+  int64_t launches = 0;
+  int64_t bytes = 0;
+
+  std::string err;
+};
+
+// ---------------------------------------------------------------------------
+// error helpers (return a status from the enclosing C-ABI function)
+// ---------------------------------------------------------------------------
+int axg_set_error(axg_ctx *ctx, int code, const std::string &msg);
+
+#define AXG_CUDA_TRY(ctx, call)                                                       \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return axg_set_error((ctx), AXG_ERR_CUDA,                                       \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+#define AXG_CUFFT_TRY(ctx, call)                                                      \
+  do {                                                                                \
+    cufftResult r_ = (call);                                                          \
+    if (r_ != CUFFT_SUCCESS)                                                          \
+      return axg_set_error((ctx), AXG_ERR_CUDA,                                       \
+                           std::string(#call) + ": cufft error " + std::to_string((int)r_)); \
+  } while (0)
+
+#define AXG_TRY(expr)        \
+  do {                       \
+    int s_ = (expr);         \
+    if (s_ != AXG_OK) return s_; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// kernel launch bookkeeping (per-kernel event timing for the roofline)
+// ---------------------------------------------------------------------------
+void axg_kt_begin(axg_ctx *ctx, const char *name);
+void axg_kt_end(axg_ctx *ctx);
+int axg_kt_flush(axg_ctx *ctx);
+
+#define AXG_LAUNCH(ctx, name, kern, grid, block, smem, ...)                         \
+  do {                                                                              \
+    axg_kt_begin((ctx), (name));                                                    \
+    kern<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);                  \
+    axg_kt_end((ctx));                                                              \
+    (ctx)->launches++;                                                              \
+    cudaError_t le_ = cudaGetLastError();                                           \
+    if (le_ != cudaSuccess)                                                         \
+      return axg_set_error((ctx), AXG_ERR_CUDA,                                     \
+                           std::string("launch ") + (name) + ": " + cudaGetErrorString(le_)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// device allocation helper (counts bytes)
+// ---------------------------------------------------------------------------
+int axg_alloc(axg_ctx *ctx, void **ptr, size_t bytes, const char *what);
+void axg_free(axg_ctx *ctx, void **ptr);
+
+// ---------------------------------------------------------------------------
+// internal entry points implemented in the kernel files
+// ---------------------------------------------------------------------------
+// evolution (axg_evolve.cu)
+int axg_evo_drift(axg_ctx *ctx, double h);                  // drift of current state
+int axg_evo_kick_plain(axg_ctx *ctx, double t, double dt);  // FP64-plain kick (phi, u)
+int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd);  // fused step
+int axg_evo_check_error(axg_ctx *ctx);
+int axg_evo_tile_count();
+axg_tile_cfg axg_evo_tile(int i);
+int axg_evo_tile_supported(const axg_ctx *ctx, int i);
+int axg_evo_default_tile(const axg_ctx *ctx);
+
+// kick coefficients (axg_capi.cu) -- evolve.f90:291-305
+void axg_kick_coeffs(const axg_params *p, double t, double dt, double f[4], double pot[4]);
+
+// GW (axg_gw.cu)
+int axg_gw_init(axg_ctx *ctx);
+int axg_gw_integration(axg_ctx *ctx, double tau, double dtau);
+int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *power,
+                double *numer, double *denom);
+
+// defects (axg_defects.cu)
+int axg_def_classify(axg_ctx *ctx, int which, int64_t counts[3]);
+int axg_def_winding(axg_ctx *ctx, int64_t counts[3]);
+int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], double svel[3],
+                       int64_t counts[3]);
+
+// spectrum (axg_spectrum.cu)
+int axg_spec_init(axg_ctx *ctx);
+int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, double *conv,
+                        double *count);
+
+// initial conditions / moments (axg_ic.cu)
+int axg_ic_gauss(axg_ctx *ctx, double kcut, uint32_t realisation);
+int axg_ic_therm(axg_ctx *ctx, double tau_ini, uint32_t realisation);
+int axg_moments(axg_ctx *ctx, double tau, double out[4]);
+
+// conversion helpers (axg_capi.cu)
+int axg_phi_to_fp64(axg_ctx *ctx, double2 *dst);   // current phi as complex128 (device)
+int axg_phid_to_fp64(axg_ctx *ctx, double2 *dst);  // current phidot as complex128 (device)

@@ -1,0 +1,363 @@
+"""Throughput benchmark of the lattice hot path (one JSON line on rank 0).
+
+Metric: site-updates/s at 512^3 -- one site-update is one full leapfrog step
+(kick + drift) of the complex field phi and all six u_ij at one lattice site.
+The headline arm is the FP32-mixed fused path (FP32 fields and stencil,
+Kahan-compensated drifts, FP64 host scalars); the FP64-plain drop-in path
+(reference-structured separate kick and drift passes) is measured in the same
+run and reported beside it.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+--impl reference times the reference algorithm on the host cores: the CPU
+restatement of evolve.f90 (the reference Fortran/MPI/MKL build cannot be
+compiled in this environment), FP64, all host threads, same lattice.
+Multi-GPU: the path runs as independent replicas (one lattice per rank, no
+data-path collective); value is the aggregate over ranks (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "site-updates/s at 512³ (FP32-mixed vs FP64 plain, 1 GB300); % HBM roofline"
+UNIT = "site-updates/s"
+# algorithmic HBM bytes per site-update (state read once + written once):
+#   FP32-mixed fused Mode U: read phi 8 + phi' 8 + c_phi 8 + u 24 + u' 24 + c_u 24, write the same
+#   FP64-plain Mode U:       drift 192 + kick 192 (phi 16, phi' 16, u 48, u' 48 read; 16 + 48 written each)
+BYTES_PER_SITE = {"fused_kd_fp32_uij": 192, "fused_kd_fp32_phi": 48, "fused_kd_fp64_uij": 256,
+                  "fused_kd_fp64_phi": 64, "kick_fp64_plain": 192, "drift_fp64": 192}
+BYTES_PER_SITE_PHI_ONLY = {"kick_fp64_plain": 48, "drift_fp64": 48}
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic_per_site(kernel: str):
+    """DRAM bytes per site of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_site:\s*([0-9.eE+-]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload_params(ag, n, precision, gw, device=0):
+    # 512^3 periodic lattice, reference potential (potential.f90), sigma_cr = 1,
+    # dx = boxsize * tau_fin / N with boxsize 1, tau_fin 32; kappa 0.1.
+    return ag.default_params(ngrid=n, precision=precision, gw_mode=gw, potential=ag.POT_REFERENCE,
+                             dspa=32.0 / n, sigma_cr=1.0, kappa=0.1, seed=1, device=device)
+
+
+def bench_ours(ag, n, precision, gw, steps, warmup, dist, device, t0=2.0, eps=0.25, clocks=False,
+               tune=True):
+    p = workload_params(ag, n, precision, gw, device)
+    lat = ag.Lattice(p)
+    try:
+        lat.ic_gaussian_flat(kcut=2.0 * np.pi / (8 * p.dspa))
+        dt, _ = lat.get_dtau(t0, 32.0, eps)
+        tile = None
+        if tune and precision != ag.PREC_FP64_PLAIN:
+            tile, _ = lat.autotune(3)
+        t = t0
+        lat.leapfrog(t, dt, 1, True, False)  # half drift + one step
+        t += dt * 1.5
+        lat.leapfrog(t, dt, warmup, False, False)
+        t += dt * warmup
+        lat.synchronize()
+        lat.set_kernel_timing(True)
+        if dist is not None:
+            dist.barrier()
+        lat.synchronize()
+        sampler = ClockSampler(device) if clocks else None
+        if sampler:
+            sampler.__enter__()
+        l0 = lat.launch_count()
+        lat.event_record(0)
+        lat.leapfrog(t, dt, steps, False, False)
+        lat.event_record(1)
+        ms = lat.event_elapsed(0, 1)
+        lat.synchronize()
+        l1 = lat.launch_count()
+        if sampler:
+            sampler.__exit__(None, None, None)
+        if dist is not None:
+            dist.barrier()
+        kt = lat.kernel_timings()
+        lat.set_kernel_timing(False)
+        return {"ms": ms, "launches": l1 - l0, "kernels": kt, "tile": tile,
+                "tile_shape": lat.tiles()[tile] if tile is not None else None,
+                "clocks": sampler.summary() if sampler else None, "dt": dt, "lat": lat, "t": t + dt * steps}
+    except Exception:
+        lat.close()
+        raise
+
+
+def bench_e2e(ag, lat, n, nsub, reps, t, dt):
+    """Through the public C-ABI with host buffers: per interval upload phi and
+    phidot (complex128, pinned host memory), nsub leapfrog steps, download
+    phi and phidot -- the host-resident data1/data2 of the reference."""
+    import torch
+
+    shape = (n, n, n, 2)
+    h_phi = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    h_phid = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    lib = ag.load_library()
+    import ctypes
+
+    dp = lambda tt: ctypes.cast(tt.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    rc = lib.axg_download(lat.handle, dp(h_phi), dp(h_phid), n * n, 0)
+    assert rc == 0
+    times = []
+    for r in range(reps + 1):
+        t_start = time.perf_counter()
+        assert lib.axg_upload(lat.handle, dp(h_phi), dp(h_phid), n * n, 0) == 0
+        assert lib.axg_leapfrog(lat.handle, t, dt, nsub, 1, 1) == 0
+        assert lib.axg_download(lat.handle, dp(h_phi), dp(h_phid), n * n, 0) == 0
+        times.append(time.perf_counter() - t_start)
+        t += dt * nsub
+    per = float(np.median(times[1:]))
+    bytes_each = 2 * n ** 3 * 16
+    return {"value": nsub * n ** 3 / per, "unit": UNIT, "h2d_bytes_per_step": bytes_each / nsub,
+            "d2h_bytes_per_step": bytes_each / nsub, "interval_steps": nsub, "s_per_interval": per,
+            "note": "public C-ABI, host-resident complex128 phi and phidot uploaded and downloaded "
+                    "once per interval of %d leapfrog steps (pinned host memory); u_ij device-resident" % nsub}
+
+
+def cpu_oracle_rate(n, steps, threads=None):
+    """FP64 CPU restatement of evolve.f90 (phi + six u_ij), all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import axo
+    import axion_grav_gb300 as ag
+
+    p = workload_params(ag, n, ag.PREC_FP64_PLAIN, ag.GW_UIJ)
+    rng = np.random.default_rng(0)
+    phi = np.empty((n, n, n), np.complex128)
+    phid = np.zeros((n, n, n), np.complex128)
+    for z in range(n):  # chunked fill keeps peak memory low
+        phi[z] = np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
+    u = np.zeros((6, n, n, n))
+    ud = np.zeros((6, n, n, n))
+    dt, _ = axo.get_dtau(p, 2.0, 32.0, 0.25)
+    axo.leapfrog(p, phi, phid, u, ud, None, 2.0, dt, 1, True, False)  # warm-up
+    t = 2.0 + 1.5 * dt
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        axo.leapfrog(p, phi, phid, u, ud, None, t, dt, 1, False, False)
+        times.append(time.perf_counter() - t0)
+        t += dt
+    per = float(np.median(times))
+    return n ** 3 / per, per, axo.lib().axo_num_threads()
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    n = args.n
+    steps = max(1, args.steps)
+    rate, per, cores = cpu_oracle_rate(n, steps)
+    sample = f"{steps} leapfrog steps (phi + 6 u_ij, FP64) of the {n}^3 lattice after 1 warm-up step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{n}^3 lattice leapfrog of phi + 6 u_ij (one site-update = one kick+drift of all "
+                               f"7 fields at one site)", "n": n, "gw_mode": "uij",
+                   "implementation": "CPU restatement of evolve.f90 (oracle/, C + OpenMP, FP64); the Fortran "
+                                     "reference needs ifort/MPI/MKL/FFTW, none present"},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-plain comparison arm")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--e2e-interval", type=int, default=20)
+    ap.add_argument("--e2e-reps", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        backend = "nccl" if os.environ.get("AXG_BENCH_GLOO") is None else "gloo"
+        tdist.init_process_group(backend=backend)
+        dist = tdist
+    import torch
+
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    import axion_grav_gb300 as ag
+
+    n = args.n
+    r32 = bench_ours(ag, n, ag.PREC_FP32_MIXED, ag.GW_UIJ, args.steps, args.warmup, dist, local, clocks=True)
+    lat = r32.pop("lat")
+    e2e = bench_e2e(ag, lat, n, args.e2e_interval, args.e2e_reps, r32["t"], r32["dt"]) if rank == 0 else None
+    lat.close()
+
+    ms = r32["ms"]
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    sites = float(n) ** 3
+    value = world * sites * args.steps / (ms * 1e-3)
+
+    peak, peak_kind = measured_peaks()
+    kern = {k: (l, t) for k, l, t in r32["kernels"]}
+    dom = max(kern, key=lambda k: kern[k][1])
+    l, tot = kern[dom]
+    avg_ms = tot / max(l, 1)
+    alg = BYTES_PER_SITE.get(dom, 0) * sites
+    achieved = alg / (avg_ms * 1e-3) / 1e9
+    tps = ncu_traffic_per_site(dom)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": tps * sites if tps is not None else None, "kernel": dom,
+            "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms,
+            "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback 6.8 TB/s"}
+
+    fp64 = None
+    if not args.no_fp64:
+        r64 = bench_ours(ag, n, ag.PREC_FP64_PLAIN, ag.GW_UIJ, max(3, args.steps // 4), args.warmup, dist, local)
+        r64.pop("lat").close()
+        k64 = {k: (l, t) for k, l, t in r64["kernels"]}
+        st64 = max(3, args.steps // 4)
+        v64 = world * sites * st64 / (r64["ms"] * 1e-3)
+        byts = sum(BYTES_PER_SITE.get(k, 0) * sites * l for k, (l, t) in k64.items())
+        tms = sum(t for k, (l, t) in k64.items())
+        fp64 = {"value": v64, "ms_per_step": r64["ms"] / st64, "steps": st64,
+                "kernels": {k: {"launches": l, "avg_ms": t / max(l, 1)} for k, (l, t) in k64.items()},
+                "hbm_frac": (byts / (tms * 1e-3) / 1e9) / peak if tms > 0 else None,
+                "fp32_mixed_speedup": value / v64 / world * world}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            rate, per, cores = cpu_oracle_rate(n, args.cpu_steps)
+            cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": f"{args.cpu_steps} leapfrog steps (phi + 6 u_ij, FP64) of the {n}^3 lattice, "
+                             f"CPU restatement of evolve.f90 (oracle/), OpenMP"}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {exc}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{n}^3 periodic lattice, one leapfrog step (kick+drift) of phi and six u_ij "
+                                   f"per site, FP32-mixed fused TMA kernel with Kahan drift; reference potential "
+                                   f"(potential.f90), Gaussian-flat seeded IC",
+                       "n": n, "gw_mode": "uij", "precision": "fp32_mixed", "parallelism": f"replicas x{world}",
+                       "l2": "no flush: state %.1f GiB >> 126 MB L2" % (sites * 96 / 2 ** 30),
+                       "tile": r32["tile_shape"]},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r32["launches"],
+            "clocks": r32["clocks"], "fp64_plain": fp64,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,262 @@
+/*
+ * axgpu.h -- C-ABI of the GB300 lattice hot path of axion_grav.
+ *
+ * The reference program (Fortran 90 + MPI + FFTW) keeps its host side
+ * (main.f90, settings.f90, inifile.f90) and replaces the bodies of its module
+ * routines with calls into this library through iso_c_binding.  Every entry
+ * point names the reference routine it replaces (file:line in the reference
+ * project).  All scalars are passed by value, all arrays by pointer; complex
+ * arrays are interleaved (re, im) complex128, x fastest, i.e. Fortran
+ * complex(C_DOUBLE_COMPLEX) data1(ngrid, ngrid, ...).
+ *
+ * Ownership: the caller owns every host array; the library owns all device
+ * memory and copies only inside axg_upload* / axg_download* and the explicit
+ * I/O calls.  One host thread per context; all work of a context is ordered
+ * on one CUDA stream.  Every function returns AXG_OK (0) or a negative status;
+ * axg_last_error() gives the message.  The library never calls exit().
+ */
+#ifndef AXGPU_H
+#define AXGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the Fortran wrapper maps any nonzero status onto
+ *      MpiStop(msg), utils.f90:44-73) ---- */
+#define AXG_OK 0
+#define AXG_ERR_ARG (-1)
+#define AXG_ERR_CUDA (-2)
+#define AXG_ERR_NOMEM (-3)
+#define AXG_ERR_STATE (-4)
+#define AXG_ERR_IO (-5)
+#define AXG_ERR_TIMEOUT (-6)
+#define AXG_ERR_UNSUPPORTED (-7)
+#define AXG_ERR_NUMERIC (-8)
+
+/* ---- field storage / arithmetic of the evolution ---- */
+#define AXG_PREC_FP64_PLAIN 0 /* reference-structured: separate drift and kick passes, FP64 */
+#define AXG_PREC_FP64_FUSED 1 /* one kick+drift pass per step, FP64 */
+#define AXG_PREC_FP32_MIXED 2 /* one pass, FP32 fields, Kahan-compensated drifts */
+
+/* ---- gravitational-wave method ---- */
+#define AXG_GW_NONE 0
+#define AXG_GW_GREEN 1 /* grav_waves.f90:193-255 Green's-function accumulation */
+#define AXG_GW_UIJ 2   /* real-space leapfrog of six u_ij, TT projection at output */
+
+/* ---- settings.f90 logical switches ---- */
+#define AXG_F_ID_STRINGS 1
+#define AXG_F_ID_WALLS 2
+#define AXG_F_SPEC_EST 4
+#define AXG_F_GRAV_SPEC 8
+#define AXG_F_INITIAL_LOOP 16
+
+/* ---- potential model ---- */
+#define AXG_POT_REFERENCE 0 /* potential.f90:34-79 thermal mass + IILM tilt */
+#define AXG_POT_QUARTIC 1   /* lambda/4 (|phi|^2 - v^2)^2 + m_a^2 v^2 (1 - cos N_DW theta)/N_DW^2 */
+
+/* ---- literal reproduction of reference quirks ---- */
+#define AXG_COMPAT_INTENDED 0
+#define AXG_COMPAT_REF 1 /* grav_waves.f90:240-241 cross-wired accumulators */
+
+typedef struct axg_params {
+  int32_t ngrid;        /* N (even); lattice N^3, periodic (settings.f90:148) */
+  int32_t precision;    /* AXG_PREC_* */
+  int32_t gw_mode;      /* AXG_GW_* */
+  int32_t num_bin;      /* field-spectrum bins (settings.f90:158, default 50) */
+  int32_t degrade_spec; /* spectra coarse-grained by 2^degrade_spec (settings.f90:202) */
+  int32_t flags;        /* AXG_F_* */
+  int32_t compat;       /* AXG_COMPAT_* */
+  int32_t potential;    /* AXG_POT_* */
+  int32_t n_dw;         /* domain-wall number of the quartic model's axion term (1 or 2) */
+  int32_t num_bin_grav; /* GW bins (grav_waves.f90:6, 25) */
+  int32_t gw_log_bins;  /* >0: additionally bin the GW spectrum in this many log bins */
+  int32_t device;       /* CUDA device ordinal of the context */
+  double dspa;          /* lattice spacing dx in tau_cr (settings.f90:294) */
+  double sigma_cr;      /* sigma * tau_cr (settings.f90:276) */
+  double kappa;         /* axion-mass scale (potential.f90:25) */
+  double tau_cr;        /* tau_cr in reduced-Planck units (settings.f90:275) */
+  double a_now;         /* present scale factor (settings.f90:274) */
+  double width_cr;      /* string width (settings.f90:279) */
+  double thickness_cr;  /* wall thickness (settings.f90:280) */
+  double lambda;        /* quartic model coupling */
+  double vev;           /* quartic model v */
+  double ma2_0;         /* quartic model: m_a^2 at tau_axion_on */
+  double tau_axion_on;  /* quartic model: axion term switched on at this tau */
+  double ma2_power;     /* quartic model: m_a^2 ~ (tau/tau_on)^ma2_power */
+  uint64_t seed;        /* Philox key of every random draw (IC, fit starts) */
+  uint64_t reserved1;
+} axg_params;
+
+typedef struct axg_ctx axg_ctx;
+
+/* ------------------------------------------------------------------ */
+/* library / context                                                    */
+/* ------------------------------------------------------------------ */
+int axg_version(void);
+/* Fill *p with the defaults of settings.f90 (num_bin 50, 25 GW bins ...). */
+int axg_params_default(axg_params *p);
+/* init_grav (grav_waves.f90:27-82) + init_spectrum (spectrum.f90:23-103) +
+ * allocate_data (initial.f90:240-285): allocates all device state. */
+int axg_create(const axg_params *p, axg_ctx **out);
+/* fin_grav (grav_waves.f90:84-90) + fin_spectrum + deallocate_data. */
+int axg_destroy(axg_ctx *ctx);
+/* Message of the last failing call on ctx (NULL ctx: last axg_create error). */
+const char *axg_last_error(const axg_ctx *ctx);
+/* Device bytes held by the context (memory_check_mkl, settings.f90:392-422). */
+int axg_memory_bytes(const axg_ctx *ctx, int64_t *bytes);
+
+/* ------------------------------------------------------------------ */
+/* state transfer                                                       */
+/* ------------------------------------------------------------------ */
+/* Copy the interior N^3 sites of data1 (phi) and data2 (phidot) in.
+ * plane_stride = elements between z-planes of the host array (N*N for a dense
+ * array); first_plane = index of the first interior plane (1 for the
+ * reference's [N,N,local_0+2] arrays with one halo plane, 0 for dense).
+ * Either pointer may be NULL to skip that field. */
+int axg_upload(axg_ctx *ctx, const double *phi, const double *phidot, int64_t plane_stride,
+               int64_t first_plane);
+int axg_download(axg_ctx *ctx, double *phi, double *phidot, int64_t plane_stride,
+                 int64_t first_plane);
+/* Six u_ij and u_ij' as real FP64 [6][N^3], component order
+ * (1,1),(2,1),(2,2),(3,1),(3,2),(3,3) (grav_waves.f90:210-211 loop order). */
+int axg_upload_uij(axg_ctx *ctx, const double *u, const double *udot);
+int axg_download_uij(axg_ctx *ctx, double *u, double *udot);
+/* Four Green's-function accumulators arr_grav(2,2,N^3) as complex128
+ * [4][N^3] in the order (1,1),(2,1),(1,2),(2,2) (grav_waves.f90:74). */
+int axg_upload_gw_green(axg_ctx *ctx, const double *acc);
+int axg_download_gw_green(axg_ctx *ctx, double *acc);
+
+/* ------------------------------------------------------------------ */
+/* evolution (evolve.f90)                                              */
+/* ------------------------------------------------------------------ */
+/* get_dtau (evolve.f90:10-24). */
+int axg_get_dtau(const axg_params *p, double tau1, double tau2, double eps_dtau, double *dtau,
+                 int64_t *nsteps);
+/* evolve_phi (evolve.f90:259-281): phi += dt phidot (and u_ij += dt u_ij').
+ * *t is advanced by dt like the reference's intent(inout) t. */
+int axg_evolve_phi(axg_ctx *ctx, double *t, double dt);
+/* evolve_phidot (evolve.f90:283-339): one kick at conformal time t; with
+ * AXG_GW_GREEN also grav_wave_integration(t, dt) (grav_waves.f90:193-255);
+ * with AXG_GW_UIJ the u_ij kick with the d_i phi d_j phi* source. */
+int axg_evolve_phidot(axg_ctx *ctx, double t, double dt);
+/* symplectic_integration (evolve.f90:238-257): drift-kick-drift from t1 to t2
+ * with dt from get_dtau.  *nsteps_out receives nt (may be NULL). */
+int axg_symplectic_integration(axg_ctx *ctx, double t1, double t2, double eps_dtau,
+                               int64_t *nsteps_out);
+/* nsteps kick+drift steps of size dt starting at kick time t (fused paths:
+ * one pass per step); first_half / last_half apply the half drifts of the DKD
+ * scheme before the first / instead of the last full drift. */
+int axg_leapfrog(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half,
+                 int last_half);
+
+/* Tile shapes of the fused kick+drift kernel: a CTA owns a tx x ty column of
+ * the lattice and marches through zc z-planes.  The autotuner times every
+ * shape the lattice supports for `steps` steps on a snapshot of the state
+ * (restored afterwards) and keeps the fastest. */
+int axg_tile_count(void);
+int axg_tile_info(int i, int32_t *tx, int32_t *ty, int32_t *zc);
+int axg_set_tile(axg_ctx *ctx, int cfg);
+int axg_autotune(axg_ctx *ctx, int steps, int *best_cfg, double *best_ms_per_step);
+
+/* ------------------------------------------------------------------ */
+/* gravitational waves (grav_waves.f90)                                */
+/* ------------------------------------------------------------------ */
+/* grav_spec_estimation (grav_waves.f90:257-321) for the current state.
+ * Outputs are nbins = num_bin_grav long: bin centres (wave), power_grav,
+ * numer and denom.  With AXG_GW_UIJ the TT-projected spectrum of u_ij. */
+int axg_grav_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, double *numer,
+                             double *denom);
+/* Same quantity binned in params.gw_log_bins logarithmic bins on
+ * [2 pi/(N dx), pi/dx]; edges has nbins+1 entries. */
+int axg_grav_spec_log(axg_ctx *ctx, double tau, double *edges, double *power, double *numer,
+                      double *denom);
+
+/* ------------------------------------------------------------------ */
+/* defects (defects_3d.f90)                                            */
+/* ------------------------------------------------------------------ */
+/* Cell classification pass of id_defects (defects_3d.f90:67-103, 309-349):
+ * int8 flags per cell (1 string, 2 wall, 4 mask) kept on the device;
+ * counts = (ns, nw, nm).  which = AXG_F_ID_STRINGS|AXG_F_ID_WALLS|AXG_F_SPEC_EST. */
+int axg_classify_cells(axg_ctx *ctx, int which, int64_t counts[3]);
+int axg_download_defect_flags(axg_ctx *ctx, int8_t *flags);
+/* Plaquette winding: number of plaquettes pierced by a string, per
+ * orientation (normal x, y, z). */
+int axg_string_winding(axg_ctx *ctx, int64_t counts[3]);
+/* Whole id_defects (defects_3d.f90:31-307): classification, per-cell string
+ * and wall fits (position_string, velocity_string, position_wall) and the sums
+ * of add_string_length / add_wall_area (defects_3d.f90:1654-1733, 2145-2204).
+ * sl, wa, svel as in the reference (lattice units); counts = (ns, nw, nm). */
+int axg_id_defects(axg_ctx *ctx, int64_t idx, double tau, double sl[3], double wa[3],
+                   double svel[3], int64_t counts[3]);
+/* Per-cell fit results of the last axg_id_defects, in cell order (z, y, x).
+ * strings: [ns][12] = pos(3) dir(3) vel(3) gof sl cell; walls: [nw][10] =
+ * pos(3) dir(3) gof wa cell pad. */
+int axg_download_defect_lists(axg_ctx *ctx, double *strings, int64_t max_strings, double *walls,
+                              int64_t max_walls);
+
+/* ------------------------------------------------------------------ */
+/* field spectrum (spectrum.f90)                                       */
+/* ------------------------------------------------------------------ */
+/* spectrum_estimation core (spectrum.f90:242-287 without the MC covariance):
+ * masked, degraded phidot spectrum, deconvolved with the mode-coupling
+ * matrix of the mask of the last classification.  Arrays of num_bin:
+ * wave (bin centres), power (power_spec), conv (conv_spec/num_conv_spec),
+ * count (num_conv_spec).  tau is tau_id(idx). */
+int axg_spectrum_estimation(axg_ctx *ctx, double tau, double *wave, double *power, double *conv,
+                            double *count);
+/* compute_crho (spectrum.f90:316-342) from the last power spectrum (no
+ * covariance: drho = 0). */
+int axg_compute_crho(axg_ctx *ctx, double *rho);
+
+/* ------------------------------------------------------------------ */
+/* initial conditions (initial.f90) and diagnostics                    */
+/* ------------------------------------------------------------------ */
+/* Seeded Gaussian random field: every Fourier mode with |k| <= kcut an
+ * independent complex normal, others zero; normalised to <|phi|^2> = vev^2;
+ * phidot = 0; u = u' = 0. */
+int axg_ic_gaussian_flat(axg_ctx *ctx, double kcut, uint32_t realisation);
+/* get_initial_thermal (initial.f90:80-238, 363-390) at tau_ini with the
+ * project's Philox draws in place of MKL VSL streams. */
+int axg_ic_thermal(axg_ctx *ctx, double tau_ini, uint32_t realisation);
+/* Volume averages in FP64: out = (<|phi|^2>, <|phi'|^2>, <|grad phi|^2>, <V(phi)>)
+ * at conformal time tau. */
+int axg_field_moments(axg_ctx *ctx, double tau, double out[4]);
+
+/* ------------------------------------------------------------------ */
+/* checkpoint / resume (evolve.f90:401-546)                            */
+/* ------------------------------------------------------------------ */
+/* io_chk: raw complex128 phi block then phidot block, x fastest, global order
+ * (evolve.f90:498-503); plus u_ij blocks when present and a CRC32 sidecar
+ * file path+".crc".  write_chk's param.chk is written by axg_write_param_chk. */
+int axg_write_chk(axg_ctx *ctx, const char *path);
+int axg_read_chk(axg_ctx *ctx, const char *path);
+/* param.chk "idx tau flag" (evolve.f90:407-421, 445-448). */
+int axg_write_param_chk(const char *path, int64_t idx, double tau, int flag_defects);
+int axg_read_param_chk(const char *path, int64_t *idx, double *tau, int *flag_defects);
+
+/* ------------------------------------------------------------------ */
+/* timing / profiling                                                  */
+/* ------------------------------------------------------------------ */
+int axg_synchronize(axg_ctx *ctx);
+/* Record a CUDA event on the context stream (slot 0..7). */
+int axg_event_record(axg_ctx *ctx, int slot);
+/* Milliseconds between two recorded slots (synchronises on the later one). */
+int axg_event_elapsed(axg_ctx *ctx, int slot_a, int slot_b, float *ms);
+/* When on, every kernel launch is bracketed by events and its time is
+ * accumulated per kernel name (for the roofline). */
+int axg_set_kernel_timing(axg_ctx *ctx, int on);
+/* Name, launches and total ms of the i-th timed kernel; AXG_ERR_ARG past the end. */
+int axg_kernel_timing(axg_ctx *ctx, int i, char *name, int64_t name_len, int64_t *launches,
+                      double *total_ms);
+/* Number of kernels launched on this context since creation. */
+int axg_launch_count(const axg_ctx *ctx, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AXGPU_H */

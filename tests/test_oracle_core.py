@@ -1,0 +1,118 @@
+"""CPU checks of the oracle (test infrastructure) against known answers."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import axo
+import axion_grav_gb300 as ag
+
+
+def params(**kw):
+    p = ag.Params()
+    base = dict(ngrid=8, precision=0, gw_mode=0, num_bin=50, degrade_spec=0, flags=7, compat=1,
+                potential=0, n_dw=1, num_bin_grav=25, gw_log_bins=16, dspa=1.0, sigma_cr=1.0,
+                kappa=1.0, tau_cr=1.0, a_now=1.0, width_cr=0.7, thickness_cr=1.0, vev=1.0,
+                ma2_power=2.0, seed=1)
+    base["lambda"] = 1.0
+    base.update(kw)
+    return p.update(**base)
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for Philox4x32-10
+    assert axo.philox((0, 0, 0, 0), (0, 0)) == (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)
+    assert axo.philox((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2) == (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)
+    assert axo.philox((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0)) == (
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)
+
+
+@pytest.mark.parametrize("n", [4, 8, 6, 10])
+def test_fft_matches_numpy(n):
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))
+    np.testing.assert_allclose(axo.fft3d(a, -1), np.fft.fftn(a), atol=1e-12 * n ** 3)
+    np.testing.assert_allclose(axo.fft3d(a, +1), np.fft.ifftn(a) * a.size, atol=1e-12 * n ** 3)
+
+
+def test_det_atan2_accuracy_and_special_cases():
+    rng = np.random.default_rng(0)
+    pts = rng.uniform(-3, 3, (20000, 2))
+    pts = np.concatenate([pts, rng.standard_normal((2000, 2)) * 1e-8, [[1, 1], [-1, 1], [1, -1], [-1, -1]]])
+    for y, x in pts:
+        ref = math.atan2(y, x)
+        got = axo.det_atan2(y, x)
+        assert abs(got - ref) <= 2.5e-16 * abs(ref) + 1e-300
+    assert axo.det_atan2(0.0, 1.0) == 0.0
+    assert axo.det_atan2(0.0, -1.0) == math.pi
+    assert axo.det_atan2(-0.0, -1.0) == -math.pi
+    assert axo.det_atan2(1.0, 0.0) == math.pi / 2
+    assert axo.det_atan2(-1.0, 0.0) == -math.pi / 2
+
+
+def test_det_sincos_accuracy():
+    for x in np.random.default_rng(1).uniform(-50, 50, 20000):
+        s, c = axo.det_sincos(x)
+        assert abs(s - math.sin(x)) < 3e-16 and abs(c - math.cos(x)) < 3e-16
+
+
+def test_potential_scalars():
+    # potential.f90:34-41: m^2(T) = (T^2 - 6)/3
+    assert axo.lib().axo_msquared(0.0) == pytest.approx(-2.0, rel=1e-15)
+    assert axo.lib().axo_msquared(2.449489742783178) == pytest.approx(0.0, abs=1e-15)
+    # potential.f90:62-79: low-T plateau c0 kappa^4, high-T power law
+    k = 0.5
+    thr = k * (6.26) ** (1 / 6.68)
+    assert axo.lib().axo_maxion2(thr * 0.9, k) == pytest.approx(k ** 4)
+    assert axo.lib().axo_maxion2(thr * 2, k) == pytest.approx(6.26 * (k / (thr * 2)) ** 6.68 * k ** 4)
+
+
+def test_get_dtau_matches_formula():
+    p = params(ngrid=64, dspa=0.25, sigma_cr=2.0)
+    dt, n = axo.get_dtau(p, 1.0, 3.0, 0.5)
+    omega = math.sqrt((2 * 3.14159265359 / 0.25) ** 2 + (2.449489742783178 * 3.0 * 2.0) ** 2)
+    assert n == math.ceil(2.0 / (0.5 / omega))
+    assert dt == pytest.approx(2.0 / n, rel=1e-15)
+
+
+def test_free_field_dispersion():
+    """dV = 0 and H -> 0: a lattice plane wave follows the leapfrog dispersion
+    cos(w dt) = 1 - kappa^2 dt^2/2, kappa^2 = (4/dx^2) sum sin^2(k_i dx/2)."""
+    n, dx = 16, 1.0
+    p = params(ngrid=n, dspa=dx, potential=1, vev=1.0, **{"lambda": 0.0})
+    kv = 2 * np.pi * np.array([1, 2, 3]) / (n * dx)
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    phase = (kv[0] * x + kv[1] * y + kv[2] * z) * dx
+    kap2 = (4 / dx ** 2) * np.sum(np.sin(kv * dx / 2) ** 2)
+    dt = 0.1
+    w = math.acos(1 - kap2 * dt * dt / 2) / dt
+    t0 = 1e15  # H = 1/t ~ 0
+    phi = np.exp(1j * phase).astype(np.complex128)
+    # half-step staggered start: phidot at t0+dt/2 for the DKD scheme after the first half drift
+    phid = (-1j * (2 / dt) * math.sin(w * dt / 2) * np.exp(1j * phase)).astype(np.complex128)
+    # DKD of the restatement from a synchronized state: the leapfrog maps
+    # (phi, phid) exactly like the 2x2 rotation of the discrete oscillator
+    nsteps = 20
+    ph, pd = phi.copy(), phid.copy()
+    axo.leapfrog(p, ph, pd, None, None, None, t0, dt, nsteps, True, True)
+    # reference: same DKD on the single mode amplitude
+    a, v = 1.0 + 0j, phid.flat[0] / phi.flat[0]
+    a = a + dt / 2 * v
+    for it in range(nsteps):
+        v = v - dt * kap2 * a
+        a = a + (dt / 2 if it == nsteps - 1 else dt) * v
+    np.testing.assert_allclose(ph, a * phi, rtol=0, atol=1e-9)
+    # amplitude conserved to leapfrog accuracy
+    assert abs(abs(a) - 1) < 0.05
+
+
+def test_gaussian_flat_ic_normalisation():
+    p = params(ngrid=16, dspa=1.0, potential=1, vev=1.0)
+    phi, phid = axo.ic_gaussian_flat(p, kcut=1.0)
+    assert np.mean(np.abs(phi) ** 2) == pytest.approx(1.0, rel=1e-12)
+    assert not np.any(phid)
+    F = np.fft.fftn(phi)
+    kk = np.fft.fftfreq(16) * 2 * np.pi
+    kz, ky, kx = np.meshgrid(kk, kk, kk, indexing="ij")
+    outside = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2) > 1.0 + 1e-9
+    assert np.max(np.abs(F[outside])) < 1e-10 * np.max(np.abs(F))
