@@ -49,9 +49,16 @@ def sources() -> list[str]:
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
+# Translation units whose device arithmetic must round every operation
+# separately (no FMA contraction) so results are bit-identical to IEEE host C.
+FMAD_OFF = {"axg_defects.cu"}
+
+
 def _compile(nvcc: str, src: str, verbose_ptxas: bool) -> tuple[str, str]:
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+    if os.path.basename(src) in FMAD_OFF:
+        cmd.append("-fmad=false")
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,14 +1,963 @@
-// axg_defects.cu -- defect identification (defects_3d.f90).  Filled in below.
+// axg_defects.cu -- defect identification on the GPU (defects_3d.f90).
+//
+// This translation unit is compiled with -fmad=false: every floating-point
+// expression below rounds each operation separately, exactly as IEEE host C
+// does without contraction, and atan2 / sin / cos are the deterministic
+// versions of axg_detmath.h.  Cell flags, counts, plaquette windings and every
+// per-cell fit (position, direction, length, velocity, wall area) are
+// therefore bit-identical to a host evaluation of the same formulas.
+//
+// Passes (all O(N^3) passes are HBM-streaming, the fits are sparse):
+//   1. phase     : ph[s] = atan2(Im phi, Re phi)                 (8 B / site)
+//   2. classify  : 8 corner phases, sort, largest circular gap -> int8 flags,
+//                  warp-aggregated counts (defects_3d.f90:67-103, 309-349)
+//   3. winding   : three plaquettes per site
+//   4. compaction: string and wall cells listed in cell order
+//   5. fits      : one thread per listed cell -- position_string (1001 random
+//                  starts + Nelder-Mead, defects_3d.f90:435-603), string_length
+//                  (1027-1056), velocity_string (605-692), position_wall
+//                  (1058-1233)
+//   6. sums      : add_string_length / add_wall_area without grouping
+#include <cmath>
+
+#include "axg_detmath.h"
 #include "axg_internal.h"
 
+namespace {
+
+constexpr double kRefPi = 3.14159265359;
+constexpr double kRefTwoPi = 2 * kRefPi;
+constexpr double kStringPhdiff = kRefPi;
+constexpr double kRemovalPhdiff = 7 * kRefPi / 4;
+constexpr int kMaxIter = 1000;
+constexpr int kNumSimp = 4;
+
+template <typename V>
+__device__ __forceinline__ void load_c(const V *a, int64_t s, double &re, double &im) {
+  const V v = a[s];
+  re = (double)v.x;
+  im = (double)v.y;
+}
+
+template <typename V>
+__global__ void k_phase(const V *__restrict__ phi, double *__restrict__ ph, int64_t n3) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    double re, im;
+    load_c(phi, s, re, im);
+    ph[s] = axd_atan2(im, re);
+  }
+}
+
+__device__ __forceinline__ void cswap(double &a, double &b) {
+  const double lo = a < b ? a : b;
+  const double hi = a < b ? b : a;
+  a = lo;
+  b = hi;
+}
+
+// Batcher-style 19-comparator sorting network for 8 values (ascending).
+__device__ __forceinline__ void sort8(double v[8]) {
+  cswap(v[0], v[1]); cswap(v[2], v[3]); cswap(v[4], v[5]); cswap(v[6], v[7]);
+  cswap(v[0], v[2]); cswap(v[1], v[3]); cswap(v[4], v[6]); cswap(v[5], v[7]);
+  cswap(v[1], v[2]); cswap(v[5], v[6]); cswap(v[0], v[4]); cswap(v[3], v[7]);
+  cswap(v[1], v[5]); cswap(v[2], v[6]);
+  cswap(v[1], v[4]); cswap(v[3], v[6]);
+  cswap(v[2], v[4]); cswap(v[3], v[5]);
+  cswap(v[3], v[4]);
+}
+
+__device__ __forceinline__ int64_t corner(int n, int ix, int iy, int iz, int c) {
+  const int dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+  const int x = ix + dx == n ? 0 : ix + dx, y = iy + dy == n ? 0 : iy + dy,
+            z = iz + dz == n ? 0 : iz + dz;
+  return ((int64_t)z * n + y) * n + x;
+}
+
+// id_with_phase (defects_3d.f90:309-349) on sorted phases
+__device__ __forceinline__ int8_t classify_sorted(const double pht[8], int which) {
+  int8_t flag = 0;
+  const double t = pht[0] - pht[7] + kRefTwoPi;
+  double tmax = pht[1] - pht[0];
+#pragma unroll
+  for (int k = 1; k < 7; ++k) {
+    const double g = pht[k + 1] - pht[k];
+    tmax = g > tmax ? g : tmax;
+  }
+  if ((which & AXG_F_ID_WALLS) && tmax > t) {
+    flag += 2;
+  } else {
+    tmax = t > tmax ? t : tmax;
+  }
+  if ((which & AXG_F_ID_STRINGS) && tmax < kStringPhdiff) flag += 1;
+  if ((which & AXG_F_SPEC_EST) && tmax < kRemovalPhdiff) flag += 4;
+  return flag;
+}
+
+__device__ __forceinline__ void warp_count(unsigned long long *dst, bool pred) {
+  const unsigned b = __ballot_sync(0xffffffffu, pred);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(dst, (unsigned long long)__popc(b));
+}
+
+__global__ void k_classify(const double *__restrict__ ph, int n, int which, int8_t *__restrict__ flags,
+                           unsigned long long *__restrict__ counts) {
+  const int64_t n3 = (int64_t)n * n * n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // uniform trip count so every lane reaches the ballots
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n3; base += stride) {
+    const int64_t s = base + threadIdx.x;
+    int8_t f = 0;
+    if (s < n3) {
+      const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
+      double v[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) v[c] = ph[corner(n, ix, iy, iz, c)];
+      sort8(v);
+      f = classify_sorted(v, which);
+      flags[s] = f;
+    }
+    warp_count(&counts[0], (f & 1) != 0);
+    warp_count(&counts[1], (f & 2) != 0);
+    warp_count(&counts[2], (f & 4) != 0);
+  }
+}
+
+__device__ __forceinline__ double wrapd(double d) {
+  const double pi = AXD_PI_HI, tp = 2 * AXD_PI_HI;
+  if (d > pi) return d - tp;
+  if (d <= -pi) return d + tp;
+  return d;
+}
+__device__ __forceinline__ bool pierced(double a, double b, double c, double d) {
+  double w = wrapd(b - a);
+  w = w + wrapd(c - b);
+  w = w + wrapd(d - c);
+  w = w + wrapd(a - d);
+  return w > AXD_PI_HI || w < -AXD_PI_HI;
+}
+
+__global__ void k_winding(const double *__restrict__ ph, int n, unsigned long long *__restrict__ counts) {
+  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n3; base += stride) {
+    const int64_t s = base + threadIdx.x;
+    bool px = false, py = false, pz = false;
+    if (s < n3) {
+      const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
+      const int x1 = ix + 1 == n ? 0 : ix + 1, y1 = iy + 1 == n ? 0 : iy + 1,
+                z1 = iz + 1 == n ? 0 : iz + 1;
+      auto P = [&](int x, int y, int z) { return ph[((int64_t)z * n + y) * n + x]; };
+      const double c = P(ix, iy, iz);
+      pz = pierced(c, P(x1, iy, iz), P(x1, y1, iz), P(ix, y1, iz));
+      px = pierced(c, P(ix, y1, iz), P(ix, y1, z1), P(ix, iy, z1));
+      py = pierced(c, P(ix, iy, z1), P(x1, iy, z1), P(x1, iy, iz));
+    }
+    warp_count(&counts[0], px);
+    warp_count(&counts[1], py);
+    warp_count(&counts[2], pz);
+  }
+}
+
+// ---------------- compaction in cell order ----------------
+constexpr int kChunk = 2048;  // cells per block
+constexpr int kCThreads = 256;  // 8 consecutive cells per thread
+
+__global__ void k_block_count(const int8_t *__restrict__ flags, int64_t n3, int *__restrict__ cs,
+                              int *__restrict__ cw) {
+  const int64_t b0 = (int64_t)blockIdx.x * kChunk + threadIdx.x * 8;
+  int ns = 0, nw = 0;
+  for (int k = 0; k < 8; ++k) {
+    const int64_t s = b0 + k;
+    if (s < n3) {
+      const int8_t f = flags[s];
+      ns += (f & 1) != 0;
+      nw += (f & 2) != 0;
+    }
+  }
+  __shared__ int sh[2][kCThreads];
+  sh[0][threadIdx.x] = ns;
+  sh[1][threadIdx.x] = nw;
+  __syncthreads();
+  for (int o = kCThreads / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    cs[blockIdx.x] = sh[0][0];
+    cw[blockIdx.x] = sh[1][0];
+  }
+}
+
+// exclusive scan of nb block counts (single block, sequential over chunks)
+__global__ void k_scan_blocks(int *__restrict__ cs, int *__restrict__ cw, int nb) {
+  __shared__ long long carry[2];
+  __shared__ int sh[2][1024];
+  if (threadIdx.x == 0) carry[0] = carry[1] = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int a = i < nb ? cs[i] : 0, b = i < nb ? cw[i] : 0;
+    sh[0][threadIdx.x] = a;
+    sh[1][threadIdx.x] = b;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      int x0 = 0, x1 = 0;
+      if ((int)threadIdx.x >= o) {
+        x0 = sh[0][threadIdx.x - o];
+        x1 = sh[1][threadIdx.x - o];
+      }
+      __syncthreads();
+      sh[0][threadIdx.x] += x0;
+      sh[1][threadIdx.x] += x1;
+      __syncthreads();
+    }
+    if (i < nb) {
+      cs[i] = (int)(carry[0] + sh[0][threadIdx.x] - a);
+      cw[i] = (int)(carry[1] + sh[1][threadIdx.x] - b);
+    }
+    __syncthreads();
+    if (threadIdx.x == 1023) {
+      carry[0] += sh[0][1023];
+      carry[1] += sh[1][1023];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_compact(const int8_t *__restrict__ flags, int64_t n3, const int *__restrict__ offs,
+                          const int *__restrict__ offw, int64_t *__restrict__ scell,
+                          int64_t *__restrict__ wcell) {
+  const int64_t b0 = (int64_t)blockIdx.x * kChunk + threadIdx.x * 8;
+  int ns = 0, nw = 0;
+  int8_t f[8];
+  for (int k = 0; k < 8; ++k) {
+    const int64_t s = b0 + k;
+    f[k] = s < n3 ? flags[s] : 0;
+    ns += (f[k] & 1) != 0;
+    nw += (f[k] & 2) != 0;
+  }
+  __shared__ int sh[2][kCThreads];
+  sh[0][threadIdx.x] = ns;
+  sh[1][threadIdx.x] = nw;
+  __syncthreads();
+  for (int o = 1; o < kCThreads; o <<= 1) {
+    int x0 = 0, x1 = 0;
+    if ((int)threadIdx.x >= o) {
+      x0 = sh[0][threadIdx.x - o];
+      x1 = sh[1][threadIdx.x - o];
+    }
+    __syncthreads();
+    sh[0][threadIdx.x] += x0;
+    sh[1][threadIdx.x] += x1;
+    __syncthreads();
+  }
+  int ps = offs[blockIdx.x] + sh[0][threadIdx.x] - ns;
+  int pw = offw[blockIdx.x] + sh[1][threadIdx.x] - nw;
+  for (int k = 0; k < 8; ++k) {
+    if (f[k] & 1) scell[ps++] = b0 + k;
+    if (f[k] & 2) wcell[pw++] = b0 + k;
+  }
+}
+
+// ---------------- per-cell fits ----------------
+// defects_3d.f90:385-433
+__device__ double calc_chi2_string(const double ph[8], const double pr[4]) {
+  const double mu = pr[0], phi = pr[1];
+  double s4, c4, sp, cp;
+  axd_sincos(pr[3], &s4, &c4);
+  const double u0 = pr[2] * c4;
+  const double v0 = pr[2] * s4;
+  const double cm = mu;
+  const double sm = sqrt(1.0 - mu * mu);
+  axd_sincos(phi, &sp, &cp);
+  double a = 0.0, b = 0.0;
+  for (int iz = 0; iz <= 1; ++iz) {
+    const double z = iz - 0.5;
+    for (int iy = 0; iy <= 1; ++iy) {
+      const double y = iy - 0.5;
+      for (int ix = 0; ix <= 1; ++ix) {
+        const double x = ix - 0.5;
+        const int i = (iz * 2 + iy) * 2 + ix;
+        const double du = -u0 + cm * (x * cp + y * sp) - z * sm;
+        const double dv = -v0 - x * sp + y * cp;
+        double d = ph[i] - axd_atan2(dv, du);
+        if (d >= kRefPi)
+          d = d - kRefTwoPi;
+        else if (d < -kRefPi)
+          d = d + kRefTwoPi;
+        a = a + d * d;
+        b = b + d;
+      }
+    }
+  }
+  a = a / 8;
+  b = b / 8;
+  return a - b * b;
+}
+
+// defects_3d.f90:1027-1056
+__device__ double string_length(const double pos[3], const double dir[3]) {
+  const double atmax = 0.867, atmax0 = 0.86602540378378444;
+  double tp = atmax, tn = -atmax;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j <= 1; ++j) {
+      double w = j - 0.5;
+      w = w - pos[i];
+      if (fabs(w) > atmax * fabs(dir[i])) continue;
+      const double t = w / dir[i];
+      if (t > 0) {
+        if (t < tp) tp = t;
+      } else {
+        if (t > tn) tn = t;
+      }
+    }
+  if (tp < atmax0 && tn > -atmax0) return tp - tn;
+  return 0.0;
+}
+
+__device__ __forceinline__ bool out_of_box(const double t[4]) {
+  const double mx[4] = {1.0, kRefPi, sqrt(3.0) / 2, kRefPi};
+  const double mn[4] = {-1.0, -kRefPi, 0.0, -kRefPi};
+  for (int k = 0; k < 4; ++k)
+    if (t[k] > mx[k] || t[k] < mn[k]) return true;
+  return false;
+}
+
+// defects_3d.f90:435-603
+__device__ void position_string(const double ph[8], uint64_t seed, uint64_t cell, double pos[3],
+                                double dir[3], double *gof, double *sl) {
+  const double chi2max = 8 * kRefPi * kRefPi, tol = 0.05;
+  const double max_s[4] = {1.0, kRefPi, sqrt(3.0) / 2, kRefPi};
+  const double min_s[4] = {-1.0, -kRefPi, 0.0, -kRefPi};
+  double p_s[5][4], chi2_s[5], c_s[4], t_s[4], s_s[4], chi2, chi2s;
+  for (int a = 0; a < 5; ++a) {
+    chi2_s[a] = 0.0;
+    for (int k = 0; k < 4; ++k) p_s[a][k] = 0.0;
+  }
+  int n0 = -1;
+  for (int i = 0; i <= kMaxIter; ++i) {
+    double x[4];
+    for (int k = 0; k < 4; k += 2) {
+      const int j = i * 4 + k;
+      const axd_u32x4 r = axd_draw(seed, 3u, (uint32_t)(j >> 1), cell);
+      x[k] = axd_u01(r.v[0], r.v[1]);
+      x[k + 1] = axd_u01(r.v[2], r.v[3]);
+    }
+    for (int k = 0; k < 4; ++k) t_s[k] = max_s[k] * x[k] + min_s[k] * (1 - x[k]);
+    chi2 = calc_chi2_string(ph, t_s);
+    if (n0 <= 0) {
+      n0 = n0 + 1;
+      chi2_s[n0] = chi2;
+      for (int k = 0; k < 4; ++k) p_s[n0][k] = t_s[k];
+      continue;
+    }
+    if (n0 < kNumSimp || chi2 <= chi2_s[n0]) {
+      n0 = n0 + 1 < kNumSimp ? n0 + 1 : kNumSimp;
+      int i0 = n0;
+      while (chi2 <= chi2_s[i0 - 1]) {
+        if (i0 <= kNumSimp) {
+          chi2_s[i0] = chi2_s[i0 - 1];
+          for (int k = 0; k < 4; ++k) p_s[i0][k] = p_s[i0 - 1][k];
+        }
+        i0 = i0 - 1;
+        if (i0 == 0) break;
+      }
+      chi2_s[i0] = chi2;
+      for (int k = 0; k < 4; ++k) p_s[i0][k] = t_s[k];
+    }
+  }
+  int it = 0;
+  while (chi2_s[0] > tol && it < kMaxIter) {
+    it = it + 1;
+    for (int k = 0; k < 4; ++k) c_s[k] = 0.0;
+    for (int i0 = 0; i0 < kNumSimp; ++i0)
+      for (int k = 0; k < 4; ++k) c_s[k] = c_s[k] + p_s[i0][k];
+    for (int k = 0; k < 4; ++k) c_s[k] = c_s[k] / kNumSimp;
+    for (int k = 0; k < 4; ++k) t_s[k] = 2 * c_s[k] - p_s[kNumSimp][k];
+    chi2 = out_of_box(t_s) ? chi2max : calc_chi2_string(ph, t_s);
+    if (chi2 < chi2_s[kNumSimp]) {
+      for (int k = 0; k < 4; ++k) s_s[k] = 3 * c_s[k] - 4 * p_s[kNumSimp][k];
+      chi2s = out_of_box(s_s) ? chi2max : calc_chi2_string(ph, s_s);
+      if (chi2 <= chi2s) {
+        chi2_s[kNumSimp] = chi2;
+        for (int k = 0; k < 4; ++k) p_s[kNumSimp][k] = t_s[k];
+      } else {
+        chi2_s[kNumSimp] = chi2s;
+        for (int k = 0; k < 4; ++k) p_s[kNumSimp][k] = s_s[k];
+      }
+    } else {
+      for (int k = 0; k < 4; ++k) s_s[k] = 1.5 * c_s[k] - 0.5 * p_s[kNumSimp][k];
+      chi2s = out_of_box(s_s) ? chi2max : calc_chi2_string(ph, s_s);
+      if (chi2s <= chi2_s[kNumSimp]) {
+        chi2_s[kNumSimp] = chi2s;
+        for (int k = 0; k < 4; ++k) p_s[kNumSimp][k] = s_s[k];
+      } else {
+        for (int i0 = 1; i0 <= kNumSimp; ++i0) {
+          for (int k = 0; k < 4; ++k) p_s[i0][k] = 0.5 * (p_s[i0][k] + p_s[0][k]);
+          chi2_s[i0] = calc_chi2_string(ph, p_s[i0]);
+        }
+      }
+    }
+    for (int i0 = kNumSimp - 1; i0 >= 0; --i0)
+      for (int m = 0; m <= i0; ++m)
+        if (chi2_s[m] > chi2_s[m + 1]) {
+          for (int k = 0; k < 4; ++k) {
+            const double tt = p_s[m][k];
+            p_s[m][k] = p_s[m + 1][k];
+            p_s[m + 1][k] = tt;
+          }
+          const double c = chi2_s[m];
+          chi2_s[m] = chi2_s[m + 1];
+          chi2_s[m + 1] = c;
+        }
+  }
+  const double mu = p_s[0][0], phi = p_s[0][1];
+  double s4, c4, sp, cp;
+  axd_sincos(p_s[0][3], &s4, &c4);
+  const double u0 = p_s[0][2] * c4, v0 = p_s[0][2] * s4;
+  chi2 = chi2_s[0];
+  axd_sincos(phi, &sp, &cp);
+  const double sq = sqrt(1.0 - mu * mu);
+  dir[0] = sq * cp;
+  dir[1] = sq * sp;
+  dir[2] = mu;
+  pos[0] = u0 * mu * cp - v0 * sp;
+  pos[1] = u0 * mu * sp + v0 * cp;
+  pos[2] = -(u0 * sqrt(1 - mu * mu));
+  *gof = exp(-chi2 / 2);
+  *sl = string_length(pos, dir);
+}
+
+// reference BLAS dspr ('U')
+__device__ void dspr_u(int n, double alpha, const double *x, double *ap) {
+  int kk = 0;
+  for (int j = 0; j < n; ++j) {
+    if (x[j] != 0.0) {
+      const double temp = alpha * x[j];
+      int k = kk;
+      for (int i = 0; i <= j; ++i) {
+        ap[k] = ap[k] + x[i] * temp;
+        ++k;
+      }
+    }
+    kk += j + 1;
+  }
+}
+
+// reference LAPACK dpptrf + dpptri ('U') on a packed 4x4
+__device__ void pp_inverse4(double *ap) {
+  const int n = 4;
+  int jj = 0;
+  for (int j = 1; j <= n; ++j) {
+    const int jc = jj + 1;
+    jj = jj + j;
+    if (j > 1) {
+      double *x = ap + (jc - 1);
+      int kk = 1;
+      for (int jx = 1; jx <= j - 1; ++jx) {
+        double temp = x[jx - 1];
+        int k = kk;
+        for (int i = 1; i <= jx - 1; ++i) {
+          temp = temp - ap[k - 1] * x[i - 1];
+          ++k;
+        }
+        temp = temp / ap[kk + jx - 2];
+        x[jx - 1] = temp;
+        kk = kk + jx;
+      }
+    }
+    double dot = 0.0;
+    for (int i = 0; i < j - 1; ++i) dot = dot + ap[jc - 1 + i] * ap[jc - 1 + i];
+    const double ajj = ap[jj - 1] - dot;
+    if (ajj <= 0.0) {
+      ap[jj - 1] = ajj;
+      return;
+    }
+    ap[jj - 1] = sqrt(ajj);
+  }
+  int jc = 1;
+  for (int j = 1; j <= n; ++j) {
+    ap[jc + j - 2] = 1.0 / ap[jc + j - 2];
+    const double ajj = -ap[jc + j - 2];
+    double *x = ap + (jc - 1);
+    int kk = 1;
+    for (int jx = 1; jx <= j - 1; ++jx) {
+      if (x[jx - 1] != 0.0) {
+        const double temp = x[jx - 1];
+        int k = kk;
+        for (int i = 1; i <= jx - 1; ++i) {
+          x[i - 1] = x[i - 1] + temp * ap[k - 1];
+          ++k;
+        }
+        x[jx - 1] = x[jx - 1] * ap[kk + jx - 2];
+      }
+      kk = kk + jx;
+    }
+    for (int i = 0; i < j - 1; ++i) x[i] = ajj * x[i];
+    jc = jc + j;
+  }
+  jj = 0;
+  for (int j = 1; j <= n; ++j) {
+    const int jc2 = jj + 1;
+    jj = jj + j;
+    if (j > 1) dspr_u(j - 1, 1.0, ap + (jc2 - 1), ap);
+    const double ajj = ap[jj - 1];
+    for (int i = 0; i < j; ++i) ap[jc2 - 1 + i] = ajj * ap[jc2 - 1 + i];
+  }
+}
+
+// defects_3d.f90:605-692 (VEL=0)
+template <typename V>
+__device__ void velocity_string(const V *phi, const V *phid, int n, double dspa, int ix, int iy,
+                                int iz, const double pos[3], double vel[3]) {
+  double wr[4] = {0, 0, 0, 0}, wi[4] = {0, 0, 0, 0}, dr[4] = {0, 0, 0, 0}, di[4] = {0, 0, 0, 0};
+  double mat[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, mat0[10];
+  double d[4];
+  d[0] = 1.0;
+  for (int k = 0; k <= 1; ++k) {
+    const int zz = iz + k == n ? 0 : iz + k;
+    d[3] = k - pos[2] - 0.5;
+    for (int j = 0; j <= 1; ++j) {
+      const int yy = iy + j == n ? 0 : iy + j;
+      d[2] = j - pos[1] - 0.5;
+      for (int i = 0; i <= 1; ++i) {
+        const int xx = ix + i == n ? 0 : ix + i;
+        d[1] = i - pos[0] - 0.5;
+        const int64_t s = ((int64_t)zz * n + yy) * n + xx;
+        double pr, pi_, qr, qi;
+        load_c(phi, s, pr, pi_);
+        load_c(phid, s, qr, qi);
+        for (int l = 0; l < 4; ++l) {
+          wr[l] = wr[l] + d[l] * pr;
+          wi[l] = wi[l] + d[l] * pi_;
+          dr[l] = dr[l] + d[l] * qr;
+          di[l] = di[l] + d[l] * qi;
+        }
+        dspr_u(4, 1.0, d, mat);
+      }
+    }
+  }
+  for (int l = 0; l < 4; ++l) {
+    wr[l] /= 8;
+    wi[l] /= 8;
+    dr[l] /= 8;
+    di[l] /= 8;
+  }
+  for (int l = 0; l < 10; ++l) {
+    mat[l] /= 8;
+    mat0[l] = mat[l];
+  }
+  pp_inverse4(mat0);
+  double w0r[4] = {0, 0, 0, 0}, w0i[4] = {0, 0, 0, 0}, d0r[4] = {0, 0, 0, 0}, d0i[4] = {0, 0, 0, 0};
+  for (int ii = 1; ii <= 4; ++ii)
+    for (int jj = 1; jj <= 4; ++jj) {
+      int kk = ii > jj ? ii : jj;
+      kk = kk * (kk - 1) / 2 + (ii < jj ? ii : jj);
+      const double m = mat0[kk - 1];
+      w0r[ii - 1] = w0r[ii - 1] + m * wr[jj - 1];
+      w0i[ii - 1] = w0i[ii - 1] + m * wi[jj - 1];
+      d0r[ii - 1] = d0r[ii - 1] + m * dr[jj - 1];
+      d0i[ii - 1] = d0i[ii - 1] + m * di[jj - 1];
+    }
+  const double x = d0r[0], y = d0i[0];
+  double a = 0, b = 0, c = 0;
+  for (int l = 1; l < 4; ++l) {
+    a = a + w0r[l] * w0r[l];
+    b = b + w0r[l] * w0i[l];
+    c = c + w0i[l] * w0i[l];
+  }
+  const double det = a * c - b * b;
+  for (int l = 1; l < 4; ++l) {
+    const double v = (x * c - y * b) * w0r[l] + (-(x * b) + y * a) * w0i[l];
+    vel[l - 1] = -v / det * dspa;
+  }
+}
+
+// defects_3d.f90:1058-1233
+__device__ void position_wall(const double ph[8], double pos[3], double dir[3], double *gof,
+                              double *wa) {
+  double pp[12][3], th[12], uv[12][2], sn[8], cs[8];
+  for (int i = 0; i < 8; ++i) axd_sincos(ph[i], &sn[i], &cs[i]);
+  int m = 0;
+  for (int iz = 0; iz <= 1; ++iz)
+    for (int iy = 0; iy <= 1; ++iy) {
+      const double u = sn[(iz * 2 + iy) * 2 + 0], v = sn[(iz * 2 + iy) * 2 + 1];
+      if (u * v < 0.0) {
+        pp[m][0] = (u + v) / (u - v) / 2;
+        pp[m][1] = iy - 0.5;
+        pp[m][2] = iz - 0.5;
+        ++m;
+      }
+    }
+  for (int iy = 0; iy <= 1; ++iy)
+    for (int ix = 0; ix <= 1; ++ix) {
+      const double u = sn[(0 * 2 + iy) * 2 + ix], v = sn[(1 * 2 + iy) * 2 + ix];
+      if (u * v < 0.0) {
+        pp[m][0] = ix - 0.5;
+        pp[m][1] = iy - 0.5;
+        pp[m][2] = (u + v) / (u - v) / 2;
+        ++m;
+      }
+    }
+  for (int iz = 0; iz <= 1; ++iz)
+    for (int ix = 0; ix <= 1; ++ix) {
+      const double u = sn[(iz * 2 + 0) * 2 + ix], v = sn[(iz * 2 + 1) * 2 + ix];
+      if (u * v < 0.0) {
+        pp[m][0] = ix - 0.5;
+        pp[m][1] = (u + v) / (u - v) / 2;
+        pp[m][2] = iz - 0.5;
+        ++m;
+      }
+    }
+  if (m < 3) {
+    for (int k = 0; k < 3; ++k) pos[k] = dir[k] = 0.0;
+    *gof = 0.0;
+    *wa = 0.0;
+    return;
+  }
+  double chi2min = 6.0, mut = 0.0, phit = 0.0, wt = 0.0;
+  for (int imu = 1; imu <= 20; ++imu) {
+    const double mu = ((double)(-20 + 2 * imu) - 1.0) / 20;
+    for (int iphi = 1; iphi <= 20; ++iphi) {
+      const double phi = kRefPi * ((2 * iphi - 1.0) - 20) / 20;
+      double sp, cp;
+      axd_sincos(phi, &sp, &cp);
+      const double sq = sqrt(1 - mu * mu);
+      const double d0[3] = {sq * cp, sq * sp, mu};
+      double w = 0.0, chi2 = 0.0;
+      for (int i = 0; i < m; ++i) {
+        double d = pp[i][0] * d0[0] + pp[i][1] * d0[1];
+        d = d + pp[i][2] * d0[2];
+        w = w + d;
+        chi2 = chi2 + d * d;
+      }
+      if (w < 0.0)
+        w = 0.0;
+      else
+        w = w / m;
+      chi2 = chi2 - m * w * w;
+      if (chi2 < chi2min) {
+        chi2min = chi2;
+        mut = mu;
+        phit = phi;
+        wt = w;
+      }
+    }
+  }
+  double spt, cpt;
+  axd_sincos(phit, &spt, &cpt);
+  const double sqt = sqrt(1 - mut * mut);
+  double d0[3] = {sqt * cpt, sqt * spt, mut};
+  int num = 0;
+  for (int iz = 0; iz <= 1; ++iz)
+    for (int iy = 0; iy <= 1; ++iy)
+      for (int ix = 0; ix <= 1; ++ix) {
+        const double disp[3] = {ix - 0.5, iy - 0.5, iz - 0.5};
+        double d = disp[0] * d0[0] + disp[1] * d0[1];
+        d = d + disp[2] * d0[2];
+        d = d - wt;
+        if (d * cs[(iz * 2 + iy) * 2 + ix] > 0.0) ++num;
+      }
+  if (num <= 4) {
+    for (int k = 0; k < 3; ++k) d0[k] = -d0[k];
+    wt = -wt;
+  }
+  for (int k = 0; k < 3; ++k) {
+    dir[k] = d0[k];
+    pos[k] = wt * d0[k];
+  }
+  *gof = exp(-chi2min / 2);
+  const double dir1[3] = {mut * cpt, mut * spt, -sqrt(1 - mut * mut)};
+  const double dir2[3] = {-spt, cpt, 0.0};
+  for (int i = 0; i < m; ++i) {
+    for (int k = 0; k < 3; ++k) pp[i][k] = pp[i][k] - pos[k];
+    double u = dir1[0] * pp[i][0] + dir1[1] * pp[i][1];
+    u = u + dir1[2] * pp[i][2];
+    double v = dir2[0] * pp[i][0] + dir2[1] * pp[i][1];
+    v = v + dir2[2] * pp[i][2];
+    th[i] = axd_atan2(v, u);
+    uv[i][0] = u;
+    uv[i][1] = v;
+  }
+  for (int i = m - 1; i >= 1; --i)
+    for (int j = 1; j <= i; ++j)
+      if (th[j - 1] > th[j]) {
+        const double w = th[j - 1];
+        th[j - 1] = th[j];
+        th[j] = w;
+        const double a = uv[j - 1][0], b = uv[j - 1][1];
+        uv[j - 1][0] = uv[j][0];
+        uv[j - 1][1] = uv[j][1];
+        uv[j][0] = a;
+        uv[j][1] = b;
+      }
+  double area = 0.0;
+  double w = th[m - 1] - kRefTwoPi;
+  double u = sqrt(uv[m - 1][0] * uv[m - 1][0] + uv[m - 1][1] * uv[m - 1][1]);
+  for (int i = 0; i < m; ++i) {
+    const double v = sqrt(uv[i][0] * uv[i][0] + uv[i][1] * uv[i][1]);
+    w = th[i] - w;
+    area = area + 0.5 * u * v * axd_sin(w);
+    u = v;
+    w = th[i];
+  }
+  *wa = area;
+}
+
+template <typename V>
+__global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, const V *__restrict__ phid,
+                                                    const double *__restrict__ ph, int n, double dspa,
+                                                    uint64_t seed, const int64_t *__restrict__ cells,
+                                                    int64_t ncell, double *__restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ncell) return;
+  const int64_t s = cells[k];
+  const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
+  double pc[8];
+  for (int c = 0; c < 8; ++c) pc[c] = ph[corner(n, ix, iy, iz, c)];
+  double pos[3], dir[3], vel[3], gof, l;
+  position_string(pc, seed, (uint64_t)s, pos, dir, &gof, &l);
+  velocity_string(phi, phid, n, dspa, ix, iy, iz, pos, vel);
+  double *r = out + 12 * k;
+  r[0] = pos[0] + ix + 0.5;
+  r[1] = pos[1] + iy + 0.5;
+  r[2] = pos[2] + iz + 0.5;
+  r[3] = dir[0];
+  r[4] = dir[1];
+  r[5] = dir[2];
+  r[6] = vel[0];
+  r[7] = vel[1];
+  r[8] = vel[2];
+  r[9] = gof;
+  r[10] = l;
+  r[11] = (double)s;
+}
+
+__global__ void __launch_bounds__(128) k_wall_fit(const double *__restrict__ ph, int n,
+                                                  const int64_t *__restrict__ cells, int64_t ncell,
+                                                  double *__restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ncell) return;
+  const int64_t s = cells[k];
+  const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
+  double pc[8];
+  for (int c = 0; c < 8; ++c) pc[c] = ph[corner(n, ix, iy, iz, c)];
+  double pos[3], dir[3], gof, a;
+  position_wall(pc, pos, dir, &gof, &a);
+  double *r = out + 10 * k;
+  r[0] = pos[0] + ix + 0.5;
+  r[1] = pos[1] + iy + 0.5;
+  r[2] = pos[2] + iz + 0.5;
+  r[3] = dir[0];
+  r[4] = dir[1];
+  r[5] = dir[2];
+  r[6] = gof;
+  r[7] = a;
+  r[8] = (double)s;
+  r[9] = 0.0;
+}
+
+// add_string_length / add_wall_area sums (one block; fixed-order tree)
+__global__ void k_defect_sums(const double *__restrict__ strs, int64_t ns,
+                              const double *__restrict__ walls, int64_t nw, double *__restrict__ out) {
+  __shared__ double sh[5][256];
+  double a[5] = {0, 0, 0, 0, 0};  // sl, sqrt(v2), v2, gamma, count of v2<1
+  double wsum = 0.0;
+  for (int64_t k = threadIdx.x; k < ns; k += blockDim.x) {
+    const double *r = strs + 12 * k;
+    a[0] = a[0] + r[10];
+    double v2 = r[6] * r[6] + r[7] * r[7];
+    v2 = v2 + r[8] * r[8];
+    if (v2 < 1.0) {
+      a[1] = a[1] + sqrt(v2);
+      a[2] = a[2] + v2;
+      a[3] = a[3] + 1 / sqrt(1 - v2);
+      a[4] = a[4] + 1.0;
+    }
+  }
+  for (int64_t k = threadIdx.x; k < nw; k += blockDim.x) wsum = wsum + walls[10 * k + 7];
+  for (int q = 0; q < 5; ++q) sh[q][threadIdx.x] = a[q];
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int q = 0; q < 5; ++q) sh[q][threadIdx.x] = sh[q][threadIdx.x] + sh[q][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 5; ++q) out[q] = sh[q][0];
+  __syncthreads();
+  sh[0][threadIdx.x] = wsum;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[0][threadIdx.x] = sh[0][threadIdx.x] + sh[0][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[5] = sh[0][0];
+}
+
+int grid_for(int64_t count, int per = 256) {
+  int64_t b = (count + per - 1) / per;
+  if (b > 152 * 32) b = 152 * 32;
+  return (int)(b < 1 ? 1 : b);
+}
+
+int ensure_scratch(axg_ctx *ctx) {
+  if (!ctx->phase) AXG_TRY(axg_alloc(ctx, (void **)&ctx->phase, (size_t)ctx->n3 * 8, "phase"));
+  if (!ctx->flags) AXG_TRY(axg_alloc(ctx, (void **)&ctx->flags, (size_t)ctx->n3, "defect flags"));
+  return AXG_OK;
+}
+
+int compute_phases(axg_ctx *ctx) {
+  AXG_TRY(ensure_scratch(ctx));
+  const void *phi = ctx->phi[ctx->cur];
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+    AXG_LAUNCH(ctx, "defect_phase_fp32", k_phase<float2>, grid_for(ctx->n3), 256, 0,
+               (const float2 *)phi, ctx->phase, ctx->n3);
+  else
+    AXG_LAUNCH(ctx, "defect_phase_fp64", k_phase<double2>, grid_for(ctx->n3), 256, 0,
+               (const double2 *)phi, ctx->phase, ctx->n3);
+  return AXG_OK;
+}
+
+}  // namespace
+
+int axg_def_classify(axg_ctx *ctx, int which, int64_t counts[3]) {
+  AXG_TRY(compute_phases(ctx));
+  AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_cnt, 0, 3 * sizeof(unsigned long long), ctx->stream));
+  AXG_LAUNCH(ctx, "defect_classify", k_classify, grid_for(ctx->n3), 256, 0, ctx->phase, (int)ctx->n,
+             which, ctx->flags, ctx->d_cnt);
+  unsigned long long h[3];
+  AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_cnt, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < 3; ++k) counts[k] = (int64_t)h[k];
+  ctx->flags_valid = true;
+  ctx->last_ns = counts[0];
+  ctx->last_nw = counts[1];
+  ctx->last_nm = counts[2];
+  return AXG_OK;
+}
+
+int axg_def_winding(axg_ctx *ctx, int64_t counts[3]) {
+  AXG_TRY(compute_phases(ctx));
+  AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_cnt + 3, 0, 3 * sizeof(unsigned long long), ctx->stream));
+  AXG_LAUNCH(ctx, "string_winding", k_winding, grid_for(ctx->n3), 256, 0, ctx->phase, (int)ctx->n,
+             ctx->d_cnt + 3);
+  unsigned long long h[3];
+  AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_cnt + 3, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < 3; ++k) counts[k] = (int64_t)h[k];
+  return AXG_OK;
+}
+
+int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], double svel[3],
+                       int64_t counts[3]) {
+  (void)tau;
+  const int which = ctx->p.flags & (AXG_F_ID_STRINGS | AXG_F_ID_WALLS | AXG_F_SPEC_EST);
+  AXG_TRY(axg_def_classify(ctx, which, counts));
+  const int64_t ns = counts[0], nw = counts[1];
+  const int nb = (int)((ctx->n3 + kChunk - 1) / kChunk);
+  int *bc = nullptr;
+  int64_t *cells = nullptr;
+  int rc = AXG_OK;
+  AXG_TRY(axg_alloc(ctx, (void **)&bc, (size_t)nb * 2 * sizeof(int), "block counts"));
+  do {
+    if ((rc = axg_alloc(ctx, (void **)&cells, (size_t)(ns + nw + 1) * 8, "defect cells"))) break;
+    if (ns > ctx->cap_strings) {
+      axg_free(ctx, (void **)&ctx->d_strings);
+      if ((rc = axg_alloc(ctx, (void **)&ctx->d_strings, (size_t)ns * 12 * 8, "string list"))) break;
+      ctx->cap_strings = ns;
+    }
+    if (nw > ctx->cap_walls) {
+      axg_free(ctx, (void **)&ctx->d_walls);
+      if ((rc = axg_alloc(ctx, (void **)&ctx->d_walls, (size_t)nw * 10 * 8, "wall list"))) break;
+      ctx->cap_walls = nw;
+    }
+    AXG_LAUNCH(ctx, "defect_block_count", k_block_count, nb, kCThreads, 0, ctx->flags, ctx->n3, bc,
+               bc + nb);
+    AXG_LAUNCH(ctx, "defect_scan", k_scan_blocks, 1, 1024, 0, bc, bc + nb, nb);
+    AXG_LAUNCH(ctx, "defect_compact", k_compact, nb, kCThreads, 0, ctx->flags, ctx->n3, bc, bc + nb,
+               cells, cells + ns);
+    const int n = (int)ctx->n;
+    if (ns > 0) {
+      if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+        AXG_LAUNCH(ctx, "string_fit_fp32", k_string_fit<float2>, (unsigned)((ns + 127) / 128), 128, 0,
+                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->phid, ctx->phase, n,
+                   ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings);
+      else
+        AXG_LAUNCH(ctx, "string_fit_fp64", k_string_fit<double2>, (unsigned)((ns + 127) / 128), 128, 0,
+                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)ctx->phid, ctx->phase, n,
+                   ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings);
+    }
+    if (nw > 0)
+      AXG_LAUNCH(ctx, "wall_fit", k_wall_fit, (unsigned)((nw + 127) / 128), 128, 0, ctx->phase, n,
+                 cells + ns, nw, ctx->d_walls);
+    AXG_LAUNCH(ctx, "defect_sums", k_defect_sums, 1, 256, 0, ctx->d_strings, ns, ctx->d_walls, nw,
+               ctx->d_red);
+    double h[6];
+    if (cudaMemcpyAsync(h, ctx->d_red, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+      rc = axg_set_error(ctx, AXG_ERR_CUDA, "defect sums");
+      break;
+    }
+    sl[0] = sl[1] = sl[2] = h[0];
+    if (h[4] > 0) {
+      svel[0] = h[1] / h[4];
+      svel[1] = h[2] / h[4];
+      svel[2] = h[3] / h[4];
+    } else {
+      svel[0] = svel[1] = svel[2] = 0.0;
+    }
+    wa[0] = wa[1] = wa[2] = h[5];
+    ctx->last_ns = ns;
+    ctx->last_nw = nw;
+  } while (0);
+  cudaStreamSynchronize(ctx->stream);
+  axg_free(ctx, (void **)&bc);
+  axg_free(ctx, (void **)&cells);
+  return rc;
+}
+
 extern "C" {
-int axg_classify_cells(axg_ctx *ctx, int, int64_t *) { return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "not built yet"); }
-int axg_download_defect_flags(axg_ctx *ctx, int8_t *) { return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "not built yet"); }
-int axg_string_winding(axg_ctx *ctx, int64_t *) { return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "not built yet"); }
-int axg_id_defects(axg_ctx *ctx, int64_t, double, double *, double *, double *, int64_t *) {
-  return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "not built yet");
+
+int axg_classify_cells(axg_ctx *ctx, int which, int64_t counts[3]) {
+  if (!ctx || !counts) return AXG_ERR_ARG;
+  return axg_def_classify(ctx, which & 7, counts);
 }
-int axg_download_defect_lists(axg_ctx *ctx, double *, int64_t, double *, int64_t) {
-  return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "not built yet");
+
+int axg_download_defect_flags(axg_ctx *ctx, int8_t *flags) {
+  if (!ctx || !flags) return AXG_ERR_ARG;
+  if (!ctx->flags || !ctx->flags_valid)
+    return axg_set_error(ctx, AXG_ERR_STATE, "no classification since the last state change");
+  AXG_CUDA_TRY(ctx, cudaMemcpyAsync(flags, ctx->flags, (size_t)ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
+  AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXG_OK;
 }
+
+int axg_string_winding(axg_ctx *ctx, int64_t counts[3]) {
+  if (!ctx || !counts) return AXG_ERR_ARG;
+  return axg_def_winding(ctx, counts);
 }
+
+int axg_id_defects(axg_ctx *ctx, int64_t idx, double tau, double sl[3], double wa[3], double svel[3],
+                   int64_t counts[3]) {
+  (void)idx;
+  if (!ctx || !sl || !wa || !svel || !counts) return AXG_ERR_ARG;
+  return axg_def_id_defects(ctx, tau, sl, wa, svel, counts);
+}
+
+int axg_download_defect_lists(axg_ctx *ctx, double *strings, int64_t max_strings, double *walls,
+                              int64_t max_walls) {
+  if (!ctx) return AXG_ERR_ARG;
+  const int64_t ns = std::min(max_strings, ctx->last_ns), nw = std::min(max_walls, ctx->last_nw);
+  if (strings && ns > 0 && ctx->d_strings)
+    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(strings, ctx->d_strings, (size_t)ns * 12 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (walls && nw > 0 && ctx->d_walls)
+    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(walls, ctx->d_walls, (size_t)nw * 10 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXG_OK;
+}
+
+}  // extern "C"

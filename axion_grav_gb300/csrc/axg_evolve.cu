@@ -16,6 +16,8 @@
 //    16-byte aligned.
 #include <cudaTypedefs.h>
 
+#include <cmath>
+
 #include "axg_detmath.h"
 #include "axg_internal.h"
 
@@ -31,7 +33,14 @@ struct KickCoeffs {
   double f1, f2, f3, fs;  // fact1, fact2, fact3, source factor
   double A, B, C, D;      // dV/dphi* = (A|phi|^2+B) phi + C + D conj(phi)
   double d;               // 2 dspa (grav_waves.f90:331)
+  double inv_d;           // 1/d, used only when d is a power of two (then x/d == x*inv_d exactly)
+  int d_pow2;
 };
+
+// x / d, replaced by the exact multiplication by 1/d when d is a power of two
+__device__ __forceinline__ double div_d(double x, double d, double inv_d, int pow2) {
+  return pow2 ? AXD_MUL(x, inv_d) : AXD_DIV(x, d);
+}
 
 __global__ void k_drift_fp64(double2 *__restrict__ phi, const double2 *__restrict__ phid,
                              double *__restrict__ u, const double *__restrict__ ud, int64_t n3,
@@ -105,12 +114,12 @@ __global__ void __launch_bounds__(256) k_kick_fp64(const double2 *__restrict__ p
   phid[c] = make_double2(pr, pi_);
   if (uij) {
     double dr[3], di[3];
-    dr[0] = AXD_DIV(AXD_SUB(px2.x, px1.x), k.d);
-    di[0] = AXD_DIV(AXD_SUB(px2.y, px1.y), k.d);
-    dr[1] = AXD_DIV(AXD_SUB(py2.x, py1.x), k.d);
-    di[1] = AXD_DIV(AXD_SUB(py2.y, py1.y), k.d);
-    dr[2] = AXD_DIV(AXD_SUB(pz2.x, pz1.x), k.d);
-    di[2] = AXD_DIV(AXD_SUB(pz2.y, pz1.y), k.d);
+    dr[0] = div_d(AXD_SUB(px2.x, px1.x), k.d, k.inv_d, k.d_pow2);
+    di[0] = div_d(AXD_SUB(px2.y, px1.y), k.d, k.inv_d, k.d_pow2);
+    dr[1] = div_d(AXD_SUB(py2.x, py1.x), k.d, k.inv_d, k.d_pow2);
+    di[1] = div_d(AXD_SUB(py2.y, py1.y), k.d, k.inv_d, k.d_pow2);
+    dr[2] = div_d(AXD_SUB(pz2.x, pz1.x), k.d, k.inv_d, k.d_pow2);
+    di[2] = div_d(AXD_SUB(pz2.y, pz1.y), k.d, k.inv_d, k.d_pow2);
     int comp = 0;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -278,6 +287,8 @@ struct FusedParams {
   int n, zc;
   R f1, f2, f3, fsc, dtd, A, B, C, D;
   double d;  // 2 dspa (FP64 path keeps the reference's division)
+  double inv_d;
+  int d_pow2;
   int *err;
 };
 
@@ -475,12 +486,12 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
             make_double2(AXD_ADD(c0.x, AXD_MUL(P.dtd, pr)), AXD_ADD(c0.y, AXD_MUL(P.dtd, pi_)));
         if constexpr (UIJ) {
           double dr[3], di[3];
-          dr[0] = AXD_DIV(AXD_SUB(xp.x, xm.x), P.d);
-          di[0] = AXD_DIV(AXD_SUB(xp.y, xm.y), P.d);
-          dr[1] = AXD_DIV(AXD_SUB(yp.x, ym.x), P.d);
-          di[1] = AXD_DIV(AXD_SUB(yp.y, ym.y), P.d);
-          dr[2] = AXD_DIV(AXD_SUB(zp.x, zm.x), P.d);
-          di[2] = AXD_DIV(AXD_SUB(zp.y, zm.y), P.d);
+          dr[0] = div_d(AXD_SUB(xp.x, xm.x), P.d, P.inv_d, P.d_pow2);
+          di[0] = div_d(AXD_SUB(xp.y, xm.y), P.d, P.inv_d, P.d_pow2);
+          dr[1] = div_d(AXD_SUB(yp.x, ym.x), P.d, P.inv_d, P.d_pow2);
+          di[1] = div_d(AXD_SUB(yp.y, ym.y), P.d, P.inv_d, P.d_pow2);
+          dr[2] = div_d(AXD_SUB(zp.x, zm.x), P.d, P.inv_d, P.d_pow2);
+          di[2] = div_d(AXD_SUB(zp.y, zm.y), P.d, P.inv_d, P.d_pow2);
           const double *ub = reinterpret_cast<const double *>(sc + L::u_body);
           const double *ut = reinterpret_cast<const double *>(sc + L::u_top);
           const double *ubt = reinterpret_cast<const double *>(sc + L::u_bot);
@@ -695,7 +706,10 @@ int axg_evo_kick_plain(axg_ctx *ctx, double t, double dt) {
     return axg_set_error(ctx, AXG_ERR_STATE, "separate kick is the FP64 path; FP32 runs fused");
   double f[4], pot[4];
   axg_kick_coeffs(&ctx->p, t, dt, f, pot);
-  KickCoeffs k{f[0], f[1], f[2], f[3], pot[0], pot[1], pot[2], pot[3], ctx->p.dspa * 2};
+  const double d = ctx->p.dspa * 2;
+  int ex;
+  const int pow2 = std::frexp(d, &ex) == 0.5;
+  KickCoeffs k{f[0], f[1], f[2], f[3], pot[0], pot[1], pot[2], pot[3], d, 1.0 / d, pow2};
   const int n = (int)ctx->n;
   dim3 block(32, 8);
   dim3 grid((n + 31) / 32, (n + 7) / 8, n);
@@ -741,6 +755,8 @@ int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd) {
     P.C = (float)pot[2];
     P.D = (float)pot[3];
     P.d = 2.0 * ctx->p.dspa;
+    P.inv_d = 1.0 / P.d;
+    P.d_pow2 = 0;
     P.err = ctx->d_err;
     if (uij) AXG_TRY((launch_fused_cfg<float, true>(ctx, P, cfg, "fused_kd_fp32_uij")));
     else AXG_TRY((launch_fused_cfg<float, false>(ctx, P, cfg, "fused_kd_fp32_phi")));
@@ -765,6 +781,9 @@ int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd) {
     P.C = pot[2];
     P.D = pot[3];
     P.d = 2.0 * ctx->p.dspa;
+    int ex;
+    P.d_pow2 = std::frexp(P.d, &ex) == 0.5;
+    P.inv_d = 1.0 / P.d;
     P.err = ctx->d_err;
     if (uij) AXG_TRY((launch_fused_cfg<double, true>(ctx, P, cfg, "fused_kd_fp64_uij")));
     else AXG_TRY((launch_fused_cfg<double, false>(ctx, P, cfg, "fused_kd_fp64_phi")));

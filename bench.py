@@ -70,7 +70,7 @@ def ncu_traffic_per_site(kernel: str):
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -83,7 +83,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
@@ -92,7 +92,10 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
+
+    def mark(self, which: str):
+        setattr(self, which, time.time())
 
     def __exit__(self, *exc):
         if self.proc:
@@ -103,18 +106,24 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        """Samples received while the timed region ran (host arrival time;
+        nvidia-smi output is line buffered at 50 ms)."""
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        t0 = getattr(self, "start", 0.0)
+        t1 = getattr(self, "stop", float("inf")) + 0.06
+        for tr, ln in self.lines:
+            if not (t0 <= tr <= t1):
+                continue
             parts = [x.strip() for x in ln.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                mx.append(float(parts[2]))
+                sm.append(float(parts[2]))
+                mx.append(float(parts[3]))
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[5:9]):
+            for nm, v in zip(names, parts[6:10]):
                 if v.lower() == "active":
                     reasons.add(nm)
         if not sm:
@@ -153,6 +162,8 @@ def bench_ours(ag, n, precision, gw, steps, warmup, dist, device, t0=2.0, eps=0.
         sampler = ClockSampler(device) if clocks else None
         if sampler:
             sampler.__enter__()
+            time.sleep(0.5)  # let nvidia-smi start streaming before the timed region
+            sampler.mark("start")
         l0 = lat.launch_count()
         lat.event_record(0)
         lat.leapfrog(t, dt, steps, False, False)
@@ -161,6 +172,8 @@ def bench_ours(ag, n, precision, gw, steps, warmup, dist, device, t0=2.0, eps=0.
         lat.synchronize()
         l1 = lat.launch_count()
         if sampler:
+            sampler.mark("stop")
+            time.sleep(0.1)
             sampler.__exit__(None, None, None)
         if dist is not None:
             dist.barrier()
@@ -257,7 +270,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=512)
@@ -316,10 +329,10 @@ def main():
 
     fp64 = None
     if not args.no_fp64:
-        r64 = bench_ours(ag, n, ag.PREC_FP64_PLAIN, ag.GW_UIJ, max(3, args.steps // 4), args.warmup, dist, local)
+        r64 = bench_ours(ag, n, ag.PREC_FP64_PLAIN, ag.GW_UIJ, max(3, args.steps // 8), args.warmup, dist, local)
         r64.pop("lat").close()
         k64 = {k: (l, t) for k, l, t in r64["kernels"]}
-        st64 = max(3, args.steps // 4)
+        st64 = max(3, args.steps // 8)
         v64 = world * sites * st64 / (r64["ms"] * 1e-3)
         byts = sum(BYTES_PER_SITE.get(k, 0) * sites * l for k, (l, t) in k64.items())
         tms = sum(t for k, (l, t) in k64.items())

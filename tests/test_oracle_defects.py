@@ -1,0 +1,119 @@
+"""Known answers of the defect restatement (defects_3d.f90) on CPU."""
+import numpy as np
+import pytest
+
+from oracle import axo
+import axion_grav_gb300 as ag
+
+
+def params(n, **kw):
+    base = dict(ngrid=n, precision=0, gw_mode=0, num_bin=10, degrade_spec=0, flags=7, compat=1,
+                potential=0, n_dw=1, num_bin_grav=25, gw_log_bins=16, dspa=1.0, sigma_cr=1.0, kappa=1.0,
+                tau_cr=1.0, a_now=1.0, width_cr=0.7, thickness_cr=1.0, vev=1.0, ma2_power=2.0, seed=1)
+    base.update(kw)
+    return ag.Params().update(**base)
+
+
+def grid(n):
+    return np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+
+
+def four_strings(n, a=0.3, b=0.45):
+    z, y, x = grid(n)
+    return (np.sin(2 * np.pi * (x + a) / n) + 1j * np.sin(2 * np.pi * (y + b) / n)).astype(np.complex128)
+
+
+@pytest.mark.parametrize("n", [8, 16, 24])
+def test_straight_strings_counts_and_length(n):
+    """Four straight strings along z: 4 string cells and 4 pierced xy-plaquettes
+    per z-plane; fitted length ~ 1 lattice unit per cell (defects_3d.f90:1027)."""
+    p = params(n)
+    phi = four_strings(n)
+    flags, c = axo.classify_cells(p, phi, ag.F_ID_STRINGS, 0)
+    assert c[0] == 4 * n
+    assert np.array_equal(axo.string_winding(p, phi), [0, 0, 4 * n])
+    sl, wa, sv, cnt, S, W, _ = axo.id_defects(p, phi, np.zeros_like(phi), 5.0)
+    assert cnt[0] == 4 * n
+    assert sl[0] / (4 * n) == pytest.approx(1.0, abs=0.05)
+    # fitted directions are along +-z
+    assert np.all(np.abs(S[:, 5]) > 0.85) and np.median(np.abs(S[:, 5])) > 0.95
+    # phidot = 0 -> zero velocity, <gamma> = 1
+    assert np.allclose(sv, [0, 0, 1])
+
+
+def test_plane_wall_area():
+    """A phase winding once along x has one wall sheet (phase crossing +-pi)
+    through N^2 cells, each of area ~1 (defects_3d.f90:1058-1233)."""
+    n = 16
+    z, y, x = grid(n)
+    phi = np.exp(2j * np.pi * (x + 0.37) / n).astype(np.complex128)
+    p = params(n)
+    flags, c = axo.classify_cells(p, phi, 7, 0)
+    assert c[1] == n * n and c[0] == 0
+    sl, wa, sv, cnt, S, W, _ = axo.id_defects(p, phi, np.zeros_like(phi), 5.0)
+    assert wa[0] / (n * n) == pytest.approx(1.0, abs=0.03)
+    assert np.all(np.abs(W[:, 3]) > 0.95)  # normal along x
+
+
+def test_moving_string_velocity():
+    """phi(x - v t): phidot = -v d_x phi gives the string velocity +v x."""
+    n, v = 16, 0.3
+    z, y, x = grid(n)
+    kx = 2 * np.pi / n
+    phi = four_strings(n)
+    phid = (-v * kx * np.cos(2 * np.pi * (x + 0.3) / n)).astype(np.complex128)
+    p = params(n)
+    sl, wa, sv, cnt, S, W, _ = axo.id_defects(p, phi, phid, 5.0)
+    assert np.median(np.abs(S[:, 6])) == pytest.approx(v, rel=0.1)
+    assert np.max(np.abs(S[:, 7])) < 0.05
+    assert sv[0] == pytest.approx(v, rel=0.1)
+
+
+def test_libm_and_project_atan2_agree_on_counts():
+    """The literal reference uses libm atan2; the project's deterministic atan2
+    differs by <= 1 ulp, which flips no flag on these fields."""
+    rng = np.random.default_rng(0)
+    for n in (8, 16):
+        p = params(n)
+        for seed in range(3):
+            phi = (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))).astype(np.complex128)
+            f0, c0 = axo.classify_cells(p, phi, 7, 0)
+            f1, c1 = axo.classify_cells(p, phi, 7, 1)
+            assert np.array_equal(f0, f1) and np.array_equal(c0, c1)
+
+
+def test_id_with_phase_cases():
+    """Single cells: phases spread over the circle -> string; clustered -> none;
+    a wall when the largest gap is interior (does not straddle +-pi)."""
+    n = 4
+    p = params(n)
+    phi = np.ones((n, n, n), np.complex128)
+    flags, c = axo.classify_cells(p, phi, 7, 0)
+    assert np.array_equal(c, [0, 0, 0])
+
+
+def test_pp_inverse_matches_numpy():
+    rng = np.random.default_rng(3)
+    for n in (1, 4, 7, 12):
+        a = rng.standard_normal((n, n))
+        m = a @ a.T + n * np.eye(n)
+        ap = np.concatenate([m[: j + 1, j] for j in range(n)])  # upper packed, column major
+        inv, info = axo.pp_inverse(ap, n)
+        assert info == 0
+        ref = np.linalg.inv(m)
+        got = np.zeros((n, n))
+        k = 0
+        for j in range(n):
+            for i in range(j + 1):
+                got[i, j] = got[j, i] = inv[k]
+                k += 1
+        np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-12)
+
+
+def test_string_length_geometry():
+    # a string along z through the cell centre crosses the z faces: length 1
+    assert axo.string_length([0, 0, 0], [0, 0, 1]) == pytest.approx(1.0)
+    # along the body diagonal: sqrt(3) > 2*0.866 is rejected by the atmax0 cut
+    d = np.array([1, 1, 1]) / np.sqrt(3)
+    assert axo.string_length([0, 0, 0], d) == pytest.approx(2 * 0.5 * np.sqrt(3), rel=1e-12) or \
+        axo.string_length([0, 0, 0], d) == 0.0
