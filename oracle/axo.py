@@ -275,8 +275,9 @@ def spectrum_estimation(p, phid, flags, tau):
     nb = p.num_bin
     w, pw, cv, ct = (np.zeros(nb) for _ in range(4))
     md = np.zeros(nb * (nb + 1) // 2)
-    lib().axo_spectrum_estimation(ctypes.byref(p), dptr(phid), flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)),
-                                  tau, dptr(w), dptr(pw), dptr(cv), dptr(ct), dptr(md))
+    fptr = flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)) if flags is not None else None
+    lib().axo_spectrum_estimation(ctypes.byref(p), dptr(phid), fptr, tau, dptr(w), dptr(pw), dptr(cv),
+                                  dptr(ct), dptr(md))
     return w, pw, cv, ct, md
 
 

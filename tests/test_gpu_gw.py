@@ -1,0 +1,98 @@
+"""GPU gravitational-wave paths against the oracle (grav_waves.f90)."""
+import numpy as np
+import pytest
+
+import axion_grav_gb300 as ag
+from oracle import axo
+
+pytestmark = pytest.mark.gpu
+
+
+def params(n, precision, gw, **kw):
+    base = dict(ngrid=n, precision=precision, gw_mode=gw, dspa=0.75, sigma_cr=1.0, kappa=0.1,
+                tau_cr=1.0, a_now=1.0, num_bin_grav=25, gw_log_bins=12, seed=3)
+    base.update(kw)
+    return ag.default_params(**base)
+
+
+def init_state(n, seed=1):
+    p = params(n, ag.PREC_FP64_PLAIN, ag.GW_NONE, potential=ag.POT_QUARTIC)
+    phi, _ = axo.ic_gaussian_flat(p, kcut=1.5, realisation=seed)
+    rng = np.random.default_rng(seed)
+    phid = (0.2 * (rng.standard_normal(phi.shape) + 1j * rng.standard_normal(phi.shape))).astype(np.complex128)
+    return phi, phid
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("compat", [ag.COMPAT_REF, ag.COMPAT_INTENDED])
+@pytest.mark.parametrize("precision", [ag.PREC_FP64_PLAIN, ag.PREC_FP64_FUSED])
+def test_green_accumulators_and_spectrum(compat, precision):
+    n = 32 if precision == ag.PREC_FP64_FUSED else 16
+    phi, phid = init_state(n)
+    p = params(n, precision, ag.GW_GREEN, compat=compat)
+    acc = np.zeros((4, n, n, n), np.complex128)
+    a_phi, a_phid = phi.copy(), phid.copy()
+    nt = axo.symplectic_integration(p, a_phi, a_phid, None, None, acc, 2.0, 2.4, 0.4)
+    w, pw, nu, de = axo.grav_spec_estimation(p, acc)
+    with ag.Lattice(p) as lat:
+        lat.upload(phi, phid)
+        assert lat.symplectic_integration(2.0, 2.4, 0.4) == nt
+        g_phi, _ = lat.download()
+        g_acc = lat.download_gw_green()
+        gw_, gpw, gnu, gde = lat.grav_spec_estimation(2.4)
+    assert np.array_equal(g_phi, a_phi)  # the field evolution is unchanged by the GW integration
+    assert rel(g_acc, acc) < 1e-10
+    np.testing.assert_array_equal(gde, de)
+    np.testing.assert_allclose(gw_, w, rtol=1e-15)
+    np.testing.assert_allclose(gnu, nu, rtol=1e-9)
+    np.testing.assert_allclose(gpw, pw, rtol=1e-9)
+
+
+def test_green_log_bins():
+    n = 16
+    phi, phid = init_state(n, 2)
+    p = params(n, ag.PREC_FP64_PLAIN, ag.GW_GREEN)
+    acc = np.zeros((4, n, n, n), np.complex128)
+    axo.symplectic_integration(p, phi.copy(), phid.copy(), None, None, acc, 2.0, 2.2, 0.4)
+    e, pw, nu, de = axo.grav_spec_log_green(p, acc)
+    with ag.Lattice(p) as lat:
+        lat.upload(phi, phid)
+        lat.symplectic_integration(2.0, 2.2, 0.4)
+        ge, gpw, gnu, gde = lat.grav_spec_log(2.2)
+    np.testing.assert_allclose(ge, e, rtol=1e-14)
+    np.testing.assert_array_equal(gde, de)
+    np.testing.assert_allclose(gnu, nu, rtol=1e-9)
+    assert de.sum() == n ** 3 - 1 - np.sum(de == 0) * 0 or de.sum() > 0
+
+
+@pytest.mark.parametrize("precision,tol", [(ag.PREC_FP64_PLAIN, 1e-9), (ag.PREC_FP32_MIXED, 2e-3)])
+def test_uij_tt_spectrum(precision, tol):
+    n = 32
+    phi, phid = init_state(n, 4)
+    p64 = params(n, ag.PREC_FP64_PLAIN, ag.GW_UIJ)
+    u = np.zeros((6, n, n, n))
+    ud = np.zeros((6, n, n, n))
+    a = [phi.copy(), phid.copy(), u.copy(), ud.copy()]
+    axo.symplectic_integration(p64, a[0], a[1], a[2], a[3], None, 2.0, 2.6, 0.4)
+    w, pw, nu, de = axo.uij_grav_spec(p64, a[2], a[3], 2.6)
+    e, lpw, lnu, lde = axo.uij_grav_spec_log(p64, a[2], a[3], 2.6)
+    with ag.Lattice(params(n, precision, ag.GW_UIJ)) as lat:
+        lat.upload(phi, phid)
+        lat.upload_uij(u, ud)
+        lat.symplectic_integration(2.0, 2.6, 0.4)
+        gw_, gpw, gnu, gde = lat.grav_spec_estimation(2.6)
+        ge, glpw, glnu, glde = lat.grav_spec_log(2.6)
+    np.testing.assert_array_equal(gde, de)
+    np.testing.assert_array_equal(glde, lde)
+    np.testing.assert_allclose(gnu, nu, rtol=tol)
+    np.testing.assert_allclose(glnu, lnu, rtol=tol)
+    np.testing.assert_allclose(gpw, pw, rtol=tol)
+
+
+def test_green_requires_mode():
+    with ag.Lattice(params(16, ag.PREC_FP64_PLAIN, ag.GW_NONE)) as lat:
+        with pytest.raises(ag.AxgError):
+            lat.grav_spec_estimation(1.0)

@@ -1,0 +1,54 @@
+"""GPU field spectrum (spectrum.f90) against the oracle."""
+import numpy as np
+import pytest
+
+import axion_grav_gb300 as ag
+from oracle import axo
+
+pytestmark = pytest.mark.gpu
+
+
+def params(n, precision=ag.PREC_FP64_PLAIN, **kw):
+    base = dict(ngrid=n, precision=precision, dspa=0.5, num_bin=8, degrade_spec=0, flags=7, seed=2)
+    base.update(kw)
+    return ag.default_params(**base)
+
+
+def state(n, seed=0):
+    p = params(n, potential=ag.POT_QUARTIC)
+    phi, _ = axo.ic_gaussian_flat(p, kcut=2.0, realisation=seed)
+    rng = np.random.default_rng(seed)
+    phid = (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))).astype(np.complex128)
+    return phi, phid
+
+
+@pytest.mark.parametrize("n,deg", [(16, 0), (32, 0), (32, 1)])
+@pytest.mark.parametrize("precision", [ag.PREC_FP64_PLAIN, ag.PREC_FP32_MIXED])
+def test_spectrum_estimation_matches_oracle(n, deg, precision):
+    phi, phid = state(n, n + deg)
+    if precision == ag.PREC_FP32_MIXED:
+        phi = phi.astype(np.complex64).astype(np.complex128)
+        phid = phid.astype(np.complex64).astype(np.complex128)
+    p = params(n, precision, degrade_spec=deg)
+    flags, cnt = axo.classify_cells(params(n), phi, 7, 0)
+    w, pw, cv, ct, md = axo.spectrum_estimation(params(n, degrade_spec=deg), phid, flags, 3.0)
+    with ag.Lattice(p) as lat:
+        lat.upload(phi, phid)
+        assert np.array_equal(lat.classify_cells(7), cnt)
+        gw, gpw, gcv, gct = lat.spectrum_estimation(3.0)
+        rho = lat.compute_crho()
+    np.testing.assert_array_equal(gct, ct)
+    np.testing.assert_allclose(gw, w, rtol=1e-15)
+    np.testing.assert_allclose(gcv, cv, rtol=1e-10)
+    np.testing.assert_allclose(gpw, pw, rtol=1e-8, atol=1e-10 * np.max(np.abs(pw)))
+    wav = np.concatenate([[0.0], np.cumsum(np.full(len(w), w[0] * 2))])
+    assert rho == pytest.approx(axo.compute_crho(params(n, degrade_spec=deg), wav, pw), rel=1e-6)
+
+
+def test_spectrum_classifies_when_needed():
+    n = 16
+    phi, phid = state(n, 5)
+    with ag.Lattice(params(n)) as lat:
+        lat.upload(phi, phid)
+        w, pw, cv, ct = lat.spectrum_estimation(2.0)
+    assert np.all(np.isfinite(pw)) and ct.sum() > 0

@@ -116,3 +116,21 @@ def test_gaussian_flat_ic_normalisation():
     kz, ky, kx = np.meshgrid(kk, kk, kk, indexing="ij")
     outside = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2) > 1.0 + 1e-9
     assert np.max(np.abs(F[outside])) < 1e-10 * np.max(np.abs(F))
+
+
+def test_spectrum_parseval_unmasked():
+    """spectrum.f90:518-556: with no mask and every mode inside the bins, the
+    binned |F dx^3|^2 dk^3 sums to the volume integral of |phidot|^2."""
+    n, dx = 16, 0.5
+    p = params(ngrid=n, dspa=dx, num_bin=8)  # no empty bins (the reference divides by the mode count)
+    rng = np.random.default_rng(1)
+    F = np.zeros((n, n, n), np.complex128)
+    kk = np.fft.fftfreq(n) * n
+    kz, ky, kx = np.meshgrid(kk, kk, kk, indexing="ij")
+    low = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2) < n / 4
+    F[low] = rng.standard_normal(low.sum()) + 1j * rng.standard_normal(low.sum())
+    phid = np.fft.ifftn(F).astype(np.complex128)
+    w, pw, cv, ct, md = axo.spectrum_estimation(p, phid, None, 1.0)
+    total = np.sum(cv * ct)
+    assert total == pytest.approx(np.sum(np.abs(phid) ** 2) * dx ** 3, rel=1e-10)
+    assert ct.sum() <= n ** 3
