@@ -31,6 +31,7 @@ __all__ = [
     "PREC_FP64_PLAIN", "PREC_FP64_FUSED", "PREC_FP32_MIXED", "GW_NONE", "GW_GREEN", "GW_UIJ",
     "F_ID_STRINGS", "F_ID_WALLS", "F_SPEC_EST", "F_GRAV_SPEC", "F_INITIAL_LOOP",
     "POT_REFERENCE", "POT_QUARTIC", "COMPAT_INTENDED", "COMPAT_REF", "EXPORTED_SYMBOLS",
+    "field_moments_noalloc",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -95,6 +96,7 @@ EXPORTED_SYMBOLS = (
     "axg_read_chk", "axg_write_param_chk", "axg_read_param_chk", "axg_synchronize",
     "axg_event_record", "axg_event_elapsed", "axg_set_kernel_timing", "axg_kernel_timing",
     "axg_launch_count", "axg_tile_count", "axg_tile_info", "axg_set_tile", "axg_autotune",
+    "axg_field_moments_noalloc",
 )
 
 _lib = None
@@ -167,6 +169,8 @@ def load_library():
                           ctypes.c_int),
         "axg_set_tile": ([c_ctx, ctypes.c_int], ctypes.c_int),
         "axg_autotune": ([c_ctx, ctypes.c_int, P(ctypes.c_int), dp], ctypes.c_int),
+        "axg_field_moments_noalloc": ([P(Params), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, dp,
+                                       ctypes.c_void_p], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -180,6 +184,21 @@ def default_params(**kw) -> Params:
     p = Params()
     load_library().axg_params_default(ctypes.byref(p))
     return p.update(**kw)
+
+
+def field_moments_noalloc(params: Params, d_phi: int, d_phidot: int, tau: float,
+                          stream: Optional[int] = None) -> np.ndarray:
+    """axg_field_moments_noalloc: volume moments of caller-owned complex128
+    device arrays (raw device addresses) without any device allocation, for
+    callers that cannot allocate device memory; ngrid <= 2048."""
+    lib = load_library()
+    out = np.zeros(4)
+    rc = lib.axg_field_moments_noalloc(ctypes.byref(params), ctypes.c_void_p(d_phi), ctypes.c_void_p(d_phidot),
+                                       tau, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       ctypes.c_void_p(stream) if stream else None)
+    if rc != 0:
+        raise AxgError(rc, lib.axg_last_error(None).decode())
+    return out
 
 
 def _dptr(a: Optional[np.ndarray]):

@@ -255,6 +255,27 @@ int axg_kernel_timing(axg_ctx *ctx, int i, char *name, int64_t name_len, int64_t
 /* Number of kernels launched on this context since creation. */
 int axg_launch_count(const axg_ctx *ctx, int64_t *launches);
 
+/* ------------------------------------------------------------------ */
+/* allocation-free diagnostics                                          */
+/* ------------------------------------------------------------------ */
+/* No counterpart in the reference.  The volume moments of axg_field_moments
+ * for fields the caller already holds on the device, for callers that cannot
+ * allocate device memory at that point (their device memory is owned by their
+ * own allocator or pool, or a cudaMalloc there would stall work they have
+ * queued).  d_phi and d_phidot are complex128 device arrays of p->ngrid^3
+ * sites (x fastest); out (host) receives <|phi|^2>, <|phi'|^2>,
+ * <|grad phi|^2>, <V(phi)> at conformal time tau; stream may be NULL.  The
+ * call allocates nothing: its scratch is a fixed array inside the library
+ * (one partial sum per z-plane, so p->ngrid <= 2048; larger lattices are
+ * rejected with AXG_ERR_ARG), held by every GPU that loads the library until
+ * the process exits.  The first call on a device looks up that array's device
+ * address (once per device, with the device current); make that first call
+ * before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU race; serialise them (one stream, or synchronise).
+ * Errors are reported through axg_last_error(NULL). */
+int axg_field_moments_noalloc(const axg_params *p, const double *d_phi, const double *d_phidot,
+                              double tau, double out[4], void *stream);
+
 #ifdef __cplusplus
 }
 #endif
