@@ -31,7 +31,7 @@ __all__ = [
     "PREC_FP64_PLAIN", "PREC_FP64_FUSED", "PREC_FP32_MIXED", "GW_NONE", "GW_GREEN", "GW_UIJ",
     "F_ID_STRINGS", "F_ID_WALLS", "F_SPEC_EST", "F_GRAV_SPEC", "F_INITIAL_LOOP",
     "POT_REFERENCE", "POT_QUARTIC", "COMPAT_INTENDED", "COMPAT_REF", "EXPORTED_SYMBOLS",
-    "field_moments_noalloc",
+    "field_moments_noalloc", "Ensemble",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -96,7 +96,9 @@ EXPORTED_SYMBOLS = (
     "axg_read_chk", "axg_write_param_chk", "axg_read_param_chk", "axg_synchronize",
     "axg_event_record", "axg_event_elapsed", "axg_set_kernel_timing", "axg_kernel_timing",
     "axg_launch_count", "axg_tile_count", "axg_tile_info", "axg_set_tile", "axg_autotune",
-    "axg_field_moments_noalloc",
+    "axg_field_moments_noalloc", "axg_ensemble_create", "axg_ensemble_destroy", "axg_ensemble_last_error",
+    "axg_ensemble_size", "axg_ensemble_member", "axg_ensemble_leapfrog", "axg_ensemble_autotune",
+    "axg_ensemble_launch_count",
 )
 
 _lib = None
@@ -171,6 +173,15 @@ def load_library():
         "axg_autotune": ([c_ctx, ctypes.c_int, P(ctypes.c_int), dp], ctypes.c_int),
         "axg_field_moments_noalloc": ([P(Params), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, dp,
                                        ctypes.c_void_p], ctypes.c_int),
+        "axg_ensemble_create": ([P(Params), ctypes.c_int32, P(ctypes.c_void_p)], ctypes.c_int),
+        "axg_ensemble_destroy": ([ctypes.c_void_p], ctypes.c_int),
+        "axg_ensemble_last_error": ([ctypes.c_void_p], ctypes.c_char_p),
+        "axg_ensemble_size": ([ctypes.c_void_p, P(ctypes.c_int32)], ctypes.c_int),
+        "axg_ensemble_member": ([ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_void_p)], ctypes.c_int),
+        "axg_ensemble_leapfrog": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "axg_ensemble_autotune": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_int), dp], ctypes.c_int),
+        "axg_ensemble_launch_count": ([ctypes.c_void_p, P(ctypes.c_int64)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -210,11 +221,15 @@ def _dptr(a: Optional[np.ndarray]):
 class Lattice:
     """One GPU lattice context (owns all device state of the hot path)."""
 
-    def __init__(self, params: Params):
+    def __init__(self, params: Params, _handle=None, _owner=None):
         self.lib = load_library()
         self.params = params
         self.n = int(params.ngrid)
         self._ctx = ctypes.c_void_p()
+        self._owner = _owner  # a member of an Ensemble is destroyed with it
+        if _handle is not None:
+            self._ctx = _handle
+            return
         rc = self.lib.axg_create(ctypes.byref(params), ctypes.byref(self._ctx))
         if rc != 0:
             raise AxgError(rc, self.lib.axg_last_error(None).decode())
@@ -225,9 +240,9 @@ class Lattice:
             raise AxgError(rc, self.lib.axg_last_error(self._ctx).decode())
 
     def close(self):
-        if self._ctx:
+        if self._ctx and self._owner is None:
             self.lib.axg_destroy(self._ctx)
-            self._ctx = ctypes.c_void_p()
+        self._ctx = ctypes.c_void_p()
 
     def __enter__(self):
         return self
@@ -442,3 +457,66 @@ class Lattice:
         v = ctypes.c_int64()
         self._check(self.lib.axg_launch_count(self._ctx, ctypes.byref(v)))
         return v.value
+
+
+class Ensemble:
+    """Batched ensemble of lattices of uneven sizes stepped together
+    (axg_ensemble_*); member(i) gives a Lattice view of one realisation."""
+
+    def __init__(self, params_list):
+        self.lib = load_library()
+        arr = (Params * len(params_list))(*params_list)
+        self._params = list(params_list)
+        self._e = ctypes.c_void_p()
+        rc = self.lib.axg_ensemble_create(arr, len(params_list), ctypes.byref(self._e))
+        if rc != 0:
+            raise AxgError(rc, self.lib.axg_last_error(None).decode())
+        self.members = []
+        for i, p in enumerate(self._params):
+            h = ctypes.c_void_p()
+            self._check(self.lib.axg_ensemble_member(self._e, i, ctypes.byref(h)))
+            self.members.append(Lattice(p, _handle=h, _owner=self))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise AxgError(rc, self.lib.axg_ensemble_last_error(self._e).decode())
+
+    def __len__(self):
+        return len(self.members)
+
+    def member(self, i) -> Lattice:
+        return self.members[i]
+
+    def leapfrog(self, t1, dt, nsteps, first_half=True, last_half=True, use_graph=True):
+        self._check(self.lib.axg_ensemble_leapfrog(self._e, t1, dt, nsteps, int(first_half), int(last_half),
+                                                   int(use_graph)))
+
+    def autotune(self, steps=3):
+        best = ctypes.c_int()
+        ms = ctypes.c_double()
+        self._check(self.lib.axg_ensemble_autotune(self._e, steps, ctypes.byref(best), ctypes.byref(ms)))
+        return best.value, ms.value
+
+    def launch_count(self):
+        v = ctypes.c_int64()
+        self._check(self.lib.axg_ensemble_launch_count(self._e, ctypes.byref(v)))
+        return v.value
+
+    def close(self):
+        if self._e:
+            for m in self.members:
+                m._ctx = ctypes.c_void_p()
+            self.lib.axg_ensemble_destroy(self._e)
+            self._e = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -301,36 +301,27 @@ __device__ __forceinline__ void tma_phi(uint32_t dst, const CUtensorMap *m, int 
     tma_load_4d(dst, m, 0, x, y, z, bar);  // (re|im, x, y, z) doubles
 }
 
+// One TX x TY column of zc planes starting at (x0, y0, z0): stage the
+// stencil planes by TMA, compute kick + drift, store.  `gplane` counts the
+// planes this CTA has staged so far, so stage indices and mbarrier phases
+// continue across the columns a persistent CTA processes.  Returns false
+// (after recording the error) when a TMA wait timed out.
 template <typename R, int TX, int TY, bool UIJ>
-__global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 : 1))
-    k_fused(const __grid_constant__ CUtensorMap tm_prow, const __grid_constant__ CUtensorMap tm_pbody,
-            const __grid_constant__ CUtensorMap tm_phalo, const __grid_constant__ CUtensorMap tm_urow,
-            const __grid_constant__ CUtensorMap tm_ubody, const __grid_constant__ CUtensorMap tm_uhalo,
-            const FusedParams<R> P) {
+__device__ __forceinline__ bool fused_column(const CUtensorMap *tm_prow, const CUtensorMap *tm_pbody,
+                                             const CUtensorMap *tm_phalo, const CUtensorMap *tm_urow,
+                                             const CUtensorMap *tm_ubody, const CUtensorMap *tm_uhalo,
+                                             const FusedParams<R> &P, int x0, int y0, int z0,
+                                             unsigned char *smem, uint64_t *bars, uint32_t &gplane) {
   using L = StageLayout<R, TX, TY, UIJ>;
   using V = typename V2<R>::T;
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char *smem =
-      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * L::bytes);
-
   const int n = P.n, zc = P.zc;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-  const int ncx = n / TX;
-  const int x0 = (blockIdx.x % ncx) * TX, y0 = (blockIdx.x / ncx) * TY, z0 = blockIdx.y * zc;
   const int nplanes = zc + 2;
-
-  if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
-    fence_barrier_init();
-    fence_proxy_async();
-  }
-  __syncthreads();
 
   auto issue = [&](int p) {
     int z = z0 - 1 + p;
     z = z < 0 ? z + n : (z >= n ? z - n : z);
-    const int s = p % kStages;
+    const int s = (int)((gplane + (uint32_t)p) % kStages);
     unsigned char *st = smem + s * L::bytes;
     const uint32_t bar = smem_u32(&bars[s]);
     mbar_expect_tx(bar, (uint32_t)L::tx_bytes);
@@ -338,18 +329,18 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
     const int yp = y0 + TY == n ? 0 : y0 + TY;
     const int xpl = x0 - L::PHW < 0 ? x0 - L::PHW + n : x0 - L::PHW;
     const int xr = x0 + TX == n ? 0 : x0 + TX;
-    tma_phi<R>(smem_u32(st + L::phi_main), &tm_prow, x0, ym, z, bar);
-    tma_phi<R>(smem_u32(st + L::phi_main + TX * (int)sizeof(V)), &tm_pbody, x0, y0, z, bar);
-    tma_phi<R>(smem_u32(st + L::phi_main + (TY + 1) * TX * (int)sizeof(V)), &tm_prow, x0, yp, z, bar);
-    tma_phi<R>(smem_u32(st + L::phi_hl), &tm_phalo, xpl, y0, z, bar);
-    tma_phi<R>(smem_u32(st + L::phi_hr), &tm_phalo, xr, y0, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_main), tm_prow, x0, ym, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_main + TX * (int)sizeof(V)), tm_pbody, x0, y0, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_main + (TY + 1) * TX * (int)sizeof(V)), tm_prow, x0, yp, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_hl), tm_phalo, xpl, y0, z, bar);
+    tma_phi<R>(smem_u32(st + L::phi_hr), tm_phalo, xr, y0, z, bar);
     if constexpr (UIJ) {
       const int xul = x0 - L::UHW < 0 ? x0 - L::UHW + n : x0 - L::UHW;
-      tma_load_4d(smem_u32(st + L::u_top), &tm_urow, x0, ym, z, 0, bar);
-      tma_load_4d(smem_u32(st + L::u_body), &tm_ubody, x0, y0, z, 0, bar);
-      tma_load_4d(smem_u32(st + L::u_bot), &tm_urow, x0, yp, z, 0, bar);
-      tma_load_4d(smem_u32(st + L::u_hl), &tm_uhalo, xul, y0, z, 0, bar);
-      tma_load_4d(smem_u32(st + L::u_hr), &tm_uhalo, xr, y0, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_top), tm_urow, x0, ym, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_body), tm_ubody, x0, y0, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_bot), tm_urow, x0, yp, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_hl), tm_uhalo, xul, y0, z, 0, bar);
+      tma_load_4d(smem_u32(st + L::u_hr), tm_uhalo, xr, y0, z, 0, bar);
     }
   };
 
@@ -357,11 +348,13 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
     const int first = nplanes < kStages ? nplanes : kStages;
     for (int p = 0; p < first; ++p) issue(p);
   }
-  bool ok = mbar_wait_bounded(smem_u32(&bars[0]), 0);
-  ok = ok && mbar_wait_bounded(smem_u32(&bars[1]), 0);
+  auto stage_of = [&](int p) { return (int)((gplane + (uint32_t)p) % kStages); };
+  auto parity_of = [&](int p) { return (uint32_t)(((gplane + (uint32_t)p) / kStages) & 1); };
+  bool ok = mbar_wait_bounded(smem_u32(&bars[stage_of(0)]), parity_of(0));
+  ok = ok && mbar_wait_bounded(smem_u32(&bars[stage_of(1)]), parity_of(1));
   if (__syncthreads_or(!ok)) {
     if (tid == 0) atomicCAS(P.err, 0, AXG_KERR_MBAR_TIMEOUT);
-    return;
+    return false;
   }
 
   const int64_t n2 = (int64_t)n * n;
@@ -381,12 +374,12 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
         if constexpr (sizeof(R) == 4) cuv[c] = P.cu[c * P.n3 + s];
       }
     }
-    const int snext = (p + 1) % kStages;
-    ok = mbar_wait_bounded(smem_u32(&bars[snext]), (uint32_t)(((p + 1) / kStages) & 1));
+    const int snext = stage_of(p + 1);
+    ok = mbar_wait_bounded(smem_u32(&bars[snext]), parity_of(p + 1));
 
     if (ok) {
-      const unsigned char *sp = smem + ((p - 1) % kStages) * L::bytes;
-      const unsigned char *sc = smem + (p % kStages) * L::bytes;
+      const unsigned char *sp = smem + stage_of(p - 1) * L::bytes;
+      const unsigned char *sc = smem + stage_of(p) * L::bytes;
       const unsigned char *sn = smem + snext * L::bytes;
       const V *pm = reinterpret_cast<const V *>(sc + L::phi_main);
       const V *phl = reinterpret_cast<const V *>(sc + L::phi_hl);
@@ -531,12 +524,103 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
     // all threads are done with stage (p-1); refill it with plane p-1+kStages
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicCAS(P.err, 0, AXG_KERR_MBAR_TIMEOUT);
-      return;
+      return false;
     }
     if (tid == 0 && p - 1 + kStages < nplanes) {
       fence_proxy_async();
       issue(p - 1 + kStages);
     }
+  }
+  gplane += (uint32_t)nplanes;
+  return true;
+}
+
+__device__ __forceinline__ void init_stage_barriers(uint64_t *bars) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    fence_barrier_init();
+    fence_proxy_async();
+  }
+  __syncthreads();
+}
+
+template <typename R, int TX, int TY, bool UIJ>
+__global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 : 1))
+    k_fused(const __grid_constant__ CUtensorMap tm_prow, const __grid_constant__ CUtensorMap tm_pbody,
+            const __grid_constant__ CUtensorMap tm_phalo, const __grid_constant__ CUtensorMap tm_urow,
+            const __grid_constant__ CUtensorMap tm_ubody, const __grid_constant__ CUtensorMap tm_uhalo,
+            const FusedParams<R> P) {
+  using L = StageLayout<R, TX, TY, UIJ>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * L::bytes);
+  init_stage_barriers(bars);
+  const int ncx = P.n / TX;
+  const int x0 = (blockIdx.x % ncx) * TX, y0 = (blockIdx.x / ncx) * TY, z0 = blockIdx.y * P.zc;
+  uint32_t gplane = 0;
+  fused_column<R, TX, TY, UIJ>(&tm_prow, &tm_pbody, &tm_phalo, &tm_urow, &tm_ubody, &tm_uhalo, P, x0, y0, z0,
+                               smem, bars, gplane);
+}
+
+// ------------------------------------------------------------------------
+// persistent batched kernel: ensembles of lattices of uneven sizes in one
+// launch.  Work items are (member, column, z-chunk) in member order, columns
+// fastest; each CTA walks the items with a grid stride, re-using its TMA
+// ring (stage phases continue through `gplane`).  Per-step coefficients come
+// from device memory so the whole step sequence can be graph-captured once.
+// ------------------------------------------------------------------------
+template <typename R, int TX, int TY, bool UIJ>
+__global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 : 1))
+    k_fused_batch(const axg_ens_member_dev *__restrict__ mem, int nmem, long long total, int cur,
+                  const axg_ens_coef *__restrict__ coefs, int step, int zc, double dspa, int *err) {
+  using L = StageLayout<R, TX, TY, UIJ>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * L::bytes);
+  init_stage_barriers(bars);
+  const axg_ens_coef &K = coefs[step];
+  FusedParams<R> P;
+  P.f1 = (R)K.f[0];
+  P.f2 = (R)K.f[1];
+  P.f3 = (R)K.f[2];
+  P.fsc = sizeof(R) == 4 ? (R)(K.f[3] * 2.0 / ((2.0 * dspa) * (2.0 * dspa))) : (R)K.f[3];
+  P.dtd = (R)K.dtd;
+  P.A = (R)K.pot[0];
+  P.B = (R)K.pot[1];
+  P.C = (R)K.pot[2];
+  P.D = (R)K.pot[3];
+  P.d = 2.0 * dspa;
+  P.inv_d = 1.0 / P.d;
+  int ex;
+  P.d_pow2 = sizeof(R) == 8 && frexp(P.d, &ex) == 0.5;
+  P.zc = zc;
+  P.err = err;
+  uint32_t gplane = 0;
+  for (long long w = blockIdx.x; w < total; w += gridDim.x) {
+    int lo = 0, hi = nmem - 1;  // last member with item_begin <= w
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (mem[mid].item_begin <= w) lo = mid;
+      else hi = mid - 1;
+    }
+    const axg_ens_member_dev &D = mem[lo];
+    const long long local = w - D.item_begin;
+    const int col = (int)(local % D.ncols), chunk = (int)(local / D.ncols);
+    const int ncx = D.n / TX;
+    P.n = D.n;
+    P.n3 = D.n3;
+    P.phi_out = reinterpret_cast<typename V2<R>::T *>(D.phi[1 - cur]);
+    P.phid = reinterpret_cast<typename V2<R>::T *>(D.phid);
+    P.cphi = reinterpret_cast<typename V2<R>::T *>(D.cphi);
+    P.u_out = reinterpret_cast<R *>(D.u[1 - cur]);
+    P.ud = reinterpret_cast<R *>(D.ud);
+    P.cu = reinterpret_cast<R *>(D.cu);
+    const CUtensorMap *tm = D.tm[cur];
+    if (!fused_column<R, TX, TY, UIJ>(&tm[0], &tm[1], &tm[2], &tm[3], &tm[4], &tm[5], P, (col % ncx) * TX,
+                                      (col / ncx) * TY, chunk * zc, smem, bars, gplane))
+      return;
   }
 }
 
@@ -652,6 +736,8 @@ int launch_fused_cfg(axg_ctx *ctx, const FusedParams<R> &P, int cfg, const char 
 }  // namespace
 
 // --------------------------------------------------------------------------
+int axg_evo_build_tmaps(axg_ctx *ctx, int cfg) { return build_tmaps(ctx, cfg); }
+
 int axg_evo_tile_count() { return kNumTiles; }
 axg_tile_cfg axg_evo_tile(int i) { return kTiles[i]; }
 
@@ -807,4 +893,61 @@ int axg_evo_check_error(axg_ctx *ctx) {
     return axg_set_error(ctx, AXG_ERR_CUDA, "kernel reported error " + std::to_string(h));
   }
   return AXG_OK;
+}
+
+namespace {
+template <typename R, int TX, int TY, bool UIJ>
+int launch_batch_t(axg_ctx *ctx, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem, long long total,
+                   int cur, const axg_ens_coef *d_coef, int step, int zc, double dspa, int *d_err) {
+  using L = StageLayout<R, TX, TY, UIJ>;
+  const int smem = kStages * L::bytes + kStages * 8 + 128;
+  static bool attr_set = false;
+  if (!attr_set) {
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_fused_batch<R, TX, TY, UIJ>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr_set = true;
+  }
+  int per_sm = 0;
+  AXG_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_batch<R, TX, TY, UIJ>, TX * TY, smem));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  long long grid = (long long)std::max(per_sm, 1) * std::max(sms, 1);
+  if (grid > total) grid = total;
+  k_fused_batch<R, TX, TY, UIJ><<<(unsigned)grid, dim3(TX, TY), smem, stream>>>(d_mem, nmem, total, cur, d_coef,
+                                                                               step, zc, dspa, d_err);
+  ctx->launches++;
+  AXG_CUDA_TRY(ctx, cudaGetLastError());
+  return AXG_OK;
+}
+}  // namespace
+
+int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem,
+                       long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,
+                       int *d_err, bool fp32, bool uij, double dspa) {
+  const axg_tile_cfg t = kTiles[cfg];
+#define AXG_BATCH(R, TY_, U)                                                                              \
+  return launch_batch_t<R, 32, TY_, U>(any, stream, d_mem, nmem, total_items, cur, d_coef, step, t.zc, dspa, d_err)
+  if (fp32) {
+    if (uij) {
+      if (t.ty == 16) AXG_BATCH(float, 16, true);
+      if (t.ty == 8) AXG_BATCH(float, 8, true);
+      if (t.ty == 4) AXG_BATCH(float, 4, true);
+    } else {
+      if (t.ty == 16) AXG_BATCH(float, 16, false);
+      if (t.ty == 8) AXG_BATCH(float, 8, false);
+      if (t.ty == 4) AXG_BATCH(float, 4, false);
+    }
+  } else {
+    if (uij) {
+      if (t.ty == 16) AXG_BATCH(double, 16, true);
+      if (t.ty == 8) AXG_BATCH(double, 8, true);
+      if (t.ty == 4) AXG_BATCH(double, 4, true);
+    } else {
+      if (t.ty == 16) AXG_BATCH(double, 16, false);
+      if (t.ty == 8) AXG_BATCH(double, 8, false);
+      if (t.ty == 4) AXG_BATCH(double, 4, false);
+    }
+  }
+#undef AXG_BATCH
+  return axg_set_error(any, AXG_ERR_UNSUPPORTED, "tile configuration");
 }

@@ -22,6 +22,22 @@ struct axg_tile_cfg {
   int tx, ty, zc;
 };
 
+// Device-side descriptor of one ensemble member (tensor maps of both
+// ping-pong buffers plus the field pointers); 64-byte aligned for TMA.
+struct alignas(64) axg_ens_member_dev {
+  CUtensorMap tm[2][6];  // [buffer][phi_row, phi_body, phi_halo, u_row, u_body, u_halo]
+  void *phi[2], *phid, *cphi, *u[2], *ud, *cu;
+  int64_t n3;
+  int32_t n, ncols;
+  long long item_begin;  // first work item (column x z-chunk) of this member
+};
+
+// Per-step coefficients of the batched kick + drift (read by the kernel
+// from device memory so a captured step graph can be replayed).
+struct axg_ens_coef {
+  double f[4], pot[4], dtd, pad[3];
+};
+
 struct axg_kernel_stat {
   std::string name;
   int64_t launches = 0;
@@ -170,6 +186,11 @@ int axg_evo_tile_count();
 axg_tile_cfg axg_evo_tile(int i);
 int axg_evo_tile_supported(const axg_ctx *ctx, int i);
 int axg_evo_default_tile(const axg_ctx *ctx);
+int axg_evo_build_tmaps(axg_ctx *ctx, int cfg);
+// one persistent launch over every member's columns (ensemble.cu drives it)
+int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem,
+                       long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,
+                       int *d_err, bool fp32, bool uij, double dspa);
 
 // kick coefficients (axg_capi.cu) -- evolve.f90:291-305
 void axg_kick_coeffs(const axg_params *p, double t, double dt, double f[4], double pot[4]);

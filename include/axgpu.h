@@ -256,6 +256,31 @@ int axg_kernel_timing(axg_ctx *ctx, int i, char *name, int64_t name_len, int64_t
 int axg_launch_count(const axg_ctx *ctx, int64_t *launches);
 
 /* ------------------------------------------------------------------ */
+/* batched ensembles (no counterpart in the reference, which runs one  */
+/* realisation per job)                                                 */
+/* ------------------------------------------------------------------ */
+typedef struct axg_ensemble axg_ensemble;
+/* count member lattices of possibly different ngrid and seed; they must share
+ * a fused precision (FP32-mixed or FP64-fused), gw_mode NONE or UIJ, dspa,
+ * sigma_cr and the potential, so that one step has the same coefficients for
+ * all of them.  Each member is a full context (IC, defects, spectra,
+ * transfers through axg_ensemble_member); all work on one stream. */
+int axg_ensemble_create(const axg_params *members, int32_t count, axg_ensemble **out);
+int axg_ensemble_destroy(axg_ensemble *e);
+const char *axg_ensemble_last_error(const axg_ensemble *e);
+int axg_ensemble_size(const axg_ensemble *e, int32_t *count);
+int axg_ensemble_member(axg_ensemble *e, int32_t i, axg_ctx **member);
+/* axg_leapfrog for every member at once: each step is ONE persistent launch
+ * over all members' columns.  use_graph: the first interval of a given
+ * (nsteps, dt, half-step) shape runs eagerly and is captured into a CUDA
+ * graph that later intervals of that shape replay. */
+int axg_ensemble_leapfrog(axg_ensemble *e, double t1, double dt, int64_t nsteps, int first_half,
+                          int last_half, int use_graph);
+/* choose the tile shape shared by all members (state restored) */
+int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *best_ms_per_step);
+int axg_ensemble_launch_count(const axg_ensemble *e, int64_t *launches);
+
+/* ------------------------------------------------------------------ */
 /* allocation-free diagnostics                                          */
 /* ------------------------------------------------------------------ */
 /* No counterpart in the reference.  The volume moments of axg_field_moments
