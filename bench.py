@@ -218,6 +218,85 @@ def bench_e2e(ag, lat, n, nsub, reps, t, dt):
                     "once per interval of %d leapfrog steps (pinned host memory); u_ij device-resident" % nsub}
 
 
+ENSEMBLE_SIZES = [(64, 32), (128, 32), (160, 24), (192, 8)]  # (N, members): 96 realisations
+
+
+def bench_ensemble(ag, steps, device, sizes=ENSEMBLE_SIZES):
+    """Config 3: 96 seeded realisations of uneven sizes stepped together, one
+    persistent launch per step, intervals replayed from a CUDA graph."""
+    ps = []
+    for n, cnt in sizes:
+        for r in range(cnt):
+            ps.append(ag.default_params(ngrid=n, precision=ag.PREC_FP32_MIXED, gw_mode=ag.GW_UIJ,
+                                        potential=ag.POT_REFERENCE, dspa=0.5, sigma_cr=1.0, kappa=0.1,
+                                        seed=1 + len(ps), device=device))
+    sites = sum(n ** 3 * c for n, c in sizes)
+    t_setup = time.perf_counter()
+    ens = ag.Ensemble(ps)
+    try:
+        for i, m in enumerate(ens.members):
+            m.ic_gaussian_flat(2.0 * np.pi / (8 * 0.5), i)
+        best, _ = ens.autotune(2)
+        setup_s = time.perf_counter() - t_setup
+        dt, interval = 0.05, max(1, steps // 4)
+        t = 2.0
+        ens.leapfrog(t, dt, interval, True, True)  # eager + capture
+        t += dt * interval
+        ens.leapfrog(t, dt, interval, True, True)  # replay (warm)
+        t += dt * interval
+        l0 = ens.launch_count()
+        t_start = time.perf_counter()
+        for _ in range(4):
+            ens.leapfrog(t, dt, interval, True, True)
+            t += dt * interval
+        wall = time.perf_counter() - t_start
+        launches = ens.launch_count() - l0
+        nsteps = 4 * interval
+        xi = [m.id_defects(1, t)[0][0] for m in ens.members[:8]]
+        return {"members": len(ps), "sizes": {f"{n}^3": c for n, c in sizes}, "sites": sites,
+                "value": sites * nsteps / wall, "unit": UNIT, "ms_per_step": 1e3 * wall / nsteps,
+                "steps": nsteps, "intervals": 4, "graph": True, "launches": launches,
+                "batched_launches_per_step": 1, "tile": ens.members[0].tiles()[best],
+                "setup_s": setup_s, "string_length_sample": float(np.mean(xi)),
+                "timing": "host wall clock around graph replays (each call synchronises)"}
+    finally:
+        ens.close()
+
+
+def accuracy_fp32(ag, n, steps, device):
+    """GW (u_ij TT) spectrum and field moments of the FP32-mixed path against
+    the FP64-plain path (bit-identical to the FP64 CPU restatement) after the
+    same evolution from the same initial state."""
+    out = {}
+    res = {}
+    for name, prec in (("fp64", ag.PREC_FP64_PLAIN), ("fp32", ag.PREC_FP32_MIXED)):
+        p = workload_params(ag, n, prec, ag.GW_UIJ, device)
+        with ag.Lattice(p) as lat:
+            lat.ic_gaussian_flat(kcut=2.0 * np.pi / (8 * p.dspa))
+            dt, _ = lat.get_dtau(2.0, 32.0, 0.25)
+            lat.leapfrog(2.0, dt, steps, True, True)
+            tau = 2.0 + dt * steps
+            w, pw, nu, de = lat.grav_spec_estimation(tau)
+            e, lpw, lnu, lde = lat.grav_spec_log(tau)
+            mom = lat.field_moments(tau)
+            counts = lat.classify_cells(7)
+            res[name] = (nu, lnu, mom, counts)
+    nu64, lnu64, m64, c64 = res["fp64"]
+    nu32, lnu32, m32, c32 = res["fp32"]
+    ok = nu64 > 0
+    okl = lnu64 > 0
+    out["gw_linear_bins_max_rel_err"] = float(np.max(np.abs(nu32[ok] - nu64[ok]) / nu64[ok])) if ok.any() else None
+    out["gw_log_bins_max_rel_err"] = float(np.max(np.abs(lnu32[okl] - lnu64[okl]) / lnu64[okl])) if okl.any() else None
+    out["moments_rel_err"] = [float(abs(a - b) / abs(b)) if b != 0 else None for a, b in zip(m32, m64)]
+    out["defect_counts_fp32"] = [int(x) for x in c32]
+    out["defect_counts_fp64"] = [int(x) for x in c64]
+    out["n"] = n
+    out["steps"] = steps
+    out["note"] = ("same seeded IC evolved by both paths; FP64-plain is bit-identical to the FP64 CPU restatement "
+                   "(tests); errors are per bin of the shell-summed |W'_TT|^2 + k^2|W_TT|^2")
+    return out
+
+
 def cpu_oracle_rate(n, steps, threads=None):
     """FP64 CPU restatement of evolve.f90 (phi + six u_ij), all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -279,6 +358,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--e2e-interval", type=int, default=20)
     ap.add_argument("--e2e-reps", type=int, default=3)
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy block")
+    ap.add_argument("--accuracy-steps", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -341,6 +423,19 @@ def main():
                 "hbm_frac": (byts / (tms * 1e-3) / 1e9) / peak if tms > 0 else None,
                 "fp32_mixed_speedup": value / v64 / world * world}
 
+    ensemble = None
+    if not args.no_ensemble:
+        try:
+            ensemble = bench_ensemble(ag, max(8, args.steps // 2), local)
+        except Exception as exc:
+            ensemble = {"error": str(exc)}
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        try:
+            accuracy = accuracy_fp32(ag, n, args.accuracy_steps, local)
+        except Exception as exc:
+            accuracy = {"error": str(exc)}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -364,7 +459,7 @@ def main():
                        "l2": "no flush: state %.1f GiB >> 126 MB L2" % (sites * 96 / 2 ** 30),
                        "tile": r32["tile_shape"]},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r32["launches"],
-            "clocks": r32["clocks"], "fp64_plain": fp64,
+            "clocks": r32["clocks"], "fp64_plain": fp64, "ensemble": ensemble, "accuracy": accuracy,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
