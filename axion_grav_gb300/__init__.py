@@ -29,9 +29,10 @@ import numpy as np
 __all__ = [
     "Params", "Lattice", "AxgError", "load_library", "library_path", "default_params",
     "PREC_FP64_PLAIN", "PREC_FP64_FUSED", "PREC_FP32_MIXED", "GW_NONE", "GW_GREEN", "GW_UIJ",
-    "F_ID_STRINGS", "F_ID_WALLS", "F_SPEC_EST", "F_GRAV_SPEC", "F_INITIAL_LOOP",
+    "F_ID_STRINGS", "F_ID_WALLS", "F_SPEC_EST", "F_GRAV_SPEC", "F_INITIAL_LOOP", "F_GROUP_STRINGS",
+    "F_GROUP_WALLS",
     "POT_REFERENCE", "POT_QUARTIC", "COMPAT_INTENDED", "COMPAT_REF", "EXPORTED_SYMBOLS",
-    "field_moments_noalloc", "Ensemble",
+    "field_moments_noalloc", "Ensemble", "epsilon", "tile_table",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -39,6 +40,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 PREC_FP64_PLAIN, PREC_FP64_FUSED, PREC_FP32_MIXED = 0, 1, 2
 GW_NONE, GW_GREEN, GW_UIJ = 0, 1, 2
 F_ID_STRINGS, F_ID_WALLS, F_SPEC_EST, F_GRAV_SPEC, F_INITIAL_LOOP = 1, 2, 4, 8, 16
+F_GROUP_STRINGS, F_GROUP_WALLS = 32, 64
 POT_REFERENCE, POT_QUARTIC = 0, 1
 COMPAT_INTENDED, COMPAT_REF = 0, 1
 
@@ -98,7 +100,8 @@ EXPORTED_SYMBOLS = (
     "axg_launch_count", "axg_tile_count", "axg_tile_info", "axg_set_tile", "axg_autotune",
     "axg_field_moments_noalloc", "axg_ensemble_create", "axg_ensemble_destroy", "axg_ensemble_last_error",
     "axg_ensemble_size", "axg_ensemble_member", "axg_ensemble_leapfrog", "axg_ensemble_autotune",
-    "axg_ensemble_launch_count",
+    "axg_ensemble_launch_count", "axg_adjoint_gw_band", "axg_spectrum_covariance", "axg_compute_crho_cov",
+    "axg_epsilon", "axg_ensemble_set_tile",
 )
 
 _lib = None
@@ -167,14 +170,15 @@ def load_library():
                               ctypes.c_int),
         "axg_launch_count": ([c_ctx, i64p], ctypes.c_int),
         "axg_tile_count": ([], ctypes.c_int),
-        "axg_tile_info": ([ctypes.c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32)],
-                          ctypes.c_int),
+        "axg_tile_info": ([ctypes.c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32),
+                           P(ctypes.c_int32)], ctypes.c_int),
         "axg_set_tile": ([c_ctx, ctypes.c_int], ctypes.c_int),
         "axg_autotune": ([c_ctx, ctypes.c_int, P(ctypes.c_int), dp], ctypes.c_int),
         "axg_field_moments_noalloc": ([P(Params), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, dp,
                                        ctypes.c_void_p], ctypes.c_int),
         "axg_ensemble_create": ([P(Params), ctypes.c_int32, P(ctypes.c_void_p)], ctypes.c_int),
         "axg_ensemble_destroy": ([ctypes.c_void_p], ctypes.c_int),
+        "axg_ensemble_set_tile": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
         "axg_ensemble_last_error": ([ctypes.c_void_p], ctypes.c_char_p),
         "axg_ensemble_size": ([ctypes.c_void_p, P(ctypes.c_int32)], ctypes.c_int),
         "axg_ensemble_member": ([ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_void_p)], ctypes.c_int),
@@ -182,6 +186,13 @@ def load_library():
                                    ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "axg_ensemble_autotune": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_int), dp], ctypes.c_int),
         "axg_ensemble_launch_count": ([ctypes.c_void_p, P(ctypes.c_int64)], ctypes.c_int),
+        "axg_spectrum_covariance": ([c_ctx, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, P(ctypes.c_int)],
+                                    ctypes.c_int),
+        "axg_compute_crho_cov": ([c_ctx, dp, dp], ctypes.c_int),
+        "axg_epsilon": ([ctypes.c_int32, dp, dp, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp, dp], ctypes.c_int),
+        "axg_adjoint_gw_band": ([c_ctx, ctypes.c_double, ctypes.c_double, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_int64, ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp, dp],
+                                ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -210,6 +221,28 @@ def field_moments_noalloc(params: Params, d_phi: int, d_phidot: int, tau: float,
     if rc != 0:
         raise AxgError(rc, lib.axg_last_error(None).decode())
     return out
+
+
+def tile_table() -> list:
+    """(tx, ty, zc, pointwise_tma) of every fused-kernel tile shape, by index."""
+    lib = load_library()
+    out = []
+    for i in range(lib.axg_tile_count()):
+        a, b, c, d = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        lib.axg_tile_info(i, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d))
+        out.append((a.value, b.value, c.value, d.value))
+    return out
+
+
+def epsilon(wav, p1, p2, c1, c2, tau1, tau2):
+    """get_epsilon (spectrum.f90:1002-1036) for one pair of output times."""
+    lib = load_library()
+    e, d = ctypes.c_double(), ctypes.c_double()
+    arrs = [np.ascontiguousarray(a, np.float64) for a in (wav, p1, p2, c1, c2)]
+    rc = lib.axg_epsilon(len(arrs[1]), *[_dptr(a) for a in arrs], tau1, tau2, ctypes.byref(e), ctypes.byref(d))
+    if rc != 0:
+        raise AxgError(rc, "axg_epsilon")
+    return e.value, d.value
 
 
 def _dptr(a: Optional[np.ndarray]):
@@ -385,7 +418,7 @@ class Lattice:
         return sl, wa, sv, np.array(c[:], dtype=np.int64)
 
     def defect_lists(self, ns: int, nw: int):
-        s = np.zeros((max(ns, 1), 12))
+        s = np.zeros((max(ns, 1), 13))
         w = np.zeros((max(nw, 1), 10))
         self._check(self.lib.axg_download_defect_lists(self._ctx, _dptr(s), ns, _dptr(w), nw))
         return s[:ns], w[:nw]
@@ -397,10 +430,37 @@ class Lattice:
         self._check(self.lib.axg_spectrum_estimation(self._ctx, tau, _dptr(w), _dptr(p), _dptr(cv), _dptr(ct)))
         return w, p, cv, ct
 
+    def spectrum_covariance(self, min_mc: int = 10, max_mc: int = 100, tol: float = 0.1):
+        nb = int(self.params.num_bin)
+        cov = np.zeros(nb * (nb + 1) // 2)
+        it = ctypes.c_int()
+        self._check(self.lib.axg_spectrum_covariance(self._ctx, min_mc, max_mc, tol, _dptr(cov), ctypes.byref(it)))
+        return cov, it.value
+
+    def compute_crho_cov(self):
+        r, d = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.axg_compute_crho_cov(self._ctx, ctypes.byref(r), ctypes.byref(d)))
+        return r.value, d.value
+
     def compute_crho(self) -> float:
         r = ctypes.c_double()
         self._check(self.lib.axg_compute_crho(self._ctx, ctypes.byref(r)))
         return r.value
+
+    # -- adjoint ----------------------------------------------------------------
+    def adjoint_gw_band(self, t1, dt, nsteps, stride, kmin, kmax, first_half=True, last_half=True,
+                        want_grads=True):
+        """J, dJ/dlambda, dJ/dphi0, dJ/dphidot0 (complex128 arrays) and the GPU
+        ms of the forward and reverse sweeps (axg_adjoint_gw_band)."""
+        n = self.n
+        J, dl, mf, mr = (ctypes.c_double() for _ in range(4))
+        g0 = np.zeros((n, n, n), np.complex128) if want_grads else None
+        g1 = np.zeros((n, n, n), np.complex128) if want_grads else None
+        self._check(self.lib.axg_adjoint_gw_band(
+            self._ctx, t1, dt, nsteps, int(first_half), int(last_half), stride, kmin, kmax, ctypes.byref(J),
+            ctypes.byref(dl), _dptr(g0.view(np.float64)) if want_grads else None,
+            _dptr(g1.view(np.float64)) if want_grads else None, ctypes.byref(mf), ctypes.byref(mr)))
+        return J.value, dl.value, g0, g1, mf.value, mr.value
 
     # -- checkpoint (evolve.f90:401-546) ----------------------------------------
     def write_chk(self, path: str):
@@ -437,12 +497,7 @@ class Lattice:
 
     # -- fused-kernel tiles / autotuner -------------------------------------------
     def tiles(self) -> list:
-        out = []
-        for i in range(self.lib.axg_tile_count()):
-            a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-            self.lib.axg_tile_info(i, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
-            out.append((a.value, b.value, c.value))
-        return out
+        return tile_table()
 
     def set_tile(self, cfg: int):
         self._check(self.lib.axg_set_tile(self._ctx, cfg))
@@ -490,6 +545,9 @@ class Ensemble:
     def leapfrog(self, t1, dt, nsteps, first_half=True, last_half=True, use_graph=True):
         self._check(self.lib.axg_ensemble_leapfrog(self._e, t1, dt, nsteps, int(first_half), int(last_half),
                                                    int(use_graph)))
+
+    def set_tile(self, cfg: int):
+        self._check(self.lib.axg_ensemble_set_tile(self._e, cfg))
 
     def autotune(self, steps=3):
         best = ctypes.c_int()

@@ -1,0 +1,460 @@
+// axg_adjoint.cu -- hand-written adjoint of the leapfrog of phi and six u_ij.
+//
+// Objective: the band-integrated GW energy of the u_ij spectrum at the end
+// of the run,
+//   J = sum_{kmin <= |k| <= kmax} 1/2 sum_ij (|W'_TT(k)|^2 + k^2 |W_TT(k)|^2),
+//   W = dx^3 FFT(tau u), W' = dx^3 FFT(u + tau u'),
+// i.e. the band sum of the numerator of axg_grav_spec_estimation (GW_UIJ).
+// Outputs: J, dJ/dlambda (quartic model: A = lambda/2, B = -lambda v^2/2) and
+// the gradients with respect to the initial phi and phi' (complex, d/dRe +
+// i d/dIm), from which the gradients with respect to Fourier-mode amplitudes
+// follow by one FFT.
+//
+// Scheme (FP64, state in the FP64-plain layout):
+//   forward  : the plain drift / kick kernels, a checkpoint of the whole state
+//              every `stride` steps;
+//   terminal : D2Z of tau u and u + tau u' (12 fields), per k the TT-projected
+//              band weights, Z2D back: dJ/du, dJ/du' in real space;
+//   reverse  : for each step, the state is stepped BACK using the leapfrog's
+//              time-reversibility (phi = phi+ - h pi+; pi = (pi+ - f2 L phi -
+//              f3 g(phi)) / f1; same for u) and re-anchored on the exact
+//              checkpoint every `stride` steps; the adjoint step is two
+//              stencil passes (k_adj_step: Laplacians of the adjoint momenta,
+//              the transposed potential Jacobian, the source adjoint's Q_i =
+//              2 fs (sum_j wbar_ij D_j phi + wbar_ii D_i phi); k_adj_divq:
+//              phibar += sum_i D_i^T Q_i).
+#include <cmath>
+#include <vector>
+
+#include "axg_internal.h"
+
+namespace {
+
+constexpr double kRefTwoPi = 2 * 3.14159265359;
+
+__device__ __forceinline__ int64_t site(int x, int y, int z, int n) { return ((int64_t)z * n + y) * n + x; }
+__device__ __forceinline__ int wr(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+struct StepCoef {
+  double f1, f2, f3, fs, h, A, B, C, D, dA, dB, d;
+};
+
+// backward drift: phi -= h pi, u -= h w
+__global__ void k_rev_drift(double2 *phi, const double2 *pi, double *u, const double *w, int64_t n3, double h) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    double2 a = phi[s];
+    const double2 b = pi[s];
+    a.x -= h * b.x;
+    a.y -= h * b.y;
+    phi[s] = a;
+    for (int c = 0; c < 6; ++c) u[c * n3 + s] -= h * w[c * n3 + s];
+  }
+}
+
+// backward kick: pi = (pi+ - f2 L phi - f3 g(phi)) / f1; w = (w+ - f2 L u - fs S(phi)) / f1
+__global__ void k_rev_kick(const double2 *__restrict__ phi, double2 *__restrict__ pi, const double *__restrict__ u,
+                           double *__restrict__ w, int n, StepCoef k) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y, iz = blockIdx.z;
+  if (ix >= n || iy >= n) return;
+  const int64_t n3 = (int64_t)n * n * n;
+  const int64_t c = site(ix, iy, iz, n);
+  const int64_t nb[6] = {site(wr(ix - 1, n), iy, iz, n), site(wr(ix + 1, n), iy, iz, n), site(ix, wr(iy - 1, n), iz, n),
+                         site(ix, wr(iy + 1, n), iz, n), site(ix, iy, wr(iz - 1, n), n), site(ix, iy, wr(iz + 1, n), n)};
+  const double2 p0 = phi[c];
+  double lr = -6 * p0.x, li = -6 * p0.y;
+  double2 pn[6];
+  for (int q = 0; q < 6; ++q) {
+    pn[q] = phi[nb[q]];
+    lr += pn[q].x;
+    li += pn[q].y;
+  }
+  const double s = p0.x * p0.x + p0.y * p0.y, g0 = k.A * s + k.B;
+  const double gr = g0 * p0.x + k.D * p0.x + k.C, gi = g0 * p0.y - k.D * p0.y;
+  double2 v = pi[c];
+  v.x = (v.x - k.f2 * lr - k.f3 * gr) / k.f1;
+  v.y = (v.y - k.f2 * li - k.f3 * gi) / k.f1;
+  pi[c] = v;
+  double Dr[3], Di[3];
+  for (int q = 0; q < 3; ++q) {
+    Dr[q] = (pn[2 * q + 1].x - pn[2 * q].x) / k.d;
+    Di[q] = (pn[2 * q + 1].y - pn[2 * q].y) / k.d;
+  }
+  int comp = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j <= i; ++j, ++comp) {
+      const double *uc = u + comp * n3;
+      double lu = -6 * uc[c];
+      for (int q = 0; q < 6; ++q) lu += uc[nb[q]];
+      const double S = 2 * (Dr[i] * Dr[j] + Di[i] * Di[j]);
+      w[comp * n3 + c] = (w[comp * n3 + c] - k.f2 * lu - k.fs * S) / k.f1;
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Adjoint of one kick+drift at the pre-kick state phi (in: adjoint after the
+// step; out: adjoint before it, except the D^T Q part of phibar).
+__global__ void k_adj_step(const double2 *__restrict__ phi, const double2 *__restrict__ pb_in,
+                           const double2 *__restrict__ ib_in, const double *__restrict__ ub_in,
+                           const double *__restrict__ wb_in, double2 *__restrict__ pb_out,
+                           double2 *__restrict__ ib_out, double *__restrict__ ub_out, double *__restrict__ wb_out,
+                           double *__restrict__ Q, int n, StepCoef k, double *__restrict__ dlam) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y, iz = blockIdx.z;
+  double lam_part = 0.0;
+  if (ix < n && iy < n) {
+    const int64_t n3 = (int64_t)n * n * n;
+    const int64_t c = site(ix, iy, iz, n);
+    const int64_t nb[6] = {site(wr(ix - 1, n), iy, iz, n), site(wr(ix + 1, n), iy, iz, n),
+                           site(ix, wr(iy - 1, n), iz, n), site(ix, wr(iy + 1, n), iz, n),
+                           site(ix, iy, wr(iz - 1, n), n), site(ix, iy, wr(iz + 1, n), n)};
+    // pibar_t = pibar+ + h phibar+ (adjoint of the drift), at the site and its neighbours
+    auto it = [&](int64_t q) {
+      const double2 a = ib_in[q], b = pb_in[q];
+      return make_double2(a.x + k.h * b.x, a.y + k.h * b.y);
+    };
+    const double2 i0 = it(c);
+    double lr = -6 * i0.x, li = -6 * i0.y;
+    for (int q = 0; q < 6; ++q) {
+      const double2 v = it(nb[q]);
+      lr += v.x;
+      li += v.y;
+    }
+    const double2 p0 = phi[c];
+    const double s = p0.x * p0.x + p0.y * p0.y, g0 = k.A * s + k.B;
+    const double pd = p0.x * i0.x + p0.y * i0.y;
+    const double jr = g0 * i0.x + 2 * k.A * p0.x * pd + k.D * i0.x;
+    const double ji = g0 * i0.y + 2 * k.A * p0.y * pd - k.D * i0.y;
+    const double2 pbv = pb_in[c];
+    pb_out[c] = make_double2(pbv.x + k.f2 * lr + k.f3 * jr, pbv.y + k.f2 * li + k.f3 * ji);
+    ib_out[c] = make_double2(k.f1 * i0.x, k.f1 * i0.y);
+    lam_part = k.f3 * (k.dA * s + k.dB) * pd;
+    // u_ij: wbar_t = wbar+ + h ubar+
+    double Dr[3], Di[3];
+    for (int q = 0; q < 3; ++q) {
+      const double2 a = phi[nb[2 * q + 1]], b = phi[nb[2 * q]];
+      Dr[q] = (a.x - b.x) / k.d;
+      Di[q] = (a.y - b.y) / k.d;
+    }
+    double wt[6];
+    for (int cc = 0; cc < 6; ++cc) {
+      const double *wb = wb_in + cc * n3, *ub = ub_in + cc * n3;
+      const double w0 = wb[c] + k.h * ub[c];
+      wt[cc] = w0;
+      double lu = -6 * w0;
+      for (int q = 0; q < 6; ++q) lu += wb[nb[q]] + k.h * ub[nb[q]];
+      ub_out[cc * n3 + c] = ub[c] + k.f2 * lu;
+      wb_out[cc * n3 + c] = k.f1 * w0;
+    }
+    const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
+    for (int i = 0; i < 3; ++i) {
+      double qr = wt[idx[i][i]] * Dr[i], qi = wt[idx[i][i]] * Di[i];
+      for (int j = 0; j < 3; ++j) {
+        qr += wt[idx[i][j]] * Dr[j];
+        qi += wt[idx[i][j]] * Di[j];
+      }
+      Q[(2 * i) * n3 + c] = 2 * k.fs * qr;
+      Q[(2 * i + 1) * n3 + c] = 2 * k.fs * qi;
+    }
+  }
+  lam_part = warp_sum(lam_part);
+  if ((threadIdx.x & 31) == 0 && lam_part != 0.0) atomicAdd(dlam, lam_part);
+}
+
+// phibar += sum_i D_i^T Q_i,  D_i^T Q(x) = (Q(x - e_i) - Q(x + e_i)) / d
+__global__ void k_adj_divq(double2 *__restrict__ pb, const double *__restrict__ Q, int n, double d) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y, iz = blockIdx.z;
+  if (ix >= n || iy >= n) return;
+  const int64_t n3 = (int64_t)n * n * n;
+  const int64_t c = site(ix, iy, iz, n);
+  const int64_t m[3] = {site(wr(ix - 1, n), iy, iz, n), site(ix, wr(iy - 1, n), iz, n), site(ix, iy, wr(iz - 1, n), n)};
+  const int64_t p[3] = {site(wr(ix + 1, n), iy, iz, n), site(ix, wr(iy + 1, n), iz, n), site(ix, iy, wr(iz + 1, n), n)};
+  double2 v = pb[c];
+  for (int i = 0; i < 3; ++i) {
+    v.x += (Q[(2 * i) * n3 + m[i]] - Q[(2 * i) * n3 + p[i]]) / d;
+    v.y += (Q[(2 * i + 1) * n3 + m[i]] - Q[(2 * i + 1) * n3 + p[i]]) / d;
+  }
+  pb[c] = v;
+}
+
+// adjoint of the first half drift phi += h pi: pibar += h phibar (u likewise)
+__global__ void k_adj_half_drift(const double2 *pb, double2 *ib, const double *ub, double *wb, int64_t n3, double h) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    double2 a = ib[s];
+    const double2 b = pb[s];
+    a.x += h * b.x;
+    a.y += h * b.y;
+    ib[s] = a;
+    for (int c = 0; c < 6; ++c) wb[c * n3 + s] += h * ub[c * n3 + s];
+  }
+}
+
+// 12 real inputs of the terminal spectrum: a = tau u, b = u + tau w
+__global__ void k_adj_terminal_in(const double *u, const double *w, int64_t n3, double tau, double *out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride)
+    for (int c = 0; c < 6; ++c) {
+      out[c * n3 + s] = tau * u[c * n3 + s];
+      out[(6 + c) * n3 + s] = u[c * n3 + s] + tau * w[c * n3 + s];
+    }
+}
+
+// per half-spectrum k: J contribution and the band weights M k^2 dx^6 Lambda(Xa), M dx^6 Lambda(Xb)
+__global__ void k_adj_terminal_k(double2 *F, int n, double dwav, double dx6, double kmin, double kmax, double *J) {
+  const int nh = n / 2 + 1;
+  const int64_t nhalf = (int64_t)n * n * nh;
+  const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
+  double jpart = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
+    const int ix = (int)(h % nh), iy = (int)((h / nh) % n), iz = (int)(h / ((int64_t)nh * n));
+    const double q[3] = {(double)((ix + n / 2) % n - n / 2), (double)((iy + n / 2) % n - n / 2),
+                         (double)((iz + n / 2) % n - n / 2)};
+    const double qq = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+    const double kk = qq * dwav;
+    const bool in = qq > 0 && kk >= kmin && kk <= kmax;
+    for (int f = 0; f < 2; ++f) {
+      double2 X[6];
+      for (int c = 0; c < 6; ++c) X[c] = F[(f * 6 + c) * nhalf + h];
+      double2 Y[6];
+      if (in) {
+        double P[3][3];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) P[i][j] = (i == j) - q[i] * q[j] / (qq * qq);
+        double Rr[3][3], Ri[3][3];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            double ar = 0, ai = 0;
+            for (int a = 0; a < 3; ++a)
+              for (int b = 0; b < 3; ++b) {
+                ar += P[i][a] * X[idx[a][b]].x * P[b][j];
+                ai += P[i][a] * X[idx[a][b]].y * P[b][j];
+              }
+            Rr[i][j] = ar;
+            Ri[i][j] = ai;
+          }
+        const double tr = Rr[0][0] + Rr[1][1] + Rr[2][2], ti = Ri[0][0] + Ri[1][1] + Ri[2][2];
+        double e = 0;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            Rr[i][j] -= 0.5 * P[i][j] * tr;
+            Ri[i][j] -= 0.5 * P[i][j] * ti;
+            e += Rr[i][j] * Rr[i][j] + Ri[i][j] * Ri[i][j];
+          }
+        const double wgt = (f == 0 ? kk * kk : 1.0) * dx6;
+        const double herm = (ix == 0 || 2 * ix == n) ? 1.0 : 2.0;
+        jpart += herm * 0.5 * wgt * e;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j <= i; ++j) Y[idx[i][j]] = make_double2(wgt * Rr[i][j], wgt * Ri[i][j]);
+      } else {
+        for (int c = 0; c < 6; ++c) Y[c] = make_double2(0.0, 0.0);
+      }
+      for (int c = 0; c < 6; ++c) F[(f * 6 + c) * nhalf + h] = Y[c];
+    }
+  }
+  jpart = warp_sum(jpart);
+  if ((threadIdx.x & 31) == 0 && jpart != 0.0) atomicAdd(J, jpart);
+}
+
+// ubar = mult (tau ga + gb), wbar = mult tau gb from the Z2D outputs
+__global__ void k_adj_terminal_out(const double *g, int64_t n3, double tau, double *ub, double *wb) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const double mult[6] = {1, 2, 1, 2, 2, 1};
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride)
+    for (int c = 0; c < 6; ++c) {
+      const double ga = g[c * n3 + s], gb = g[(6 + c) * n3 + s];
+      ub[c * n3 + s] = mult[c] * (tau * ga + gb);
+      wb[c * n3 + s] = mult[c] * tau * gb;
+    }
+}
+
+int grid_for(int64_t count) {
+  int64_t b = (count + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  return (int)(b < 1 ? 1 : b);
+}
+
+StepCoef coef_at(const axg_params &p, double t, double dt, double h) {
+  double f[4], pot[4];
+  axg_kick_coeffs(&p, t, dt, f, pot);
+  StepCoef k;
+  k.f1 = f[0];
+  k.f2 = f[1];
+  k.f3 = f[2];
+  k.fs = f[3];
+  k.h = h;
+  k.A = pot[0];
+  k.B = pot[1];
+  k.C = pot[2];
+  k.D = pot[3];
+  if (p.potential == AXG_POT_QUARTIC) {
+    k.dA = 0.5;
+    k.dB = -(p.vev * p.vev) / 2;
+  } else {
+    k.dA = k.dB = 0.0;
+  }
+  k.d = 2 * p.dspa;
+  return k;
+}
+
+}  // namespace
+
+extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half,
+                                   int last_half, int64_t stride, double kmin, double kmax, double *J_out,
+                                   double *dJ_dlambda, double *grad_phi0, double *grad_phidot0, double *ms_forward,
+                                   double *ms_reverse) {
+  if (!ctx || nsteps < 1 || stride < 1 || !(dt > 0) || !(t1 > 0) || !J_out) return AXG_ERR_ARG;
+  if (ctx->p.precision != AXG_PREC_FP64_PLAIN || ctx->p.gw_mode != AXG_GW_UIJ)
+    return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "the adjoint runs on the FP64-plain path with gw_mode UIJ");
+  const int n = (int)ctx->n;
+  const int64_t n3 = ctx->n3, nhalf = (int64_t)n * n * (n / 2 + 1);
+  const size_t state_b = (size_t)n3 * (16 + 16 + 48 + 48);
+  const int64_t nck = nsteps / stride + 1;
+  double *ck = nullptr, *adj = nullptr, *Q = nullptr, *fbuf = nullptr;
+  int rc = AXG_OK;
+  cufftHandle pf = 0, pb = 0;
+  bool pfo = false, pbo = false;
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  do {
+    if ((rc = axg_alloc(ctx, (void **)&ck, state_b * nck, "adjoint checkpoints"))) break;
+    if ((rc = axg_alloc(ctx, (void **)&adj, state_b * 2, "adjoint state"))) break;
+    if ((rc = axg_alloc(ctx, (void **)&Q, (size_t)n3 * 6 * 8, "adjoint Q"))) break;
+    if ((rc = axg_alloc(ctx, (void **)&fbuf, (size_t)12 * n3 * 8 + (size_t)12 * nhalf * 16, "adjoint FFT"))) break;
+    int dims[3] = {n, n, n};
+    if (cufftPlanMany(&pf, 3, dims, nullptr, 1, (int)n3, nullptr, 1, (int)nhalf, CUFFT_D2Z, 12) != CUFFT_SUCCESS ||
+        cufftPlanMany(&pb, 3, dims, nullptr, 1, (int)nhalf, nullptr, 1, (int)n3, CUFFT_Z2D, 12) != CUFFT_SUCCESS) {
+      rc = axg_set_error(ctx, AXG_ERR_CUDA, "adjoint cuFFT plans");
+      break;
+    }
+    pfo = pbo = true;
+    cufftSetStream(pf, ctx->stream);
+    cufftSetStream(pb, ctx->stream);
+    double2 *phi = (double2 *)ctx->phi[ctx->cur], *pi = (double2 *)ctx->phid;
+    double *u = (double *)ctx->u[ctx->cur], *w = (double *)ctx->ud;
+    auto save = [&](int64_t k) {
+      char *dst = (char *)ck + state_b * k;
+      cudaMemcpyAsync(dst, phi, (size_t)n3 * 16, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(dst + (size_t)n3 * 16, pi, (size_t)n3 * 16, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(dst + (size_t)n3 * 32, u, (size_t)n3 * 48, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(dst + (size_t)n3 * 80, w, (size_t)n3 * 48, cudaMemcpyDeviceToDevice, ctx->stream);
+    };
+    auto load = [&](int64_t k) {
+      const char *src = (const char *)ck + state_b * k;
+      cudaMemcpyAsync(phi, src, (size_t)n3 * 16, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(pi, src + (size_t)n3 * 16, (size_t)n3 * 16, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(u, src + (size_t)n3 * 32, (size_t)n3 * 48, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(w, src + (size_t)n3 * 80, (size_t)n3 * 48, cudaMemcpyDeviceToDevice, ctx->stream);
+    };
+    // ---------------- forward with checkpoints ----------------
+    cudaEventRecord(e0, ctx->stream);
+    double t = t1;
+    if (first_half) {
+      if ((rc = axg_evo_drift(ctx, dt / 2))) break;
+      t = t + dt / 2;
+    }
+    save(0);
+    std::vector<double> kt(nsteps + 1), kh(nsteps + 1);
+    for (int64_t it = 1; it <= nsteps && rc == AXG_OK; ++it) {
+      const double h = (it == nsteps && last_half) ? dt / 2 : dt;
+      kt[it] = t;
+      kh[it] = h;
+      if ((rc = axg_evo_kick_plain(ctx, t, dt))) break;
+      if ((rc = axg_evo_drift(ctx, h))) break;
+      t = t + h;
+      if (it % stride == 0) save(it / stride);
+    }
+    if (rc) break;
+    const double tau_end = t;
+    cudaEventRecord(e1, ctx->stream);
+    // ---------------- terminal adjoint ----------------
+    double2 *pb_a = (double2 *)adj, *ib_a = pb_a + n3;
+    double *ub_a = (double *)(ib_a + n3), *wb_a = ub_a + 6 * n3;
+    double2 *pb_b = (double2 *)((char *)adj + state_b), *ib_b = pb_b + n3;
+    double *ub_b = (double *)(ib_b + n3), *wb_b = ub_b + 6 * n3;
+    double *fin = fbuf;
+    double2 *F = (double2 *)(fbuf + 12 * n3);
+    AXG_LAUNCH(ctx, "adj_terminal_in", k_adj_terminal_in, grid_for(n3), 256, 0, u, w, n3, tau_end, fin);
+    if (cufftExecD2Z(pf, fin, (cufftDoubleComplex *)F) != CUFFT_SUCCESS) {
+      rc = axg_set_error(ctx, AXG_ERR_CUDA, "adjoint D2Z");
+      break;
+    }
+    AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_red, 0, 16, ctx->stream));
+    const double dx = ctx->p.dspa, dx6 = dx * dx * dx * dx * dx * dx;
+    const double dwav = kRefTwoPi / ctx->p.dspa / n;
+    AXG_LAUNCH(ctx, "adj_terminal_k", k_adj_terminal_k, grid_for(nhalf), 256, 0, F, n, dwav, dx6, kmin, kmax,
+               ctx->d_red);
+    if (cufftExecZ2D(pb, (cufftDoubleComplex *)F, fin) != CUFFT_SUCCESS) {
+      rc = axg_set_error(ctx, AXG_ERR_CUDA, "adjoint Z2D");
+      break;
+    }
+    AXG_CUDA_TRY(ctx, cudaMemsetAsync(adj, 0, (size_t)n3 * 32, ctx->stream));  // phibar, pibar = 0
+    AXG_LAUNCH(ctx, "adj_terminal_out", k_adj_terminal_out, grid_for(n3), 256, 0, fin, n3, tau_end, ub_a, wb_a);
+    // ---------------- reverse sweep ----------------
+    double *dlam = ctx->d_red + 1;
+    dim3 blk(32, 8), grd((n + 31) / 32, (n + 7) / 8, n);
+    bool a_is_in = true;
+    for (int64_t it = nsteps; it >= 1 && rc == AXG_OK; --it) {
+      const StepCoef kc = coef_at(ctx->p, kt[it], dt, kh[it]);
+      // state after step it -> state before step it (pre-kick)
+      if ((it - 1) % stride == 0) {
+        load((it - 1) / stride);
+      } else {
+        AXG_LAUNCH(ctx, "adj_rev_drift", k_rev_drift, grid_for(n3), 256, 0, phi, pi, u, w, n3, kh[it]);
+        AXG_LAUNCH(ctx, "adj_rev_kick", k_rev_kick, grd, blk, 0, phi, pi, u, w, n, kc);
+      }
+      double2 *pbi = a_is_in ? pb_a : pb_b, *ibi = a_is_in ? ib_a : ib_b, *pbo_ = a_is_in ? pb_b : pb_a,
+              *ibo = a_is_in ? ib_b : ib_a;
+      double *ubi = a_is_in ? ub_a : ub_b, *wbi = a_is_in ? wb_a : wb_b, *ubo = a_is_in ? ub_b : ub_a,
+             *wbo = a_is_in ? wb_b : wb_a;
+      AXG_LAUNCH(ctx, "adj_step", k_adj_step, grd, blk, 0, phi, pbi, ibi, ubi, wbi, pbo_, ibo, ubo, wbo, Q, n, kc, dlam);
+      AXG_LAUNCH(ctx, "adj_divq", k_adj_divq, grd, blk, 0, pbo_, Q, n, kc.d);
+      a_is_in = !a_is_in;
+    }
+    if (rc) break;
+    double2 *pbf = a_is_in ? pb_a : pb_b, *ibf = a_is_in ? ib_a : ib_b;
+    double *ubf = a_is_in ? ub_a : ub_b, *wbf = a_is_in ? wb_a : wb_b;
+    if (first_half) AXG_LAUNCH(ctx, "adj_half_drift", k_adj_half_drift, grid_for(n3), 256, 0, pbf, ibf, ubf, wbf, n3, dt / 2);
+    cudaEventRecord(e2, ctx->stream);
+    double h2[2];
+    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h2, ctx->d_red, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad_phi0) AXG_CUDA_TRY(ctx, cudaMemcpyAsync(grad_phi0, pbf, (size_t)n3 * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad_phidot0)
+      AXG_CUDA_TRY(ctx, cudaMemcpyAsync(grad_phidot0, ibf, (size_t)n3 * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    *J_out = h2[0];
+    if (dJ_dlambda) *dJ_dlambda = h2[1];
+    float f1 = 0, f2 = 0;
+    cudaEventElapsedTime(&f1, e0, e1);
+    cudaEventElapsedTime(&f2, e1, e2);
+    if (ms_forward) *ms_forward = f1;
+    if (ms_reverse) *ms_reverse = f2;
+    // the context state is left at the end of the forward run, as after axg_leapfrog
+    load(nck - 1);
+    if (nsteps % stride != 0) {
+      // re-run the tail from the last checkpoint to restore the final state exactly
+      for (int64_t it = (nck - 1) * stride + 1; it <= nsteps && rc == AXG_OK; ++it) {
+        rc = axg_evo_kick_plain(ctx, kt[it], dt);
+        if (!rc) rc = axg_evo_drift(ctx, kh[it]);
+      }
+    }
+  } while (0);
+  cudaStreamSynchronize(ctx->stream);
+  if (pfo) cufftDestroy(pf);
+  if (pbo) cufftDestroy(pb);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  axg_free(ctx, (void **)&ck);
+  axg_free(ctx, (void **)&adj);
+  axg_free(ctx, (void **)&Q);
+  axg_free(ctx, (void **)&fbuf);
+  ctx->flags_valid = false;
+  return rc;
+}

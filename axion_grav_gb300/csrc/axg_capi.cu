@@ -783,12 +783,13 @@ extern "C" {
 
 int axg_tile_count(void) { return axg_evo_tile_count(); }
 
-int axg_tile_info(int i, int32_t *tx, int32_t *ty, int32_t *zc) {
+int axg_tile_info(int i, int32_t *tx, int32_t *ty, int32_t *zc, int32_t *pointwise_tma) {
   if (i < 0 || i >= axg_evo_tile_count() || !tx || !ty || !zc) return AXG_ERR_ARG;
   axg_tile_cfg t = axg_evo_tile(i);
   *tx = t.tx;
   *ty = t.ty;
   *zc = t.zc;
+  if (pointwise_tma) *pointwise_tma = t.pw;
   return AXG_OK;
 }
 

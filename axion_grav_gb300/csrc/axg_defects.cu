@@ -721,7 +721,7 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
   double pos[3], dir[3], vel[3], gof, l;
   position_string(pc, seed, (uint64_t)s, pos, dir, &gof, &l);
   velocity_string(phi, phid, n, dspa, ix, iy, iz, pos, vel);
-  double *r = out + 12 * k;
+  double *r = out + 13 * k;
   r[0] = pos[0] + ix + 0.5;
   r[1] = pos[1] + iy + 0.5;
   r[2] = pos[2] + iz + 0.5;
@@ -734,6 +734,7 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
   r[9] = gof;
   r[10] = l;
   r[11] = (double)s;
+  r[12] = -1.0;
 }
 
 __global__ void __launch_bounds__(128) k_wall_fit(const double *__restrict__ ph, int n,
@@ -757,7 +758,7 @@ __global__ void __launch_bounds__(128) k_wall_fit(const double *__restrict__ ph,
   r[6] = gof;
   r[7] = a;
   r[8] = (double)s;
-  r[9] = 0.0;
+  r[9] = -1.0;
 }
 
 // add_string_length / add_wall_area sums (one block; fixed-order tree)
@@ -767,7 +768,7 @@ __global__ void k_defect_sums(const double *__restrict__ strs, int64_t ns,
   double a[5] = {0, 0, 0, 0, 0};  // sl, sqrt(v2), v2, gamma, count of v2<1
   double wsum = 0.0;
   for (int64_t k = threadIdx.x; k < ns; k += blockDim.x) {
-    const double *r = strs + 12 * k;
+    const double *r = strs + 13 * k;
     a[0] = a[0] + r[10];
     double v2 = r[6] * r[6] + r[7] * r[7];
     v2 = v2 + r[8] * r[8];
@@ -798,6 +799,146 @@ __global__ void k_defect_sums(const double *__restrict__ strs, int64_t ns,
   if (threadIdx.x == 0) out[5] = sh[0][0];
 }
 
+// ---------------- grouping (defects_3d.f90:1235-1652, 1735-2143) ----------------
+// Connected components of the fitted positions under the periodic distance
+// threshold: the partition the reference's grouping produces on one rank and
+// one thread.  Hash grid of G^3 cells (cell side >= threshold) + lock-free
+// union-find linking the larger root under the smaller, so the final label
+// of every point is the smallest list index of its component.
+constexpr int kUfMaxRetries = 1 << 20;
+
+__device__ double lat_dist_periodic(int n, const double *a, const double *b) {
+  double s = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    const double dp = fabs(a[k] - b[k]);
+    const double e = (double)n - dp;
+    const double m = dp < e ? dp : e;
+    s = s + m * m;
+  }
+  return sqrt(s);
+}
+
+__device__ int uf_find(volatile int *par, int x) {
+  while (true) {
+    const int p = par[x];
+    if (p == x) return x;
+    const int gp = par[p];
+    if (gp != p) par[x] = gp;  // path halving: a valid ancestor, benign race
+    x = p;
+  }
+}
+
+__device__ void uf_union(int *par, int a, int b, int *err) {
+  for (int it = 0; it < kUfMaxRetries; ++it) {
+    a = uf_find(par, a);
+    b = uf_find(par, b);
+    if (a == b) return;
+    if (a > b) {
+      const int t = a;
+      a = b;
+      b = t;
+    }
+    const int old = atomicCAS(&par[b], b, a);
+    if (old == b) return;
+    b = old;
+  }
+  atomicExch(err, AXG_KERR_BOUNDS);
+}
+
+__device__ __forceinline__ int cell_of(double x, int n, int G) {
+  double w = x - floor(x / n) * n;  // into [0, n)
+  int c = (int)(w * G / n);
+  return c < 0 ? 0 : (c >= G ? G - 1 : c);
+}
+
+__global__ void k_grp_init(int *par, int np) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < np) par[i] = i;
+}
+
+__global__ void k_grp_count(const double *rows, int width, int np, int n, int G, int *cell, int *count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const double *r = rows + (int64_t)width * i;
+  const int c = (cell_of(r[2], n, G) * G + cell_of(r[1], n, G)) * G + cell_of(r[0], n, G);
+  cell[i] = c;
+  atomicAdd(&count[c], 1);
+}
+
+__global__ void k_scan_int(int *a, int m) {
+  __shared__ long long carry;
+  __shared__ int sh[1024];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < m; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int v = i < m ? a[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const int x = (int)threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += x;
+      __syncthreads();
+    }
+    if (i < m) a[i] = (int)(carry + sh[threadIdx.x] - v);
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += sh[1023];
+    __syncthreads();
+  }
+}
+
+__global__ void k_grp_scatter(const int *cell, int np, const int *start, int *fill, int *sorted) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const int c = cell[i];
+  sorted[start[c] + atomicAdd(&fill[c], 1)] = i;
+}
+
+__global__ void k_grp_link(const double *rows, int width, int np, int n, int G, double th, const int *cell,
+                           const int *start, const int *count, const int *sorted, int *par, int *err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const double *ri = rows + (int64_t)width * i;
+  const int c = cell[i];
+  const int cx = c % G, cy = (c / G) % G, cz = c / (G * G);
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int nc = ((cz + dz + G) % G * G + (cy + dy + G) % G) * G + (cx + dx + G) % G;
+        for (int q = start[nc]; q < start[nc] + count[nc]; ++q) {
+          const int j = sorted[q];
+          if (j <= i) continue;
+          if (lat_dist_periodic(n, ri, rows + (int64_t)width * j) <= th) uf_union(par, i, j, err);
+        }
+      }
+}
+
+__global__ void k_grp_link_all(const double *rows, int width, int np, int n, double th, int *par, int *err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const double *ri = rows + (int64_t)width * i;
+  for (int j = i + 1; j < np; ++j)
+    if (lat_dist_periodic(n, ri, rows + (int64_t)width * j) <= th) uf_union(par, i, j, err);
+}
+
+__global__ void k_grp_label(double *rows, int width, int gcol, int vcol, int np, int *par, double *tot) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const int g = uf_find(par, i);
+  rows[(int64_t)width * i + gcol] = (double)g;
+  atomicAdd(&tot[g], rows[(int64_t)width * i + vcol]);
+}
+
+__global__ void k_grp_out(const int *par, const double *tot, int np, double t2, double t3, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np || par[i] != i) return;
+  atomicAdd(&out[0], tot[i]);
+  if (tot[i] > t2) atomicAdd(&out[1], tot[i]);
+  if (tot[i] > t3) atomicAdd(&out[2], tot[i]);
+  atomicAdd(&out[3], 1.0);
+}
+
 int grid_for(int64_t count, int per = 256) {
   int64_t b = (count + per - 1) / per;
   if (b > 152 * 32) b = 152 * 32;
@@ -820,6 +961,57 @@ int compute_phases(axg_ctx *ctx) {
     AXG_LAUNCH(ctx, "defect_phase_fp64", k_phase<double2>, grid_for(ctx->n3), 256, 0,
                (const double2 *)phi, ctx->phase, ctx->n3);
   return AXG_OK;
+}
+
+// grouping_strings / grouping_walls + the grouped branch of add_string_length
+// / add_wall_area: out = (all, groups above t2, groups above t3, #groups)
+int group_and_sum(axg_ctx *ctx, double *rows, int width, int gcol, int vcol, int64_t np64, double th, double t2,
+                  double t3, double out[4]) {
+  const int np = (int)np64;
+  const int n = (int)ctx->n;
+  int G = (int)std::floor(n / th);
+  if (G > 64) G = 64;
+  const bool grid = G >= 3;
+  const int ncell = grid ? G * G * G : 1;
+  int *ib = nullptr;
+  double *db = nullptr;
+  int rc = AXG_OK;
+  AXG_TRY(axg_alloc(ctx, (void **)&ib, sizeof(int) * ((size_t)4 * np + 3 * (size_t)ncell + 4), "grouping"));
+  do {
+    if ((rc = axg_alloc(ctx, (void **)&db, sizeof(double) * ((size_t)np + 4), "group totals"))) break;
+    int *par = ib, *cell = ib + np, *sorted = ib + 2 * np, *count = ib + 3 * (size_t)np,
+        *start = count + ncell, *fill = start + ncell;
+    double *tot = db, *dout = db + np;
+    AXG_CUDA_TRY(ctx, cudaMemsetAsync(ib + 3 * (size_t)np, 0, sizeof(int) * 3 * (size_t)ncell, ctx->stream));
+    AXG_CUDA_TRY(ctx, cudaMemsetAsync(db, 0, sizeof(double) * ((size_t)np + 4), ctx->stream));
+    const int blocks = (np + 255) / 256;
+    AXG_LAUNCH(ctx, "group_init", k_grp_init, blocks, 256, 0, par, np);
+    if (grid) {
+      AXG_LAUNCH(ctx, "group_count", k_grp_count, blocks, 256, 0, rows, width, np, n, G, cell, count);
+      AXG_CUDA_TRY(ctx, cudaMemcpyAsync(start, count, sizeof(int) * ncell, cudaMemcpyDeviceToDevice, ctx->stream));
+      AXG_LAUNCH(ctx, "group_scan", k_scan_int, 1, 1024, 0, start, ncell);
+      AXG_LAUNCH(ctx, "group_scatter", k_grp_scatter, blocks, 256, 0, cell, np, start, fill, sorted);
+      AXG_LAUNCH(ctx, "group_link", k_grp_link, blocks, 256, 0, rows, width, np, n, G, th, cell, start, count, sorted,
+                 par, ctx->d_err);
+    } else {
+      AXG_LAUNCH(ctx, "group_link_all", k_grp_link_all, blocks, 256, 0, rows, width, np, n, th, par, ctx->d_err);
+    }
+    AXG_LAUNCH(ctx, "group_label", k_grp_label, blocks, 256, 0, rows, width, gcol, vcol, np, par, tot);
+    AXG_LAUNCH(ctx, "group_out", k_grp_out, blocks, 256, 0, par, tot, np, t2, t3, dout);
+    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(out, dout, sizeof(double) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    rc = axg_evo_check_error(ctx);
+  } while (0);
+  cudaStreamSynchronize(ctx->stream);
+  axg_free(ctx, (void **)&ib);
+  axg_free(ctx, (void **)&db);
+  return rc;
+}
+
+// grouping threshold max(2, (width^2 hor)^(1/3)) (defects_3d.f90:1245-1246)
+double group_threshold(double wid, double hor) {
+  const double th = std::pow(wid * wid * hor, 1.0 / 3.0);
+  return th > 2.0 ? th : 2.0;
 }
 
 }  // namespace
@@ -854,7 +1046,6 @@ int axg_def_winding(axg_ctx *ctx, int64_t counts[3]) {
 
 int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], double svel[3],
                        int64_t counts[3]) {
-  (void)tau;
   const int which = ctx->p.flags & (AXG_F_ID_STRINGS | AXG_F_ID_WALLS | AXG_F_SPEC_EST);
   AXG_TRY(axg_def_classify(ctx, which, counts));
   const int64_t ns = counts[0], nw = counts[1];
@@ -867,7 +1058,7 @@ int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], dou
     if ((rc = axg_alloc(ctx, (void **)&cells, (size_t)(ns + nw + 1) * 8, "defect cells"))) break;
     if (ns > ctx->cap_strings) {
       axg_free(ctx, (void **)&ctx->d_strings);
-      if ((rc = axg_alloc(ctx, (void **)&ctx->d_strings, (size_t)ns * 12 * 8, "string list"))) break;
+      if ((rc = axg_alloc(ctx, (void **)&ctx->d_strings, (size_t)ns * 13 * 8, "string list"))) break;
       ctx->cap_strings = ns;
     }
     if (nw > ctx->cap_walls) {
@@ -911,6 +1102,23 @@ int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], dou
       svel[0] = svel[1] = svel[2] = 0.0;
     }
     wa[0] = wa[1] = wa[2] = h[5];
+    const double kPi = 3.14159265359, hor = tau / ctx->p.dspa;
+    if ((ctx->p.flags & AXG_F_GROUP_STRINGS) && ns > 0) {
+      double g[4];
+      const double th = group_threshold(ctx->p.width_cr / ctx->p.dspa / tau, hor);
+      if ((rc = group_and_sum(ctx, ctx->d_strings, 13, 12, 10, ns, th, 2 * hor, 2 * kPi * hor, g))) break;
+      sl[0] = g[0];
+      sl[1] = g[1];
+      sl[2] = g[2];
+    }
+    if ((ctx->p.flags & AXG_F_GROUP_WALLS) && nw > 0) {
+      double g[4];
+      const double th = group_threshold(ctx->p.thickness_cr / ctx->p.dspa / tau, hor);
+      if ((rc = group_and_sum(ctx, ctx->d_walls, 10, 9, 7, nw, th, kPi * hor * hor, 4 * kPi * hor * hor, g))) break;
+      wa[0] = g[0];
+      wa[1] = g[1];
+      wa[2] = g[2];
+    }
     ctx->last_ns = ns;
     ctx->last_nw = nw;
   } while (0);
@@ -953,7 +1161,7 @@ int axg_download_defect_lists(axg_ctx *ctx, double *strings, int64_t max_strings
   if (!ctx) return AXG_ERR_ARG;
   const int64_t ns = std::min(max_strings, ctx->last_ns), nw = std::min(max_walls, ctx->last_nw);
   if (strings && ns > 0 && ctx->d_strings)
-    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(strings, ctx->d_strings, (size_t)ns * 12 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(strings, ctx->d_strings, (size_t)ns * 13 * 8, cudaMemcpyDeviceToHost, ctx->stream));
   if (walls && nw > 0 && ctx->d_walls)
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(walls, ctx->d_walls, (size_t)nw * 10 * 8, cudaMemcpyDeviceToHost, ctx->stream));
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

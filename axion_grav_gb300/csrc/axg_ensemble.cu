@@ -71,6 +71,7 @@ int build_descriptors(axg_ensemble *e, int cfg) {
       d.tm[b][3] = c->tm.u_row[b];
       d.tm[b][4] = c->tm.u_body[b];
       d.tm[b][5] = c->tm.u_halo[b];
+      for (int q = 0; q < 4; ++q) d.pw[q] = c->tm.pw[q];
       d.phi[b] = c->phi[b];
       d.u[b] = c->u[b];
     }
@@ -302,6 +303,12 @@ int axg_ensemble_leapfrog(axg_ensemble *e, double t1, double dt, int64_t nsteps,
     c->flags_valid = false;
   }
   return AXG_OK;
+}
+
+int axg_ensemble_set_tile(axg_ensemble *e, int cfg) {
+  if (!e || cfg < 0 || cfg >= axg_evo_tile_count()) return AXG_ERR_ARG;
+  if (!tile_ok_all(e, cfg)) return ens_error(e, AXG_ERR_UNSUPPORTED, "tile shape does not fit every member");
+  return build_descriptors(e, cfg);
 }
 
 int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *best_ms) {

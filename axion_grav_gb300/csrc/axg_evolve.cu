@@ -24,6 +24,7 @@
 namespace {
 
 constexpr int kStages = 4;            // TMA ring depth (z-1, z, z+1, prefetch)
+constexpr int kPwStages = 2;          // pointwise ring depth (z, prefetch of z+1)
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz: mbarrier wait limit
 
 // ------------------------------------------------------------------------
@@ -275,6 +276,38 @@ struct StageLayout {
       (UIJ ? (2 * 6 * TX + 6 * TY * TX + 2 * 6 * TY * UHW) * (int)sizeof(R) : 0);
 };
 
+// One plane of the pointwise fields of a TX x TY column (phid, cphi, ud, cu);
+// each is a body box, so the bytes delivered equal the layout's size.
+template <typename R, int TX, int TY, bool UIJ>
+struct PwLayout {
+  using V = typename V2<R>::T;
+  static constexpr bool F32 = sizeof(R) == 4;
+  static constexpr int phid = 0;
+  static constexpr int phid_sz = align128(TX * TY * (int)sizeof(V));
+  static constexpr int cphi = phid + phid_sz;
+  static constexpr int cphi_sz = F32 ? phid_sz : 0;
+  static constexpr int ud = cphi + cphi_sz;
+  static constexpr int ud_sz = UIJ ? align128(6 * TX * TY * (int)sizeof(R)) : 0;
+  static constexpr int cu = ud + ud_sz;
+  static constexpr int cu_sz = (UIJ && F32) ? ud_sz : 0;
+  static constexpr int bytes = cu + cu_sz;
+  static constexpr int tx_bytes = TX * TY * (int)sizeof(V) * (F32 ? 2 : 1) +
+                                  (UIJ ? 6 * TX * TY * (int)sizeof(R) * (F32 ? 2 : 1) : 0);
+  static_assert(tx_bytes == bytes, "pointwise boxes must fill the layout exactly");
+};
+
+// dynamic shared memory of one fused CTA: stencil ring, pointwise ring,
+// mbarriers, alignment slack
+template <typename R, int TX, int TY, bool UIJ, bool PW>
+constexpr int fused_smem_bytes() {
+  return kStages * StageLayout<R, TX, TY, UIJ>::bytes + (PW ? kPwStages * PwLayout<R, TX, TY, UIJ>::bytes : 0) +
+         (kStages + kPwStages) * 8 + 128;
+}
+
+struct PwMaps {
+  CUtensorMap m[4];  // phid, cphi, ud, cu
+};
+
 template <typename R>
 struct FusedParams {
   typename V2<R>::T *phi_out;
@@ -305,14 +338,19 @@ __device__ __forceinline__ void tma_phi(uint32_t dst, const CUtensorMap *m, int 
 // stencil planes by TMA, compute kick + drift, store.  `gplane` counts the
 // planes this CTA has staged so far, so stage indices and mbarrier phases
 // continue across the columns a persistent CTA processes.  Returns false
-// (after recording the error) when a TMA wait timed out.
-template <typename R, int TX, int TY, bool UIJ>
+// (after recording the error) when a TMA wait timed out.  With PW the
+// pointwise fields of plane k arrive by TMA in a kPwStages ring (`gpw`
+// continues across columns like `gplane`); without it they are loaded into
+// registers at the top of each plane.
+template <typename R, int TX, int TY, bool UIJ, bool PW>
 __device__ __forceinline__ bool fused_column(const CUtensorMap *tm_prow, const CUtensorMap *tm_pbody,
                                              const CUtensorMap *tm_phalo, const CUtensorMap *tm_urow,
                                              const CUtensorMap *tm_ubody, const CUtensorMap *tm_uhalo,
-                                             const FusedParams<R> &P, int x0, int y0, int z0,
-                                             unsigned char *smem, uint64_t *bars, uint32_t &gplane) {
+                                             const CUtensorMap *tm_pw, const FusedParams<R> &P, int x0, int y0,
+                                             int z0, unsigned char *smem, uint64_t *bars, uint32_t &gplane,
+                                             unsigned char *pwsmem, uint64_t *pbars, uint32_t &gpw) {
   using L = StageLayout<R, TX, TY, UIJ>;
+  using PL = PwLayout<R, TX, TY, UIJ>;
   using V = typename V2<R>::T;
   const int n = P.n, zc = P.zc;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -344,9 +382,31 @@ __device__ __forceinline__ bool fused_column(const CUtensorMap *tm_prow, const C
     }
   };
 
+  auto pslot = [&](int k) { return (int)((gpw + (uint32_t)k) % kPwStages); };
+  auto pparity = [&](int k) { return (uint32_t)(((gpw + (uint32_t)k) / kPwStages) & 1); };
+  auto issue_pw = [&](int k) {
+    const int slot = pslot(k);
+    unsigned char *st = pwsmem + slot * PL::bytes;
+    const uint32_t bar = smem_u32(&pbars[slot]);
+    mbar_expect_tx(bar, (uint32_t)PL::tx_bytes);
+    const int z = z0 + k;
+    tma_phi<R>(smem_u32(st + PL::phid), &tm_pw[0], x0, y0, z, bar);
+    if constexpr (sizeof(R) == 4) tma_phi<R>(smem_u32(st + PL::cphi), &tm_pw[1], x0, y0, z, bar);
+    if constexpr (UIJ) {
+      tma_load_4d(smem_u32(st + PL::ud), &tm_pw[2], x0, y0, z, 0, bar);
+      if constexpr (sizeof(R) == 4) tma_load_4d(smem_u32(st + PL::cu), &tm_pw[3], x0, y0, z, 0, bar);
+    }
+  };
+
   if (tid == 0) {
+    // a persistent CTA's earlier column read these buffers (generic proxy)
+    fence_proxy_async();
     const int first = nplanes < kStages ? nplanes : kStages;
     for (int p = 0; p < first; ++p) issue(p);
+    if constexpr (PW) {
+      const int pfirst = zc < kPwStages ? zc : kPwStages;
+      for (int k = 0; k < pfirst; ++k) issue_pw(k);
+    }
   }
   auto stage_of = [&](int p) { return (int)((gplane + (uint32_t)p) % kStages); };
   auto parity_of = [&](int p) { return (uint32_t)(((gplane + (uint32_t)p) / kStages) & 1); };
@@ -362,20 +422,39 @@ __device__ __forceinline__ bool fused_column(const CUtensorMap *tm_prow, const C
     const int p = k + 1;
     const int z = z0 + k;
     const int64_t s = z * n2 + (int64_t)(y0 + ty) * n + (x0 + tx);
-    // pointwise fields of this plane (issued before the stage wait)
-    const V pd = P.phid[s];
+    // pointwise fields of this plane: registers (issued before the stage
+    // wait) or the TMA ring
+    V pd;
     V cp;
-    if constexpr (sizeof(R) == 4) cp = P.cphi[s];
     R udv[UIJ ? 6 : 1], cuv[UIJ ? 6 : 1];
-    if constexpr (UIJ) {
+    if constexpr (!PW) {
+      pd = P.phid[s];
+      if constexpr (sizeof(R) == 4) cp = P.cphi[s];
+      if constexpr (UIJ) {
 #pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        udv[c] = P.ud[c * P.n3 + s];
-        if constexpr (sizeof(R) == 4) cuv[c] = P.cu[c * P.n3 + s];
+        for (int c = 0; c < 6; ++c) {
+          udv[c] = P.ud[c * P.n3 + s];
+          if constexpr (sizeof(R) == 4) cuv[c] = P.cu[c * P.n3 + s];
+        }
       }
     }
     const int snext = stage_of(p + 1);
     ok = mbar_wait_bounded(smem_u32(&bars[snext]), parity_of(p + 1));
+    if constexpr (PW) {
+      ok = ok && mbar_wait_bounded(smem_u32(&pbars[pslot(k)]), pparity(k));
+      if (ok) {
+        const unsigned char *pws = pwsmem + pslot(k) * PL::bytes;
+        pd = reinterpret_cast<const V *>(pws + PL::phid)[ty * TX + tx];
+        if constexpr (sizeof(R) == 4) cp = reinterpret_cast<const V *>(pws + PL::cphi)[ty * TX + tx];
+        if constexpr (UIJ) {
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            udv[c] = reinterpret_cast<const R *>(pws + PL::ud)[(c * TY + ty) * TX + tx];
+            if constexpr (sizeof(R) == 4) cuv[c] = reinterpret_cast<const R *>(pws + PL::cu)[(c * TY + ty) * TX + tx];
+          }
+        }
+      }
+    }
 
     if (ok) {
       const unsigned char *sp = smem + stage_of(p - 1) * L::bytes;
@@ -526,41 +605,48 @@ __device__ __forceinline__ bool fused_column(const CUtensorMap *tm_prow, const C
       if (tid == 0) atomicCAS(P.err, 0, AXG_KERR_MBAR_TIMEOUT);
       return false;
     }
-    if (tid == 0 && p - 1 + kStages < nplanes) {
-      fence_proxy_async();
-      issue(p - 1 + kStages);
+    if (tid == 0) {
+      const bool more = p - 1 + kStages < nplanes;
+      const bool pmore = PW && k + kPwStages < zc;
+      if (more || pmore) fence_proxy_async();
+      if (more) issue(p - 1 + kStages);
+      if constexpr (PW)
+        if (pmore) issue_pw(k + kPwStages);
     }
   }
   gplane += (uint32_t)nplanes;
+  if constexpr (PW) gpw += (uint32_t)zc;
   return true;
 }
 
 __device__ __forceinline__ void init_stage_barriers(uint64_t *bars) {
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    for (int s = 0; s < kStages + kPwStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
     fence_barrier_init();
     fence_proxy_async();
   }
   __syncthreads();
 }
 
-template <typename R, int TX, int TY, bool UIJ>
+template <typename R, int TX, int TY, bool UIJ, bool PW>
 __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 : 1))
     k_fused(const __grid_constant__ CUtensorMap tm_prow, const __grid_constant__ CUtensorMap tm_pbody,
             const __grid_constant__ CUtensorMap tm_phalo, const __grid_constant__ CUtensorMap tm_urow,
             const __grid_constant__ CUtensorMap tm_ubody, const __grid_constant__ CUtensorMap tm_uhalo,
-            const FusedParams<R> P) {
+            const __grid_constant__ PwMaps pwm, const FusedParams<R> P) {
   using L = StageLayout<R, TX, TY, UIJ>;
+  using PL = PwLayout<R, TX, TY, UIJ>;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem =
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * L::bytes);
+  unsigned char *pwsmem = smem + kStages * L::bytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(pwsmem + (PW ? kPwStages * PL::bytes : 0));
   init_stage_barriers(bars);
   const int ncx = P.n / TX;
   const int x0 = (blockIdx.x % ncx) * TX, y0 = (blockIdx.x / ncx) * TY, z0 = blockIdx.y * P.zc;
-  uint32_t gplane = 0;
-  fused_column<R, TX, TY, UIJ>(&tm_prow, &tm_pbody, &tm_phalo, &tm_urow, &tm_ubody, &tm_uhalo, P, x0, y0, z0,
-                               smem, bars, gplane);
+  uint32_t gplane = 0, gpw = 0;
+  fused_column<R, TX, TY, UIJ, PW>(&tm_prow, &tm_pbody, &tm_phalo, &tm_urow, &tm_ubody, &tm_uhalo, pwm.m, P, x0,
+                                   y0, z0, smem, bars, gplane, pwsmem, bars + kStages, gpw);
 }
 
 // ------------------------------------------------------------------------
@@ -570,15 +656,17 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
 // ring (stage phases continue through `gplane`).  Per-step coefficients come
 // from device memory so the whole step sequence can be graph-captured once.
 // ------------------------------------------------------------------------
-template <typename R, int TX, int TY, bool UIJ>
+template <typename R, int TX, int TY, bool UIJ, bool PW>
 __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 : 1))
     k_fused_batch(const axg_ens_member_dev *__restrict__ mem, int nmem, long long total, int cur,
                   const axg_ens_coef *__restrict__ coefs, int step, int zc, double dspa, int *err) {
   using L = StageLayout<R, TX, TY, UIJ>;
+  using PL = PwLayout<R, TX, TY, UIJ>;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem =
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * L::bytes);
+  unsigned char *pwsmem = smem + kStages * L::bytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(pwsmem + (PW ? kPwStages * PL::bytes : 0));
   init_stage_barriers(bars);
   const axg_ens_coef &K = coefs[step];
   FusedParams<R> P;
@@ -597,7 +685,7 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
   P.d_pow2 = sizeof(R) == 8 && frexp(P.d, &ex) == 0.5;
   P.zc = zc;
   P.err = err;
-  uint32_t gplane = 0;
+  uint32_t gplane = 0, gpw = 0;
   for (long long w = blockIdx.x; w < total; w += gridDim.x) {
     int lo = 0, hi = nmem - 1;  // last member with item_begin <= w
     while (lo < hi) {
@@ -618,8 +706,9 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
     P.ud = reinterpret_cast<R *>(D.ud);
     P.cu = reinterpret_cast<R *>(D.cu);
     const CUtensorMap *tm = D.tm[cur];
-    if (!fused_column<R, TX, TY, UIJ>(&tm[0], &tm[1], &tm[2], &tm[3], &tm[4], &tm[5], P, (col % ncx) * TX,
-                                      (col / ncx) * TY, chunk * zc, smem, bars, gplane))
+    if (!fused_column<R, TX, TY, UIJ, PW>(&tm[0], &tm[1], &tm[2], &tm[3], &tm[4], &tm[5], D.pw, P,
+                                          (col % ncx) * TX, (col / ncx) * TY, chunk * zc, smem, bars, gplane, pwsmem,
+                                          bars + kStages, gpw))
       return;
   }
 }
@@ -628,7 +717,8 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
 // tile table (autotuner search space) and host-side launch
 // ------------------------------------------------------------------------
 const axg_tile_cfg kTiles[] = {
-    {32, 16, 32}, {32, 8, 32}, {32, 16, 64}, {32, 8, 64}, {32, 16, 16}, {32, 8, 16}, {32, 4, 32},
+    {32, 16, 32, 0}, {32, 8, 32, 0}, {32, 16, 64, 0}, {32, 8, 64, 0}, {32, 16, 16, 0}, {32, 8, 16, 0},
+    {32, 4, 32, 0},  {32, 4, 32, 1}, {32, 8, 32, 1},  {32, 4, 64, 1}, {32, 4, 16, 1}, {32, 8, 64, 1},
 };
 constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
 
@@ -700,36 +790,67 @@ int build_tmaps(axg_ctx *ctx, int cfg) {
       ctx->tm.u_halo[b] = ctx->tm.phi_halo[b];
     }
   }
+  // pointwise planes (body boxes of phid, cphi, ud, cu); unused maps copy a valid one
+  if (fp32) {
+    cuuint64_t dims[3] = {n, n, n};
+    cuuint64_t str[2] = {n * 8, n * n * 8};
+    cuuint32_t body[3] = {(cuuint32_t)t.tx, (cuuint32_t)t.ty, 1};
+    AXG_TRY(encode(ctx, &ctx->tm.pw[0], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, ctx->phid, dims, str, body));
+    AXG_TRY(encode(ctx, &ctx->tm.pw[1], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, ctx->cphi, dims, str, body));
+  } else {
+    cuuint64_t dims[4] = {2, n, n, n};
+    cuuint64_t str[3] = {16, n * 16, n * n * 16};
+    cuuint32_t body[4] = {2, (cuuint32_t)t.tx, (cuuint32_t)t.ty, 1};
+    AXG_TRY(encode(ctx, &ctx->tm.pw[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, ctx->phid, dims, str, body));
+    ctx->tm.pw[1] = ctx->tm.pw[0];
+  }
+  if (uij) {
+    const CUtensorMapDataType dt = fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    cuuint64_t dims[4] = {n, n, n, 6};
+    cuuint64_t str[3] = {n * rs, n * n * rs, n * n * n * rs};
+    cuuint32_t body[4] = {(cuuint32_t)t.tx, (cuuint32_t)t.ty, 1, 6};
+    AXG_TRY(encode(ctx, &ctx->tm.pw[2], dt, 4, ctx->ud, dims, str, body));
+    if (fp32) AXG_TRY(encode(ctx, &ctx->tm.pw[3], dt, 4, ctx->cu, dims, str, body));
+    else ctx->tm.pw[3] = ctx->tm.pw[2];
+  } else {
+    ctx->tm.pw[2] = ctx->tm.pw[3] = ctx->tm.pw[0];
+  }
   ctx->tm.valid = true;
   ctx->tm.cfg = cfg;
   return AXG_OK;
 }
 
-template <typename R, int TX, int TY, bool UIJ>
+template <typename R, int TX, int TY, bool UIJ, bool PW>
 int launch_fused_t(axg_ctx *ctx, const FusedParams<R> &P, const char *name) {
-  using L = StageLayout<R, TX, TY, UIJ>;
-  const int smem = kStages * L::bytes + kStages * 8 + 128;
+  constexpr int smem = fused_smem_bytes<R, TX, TY, UIJ, PW>();
   static bool attr_set = false;
   if (!attr_set) {
-    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_fused<R, TX, TY, UIJ>,
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_fused<R, TX, TY, UIJ, PW>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr_set = true;
   }
   const int b = ctx->cur;
   dim3 grid((unsigned)((ctx->n / TX) * (ctx->n / TY)), (unsigned)(ctx->n / P.zc));
   dim3 block(TX, TY);
-  AXG_LAUNCH(ctx, name, (k_fused<R, TX, TY, UIJ>), grid, block, smem, ctx->tm.phi_row[b],
+  PwMaps pwm;
+  for (int q = 0; q < 4; ++q) pwm.m[q] = ctx->tm.pw[q];
+  AXG_LAUNCH(ctx, name, (k_fused<R, TX, TY, UIJ, PW>), grid, block, smem, ctx->tm.phi_row[b],
              ctx->tm.phi_body[b], ctx->tm.phi_halo[b], ctx->tm.u_row[b], ctx->tm.u_body[b],
-             ctx->tm.u_halo[b], P);
+             ctx->tm.u_halo[b], pwm, P);
   return AXG_OK;
 }
 
 template <typename R, bool UIJ>
 int launch_fused_cfg(axg_ctx *ctx, const FusedParams<R> &P, int cfg, const char *name) {
   const axg_tile_cfg t = kTiles[cfg];
-  if (t.tx == 32 && t.ty == 16) return launch_fused_t<R, 32, 16, UIJ>(ctx, P, name);
-  if (t.tx == 32 && t.ty == 8) return launch_fused_t<R, 32, 8, UIJ>(ctx, P, name);
-  if (t.tx == 32 && t.ty == 4) return launch_fused_t<R, 32, 4, UIJ>(ctx, P, name);
+  if (t.pw) {
+    if (t.tx == 32 && t.ty == 8) return launch_fused_t<R, 32, 8, UIJ, true>(ctx, P, name);
+    if (t.tx == 32 && t.ty == 4) return launch_fused_t<R, 32, 4, UIJ, true>(ctx, P, name);
+  } else {
+    if (t.tx == 32 && t.ty == 16) return launch_fused_t<R, 32, 16, UIJ, false>(ctx, P, name);
+    if (t.tx == 32 && t.ty == 8) return launch_fused_t<R, 32, 8, UIJ, false>(ctx, P, name);
+    if (t.tx == 32 && t.ty == 4) return launch_fused_t<R, 32, 4, UIJ, false>(ctx, P, name);
+  }
   return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "tile configuration");
 }
 
@@ -755,7 +876,12 @@ int axg_evo_tile_supported(const axg_ctx *ctx, int i) {
   auto a = [](int b) { return (b + 127) / 128 * 128; };
   int st = a((t.ty + 2) * t.tx * vs) + 2 * a(t.ty * phw * vs);
   if (uij) st += 2 * a(6 * t.tx * rs) + a(6 * t.ty * t.tx * rs) + 2 * a(6 * t.ty * uhw * rs);
-  if (kStages * st + kStages * 8 + 128 > 227 * 1024) return 0;
+  int pw = 0;
+  if (t.pw) {
+    if (t.ty != 4 && t.ty != 8) return 0;  // instantiated pointwise-TMA tiles
+    pw = a(t.tx * t.ty * vs) * (fp32 ? 2 : 1) + (uij ? a(6 * t.tx * t.ty * rs) * (fp32 ? 2 : 1) : 0);
+  }
+  if (kStages * st + kPwStages * pw + (kStages + kPwStages) * 8 + 128 > 227 * 1024) return 0;
   return 1;
 }
 
@@ -896,25 +1022,25 @@ int axg_evo_check_error(axg_ctx *ctx) {
 }
 
 namespace {
-template <typename R, int TX, int TY, bool UIJ>
+template <typename R, int TX, int TY, bool UIJ, bool PW>
 int launch_batch_t(axg_ctx *ctx, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem, long long total,
                    int cur, const axg_ens_coef *d_coef, int step, int zc, double dspa, int *d_err) {
-  using L = StageLayout<R, TX, TY, UIJ>;
-  const int smem = kStages * L::bytes + kStages * 8 + 128;
+  constexpr int smem = fused_smem_bytes<R, TX, TY, UIJ, PW>();
   static bool attr_set = false;
   if (!attr_set) {
-    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_fused_batch<R, TX, TY, UIJ>,
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_fused_batch<R, TX, TY, UIJ, PW>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr_set = true;
   }
   int per_sm = 0;
-  AXG_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_batch<R, TX, TY, UIJ>, TX * TY, smem));
+  AXG_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_batch<R, TX, TY, UIJ, PW>,
+                                                                  TX * TY, smem));
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   long long grid = (long long)std::max(per_sm, 1) * std::max(sms, 1);
   if (grid > total) grid = total;
-  k_fused_batch<R, TX, TY, UIJ><<<(unsigned)grid, dim3(TX, TY), smem, stream>>>(d_mem, nmem, total, cur, d_coef,
-                                                                               step, zc, dspa, d_err);
+  k_fused_batch<R, TX, TY, UIJ, PW><<<(unsigned)grid, dim3(TX, TY), smem, stream>>>(d_mem, nmem, total, cur,
+                                                                                   d_coef, step, zc, dspa, d_err);
   ctx->launches++;
   AXG_CUDA_TRY(ctx, cudaGetLastError());
   return AXG_OK;
@@ -925,29 +1051,26 @@ int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_d
                        long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,
                        int *d_err, bool fp32, bool uij, double dspa) {
   const axg_tile_cfg t = kTiles[cfg];
-#define AXG_BATCH(R, TY_, U)                                                                              \
-  return launch_batch_t<R, 32, TY_, U>(any, stream, d_mem, nmem, total_items, cur, d_coef, step, t.zc, dspa, d_err)
-  if (fp32) {
-    if (uij) {
-      if (t.ty == 16) AXG_BATCH(float, 16, true);
-      if (t.ty == 8) AXG_BATCH(float, 8, true);
-      if (t.ty == 4) AXG_BATCH(float, 4, true);
-    } else {
-      if (t.ty == 16) AXG_BATCH(float, 16, false);
-      if (t.ty == 8) AXG_BATCH(float, 8, false);
-      if (t.ty == 4) AXG_BATCH(float, 4, false);
-    }
-  } else {
-    if (uij) {
-      if (t.ty == 16) AXG_BATCH(double, 16, true);
-      if (t.ty == 8) AXG_BATCH(double, 8, true);
-      if (t.ty == 4) AXG_BATCH(double, 4, true);
-    } else {
-      if (t.ty == 16) AXG_BATCH(double, 16, false);
-      if (t.ty == 8) AXG_BATCH(double, 8, false);
-      if (t.ty == 4) AXG_BATCH(double, 4, false);
-    }
+#define AXG_BATCH(R, TY_, U, PW_)                                                                         \
+  return launch_batch_t<R, 32, TY_, U, PW_>(any, stream, d_mem, nmem, total_items, cur, d_coef, step, t.zc, dspa, \
+                                            d_err)
+#define AXG_BATCH_TY(R, U)                        \
+  if (t.pw) {                                     \
+    if (t.ty == 8) AXG_BATCH(R, 8, U, true);      \
+    if (t.ty == 4) AXG_BATCH(R, 4, U, true);      \
+  } else {                                        \
+    if (t.ty == 16) AXG_BATCH(R, 16, U, false);   \
+    if (t.ty == 8) AXG_BATCH(R, 8, U, false);     \
+    if (t.ty == 4) AXG_BATCH(R, 4, U, false);     \
   }
+  if (fp32) {
+    if (uij) { AXG_BATCH_TY(float, true) }
+    else { AXG_BATCH_TY(float, false) }
+  } else {
+    if (uij) { AXG_BATCH_TY(double, true) }
+    else { AXG_BATCH_TY(double, false) }
+  }
+#undef AXG_BATCH_TY
 #undef AXG_BATCH
   return axg_set_error(any, AXG_ERR_UNSUPPORTED, "tile configuration");
 }

@@ -18,14 +18,17 @@
 #define AXG_KERR_BOUNDS 2
 
 // Fused-kernel tile configurations known to the autotuner.
+// pw = 1: the pointwise fields (phi', u', compensations) are staged by TMA
+// too, one plane ahead, instead of being loaded into registers.
 struct axg_tile_cfg {
-  int tx, ty, zc;
+  int tx, ty, zc, pw;
 };
 
 // Device-side descriptor of one ensemble member (tensor maps of both
 // ping-pong buffers plus the field pointers); 64-byte aligned for TMA.
 struct alignas(64) axg_ens_member_dev {
   CUtensorMap tm[2][6];  // [buffer][phi_row, phi_body, phi_halo, u_row, u_body, u_halo]
+  CUtensorMap pw[4];     // pointwise planes: phid, cphi, ud, cu
   void *phi[2], *phid, *cphi, *u[2], *ud, *cu;
   int64_t n3;
   int32_t n, ncols;
@@ -49,6 +52,7 @@ struct axg_tmaps {
   int cfg = -1;
   CUtensorMap phi_row[2], phi_body[2], phi_halo[2];
   CUtensorMap u_row[2], u_body[2], u_halo[2];
+  CUtensorMap pw[4];  // phid, cphi, ud, cu (body boxes; not ping-ponged)
 };
 
 struct axg_ctx {
@@ -89,6 +93,8 @@ struct axg_ctx {
   double *spec_largeq0 = nullptr, *spec_dq = nullptr;  // per ij
   std::vector<double> h_mat_spec, h_largeq, h_dq, h_wav;
   std::vector<double> last_power;
+  std::vector<double> last_mat_div;  // deconvolution matrix after the division by mode counts
+  std::vector<double> last_cov;      // MC covariance of the last spectrum (num_cov)
   double2 *spec_buf = nullptr;  // (N/deg)^3 complex
   cufftHandle plan_spec = 0;
   bool plan_spec_ok = false;

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <vector>
 
+#include "axg_detmath.h"
 #include "axg_internal.h"
 
 namespace {
@@ -244,6 +245,50 @@ int pp_inverse(int n, double *ap) {
   return 0;
 }
 
+// estimate_covmat (spectrum.f90:593-641): Gaussian modes with the measured
+// spectrum (Philox stream 16 + iter), sigma per bin of nint(q/dq + 0.5)
+__global__ void k_mc_fill(double2 *F, int m, double dwav, double dq, int nb, const double *sigma, uint64_t seed,
+                          uint32_t iter) {
+  const int64_t m3 = (int64_t)m * m * m;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m3; s += stride) {
+    const int ix = (int)(s % m), iy = (int)((s / m) % m), iz = (int)(s / ((int64_t)m * m));
+    const double kx = kint(ix, m), ky = kint(iy, m), kz = kint(iz, m);
+    const double q = __dmul_rn(__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz))), dwav);
+    const double id = round(__dadd_rn(__ddiv_rn(q, dq), 0.5));
+    if (id <= nb) {
+      const axd_u32x4 r = axd_draw(seed, 16u + iter, 0u, (uint64_t)s);
+      const double u1 = axd_u01_open0(r.v[0], r.v[1]), u2 = axd_u01(r.v[2], r.v[3]);
+      const double rad = sqrt(-2.0 * log(u1));
+      double sn, cs;
+      sincos(6.283185307179586 * u2, &sn, &cs);
+      const double sg = sigma[(int)id - 1];
+      F[s] = make_double2(rad * cs * sg, rad * sn * sg);
+    } else {
+      F[s] = make_double2(0.0, 0.0);
+    }
+  }
+}
+
+// masking (spectrum.f90:648): zero coarse cells holding a masked fine cell
+__global__ void k_mc_mask(double2 *F, const int8_t *__restrict__ flags, int n, int deg) {
+  const int m = n / deg;
+  const int64_t m3 = (int64_t)m * m * m, n2 = (int64_t)n * n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < m3; c += stride) {
+    const int ix = (int)(c % m), iy = (int)((c / m) % m), iz = (int)(c / ((int64_t)m * m));
+    bool masked = false;
+    for (int z0 = iz * deg; z0 < (iz + 1) * deg && !masked; ++z0)
+      for (int y0 = iy * deg; y0 < (iy + 1) * deg && !masked; ++y0)
+        for (int x0 = ix * deg; x0 < (ix + 1) * deg; ++x0)
+          if (flags[z0 * n2 + (int64_t)y0 * n + x0] & 4) {
+            masked = true;
+            break;
+          }
+    if (masked) F[c] = make_double2(0.0, 0.0);
+  }
+}
+
 int grid_for(int64_t count) {
   int64_t b = (count + 255) / 256;
   if (b > 152 * 16) b = 152 * 16;
@@ -398,6 +443,8 @@ int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, d
       kk = kk + j;
     }
     ctx->last_power = pw;
+    ctx->last_mat_div = mat;
+    ctx->last_cov.clear();
     for (int i = 0; i < nb; ++i) {
       if (wave) wave[i] = (ctx->h_wav[i + 1] + ctx->h_wav[i]) / 2;
       power[i] = pw[i];
@@ -431,6 +478,160 @@ int axg_compute_crho(axg_ctx *ctx, double *rho) {
     r = r + ctx->last_power[i - 1] * q2dq;
   }
   *rho = r;
+  return AXG_OK;
+}
+}
+
+// estimate_covmat (spectrum.f90:569-734) on the last spectrum estimate
+int axg_spec_covariance(axg_ctx *ctx, int min_mc, int max_mc, double tol, double *cov_out, int *iterations) {
+  if (ctx->last_power.empty() || ctx->last_mat_div.empty())
+    return axg_set_error(ctx, AXG_ERR_STATE, "no spectrum estimated yet");
+  if (!ctx->flags_valid) return axg_set_error(ctx, AXG_ERR_STATE, "mask of the last classification is stale");
+  const int nb = ctx->p.num_bin;
+  const int num_cov = nb * (nb + 1) / 2;
+  const int deg = 1 << ctx->p.degrade_spec;
+  const int n = (int)ctx->n, m = n / deg;
+  const int64_t m3 = (int64_t)m * m * m;
+  const double dspa_spec = ctx->p.dspa * deg;
+  const double dwav = kRefTwoPi / dspa_spec / m;
+  const double dq = ctx->h_wav[1] - ctx->h_wav[0];
+  std::vector<double> sigma(nb), cov(num_cov, 0.0), tmp((size_t)num_cov * max_mc, 0.0), pw0(nb), pw(nb);
+  for (int i = 0; i < nb; ++i) {
+    const double pwr = ctx->last_power[i];
+    sigma[i] = std::sqrt(pwr > 0 ? pwr / 2 : 0.0) / (double)m3;
+  }
+  double *scr = nullptr;
+  AXG_TRY(axg_alloc(ctx, (void **)&scr, sizeof(double) * (size_t)(3 * nb), "covariance scratch"));
+  int rc = AXG_OK, iter;
+  double *d_sigma = scr, *d_pow = scr + nb, *d_cnt = scr + 2 * nb;
+  for (iter = 1; iter <= max_mc && rc == AXG_OK; ++iter) {
+    if (iter == 1) AXG_CUDA_TRY(ctx, cudaMemcpyAsync(d_sigma, sigma.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, ctx->stream));
+    AXG_CUDA_TRY(ctx, cudaMemsetAsync(d_pow, 0, sizeof(double) * 2 * nb, ctx->stream));
+    AXG_LAUNCH(ctx, "mc_fill", k_mc_fill, grid_for(m3), 256, 0, ctx->spec_buf, m, dwav, dq, nb, d_sigma,
+               (uint64_t)ctx->p.seed, (uint32_t)iter);
+    AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
+                                    (cufftDoubleComplex *)ctx->spec_buf, CUFFT_FORWARD));
+    AXG_LAUNCH(ctx, "mc_mask", k_mc_mask, grid_for(m3), 256, 0, ctx->spec_buf, ctx->flags, n, deg);
+    AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
+                                    (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
+    AXG_LAUNCH(ctx, "mc_bin", k_spec_bin, 152 * 4, 256, 2 * nb * sizeof(double), ctx->spec_buf, m, dwav, dq, 1.0,
+               1.0, nb, d_pow, d_cnt);
+    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(pw0.data(), d_pow, sizeof(double) * nb, cudaMemcpyDeviceToHost, ctx->stream));
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    // pow = mat_deconv pow0 - power (dspmv, beta = 1)
+    const std::vector<double> &M = ctx->last_mat_div;
+    for (int i = 0; i < nb; ++i) pw[i] = -ctx->last_power[i];
+    int kk = 1;
+    for (int j = 1; j <= nb; ++j) {
+      double temp1 = pw0[j - 1], temp2 = 0.0;
+      int k = kk;
+      for (int i = 1; i <= j - 1; ++i) {
+        pw[i - 1] = pw[i - 1] + temp1 * M[k - 1];
+        temp2 = temp2 + M[k - 1] * pw0[i - 1];
+        ++k;
+      }
+      pw[j - 1] = pw[j - 1] + temp1 * M[kk + j - 2] + temp2;
+      kk = kk + j;
+    }
+    for (int i = 1; i <= nb; ++i)
+      for (int j = 1; j <= i; ++j) {
+        const int ij = i * (i - 1) / 2 + j;
+        const double u = pw[i - 1] * pw[j - 1];
+        tmp[(size_t)(iter - 1) * num_cov + ij - 1] = cov[ij - 1];
+        for (int k = 1; k <= iter - 1; ++k) tmp[(size_t)(k - 1) * num_cov + ij - 1] += u;
+        cov[ij - 1] = cov[ij - 1] + u;
+      }
+    if (iter < min_mc) continue;
+    // jackknife convergence on the diagonal (spectrum.f90:696-718)
+    double diff = 0.0;
+    for (int i = 1; i <= nb; ++i) {
+      const int ij = i * (i + 1) / 2;
+      double u = 0.0, v = 0.0;
+      for (int k = 1; k <= iter; ++k) {
+        const double x = tmp[(size_t)(k - 1) * num_cov + ij - 1] / (iter - 1);
+        u = u + x;
+        v = v + x * x;
+      }
+      u = u / iter;
+      v = v / iter;
+      v = std::sqrt(v - u * u);
+      const double x = cov[ij - 1] / iter;
+      const double r = v / x;
+      diff = diff > r ? diff : r;
+    }
+    if (diff < tol) break;
+  }
+  cudaStreamSynchronize(ctx->stream);
+  axg_free(ctx, (void **)&scr);
+  if (rc != AXG_OK) return rc;
+  if (iter > max_mc) iter = max_mc + 1;
+  for (int ij = 0; ij < num_cov; ++ij) cov[ij] = cov[ij] / iter;
+  ctx->last_cov = cov;
+  if (cov_out) std::copy(cov.begin(), cov.end(), cov_out);
+  if (iterations) *iterations = iter;
+  return AXG_OK;
+}
+
+extern "C" {
+int axg_spectrum_covariance(axg_ctx *ctx, int min_mc, int max_mc, double tol, double *cov, int *iterations) {
+  if (!ctx || min_mc < 2 || max_mc < min_mc || !(tol > 0)) return AXG_ERR_ARG;
+  return axg_spec_covariance(ctx, min_mc, max_mc, tol, cov, iterations);
+}
+
+// compute_crho (spectrum.f90:316-342) with the covariance term of the last MC run
+int axg_compute_crho_cov(axg_ctx *ctx, double *rho, double *drho) {
+  if (!ctx || !rho || !drho) return AXG_ERR_ARG;
+  if (ctx->last_power.empty() || ctx->last_cov.empty())
+    return axg_set_error(ctx, AXG_ERR_STATE, "needs axg_spectrum_estimation and axg_spectrum_covariance first");
+  const int nb = ctx->p.num_bin;
+  const std::vector<double> &w = ctx->h_wav;
+  double r = 0.0, d = 0.0;
+  for (int i = 1; i <= nb; ++i) {
+    double dd = 0.0;
+    for (int j = 1; j <= i; ++j) {
+      const int ij = i * (i - 1) / 2 + j;
+      const double q = (w[j] + w[j - 1]) / 2, dq = w[j] - w[j - 1];
+      double q2dq = q * q * dq / kRefPi / kRefPi;
+      if (j == i) q2dq = q2dq / 2;
+      dd = dd + ctx->last_cov[ij - 1] * q2dq;
+    }
+    const double q = (w[i] + w[i - 1]) / 2, dq = w[i] - w[i - 1];
+    const double q2dq = q * q * dq / kRefTwoPi / kRefPi;
+    d = d + dd * q2dq;
+    r = r + ctx->last_power[i - 1] * q2dq;
+  }
+  *rho = r;
+  *drho = std::sqrt(d);
+  return AXG_OK;
+}
+
+// get_epsilon (spectrum.f90:1002-1036) for one pair of output times
+int axg_epsilon(int32_t nb, const double *wav, const double *p1, const double *p2, const double *c1,
+                const double *c2, double tau1, double tau2, double *eps, double *deps) {
+  if (nb < 1 || !wav || !p1 || !p2 || !c1 || !c2 || !eps || !deps) return AXG_ERR_ARG;
+  const double tau = (tau2 + tau1) / 2;
+  const double f = tau / 2 / kRefTwoPi;
+  double num = 0.0, den = 0.0;
+  for (int i = 1; i <= nb; ++i) {
+    const double d = p2[i - 1] - p1[i - 1];
+    const double q = (wav[i - 1] + wav[i]) / 2;
+    num = num + d * q * q;
+    den = den + d * q;
+  }
+  const double e = num / den * f;
+  double de = 0.0;
+  for (int i = 1; i <= nb; ++i) {
+    const double d1 = (wav[i - 1] + wav[i]) / 2;
+    for (int j = 1; j <= i; ++j) {
+      const int ij = i * (i - 1) / 2 + j;
+      const double d2 = (wav[j - 1] + wav[j]) / 2;
+      double d = (1 - e / d1 / f) * (1 - e / d2 / f) * (c2[ij - 1] + c1[ij - 1]) * d1 * d1 * d2 * d2;
+      if (j != i) d = d * 2;
+      de = de + d;
+    }
+  }
+  *eps = e;
+  *deps = std::sqrt(de / den / den) * f;
   return AXG_OK;
 }
 }

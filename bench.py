@@ -46,6 +46,24 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def replica_time_ms(ms: float, dist) -> float:
+    """The job's time is the slowest replica's: max over ranks of the timed
+    region (NCCL on the GPU, gloo on host tensors)."""
+    if dist is None:
+        return ms
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, sites: float, steps: int, ms: float) -> float:
+    """Whole-job site-updates/s: every replica advances its own lattice."""
+    return world * sites * steps / (ms * 1e-3)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -263,6 +281,30 @@ def bench_ensemble(ag, steps, device, sizes=ENSEMBLE_SIZES):
         ens.close()
 
 
+def bench_adjoint(ag, device, n=256, steps=256, stride=64):
+    """Config 4 at reduced length: gradient of J = band-integrated GW energy
+    (k in [m_r/8, m_r/2]) with respect to lambda and the initial fields, by
+    the hand-written adjoint (checkpoint every `stride` steps); its cost
+    against a plain FP64 forward run of the same steps."""
+    p = ag.default_params(ngrid=n, precision=ag.PREC_FP64_PLAIN, gw_mode=ag.GW_UIJ, potential=ag.POT_QUARTIC,
+                          dspa=1.0, sigma_cr=1.0, vev=1.0, seed=1, device=device, **{"lambda": 1.0})
+    t1, dt = 1.0, 0.2
+    with ag.Lattice(p) as lat:
+        lat.ic_gaussian_flat(kcut=1.0, realisation=0)
+        lat.leapfrog(t1, dt, 4, True, True)  # warm-up (plans, first launches)
+        lat.ic_gaussian_flat(kcut=1.0, realisation=0)
+        lat.synchronize()
+        lat.event_record(0)
+        lat.leapfrog(t1, dt, steps, True, True)
+        lat.event_record(1)
+        plain = lat.event_elapsed(0, 1)
+        lat.ic_gaussian_flat(kcut=1.0, realisation=0)
+        J, dl, _, _, mf, mr = lat.adjoint_gw_band(t1, dt, steps, stride, 0.125, 0.5, want_grads=False)
+    return {"n": n, "steps": steps, "stride": stride, "J": J, "dJ_dlambda": dl, "ms_plain_forward": plain,
+            "ms_forward_with_checkpoints": mf, "ms_reverse": mr, "cost_vs_forward": (mf + mr) / plain,
+            "precision": "fp64_plain", "timing": "CUDA events on the library stream"}
+
+
 def accuracy_fp32(ag, n, steps, device):
     """GW (u_ij TT) spectrum and field moments of the FP32-mixed path against
     the FP64-plain path (bit-identical to the FP64 CPU restatement) after the
@@ -361,6 +403,9 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy block")
     ap.add_argument("--accuracy-steps", type=int, default=100)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient cost block")
+    ap.add_argument("--no-phi-only", action="store_true", help="skip the phi-only (no u_ij) figures")
+    ap.add_argument("--adjoint-steps", type=int, default=256)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -388,13 +433,9 @@ def main():
     e2e = bench_e2e(ag, lat, n, args.e2e_interval, args.e2e_reps, r32["t"], r32["dt"]) if rank == 0 else None
     lat.close()
 
-    ms = r32["ms"]
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replica_time_ms(r32["ms"], dist)
     sites = float(n) ** 3
-    value = world * sites * args.steps / (ms * 1e-3)
+    value = job_rate(world, sites, args.steps, ms)
 
     peak, peak_kind = measured_peaks()
     kern = {k: (l, t) for k, l, t in r32["kernels"]}
@@ -415,13 +456,28 @@ def main():
         r64.pop("lat").close()
         k64 = {k: (l, t) for k, l, t in r64["kernels"]}
         st64 = max(3, args.steps // 8)
-        v64 = world * sites * st64 / (r64["ms"] * 1e-3)
+        v64 = job_rate(world, sites, st64, replica_time_ms(r64["ms"], dist))
         byts = sum(BYTES_PER_SITE.get(k, 0) * sites * l for k, (l, t) in k64.items())
         tms = sum(t for k, (l, t) in k64.items())
         fp64 = {"value": v64, "ms_per_step": r64["ms"] / st64, "steps": st64,
                 "kernels": {k: {"launches": l, "avg_ms": t / max(l, 1)} for k, (l, t) in k64.items()},
                 "hbm_frac": (byts / (tms * 1e-3) / 1e9) / peak if tms > 0 else None,
                 "fp32_mixed_speedup": value / v64 / world * world}
+
+    phi_only = None
+    if not args.no_phi_only:
+        phi_only = {}
+        for name, prec, st in (("fp32_mixed", ag.PREC_FP32_MIXED, args.steps),
+                               ("fp64_plain", ag.PREC_FP64_PLAIN, max(3, args.steps // 4))):
+            r = bench_ours(ag, n, prec, ag.GW_NONE, st, args.warmup, dist, local)
+            r.pop("lat").close()
+            kk = {k: (l, t) for k, l, t in r["kernels"]}
+            byts = sum(BYTES_PER_SITE_PHI_ONLY.get(k, BYTES_PER_SITE.get(k, 0)) * sites * l for k, (l, t) in kk.items())
+            tms = sum(t for k, (l, t) in kk.items())
+            phi_only[name] = {"value": job_rate(world, sites, st, replica_time_ms(r["ms"], dist)),
+                              "ms_per_step": r["ms"] / st, "steps": st,
+                              "hbm_frac": (byts / (tms * 1e-3) / 1e9) / peak if tms > 0 else None,
+                              "tile": r["tile_shape"]}
 
     ensemble = None
     if not args.no_ensemble:
@@ -435,6 +491,13 @@ def main():
             accuracy = accuracy_fp32(ag, n, args.accuracy_steps, local)
         except Exception as exc:
             accuracy = {"error": str(exc)}
+
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        try:
+            adjoint = bench_adjoint(ag, local, steps=args.adjoint_steps)
+        except Exception as exc:
+            adjoint = {"error": str(exc)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -460,6 +523,7 @@ def main():
                        "tile": r32["tile_shape"]},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r32["launches"],
             "clocks": r32["clocks"], "fp64_plain": fp64, "ensemble": ensemble, "accuracy": accuracy,
+            "adjoint": adjoint, "phi_only": phi_only,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

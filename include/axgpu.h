@@ -53,6 +53,8 @@ extern "C" {
 #define AXG_F_SPEC_EST 4
 #define AXG_F_GRAV_SPEC 8
 #define AXG_F_INITIAL_LOOP 16
+#define AXG_F_GROUP_STRINGS 32 /* group_strings: connected string groups (defects_3d.f90:1235) */
+#define AXG_F_GROUP_WALLS 64   /* group_walls (defects_3d.f90:1735) */
 
 /* ---- potential model ---- */
 #define AXG_POT_REFERENCE 0 /* potential.f90:34-79 thermal mass + IILM tilt */
@@ -156,9 +158,11 @@ int axg_leapfrog(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_h
 /* Tile shapes of the fused kick+drift kernel: a CTA owns a tx x ty column of
  * the lattice and marches through zc z-planes.  The autotuner times every
  * shape the lattice supports for `steps` steps on a snapshot of the state
- * (restored afterwards) and keeps the fastest. */
+ * (restored afterwards) and keeps the fastest.  *pointwise_tma (may be NULL)
+ * is 1 for shapes that also stage the pointwise fields (phi', u' and the
+ * compensations) by TMA, one plane ahead. */
 int axg_tile_count(void);
-int axg_tile_info(int i, int32_t *tx, int32_t *ty, int32_t *zc);
+int axg_tile_info(int i, int32_t *tx, int32_t *ty, int32_t *zc, int32_t *pointwise_tma);
 int axg_set_tile(axg_ctx *ctx, int cfg);
 int axg_autotune(axg_ctx *ctx, int steps, int *best_cfg, double *best_ms_per_step);
 
@@ -193,8 +197,9 @@ int axg_string_winding(axg_ctx *ctx, int64_t counts[3]);
 int axg_id_defects(axg_ctx *ctx, int64_t idx, double tau, double sl[3], double wa[3],
                    double svel[3], int64_t counts[3]);
 /* Per-cell fit results of the last axg_id_defects, in cell order (z, y, x).
- * strings: [ns][12] = pos(3) dir(3) vel(3) gof sl cell; walls: [nw][10] =
- * pos(3) dir(3) gof wa cell pad. */
+ * strings: [ns][13] = pos(3) dir(3) vel(3) gof sl cell group; walls: [nw][10] =
+ * pos(3) dir(3) gof wa cell group.  group = smallest list index of the
+ * connected group when AXG_F_GROUP_STRINGS / AXG_F_GROUP_WALLS is set, else -1. */
 int axg_download_defect_lists(axg_ctx *ctx, double *strings, int64_t max_strings, double *walls,
                               int64_t max_walls);
 
@@ -211,6 +216,21 @@ int axg_spectrum_estimation(axg_ctx *ctx, double tau, double *wave, double *powe
 /* compute_crho (spectrum.f90:316-342) from the last power spectrum (no
  * covariance: drho = 0). */
 int axg_compute_crho(axg_ctx *ctx, double *rho);
+/* estimate_covmat (spectrum.f90:569-734): Monte-Carlo covariance (num_bin *
+ * (num_bin+1)/2, packed) of the last spectrum estimate, Gaussian fields with
+ * that spectrum masked like the data (Philox draws in place of VSL streams);
+ * stops after the jackknife test of the diagonal falls below tol (reference:
+ * min_mc 10, max_mc 100, tol 0.1).  A negative deconvolved power contributes
+ * sigma = 0.  *iterations = MC realisations used (max_mc + 1 when the test
+ * never passed, as the reference divides by it). */
+int axg_spectrum_covariance(axg_ctx *ctx, int min_mc, int max_mc, double tol, double *cov,
+                            int *iterations);
+/* compute_crho with the covariance term of the last axg_spectrum_covariance. */
+int axg_compute_crho_cov(axg_ctx *ctx, double *rho, double *drho);
+/* get_epsilon (spectrum.f90:956-1040) for one pair of output times: wav has
+ * num_bin+1 bin edges, p1/p2 the power spectra, c1/c2 their covariances. */
+int axg_epsilon(int32_t nb, const double *wav, const double *p1, const double *p2, const double *c1,
+                const double *c2, double tau1, double tau2, double *eps, double *deps);
 
 /* ------------------------------------------------------------------ */
 /* initial conditions (initial.f90) and diagnostics                    */
@@ -256,6 +276,27 @@ int axg_kernel_timing(axg_ctx *ctx, int i, char *name, int64_t name_len, int64_t
 int axg_launch_count(const axg_ctx *ctx, int64_t *launches);
 
 /* ------------------------------------------------------------------ */
+/* adjoint (no counterpart in the reference)                            */
+/* ------------------------------------------------------------------ */
+/* Gradient of the band-integrated GW energy
+ *   J = sum_{kmin <= |k| <= kmax} 1/2 sum_ij (|W'_TT|^2 + k^2 |W_TT|^2)
+ * (the numerator of axg_grav_spec_estimation with gw_mode UIJ, summed over
+ * the band, at the end of the run) after the leapfrog of axg_leapfrog(t1, dt,
+ * nsteps, first_half, last_half) from the current state.  Forward run with a
+ * checkpoint every `stride` steps; reverse sweep steps the state back by
+ * time-reversibility (re-anchored on each checkpoint) and applies the
+ * hand-written adjoint of each kick and drift.  Returns J, dJ/dlambda
+ * (quartic model, A = lambda/2, B = -lambda v^2/2) and, when the pointers are
+ * non-NULL, dJ/dphi and dJ/dphi' of the initial state as complex128 host
+ * arrays (d/dRe + i d/dIm).  ms_forward / ms_reverse (may be NULL) give the
+ * GPU time of the two sweeps.  FP64-plain contexts with gw_mode UIJ; the
+ * context is left at the final state of the forward run. */
+int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half,
+                        int last_half, int64_t stride, double kmin, double kmax, double *J,
+                        double *dJ_dlambda, double *grad_phi0, double *grad_phidot0,
+                        double *ms_forward, double *ms_reverse);
+
+/* ------------------------------------------------------------------ */
 /* batched ensembles (no counterpart in the reference, which runs one  */
 /* realisation per job)                                                 */
 /* ------------------------------------------------------------------ */
@@ -278,6 +319,9 @@ int axg_ensemble_leapfrog(axg_ensemble *e, double t1, double dt, int64_t nsteps,
                           int last_half, int use_graph);
 /* choose the tile shape shared by all members (state restored) */
 int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *best_ms_per_step);
+/* fixes the tile shape (axg_tile_info index) of the batched kernel; it must
+ * fit every member */
+int axg_ensemble_set_tile(axg_ensemble *e, int cfg);
 int axg_ensemble_launch_count(const axg_ensemble *e, int64_t *launches);
 
 /* ------------------------------------------------------------------ */

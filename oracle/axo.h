@@ -105,6 +105,13 @@ void axo_spectrum_estimation(const axg_params *p, const double *phidot, const in
                              double tau, double *wave, double *power, double *conv,
                              double *count, double *mat_deconv_out);
 void axo_compute_crho(const axg_params *p, const double *wav, const double *power, double *rho);
+void axo_estimate_covmat(const axg_params *p, const int8_t *flags, const double *power,
+                         const double *mat_deconv, int min_mc, int max_mc, double tol, double *cov,
+                         int *iterations);
+void axo_compute_crho_cov(const axg_params *p, const double *wav, const double *power, const double *cov,
+                          double *rho, double *drho);
+void axo_epsilon(int nb, const double *wav, const double *p1, const double *p2, const double *c1,
+                 const double *c2, double tau1, double tau2, double *eps, double *deps);
 /* packed (upper) Cholesky inverse, dpptrf + dpptri; returns info */
 int axo_pp_inverse(int n, double *ap);
 
@@ -116,6 +123,13 @@ void axo_ic_thermal(const axg_params *p, double tau_ini, uint32_t realisation, d
 /* volume averages (<|phi|^2>, <|phi'|^2>, <|grad phi|^2>, <V>) */
 void axo_field_moments(const axg_params *p, const double *phi, const double *phidot, double tau,
                        double out[4]);
+
+/* FP64 tangent-linear reference (axo_adjoint.c) */
+double axo_gw_band_energy(const axg_params *p, const double *u, const double *w, double tau, double kmin,
+                          double kmax);
+void axo_tl_run(const axg_params *p, double *phi, double *phid, double *u, double *ud, double *dphi,
+                double *dphid, double *du, double *dud, double dlambda, double t1, double dt, int64_t nsteps,
+                int first_half, int last_half, double kmin, double kmax, double *J, double *dJ);
 
 /* deterministic math exports for tests */
 double axo_det_atan2(double y, double x);

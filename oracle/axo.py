@@ -70,6 +70,13 @@ def lib():
                                          dp, dp, dp], None),
             "axo_compute_crho": ([P, dp, dp, dp], None),
             "axo_pp_inverse": ([ctypes.c_int, dp], ctypes.c_int),
+            "axo_estimate_covmat": ([P, ctypes.POINTER(ctypes.c_int8), dp, dp, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_double, dp, ctypes.POINTER(ctypes.c_int)], None),
+            "axo_compute_crho_cov": ([P, dp, dp, dp, dp, dp], None),
+            "axo_epsilon": ([ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp, dp], None),
+            "axo_gw_band_energy": ([P, dp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double], ctypes.c_double),
+            "axo_tl_run": ([P, dp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                            ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, dp, dp], None),
         }
         for name, (a, r) in spec.items():
             f = getattr(L, name)
@@ -238,7 +245,7 @@ def id_defects(p, phi, phid, tau, max_strings=None, max_walls=None):
     mw = n ** 3 if max_walls is None else max_walls
     sl, wa, sv = np.zeros(3), np.zeros(3), np.zeros(3)
     c = (ctypes.c_int64 * 3)()
-    s = np.zeros((max(ms, 1), 12))
+    s = np.zeros((max(ms, 1), 13))
     w = np.zeros((max(mw, 1), 10))
     flags = np.zeros((n, n, n), np.int8)
     lib().axo_id_defects(ctypes.byref(p), dptr(phi), dptr(phid), tau, dptr(sl), dptr(wa), dptr(sv), c,
@@ -303,3 +310,56 @@ def pp_inverse(ap: np.ndarray, n: int):
     a = np.ascontiguousarray(ap, np.float64).copy()
     info = lib().axo_pp_inverse(n, dptr(a))
     return a, info
+
+
+def gw_band_energy(p, u, ud, tau, kmin, kmax):
+    return lib().axo_gw_band_energy(ctypes.byref(p), dptr(u), dptr(ud), tau, kmin, kmax)
+
+
+def tl_run(p, state, dstate, dlambda, t1, dt, nsteps, kmin, kmax, first_half=True, last_half=True):
+    """Forward + tangent-linear run (copies its inputs); returns (J, dJ)."""
+    phi, phid, u, ud = (np.ascontiguousarray(a).copy() for a in state)
+    dphi, dphid, du, dud = (np.ascontiguousarray(a).copy() for a in dstate)
+    J = ctypes.c_double()
+    dJ = ctypes.c_double()
+    lib().axo_tl_run(ctypes.byref(p), dptr(phi), dptr(phid), dptr(u), dptr(ud), dptr(dphi), dptr(dphid), dptr(du),
+                     dptr(dud), dlambda, t1, dt, nsteps, int(first_half), int(last_half), kmin, kmax,
+                     ctypes.byref(J), ctypes.byref(dJ))
+    return J.value, dJ.value
+
+
+def estimate_covmat(p, flags, power, mat_div, min_mc=10, max_mc=100, tol=0.1):
+    nb = p.num_bin
+    cov = np.zeros(nb * (nb + 1) // 2)
+    it = ctypes.c_int()
+    fptr = flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)) if flags is not None else None
+    lib().axo_estimate_covmat(ctypes.byref(p), fptr, dptr(np.ascontiguousarray(power, np.float64)),
+                              dptr(np.ascontiguousarray(mat_div, np.float64)), min_mc, max_mc, tol, dptr(cov),
+                              ctypes.byref(it))
+    return cov, it.value
+
+
+def compute_crho_cov(p, wav, power, cov):
+    r, d = ctypes.c_double(), ctypes.c_double()
+    lib().axo_compute_crho_cov(ctypes.byref(p), dptr(np.ascontiguousarray(wav, np.float64)),
+                               dptr(np.ascontiguousarray(power, np.float64)), dptr(np.ascontiguousarray(cov, np.float64)),
+                               ctypes.byref(r), ctypes.byref(d))
+    return r.value, d.value
+
+
+def epsilon(nb, wav, p1, p2, c1, c2, tau1, tau2):
+    e, d = ctypes.c_double(), ctypes.c_double()
+    a = [np.ascontiguousarray(x, np.float64) for x in (wav, p1, p2, c1, c2)]
+    lib().axo_epsilon(nb, *[dptr(x) for x in a], tau1, tau2, ctypes.byref(e), ctypes.byref(d))
+    return e.value, d.value
+
+
+def mat_divided(md, counts):
+    """spectrum.f90:267-273: the deconvolution matrix divided by the mode counts."""
+    nb = len(counts)
+    out = np.array(md, dtype=np.float64).copy()
+    for i in range(1, nb + 1):
+        for j in range(1, i + 1):
+            ij = i * (i - 1) // 2 + j
+            out[ij - 1] = out[ij - 1] / counts[i - 1] / counts[j - 1]
+    return out

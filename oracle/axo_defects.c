@@ -587,13 +587,75 @@ void axo_position_wall(const double ph[8], double pos[3], double dir[3], double 
   position_wall_m(ph, pos, dir, gof, wa);
 }
 
+/* grouping_strings / grouping_walls (defects_3d.f90:1235-1260, 1735-1760):
+ * threshold = max(2, (width^2 hor)^(1/3)) in lattice units */
+static double group_threshold(double wid, double hor) {
+  double th = pow(wid * wid * hor, 1.0 / 3.0);
+  return th > 2.0 ? th : 2.0;
+}
+
+/* lat_dist_periodic (defects_3d.f90:1645-1652) */
+static double lat_dist_periodic(int64_t n, const double *a, const double *b) {
+  double s = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    double dp = fabs(a[k] - b[k]);
+    double e = (double)n - dp;
+    double m = dp < e ? dp : e;
+    s = s + m * m;
+  }
+  return sqrt(s);
+}
+
+static int64_t uf_find(int64_t *par, int64_t x) {
+  while (par[x] != x) x = par[x];
+  return x;
+}
+
+/* Connected components of the points (rows of `rows` with positions in
+ * columns 0..2) under dist <= th: the partition the reference's grouping
+ * produces on one rank and one thread.  The group id written into column
+ * `gcol` is the smallest row index of the component. */
+static void group_points(int64_t n, double *rows, int width, int64_t np, double th, int gcol) {
+  int64_t *par = (int64_t *)malloc(sizeof(int64_t) * np);
+  for (int64_t i = 0; i < np; ++i) par[i] = i;
+  for (int64_t i = 0; i < np; ++i)
+    for (int64_t j = i + 1; j < np; ++j) {
+      if (lat_dist_periodic(n, rows + width * i, rows + width * j) <= th) {
+        int64_t a = uf_find(par, i), b = uf_find(par, j);
+        if (a != b) {
+          if (a < b) par[b] = a;
+          else par[a] = b;
+        }
+      }
+    }
+  for (int64_t i = 0; i < np; ++i) rows[width * i + gcol] = (double)uf_find(par, i);
+  free(par);
+}
+
+/* per-group totals of column vcol; out = (all, groups above t2, groups above t3) */
+static void group_sums(const double *rows, int width, int vcol, int gcol, int64_t np, double t2, double t3,
+                       double out[3]) {
+  double *tot = (double *)calloc(np, sizeof(double));
+  for (int64_t i = 0; i < np; ++i) {
+    int64_t g = (int64_t)rows[width * i + gcol];
+    tot[g] = tot[g] + rows[width * i + vcol];
+  }
+  out[0] = out[1] = out[2] = 0.0;
+  for (int64_t g = 0; g < np; ++g) {
+    if ((int64_t)rows[width * g + gcol] != g) continue; /* not a root */
+    out[0] = out[0] + tot[g];
+    if (tot[g] > t2) out[1] = out[1] + tot[g];
+    if (tot[g] > t3) out[2] = out[2] + tot[g];
+  }
+  free(tot);
+}
+
 /* defects_3d.f90:31-307 without grouping (group_strings = group_walls = .false.)
  * and the sums of add_string_length (1654-1733) / add_wall_area (2145-2204). */
 void axo_id_defects(const axg_params *p, const double *phi, const double *phidot, double tau,
                     double sl[3], double wa[3], double svel[3], int64_t counts[3],
                     double *strings, int64_t max_strings, double *walls, int64_t max_walls,
                     int8_t *flags_out) {
-  (void)tau;
   const int64_t n = p->ngrid, n2 = n * n, n3 = n2 * n;
   const int which = p->flags & (AXG_F_ID_STRINGS | AXG_F_ID_WALLS | AXG_F_SPEC_EST);
   int8_t *flags = flags_out ? flags_out : (int8_t *)malloc(n3);
@@ -606,7 +668,7 @@ void axo_id_defects(const axg_params *p, const double *phi, const double *phidot
     if (flags[s] & 1) scell[ns++] = s;
     if (flags[s] & 2) wcell[nw++] = s;
   }
-  double *sres = (double *)calloc((size_t)(ns + 1) * 12, sizeof(double));
+  double *sres = (double *)calloc((size_t)(ns + 1) * 13, sizeof(double));
   double *wres = (double *)calloc((size_t)(nw + 1) * 10, sizeof(double));
 #pragma omp parallel for schedule(dynamic, 4)
   for (int64_t k = 0; k < ns; ++k) {
@@ -618,7 +680,7 @@ void axo_id_defects(const axg_params *p, const double *phi, const double *phidot
     double pos[3], dir[3], vel[3], gof, l;
     axo_position_string(ph, p->seed, (uint64_t)s, pos, dir, &gof, &l);
     velocity_string(p, phi, phidot, ix, iy, iz, pos, vel);
-    double *r = sres + 12 * k;
+    double *r = sres + 13 * k;
     r[0] = pos[0] + ix + 0.5;
     r[1] = pos[1] + iy + 0.5;
     r[2] = pos[2] + iz + 0.5;
@@ -627,6 +689,7 @@ void axo_id_defects(const axg_params *p, const double *phi, const double *phidot
     r[9] = gof;
     r[10] = l;
     r[11] = (double)s;
+    r[12] = -1.0;
   }
 #pragma omp parallel for schedule(dynamic, 4)
   for (int64_t k = 0; k < nw; ++k) {
@@ -645,16 +708,24 @@ void axo_id_defects(const axg_params *p, const double *phi, const double *phidot
     r[6] = gof;
     r[7] = a;
     r[8] = (double)s;
-    r[9] = 0.0;
+    r[9] = -1.0;
   }
-  /* add_string_length without grouping */
-  double s1 = 0.0;
-  for (int64_t k = 0; k < ns; ++k) s1 = s1 + sres[12 * k + 10];
-  sl[0] = sl[1] = sl[2] = s1;
+  const double hor = tau / p->dspa;
+  /* add_string_length (defects_3d.f90:1654-1733) */
+  if ((p->flags & AXG_F_GROUP_STRINGS) && ns > 0) {
+    const double wid = p->width_cr / p->dspa / tau;
+    const double th = group_threshold(wid, hor);
+    group_points(p->ngrid, sres, 13, ns, th, 12);
+    group_sums(sres, 13, 10, 12, ns, 2 * hor, REF_TWOPI * hor, sl);
+  } else {
+    double s1 = 0.0;
+    for (int64_t k = 0; k < ns; ++k) s1 = s1 + sres[13 * k + 10];
+    sl[0] = sl[1] = sl[2] = s1;
+  }
   int64_t nn = 0;
   double v1 = 0, v2s = 0, v3 = 0;
   for (int64_t k = 0; k < ns; ++k) {
-    const double *v = sres + 12 * k + 6;
+    const double *v = sres + 13 * k + 6;
     double v2 = v[0] * v[0] + v[1] * v[1];
     v2 = v2 + v[2] * v[2];
     if (v2 >= 1.0) continue;
@@ -670,11 +741,19 @@ void axo_id_defects(const axg_params *p, const double *phi, const double *phidot
     svel[1] = v2s / nn;
     svel[2] = v3 / nn;
   }
-  double a1 = 0.0;
-  for (int64_t k = 0; k < nw; ++k) a1 = a1 + wres[10 * k + 7];
-  wa[0] = wa[1] = wa[2] = a1;
+  /* add_wall_area (defects_3d.f90:2145-2204) */
+  if ((p->flags & AXG_F_GROUP_WALLS) && nw > 0) {
+    const double wid = p->thickness_cr / p->dspa / tau;
+    const double th = group_threshold(wid, hor);
+    group_points(p->ngrid, wres, 10, nw, th, 9);
+    group_sums(wres, 10, 7, 9, nw, REF_PI * hor * hor, 4 * REF_PI * hor * hor, wa);
+  } else {
+    double a1 = 0.0;
+    for (int64_t k = 0; k < nw; ++k) a1 = a1 + wres[10 * k + 7];
+    wa[0] = wa[1] = wa[2] = a1;
+  }
   if (strings)
-    memcpy(strings, sres, sizeof(double) * 12 * (size_t)(ns < max_strings ? ns : max_strings));
+    memcpy(strings, sres, sizeof(double) * 13 * (size_t)(ns < max_strings ? ns : max_strings));
   if (walls)
     memcpy(walls, wres, sizeof(double) * 10 * (size_t)(nw < max_walls ? nw : max_walls));
   free(scell);

@@ -1,14 +1,15 @@
 /*
  * axo_spectrum.c -- oracle restatement of spectrum.f90 (mode-coupling table,
  * degraded and masked phidot spectrum, deconvolution matrix, packed
- * symmetric solve, conformal energy).  TEST INFRASTRUCTURE ONLY (see axo.h).
- * The Monte-Carlo covariance (spectrum.f90:569-734) is not restated.
+ * symmetric solve, conformal energy, Monte-Carlo covariance, epsilon).
+ * TEST INFRASTRUCTURE ONLY (see axo.h).
  */
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include "axo.h"
+#include "axg_detmath.h"
 
 #define REF_PI 3.14159265359
 #define REF_TWOPI (2 * REF_PI)
@@ -229,4 +230,155 @@ void axo_compute_crho(const axg_params *p, const double *wav, const double *powe
     r = r + power[i - 1] * q2dq;
   }
   *rho = r;
+}
+
+/* estimate_covmat (spectrum.f90:569-734): Gaussian fields with the measured
+ * spectrum, masked like the data, re-estimated through the deconvolution
+ * matrix; covariance of the estimates with a jackknife convergence test.
+ * mat_deconv is the matrix after the division by the mode counts
+ * (spectrum.f90:271).  Gaussian draws: Philox stream 16 + iter (the
+ * reference uses MKL VSL streams).  A negative deconvolved power gives
+ * sigma = 0 for that bin (the reference would take sqrt of a negative). */
+void axo_estimate_covmat(const axg_params *p, const int8_t *flags, const double *power,
+                         const double *mat_deconv, int min_mc, int max_mc, double tol, double *cov,
+                         int *iterations) {
+  const int nb = p->num_bin;
+  const int num_cov = nb * (nb + 1) / 2;
+  const int64_t n = p->ngrid, deg = 1 << p->degrade_spec, m = n / deg, m3 = m * m * m;
+  const double dspa_spec = p->dspa * deg;
+  const double dwav = REF_TWOPI / dspa_spec / m;
+  const double dq = REF_PI / dspa_spec / nb;
+  unsigned char *mask = (unsigned char *)malloc((size_t)m3);
+  build_mask(p, flags, mask);
+  double *buf = (double *)malloc(sizeof(double) * 2 * m3);
+  double *sigma = (double *)malloc(sizeof(double) * nb);
+  double *tmp = (double *)calloc((size_t)num_cov * max_mc, sizeof(double));
+  double *pw0 = (double *)malloc(sizeof(double) * nb), *pw = (double *)malloc(sizeof(double) * nb);
+  for (int i = 0; i < nb; ++i) sigma[i] = sqrt(power[i] > 0 ? power[i] / 2 : 0.0) / (double)m3;
+  for (int ij = 0; ij < num_cov; ++ij) cov[ij] = 0.0;
+  int iter;
+  for (iter = 1; iter <= max_mc; ++iter) {
+    for (int64_t s = 0; s < m3; ++s) {
+      int64_t qx = kint(s % m, m), qy = kint((s / m) % m, m), qz = kint(s / (m * m), m);
+      double q = sqrt((double)(qx * qx + qy * qy + qz * qz)) * dwav;
+      double id = round(q / dq + 0.5);
+      if (id <= nb) {
+        axd_u32x4 r = axd_draw(p->seed, 16u + (uint32_t)iter, 0u, (uint64_t)s);
+        double u1 = axd_u01_open0(r.v[0], r.v[1]), u2 = axd_u01(r.v[2], r.v[3]);
+        double rad = sqrt(-2.0 * log(u1)), th = 6.283185307179586 * u2;
+        buf[2 * s] = rad * cos(th) * sigma[(int)id - 1];
+        buf[2 * s + 1] = rad * sin(th) * sigma[(int)id - 1];
+      } else {
+        buf[2 * s] = buf[2 * s + 1] = 0.0;
+      }
+    }
+    axo_fft3d(m, buf, -1);
+    for (int64_t s = 0; s < m3; ++s)
+      if (mask[s]) buf[2 * s] = buf[2 * s + 1] = 0.0;
+    axo_fft3d(m, buf, +1);
+    for (int i = 0; i < nb; ++i) pw0[i] = 0.0;
+    for (int64_t s = 0; s < m3; ++s) {
+      int64_t qx = kint(s % m, m), qy = kint((s / m) % m, m), qz = kint(s / (m * m), m);
+      double q = sqrt((double)(qx * qx + qy * qy + qz * qz)) * dwav;
+      double id = round(q / dq + 0.5);
+      if (id <= nb) pw0[(int)id - 1] += buf[2 * s] * buf[2 * s] + buf[2 * s + 1] * buf[2 * s + 1];
+    }
+    /* pow = mat_deconv pow0 - power (dspmv with beta = 1) */
+    for (int i = 0; i < nb; ++i) pw[i] = -power[i];
+    int kk = 1;
+    for (int j = 1; j <= nb; ++j) {
+      double temp1 = pw0[j - 1], temp2 = 0.0;
+      int k = kk;
+      for (int i = 1; i <= j - 1; ++i) {
+        pw[i - 1] = pw[i - 1] + temp1 * mat_deconv[k - 1];
+        temp2 = temp2 + mat_deconv[k - 1] * pw0[i - 1];
+        ++k;
+      }
+      pw[j - 1] = pw[j - 1] + temp1 * mat_deconv[kk + j - 2] + temp2;
+      kk = kk + j;
+    }
+    for (int i = 1; i <= nb; ++i)
+      for (int j = 1; j <= i; ++j) {
+        int ij = i * (i - 1) / 2 + j;
+        double u = pw[i - 1] * pw[j - 1];
+        tmp[(size_t)(iter - 1) * num_cov + ij - 1] = cov[ij - 1];
+        for (int k = 1; k <= iter - 1; ++k) tmp[(size_t)(k - 1) * num_cov + ij - 1] += u;
+        cov[ij - 1] = cov[ij - 1] + u;
+      }
+    if (iter < min_mc) continue;
+    double diff = 0.0;
+    for (int i = 1; i <= nb; ++i) {
+      int ij = i * (i + 1) / 2;
+      double u = 0.0, v = 0.0;
+      for (int k = 1; k <= iter; ++k) {
+        double x = tmp[(size_t)(k - 1) * num_cov + ij - 1] / (iter - 1);
+        u = u + x;
+        v = v + x * x;
+      }
+      u = u / iter;
+      v = v / iter;
+      v = sqrt(v - u * u);
+      double x = cov[ij - 1] / iter;
+      double r = v / x;
+      diff = diff > r ? diff : r;
+    }
+    if (diff < tol) break;
+  }
+  if (iter > max_mc) iter = max_mc + 1; /* not converged: the reference divides by max_mc + 1 */
+  for (int ij = 0; ij < num_cov; ++ij) cov[ij] = cov[ij] / iter;
+  *iterations = iter;
+  free(mask); free(buf); free(sigma); free(tmp); free(pw0); free(pw);
+}
+
+/* compute_crho (spectrum.f90:316-342) with the covariance term */
+void axo_compute_crho_cov(const axg_params *p, const double *wav, const double *power, const double *cov,
+                          double *rho, double *drho) {
+  const int nb = p->num_bin;
+  double r = 0.0, d = 0.0;
+  for (int i = 1; i <= nb; ++i) {
+    double dd = 0.0;
+    for (int j = 1; j <= i; ++j) {
+      int ij = i * (i - 1) / 2 + j;
+      double q = (wav[j] + wav[j - 1]) / 2;
+      double dq = wav[j] - wav[j - 1];
+      double q2dq = q * q * dq / REF_PI / REF_PI;
+      if (j == i) q2dq = q2dq / 2;
+      dd = dd + cov[ij - 1] * q2dq;
+    }
+    double q = (wav[i] + wav[i - 1]) / 2;
+    double dq = wav[i] - wav[i - 1];
+    double q2dq = q * q * dq / REF_TWOPI / REF_PI;
+    d = d + dd * q2dq;
+    r = r + power[i - 1] * q2dq;
+  }
+  *rho = r;
+  *drho = sqrt(d);
+}
+
+/* get_epsilon (spectrum.f90:1002-1036) for one pair of output times */
+void axo_epsilon(int nb, const double *wav, const double *p1, const double *p2, const double *c1,
+                 const double *c2, double tau1, double tau2, double *eps, double *deps) {
+  double tau = (tau2 + tau1) / 2;
+  double f = tau / 2 / REF_TWOPI;
+  double num = 0.0, den = 0.0;
+  for (int i = 1; i <= nb; ++i) {
+    double d = p2[i - 1] - p1[i - 1];
+    double q = (wav[i - 1] + wav[i]) / 2;
+    num = num + d * q * q;
+    den = den + d * q;
+  }
+  double e = num / den * f;
+  double de = 0.0;
+  for (int i = 1; i <= nb; ++i) {
+    double d1 = (wav[i - 1] + wav[i]) / 2;
+    for (int j = 1; j <= i; ++j) {
+      int ij = i * (i - 1) / 2 + j;
+      double d2 = (wav[j - 1] + wav[j]) / 2;
+      double d = (1 - e / d1 / f) * (1 - e / d2 / f) * (c2[ij - 1] + c1[ij - 1]) * d1 * d1 * d2 * d2;
+      if (j != i) d = d * 2;
+      de = de + d;
+    }
+  }
+  *eps = e;
+  *deps = sqrt(de / den / den) * f;
 }

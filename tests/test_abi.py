@@ -59,11 +59,15 @@ def test_tile_table(built):
     lib = ag.load_library()
     n = lib.axg_tile_count()
     assert n >= 3
-    a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    a, b, c, d = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    pw = 0
     for i in range(n):
-        assert lib.axg_tile_info(i, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)) == 0
-        assert a.value % 32 == 0 and b.value >= 4 and c.value >= 2
-    assert lib.axg_tile_info(n, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)) == -1
+        assert lib.axg_tile_info(i, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d)) == 0
+        assert a.value % 32 == 0 and b.value >= 4 and c.value >= 2 and d.value in (0, 1)
+        pw += d.value
+    assert 0 < pw < n  # both pointwise paths (registers, TMA ring) are in the search space
+    assert lib.axg_tile_info(0, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), None) == 0
+    assert lib.axg_tile_info(n, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), None) == -1
 
 
 def test_create_without_gpu_fails_loudly(built):

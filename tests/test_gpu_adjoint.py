@@ -1,0 +1,110 @@
+"""Hand-written adjoint of the leapfrog (phi + six u_ij) against the FP64
+tangent-linear reference and central finite differences."""
+import numpy as np
+import pytest
+
+import axion_grav_gb300 as ag
+from oracle import axo
+
+pytestmark = pytest.mark.gpu
+
+ARGS = dict(t1=1.5, dt=0.05, nsteps=12, stride=4, kmin=0.5, kmax=3.0)
+
+
+def params(n, lam=1.0):
+    return ag.default_params(ngrid=n, precision=ag.PREC_FP64_PLAIN, gw_mode=ag.GW_UIJ, potential=ag.POT_QUARTIC,
+                             dspa=0.7, sigma_cr=1.0, vev=1.0, seed=4, **{"lambda": lam})
+
+
+def state(n, seed=0):
+    rng = np.random.default_rng(seed)
+    phi = (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))).astype(np.complex128)
+    phid = (0.2 * (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n)))).astype(np.complex128)
+    u = 0.01 * rng.standard_normal((6, n, n, n))
+    ud = 0.01 * rng.standard_normal((6, n, n, n))
+    return phi, phid, u, ud
+
+
+def gpu_adjoint(p, st, **kw):
+    a = dict(ARGS)
+    a.update(kw)
+    with ag.Lattice(p) as lat:
+        lat.upload(st[0], st[1])
+        lat.upload_uij(st[2], st[3])
+        out = lat.adjoint_gw_band(a["t1"], a["dt"], a["nsteps"], a["stride"], a["kmin"], a["kmax"])
+        final = lat.download(), lat.download_uij()
+    return out, final
+
+
+def rdot(g, d):
+    return float(np.sum(g.real * d.real + g.imag * d.imag))
+
+
+@pytest.mark.parametrize("stride", [4, 5, 12, 1])
+def test_adjoint_dot_product_against_tangent_linear(stride):
+    n = 16
+    p = params(n)
+    st = state(n, 1)
+    (J, dl, gphi, gpid, _, _), _ = gpu_adjoint(p, st, stride=stride)
+    rng = np.random.default_rng(2)
+    dphi = (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))).astype(np.complex128)
+    dpid = (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))).astype(np.complex128)
+    z6 = np.zeros((6, n, n, n))
+    Jt, dJ = axo.tl_run(p, st, (dphi, dpid, z6, z6), 0.7, ARGS["t1"], ARGS["dt"], ARGS["nsteps"], ARGS["kmin"],
+                        ARGS["kmax"])
+    assert J == pytest.approx(Jt, rel=1e-9)
+    adj = rdot(gphi, dphi) + rdot(gpid, dpid) + 0.7 * dl
+    assert adj == pytest.approx(dJ, rel=1e-8)
+
+
+def test_adjoint_lambda_against_finite_differences():
+    n, eps = 16, 1e-4
+    st = state(n, 3)
+    (J, dl, *_), _ = gpu_adjoint(params(n), st)
+    (Jp, *_), _ = gpu_adjoint(params(n, 1.0 + eps), st)
+    (Jm, *_), _ = gpu_adjoint(params(n, 1.0 - eps), st)
+    assert dl == pytest.approx((Jp - Jm) / (2 * eps), rel=1e-6)
+
+
+def test_adjoint_mode_amplitudes_against_finite_differences():
+    """32 random Fourier modes below k_cut (selection seed 7): the gradient
+    with respect to each mode's amplitude is <dJ/dphi0, e^{ikx}>."""
+    n, eps, kcut = 16, 1e-4, 1.5
+    p = params(n)
+    st = state(n, 5)
+    (J, dl, gphi, gpid, _, _), _ = gpu_adjoint(p, st)
+    dwav = 2 * 3.14159265359 / 0.7 / n
+    q = np.fft.fftfreq(n) * n
+    kz, ky, kx = np.meshgrid(q, q, q, indexing="ij")
+    kmag = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2) * dwav
+    cand = np.argwhere((kmag <= kcut) & (kmag > 0))
+    sel = cand[np.random.default_rng(7).choice(len(cand), 32, replace=False)]
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    G = np.fft.fftn(gphi)  # sum_x gphi e^{-ikx}
+    for (iz, iy, ix) in sel:
+        mode = np.exp(2j * np.pi * (q[ix] * x + q[iy] * y + q[iz] * z) / n)
+        grad = rdot(gphi, mode)
+        assert grad == pytest.approx(float(np.real(np.conj(G[iz, iy, ix]))), rel=1e-9, abs=1e-9 * abs(grad) + 1e-12)
+        (Jp, *_), _ = gpu_adjoint(p, (st[0] + eps * mode, st[1], st[2], st[3]))
+        (Jm, *_), _ = gpu_adjoint(p, (st[0] - eps * mode, st[1], st[2], st[3]))
+        fd = (Jp - Jm) / (2 * eps)
+        assert grad == pytest.approx(fd, rel=2e-5, abs=1e-7 * abs(J))
+
+
+def test_adjoint_leaves_final_state_of_forward_run():
+    n = 16
+    p = params(n)
+    st = state(n, 6)
+    _, ((phi, phid), (u, ud)) = gpu_adjoint(p, st, stride=5)
+    a = [x.copy() for x in st]
+    axo.leapfrog(p, a[0], a[1], a[2], a[3], None, ARGS["t1"], ARGS["dt"], ARGS["nsteps"], True, True)
+    assert np.array_equal(phi, a[0]) and np.array_equal(phid, a[1])
+    assert np.array_equal(u, a[2]) and np.array_equal(ud, a[3])
+
+
+def test_adjoint_rejects_unsupported_paths():
+    p = params(16)
+    p.precision = ag.PREC_FP32_MIXED
+    with ag.Lattice(p) as lat:
+        with pytest.raises(ag.AxgError, match="UNSUPPORTED"):
+            lat.adjoint_gw_band(1.5, 0.05, 4, 2, 0.5, 3.0)

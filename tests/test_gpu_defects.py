@@ -105,3 +105,19 @@ def test_flags_require_fresh_classification():
         lat.upload(fields("random", n), np.zeros((n, n, n), np.complex128))
         with pytest.raises(ag.AxgError, match="STATE"):
             lat.defect_flags()
+
+
+@pytest.mark.parametrize("kind,n", [("random", 16), ("smooth", 32), ("strings", 32)])
+def test_grouping_matches_oracle(kind, n):
+    flags = 7 | ag.F_GROUP_STRINGS | ag.F_GROUP_WALLS
+    phi = fields(kind, n, 9)
+    p = params(n, flags=flags, width_cr=1.2, thickness_cr=2.0)
+    sl, wa, sv, cnt, S, W, _ = axo.id_defects(p, phi, np.zeros_like(phi), 3.0)
+    with ag.Lattice(p) as lat:
+        lat.upload(phi, np.zeros_like(phi))
+        gsl, gwa, gsv, gcnt = lat.id_defects(1, 3.0)
+        gS, gW = lat.defect_lists(int(gcnt[0]), int(gcnt[1]))
+    assert np.array_equal(gcnt, cnt)
+    assert np.array_equal(gS[:, 12], S[:, 12]) and np.array_equal(gW[:, 9], W[:, 9])
+    np.testing.assert_allclose(gsl, sl, rtol=1e-12)
+    np.testing.assert_allclose(gwa, wa, rtol=1e-12)

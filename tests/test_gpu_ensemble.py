@@ -50,6 +50,32 @@ def test_ensemble_matches_single_runs(use_graph):
         assert np.array_equal(gu, u) and np.array_equal(gud, ud), i
 
 
+def test_ensemble_every_tile_matches_single_runs():
+    """The batched kernel on every tile shape that fits all members, with the
+    pointwise fields in registers or in the TMA ring."""
+    sizes = [32, 64, 96]
+    ps = [member_params(n, 200 + i) for i, n in enumerate(sizes)]
+    dt, t0, nsteps = 0.02, 1.6, 6
+    singles = [run_single(p, 1, nsteps, dt, t0) for p in ps]
+    lib = ag.load_library()
+    tested = 0
+    for cfg in range(lib.axg_tile_count()):
+        with ag.Ensemble(ps) as ens:
+            try:
+                ens.set_tile(cfg)
+            except ag.AxgError:
+                continue
+            for i, m in enumerate(ens.members):
+                m.ic_gaussian_flat(1.5, 200 + i)
+            ens.leapfrog(t0, dt, nsteps, True, True, use_graph=True)
+            got = [(m.download(), m.download_uij()) for m in ens.members]
+        tested += 1
+        for ((phi, phid), (u, ud)), ((gphi, gphid), (gu, gud)) in zip(singles, got):
+            assert np.array_equal(gphi, phi) and np.array_equal(gphid, phid), cfg
+            assert np.array_equal(gu, u) and np.array_equal(gud, ud), cfg
+    assert tested >= 4
+
+
 def test_fp64_fused_ensemble_matches_oracle():
     sizes = [32, 64]
     ps = [member_params(n, 7 + i, ag.PREC_FP64_FUSED) for i, n in enumerate(sizes)]

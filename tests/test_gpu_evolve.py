@@ -103,6 +103,37 @@ def test_fp64_fused_bit_exact_all_tiles(n, gw):
     assert tested >= 3
 
 
+@pytest.mark.parametrize("gw", [ag.GW_NONE, ag.GW_UIJ])
+def test_fp32_mixed_identical_on_all_tiles(gw):
+    """Each site's FP32 arithmetic does not depend on the tile shape or on
+    whether the pointwise fields arrive through registers or the TMA ring."""
+    n = 64
+    p = make_params(n, ag.PREC_FP32_MIXED, gw)
+    st = random_state(n, 4, 0.05)
+    lib = ag.load_library()
+    ref, tested, pw = None, 0, 0
+    for cfg in range(lib.axg_tile_count()):
+        def fn(lat, cfg=cfg):
+            try:
+                lat.set_tile(cfg)
+            except ag.AxgError:
+                return False
+            lat.leapfrog(1.5, 0.02, 9, True, True)
+            return True
+        out = run_gpu(p, st, fn)
+        if not out[4]:
+            continue
+        tested += 1
+        pw += ag.tile_table()[cfg][3]
+        if ref is None:
+            ref = out
+            continue
+        for a, b in zip(out[:4], ref[:4]):
+            if a is not None:
+                assert np.array_equal(a, b), cfg
+    assert tested >= 4 and pw >= 2
+
+
 @pytest.mark.parametrize("n", [32, 64])
 def test_fp32_mixed_matches_fp64_oracle(n):
     """FP32 fields and stencil with Kahan drift: tolerance against FP64."""

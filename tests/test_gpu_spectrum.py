@@ -52,3 +52,27 @@ def test_spectrum_classifies_when_needed():
         lat.upload(phi, phid)
         w, pw, cv, ct = lat.spectrum_estimation(2.0)
     assert np.all(np.isfinite(pw)) and ct.sum() > 0
+
+
+@pytest.mark.parametrize("n,deg", [(32, 0), (32, 1)])
+def test_spectrum_covariance_matches_oracle(n, deg):
+    """estimate_covmat (spectrum.f90:569-734) with a fixed number of MC
+    realisations; the same Philox draws on both sides."""
+    phi, phid = state(n, 40 + deg)
+    p = params(n, degrade_spec=deg)
+    flags, cnt = axo.classify_cells(params(n), phi, 7, 0)
+    w, pw, cv, ct, md = axo.spectrum_estimation(p, phid, flags, 3.0)
+    cov, it = axo.estimate_covmat(p, flags, pw, axo.mat_divided(md, ct), 6, 6, 0.05)
+    wav = np.concatenate([[0.0], np.cumsum(np.full(len(w), w[0] * 2))])
+    rho, drho = axo.compute_crho_cov(p, wav, pw, cov)
+    with ag.Lattice(p) as lat:
+        lat.upload(phi, phid)
+        lat.classify_cells(7)
+        lat.spectrum_estimation(3.0)
+        gcov, git = lat.spectrum_covariance(6, 6, 0.05)
+        grho, gdrho = lat.compute_crho_cov()
+    assert git == it
+    scale = np.max(np.abs(cov))
+    np.testing.assert_allclose(gcov, cov, rtol=1e-7, atol=1e-9 * scale)
+    assert grho == pytest.approx(rho, rel=1e-6)
+    assert gdrho == pytest.approx(drho, rel=1e-6)

@@ -134,3 +134,68 @@ def test_spectrum_parseval_unmasked():
     total = np.sum(cv * ct)
     assert total == pytest.approx(np.sum(np.abs(phid) ** 2) * dx ** 3, rel=1e-10)
     assert ct.sum() <= n ** 3
+
+
+def _white_spectrum(n, dx, nb, seed):
+    p = params(ngrid=n, dspa=dx, num_bin=nb)
+    rng = np.random.default_rng(seed)
+    phid = rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))
+    w, pw, cv, ct, md = axo.spectrum_estimation(p, phid, None, 1.0)
+    return p, w, pw, ct, axo.mat_divided(md, ct)
+
+
+def test_covmat_is_a_sum_of_outer_products():
+    """estimate_covmat (spectrum.f90:569-734) accumulates pow pow^T over the MC
+    realisations and divides by iter: a positive semi-definite matrix of rank
+    at most the number of realisations; never converging at a tiny tol, it
+    divides by max_mc + 1 as the reference's loop counter ends there."""
+    p, w, pw, ct, mdiv = _white_spectrum(16, 0.5, 8, 3)
+    cov, it = axo.estimate_covmat(p, None, pw, mdiv, 5, 5, 1e-12)
+    assert it == 6
+    nb = 8
+    full = np.zeros((nb, nb))
+    for i in range(1, nb + 1):
+        for j in range(1, i + 1):
+            full[i - 1, j - 1] = full[j - 1, i - 1] = cov[i * (i - 1) // 2 + j - 1]
+    ev = np.linalg.eigvalsh(full)
+    assert np.all(np.diag(full) > 0)
+    assert ev.min() > -1e-10 * ev.max()
+    assert np.sum(ev > 1e-9 * ev.max()) <= 5
+
+
+def test_covmat_converges_and_is_deterministic():
+    p, w, pw, ct, mdiv = _white_spectrum(16, 0.5, 8, 4)
+    cov1, it1 = axo.estimate_covmat(p, None, pw, mdiv, 10, 100, 0.5)
+    cov2, it2 = axo.estimate_covmat(p, None, pw, mdiv, 10, 100, 0.5)
+    assert 10 <= it1 <= 100 and it1 == it2
+    np.testing.assert_array_equal(cov1, cov2)
+
+
+def test_crho_cov_without_covariance_matches_crho():
+    p, w, pw, ct, mdiv = _white_spectrum(16, 0.5, 8, 5)
+    wav = np.concatenate([[0.0], np.cumsum(np.full(len(w), w[0] * 2))])
+    r, d = axo.compute_crho_cov(p, wav, pw, np.zeros(len(w) * (len(w) + 1) // 2))
+    assert r == axo.compute_crho(p, wav, pw) and d == 0.0
+    cov, _ = axo.estimate_covmat(p, None, pw, mdiv, 10, 10, 0.1)
+    r2, d2 = axo.compute_crho_cov(p, wav, pw, cov)
+    assert r2 == r and 0.0 < d2 < abs(r)
+
+
+def test_epsilon_single_bin_and_library_parity():
+    """get_epsilon (spectrum.f90:1002-1036): a change of power in one bin gives
+    eps = q_bin tau / (4 pi); the library's host routine matches the oracle."""
+    nb = 6
+    wav = np.arange(nb + 1) * 0.3
+    p1 = np.zeros(nb)
+    p2 = np.zeros(nb)
+    p2[3] = 2.0
+    c0 = np.zeros(nb * (nb + 1) // 2)
+    e, d = axo.epsilon(nb, wav, p1, p2, c0, c0, 3.0, 5.0)
+    assert e == pytest.approx((wav[3] + wav[4]) / 2 * 4.0 / 2 / (2 * 3.14159265359), rel=1e-14)
+    assert d == 0.0
+    rng = np.random.default_rng(0)
+    p1, p2 = rng.random(nb), rng.random(nb) + 1.0
+    c1, c2 = rng.random(len(c0)) * 1e-3, rng.random(len(c0)) * 1e-3
+    ref = axo.epsilon(nb, wav, p1, p2, c1, c2, 3.0, 5.0)
+    got = ag.epsilon(wav, p1, p2, c1, c2, 3.0, 5.0)
+    assert got == ref

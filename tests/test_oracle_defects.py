@@ -117,3 +117,49 @@ def test_string_length_geometry():
     d = np.array([1, 1, 1]) / np.sqrt(3)
     assert axo.string_length([0, 0, 0], d) == pytest.approx(2 * 0.5 * np.sqrt(3), rel=1e-12) or \
         axo.string_length([0, 0, 0], d) == 0.0
+
+
+def _components(pos, n, th):
+    from scipy.sparse import csr_matrix
+    from scipy.sparse.csgraph import connected_components
+    d = np.abs(pos[:, None, :] - pos[None, :, :])
+    d = np.minimum(d, n - d)
+    adj = np.sqrt((d ** 2).sum(-1)) <= th
+    ncomp, lab = connected_components(csr_matrix(adj), directed=False)
+    return ncomp, lab
+
+
+def test_grouping_matches_connected_components():
+    """group_strings / group_walls: single-linkage groups under the periodic
+    threshold max(2, (w^2 hor)^(1/3)) (defects_3d.f90:1235-1652, 1735-2143)."""
+    n = 16
+    rng = np.random.default_rng(11)
+    phi = (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))).astype(np.complex128)
+    tau = 3.0
+    p = params(n, flags=ag.F_ID_STRINGS | ag.F_ID_WALLS | ag.F_SPEC_EST | ag.F_GROUP_STRINGS | ag.F_GROUP_WALLS,
+               width_cr=1.2, thickness_cr=2.0)
+    sl, wa, sv, cnt, S, W, _ = axo.id_defects(p, phi, np.zeros_like(phi), tau)
+    hor = tau / p.dspa
+    for rows, gcol, vcol, wid, t2, t3, out in (
+            (S, 12, 10, p.width_cr / p.dspa / tau, 2 * hor, 2 * 3.14159265359 * hor, sl),
+            (W, 9, 7, p.thickness_cr / p.dspa / tau, 3.14159265359 * hor ** 2, 4 * 3.14159265359 * hor ** 2, wa)):
+        th = max(2.0, (wid * wid * hor) ** (1 / 3))
+        ncomp, lab = _components(rows[:, :3], n, th)
+        groups = rows[:, gcol].astype(int)
+        # same partition, labelled by the smallest member index
+        for c in range(ncomp):
+            members = np.where(lab == c)[0]
+            assert np.all(groups[members] == members.min())
+        tot = np.array([rows[lab == c, vcol].sum() for c in range(ncomp)])
+        assert out[0] == pytest.approx(tot.sum(), rel=1e-12)
+        assert out[1] == pytest.approx(tot[tot > t2].sum(), rel=1e-12, abs=1e-12)
+        assert out[2] == pytest.approx(tot[tot > t3].sum(), rel=1e-12, abs=1e-12)
+
+
+def test_grouping_four_straight_strings():
+    n = 16
+    p = params(n, flags=ag.F_ID_STRINGS | ag.F_GROUP_STRINGS, width_cr=0.5)
+    sl, wa, sv, cnt, S, W, _ = axo.id_defects(p, four_strings(n), np.zeros((n, n, n), np.complex128), 2.0)
+    assert len(set(S[:, 12].astype(int))) == 4
+    # each string is one group of length ~N; 2*hor = 4 < N so all count as long strings
+    assert sl[1] == pytest.approx(sl[0]) and sl[0] / (4 * n) == pytest.approx(1.0, abs=0.05)
