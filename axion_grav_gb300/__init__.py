@@ -311,13 +311,14 @@ class Lattice:
                                         _dptr(phidot.view(np.float64) if phidot is not None else None),
                                         n * n, 0))
 
-    def download(self):
+    def download(self, phi: bool = True, phidot: bool = True):
+        """(phi, phidot) as complex128 host arrays; a field not asked for is None."""
         n = self.n
-        phi = np.empty((n, n, n), np.complex128)
-        phid = np.empty((n, n, n), np.complex128)
-        self._check(self.lib.axg_download(self._ctx, _dptr(phi.view(np.float64)),
-                                          _dptr(phid.view(np.float64)), n * n, 0))
-        return phi, phid
+        a = np.empty((n, n, n), np.complex128) if phi else None
+        b = np.empty((n, n, n), np.complex128) if phidot else None
+        self._check(self.lib.axg_download(self._ctx, _dptr(a.view(np.float64)) if phi else None,
+                                          _dptr(b.view(np.float64)) if phidot else None, n * n, 0))
+        return a, b
 
     def upload_uij(self, u: np.ndarray, udot: np.ndarray):
         for a in (u, udot):

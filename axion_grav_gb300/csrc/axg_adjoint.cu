@@ -10,19 +10,27 @@
 // i d/dIm), from which the gradients with respect to Fourier-mode amplitudes
 // follow by one FFT.
 //
-// Scheme (FP64, state in the FP64-plain layout):
-//   forward  : the plain drift / kick kernels, a checkpoint of the whole state
-//              every `stride` steps;
-//   terminal : D2Z of tau u and u + tau u' (12 fields), per k the TT-projected
-//              band weights, Z2D back: dJ/du, dJ/du' in real space;
-//   reverse  : for each step, the state is stepped BACK using the leapfrog's
-//              time-reversibility (phi = phi+ - h pi+; pi = (pi+ - f2 L phi -
-//              f3 g(phi)) / f1; same for u) and re-anchored on the exact
-//              checkpoint every `stride` steps; the adjoint step is two
-//              stencil passes (k_adj_step: Laplacians of the adjoint momenta,
-//              the transposed potential Jacobian, the source adjoint's Q_i =
-//              2 fs (sum_j wbar_ij D_j phi + wbar_ii D_i phi); k_adj_divq:
-//              phibar += sum_i D_i^T Q_i).
+// Scheme, in the precision of the context (R = double for FP64-plain and
+// FP64-fused, float for FP32-mixed):
+//   forward  : the context's own step (plain drift / kick kernels, or the
+//              fused TMA kernel with its ping-pong buffers and Kahan drift),
+//              a checkpoint of phi and phi' (and the FP32 compensation of
+//              phi) every `stride` steps;
+//   terminal : D2Z of tau u and u + tau u' (12 fields, FP64), per k the
+//              TT-projected band weights, Z2D back: dJ/du, dJ/du';
+//   reverse  : for each step, phi and phi' are stepped BACK using the
+//              leapfrog's time-reversibility (phi = phi+ - h pi+; pi = (pi+ -
+//              f2 L phi - f3 g(phi)) / f1) and re-anchored on the exact
+//              checkpoint every `stride` steps.  u_ij enters the equations
+//              linearly and its adjoint never reads u, so u and u' are not
+//              stepped back (they stay at the final state).  The adjoint step
+//              is two stencil passes (k_adj_step: Laplacians of the adjoint
+//              momenta, the transposed potential Jacobian, the source
+//              adjoint's Q_i = 2 fs (sum_j wbar_ij D_j phi + wbar_ii D_i phi);
+//              k_adj_divq: phibar += sum_i D_i^T Q_i).  Laplacians are summed
+//              as differences from the centre (exact for smooth fields in
+//              FP32); divisions by f1 and 2 dx are multiplications by
+//              reciprocals computed once per step on the host.
 #include <cmath>
 #include <vector>
 
@@ -35,60 +43,89 @@ constexpr double kRefTwoPi = 2 * 3.14159265359;
 __device__ __forceinline__ int64_t site(int x, int y, int z, int n) { return ((int64_t)z * n + y) * n + x; }
 __device__ __forceinline__ int wr(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-struct StepCoef {
-  double f1, f2, f3, fs, h, A, B, C, D, dA, dB, d;
+template <typename R>
+struct V2T;
+template <>
+struct V2T<float> {
+  using T = float2;
+};
+template <>
+struct V2T<double> {
+  using T = double2;
 };
 
-// backward drift: phi -= h pi, u -= h w
-__global__ void k_rev_drift(double2 *phi, const double2 *pi, double *u, const double *w, int64_t n3, double h) {
+template <typename R>
+__device__ __forceinline__ typename V2T<R>::T mk(R x, R y) {
+  typename V2T<R>::T v;
+  v.x = x;
+  v.y = y;
+  return v;
+}
+
+// per-step coefficients in the arithmetic type of the adjoint
+template <typename R>
+struct Coef {
+  R f1, f2, f3, fs, h, A, B, C, D, dA, dB, inv_f1, inv_d;
+};
+
+struct StepCoef {
+  double f1, f2, f3, fs, h, A, B, C, D, dA, dB, d, inv_f1, inv_d;
+  template <typename R>
+  Coef<R> as() const {
+    return Coef<R>{(R)f1, (R)f2, (R)f3, (R)fs, (R)h, (R)A, (R)B, (R)C, (R)D, (R)dA, (R)dB, (R)inv_f1, (R)inv_d};
+  }
+};
+
+__device__ __forceinline__ void kahan_sub(float &x, float &c, float dec) {
+  const float y = -dec - c;
+  const float t = x + y;
+  c = (t - x) - y;
+  x = t;
+}
+
+// backward drift: phi -= h pi (FP32: Kahan-compensated like the forward drift)
+template <typename R>
+__global__ void k_rev_drift(typename V2T<R>::T *phi, typename V2T<R>::T *cphi, const typename V2T<R>::T *pi,
+                            int64_t n3, R h) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-    double2 a = phi[s];
-    const double2 b = pi[s];
-    a.x -= h * b.x;
-    a.y -= h * b.y;
+    auto a = phi[s];
+    const auto b = pi[s];
+    if constexpr (sizeof(R) == 4) {
+      float2 c = cphi[s];
+      kahan_sub(a.x, c.x, h * b.x);
+      kahan_sub(a.y, c.y, h * b.y);
+      cphi[s] = c;
+    } else {
+      a.x -= h * b.x;
+      a.y -= h * b.y;
+    }
     phi[s] = a;
-    for (int c = 0; c < 6; ++c) u[c * n3 + s] -= h * w[c * n3 + s];
   }
 }
 
-// backward kick: pi = (pi+ - f2 L phi - f3 g(phi)) / f1; w = (w+ - f2 L u - fs S(phi)) / f1
-__global__ void k_rev_kick(const double2 *__restrict__ phi, double2 *__restrict__ pi, const double *__restrict__ u,
-                           double *__restrict__ w, int n, StepCoef k) {
+// backward kick: pi = (pi+ - f2 L phi - f3 g(phi)) / f1
+template <typename R>
+__global__ void k_rev_kick(const typename V2T<R>::T *__restrict__ phi, typename V2T<R>::T *__restrict__ pi, int n,
+                           Coef<R> k) {
   const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y, iz = blockIdx.z;
   if (ix >= n || iy >= n) return;
-  const int64_t n3 = (int64_t)n * n * n;
   const int64_t c = site(ix, iy, iz, n);
   const int64_t nb[6] = {site(wr(ix - 1, n), iy, iz, n), site(wr(ix + 1, n), iy, iz, n), site(ix, wr(iy - 1, n), iz, n),
                          site(ix, wr(iy + 1, n), iz, n), site(ix, iy, wr(iz - 1, n), n), site(ix, iy, wr(iz + 1, n), n)};
-  const double2 p0 = phi[c];
-  double lr = -6 * p0.x, li = -6 * p0.y;
-  double2 pn[6];
+  const auto p0 = phi[c];
+  R lr = 0, li = 0;
   for (int q = 0; q < 6; ++q) {
-    pn[q] = phi[nb[q]];
-    lr += pn[q].x;
-    li += pn[q].y;
+    const auto v = phi[nb[q]];
+    lr += v.x - p0.x;
+    li += v.y - p0.y;
   }
-  const double s = p0.x * p0.x + p0.y * p0.y, g0 = k.A * s + k.B;
-  const double gr = g0 * p0.x + k.D * p0.x + k.C, gi = g0 * p0.y - k.D * p0.y;
-  double2 v = pi[c];
-  v.x = (v.x - k.f2 * lr - k.f3 * gr) / k.f1;
-  v.y = (v.y - k.f2 * li - k.f3 * gi) / k.f1;
+  const R s = p0.x * p0.x + p0.y * p0.y, g0 = k.A * s + k.B;
+  const R gr = g0 * p0.x + k.D * p0.x + k.C, gi = g0 * p0.y - k.D * p0.y;
+  auto v = pi[c];
+  v.x = (v.x - k.f2 * lr - k.f3 * gr) * k.inv_f1;
+  v.y = (v.y - k.f2 * li - k.f3 * gi) * k.inv_f1;
   pi[c] = v;
-  double Dr[3], Di[3];
-  for (int q = 0; q < 3; ++q) {
-    Dr[q] = (pn[2 * q + 1].x - pn[2 * q].x) / k.d;
-    Di[q] = (pn[2 * q + 1].y - pn[2 * q].y) / k.d;
-  }
-  int comp = 0;
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j <= i; ++j, ++comp) {
-      const double *uc = u + comp * n3;
-      double lu = -6 * uc[c];
-      for (int q = 0; q < 6; ++q) lu += uc[nb[q]];
-      const double S = 2 * (Dr[i] * Dr[j] + Di[i] * Di[j]);
-      w[comp * n3 + c] = (w[comp * n3 + c] - k.f2 * lu - k.fs * S) / k.f1;
-    }
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -98,11 +135,12 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 // Adjoint of one kick+drift at the pre-kick state phi (in: adjoint after the
 // step; out: adjoint before it, except the D^T Q part of phibar).
-__global__ void k_adj_step(const double2 *__restrict__ phi, const double2 *__restrict__ pb_in,
-                           const double2 *__restrict__ ib_in, const double *__restrict__ ub_in,
-                           const double *__restrict__ wb_in, double2 *__restrict__ pb_out,
-                           double2 *__restrict__ ib_out, double *__restrict__ ub_out, double *__restrict__ wb_out,
-                           double *__restrict__ Q, int n, StepCoef k, double *__restrict__ dlam) {
+template <typename R>
+__global__ void k_adj_step(const typename V2T<R>::T *__restrict__ phi, const typename V2T<R>::T *__restrict__ pb_in,
+                           const typename V2T<R>::T *__restrict__ ib_in, const R *__restrict__ ub_in,
+                           const R *__restrict__ wb_in, typename V2T<R>::T *__restrict__ pb_out,
+                           typename V2T<R>::T *__restrict__ ib_out, R *__restrict__ ub_out, R *__restrict__ wb_out,
+                           R *__restrict__ Q, int n, Coef<R> k, double *__restrict__ dlam) {
   const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y, iz = blockIdx.z;
   double lam_part = 0.0;
   if (ix < n && iy < n) {
@@ -113,45 +151,45 @@ __global__ void k_adj_step(const double2 *__restrict__ phi, const double2 *__res
                            site(ix, iy, wr(iz - 1, n), n), site(ix, iy, wr(iz + 1, n), n)};
     // pibar_t = pibar+ + h phibar+ (adjoint of the drift), at the site and its neighbours
     auto it = [&](int64_t q) {
-      const double2 a = ib_in[q], b = pb_in[q];
-      return make_double2(a.x + k.h * b.x, a.y + k.h * b.y);
+      const auto a = ib_in[q], b = pb_in[q];
+      return mk<R>(a.x + k.h * b.x, a.y + k.h * b.y);
     };
-    const double2 i0 = it(c);
-    double lr = -6 * i0.x, li = -6 * i0.y;
+    const auto i0 = it(c);
+    R lr = 0, li = 0;
     for (int q = 0; q < 6; ++q) {
-      const double2 v = it(nb[q]);
-      lr += v.x;
-      li += v.y;
+      const auto v = it(nb[q]);
+      lr += v.x - i0.x;
+      li += v.y - i0.y;
     }
-    const double2 p0 = phi[c];
-    const double s = p0.x * p0.x + p0.y * p0.y, g0 = k.A * s + k.B;
-    const double pd = p0.x * i0.x + p0.y * i0.y;
-    const double jr = g0 * i0.x + 2 * k.A * p0.x * pd + k.D * i0.x;
-    const double ji = g0 * i0.y + 2 * k.A * p0.y * pd - k.D * i0.y;
-    const double2 pbv = pb_in[c];
-    pb_out[c] = make_double2(pbv.x + k.f2 * lr + k.f3 * jr, pbv.y + k.f2 * li + k.f3 * ji);
-    ib_out[c] = make_double2(k.f1 * i0.x, k.f1 * i0.y);
-    lam_part = k.f3 * (k.dA * s + k.dB) * pd;
+    const auto p0 = phi[c];
+    const R s = p0.x * p0.x + p0.y * p0.y, g0 = k.A * s + k.B;
+    const R pd = p0.x * i0.x + p0.y * i0.y;
+    const R jr = g0 * i0.x + 2 * k.A * p0.x * pd + k.D * i0.x;
+    const R ji = g0 * i0.y + 2 * k.A * p0.y * pd - k.D * i0.y;
+    const auto pbv = pb_in[c];
+    pb_out[c] = mk<R>(pbv.x + k.f2 * lr + k.f3 * jr, pbv.y + k.f2 * li + k.f3 * ji);
+    ib_out[c] = mk<R>(k.f1 * i0.x, k.f1 * i0.y);
+    lam_part = (double)k.f3 * ((double)k.dA * (double)s + (double)k.dB) * (double)pd;
     // u_ij: wbar_t = wbar+ + h ubar+
-    double Dr[3], Di[3];
+    R Dr[3], Di[3];
     for (int q = 0; q < 3; ++q) {
-      const double2 a = phi[nb[2 * q + 1]], b = phi[nb[2 * q]];
-      Dr[q] = (a.x - b.x) / k.d;
-      Di[q] = (a.y - b.y) / k.d;
+      const auto a = phi[nb[2 * q + 1]], b = phi[nb[2 * q]];
+      Dr[q] = (a.x - b.x) * k.inv_d;
+      Di[q] = (a.y - b.y) * k.inv_d;
     }
-    double wt[6];
+    R wt[6];
     for (int cc = 0; cc < 6; ++cc) {
-      const double *wb = wb_in + cc * n3, *ub = ub_in + cc * n3;
-      const double w0 = wb[c] + k.h * ub[c];
+      const R *wb = wb_in + cc * n3, *ub = ub_in + cc * n3;
+      const R w0 = wb[c] + k.h * ub[c];
       wt[cc] = w0;
-      double lu = -6 * w0;
-      for (int q = 0; q < 6; ++q) lu += wb[nb[q]] + k.h * ub[nb[q]];
+      R lu = 0;
+      for (int q = 0; q < 6; ++q) lu += (wb[nb[q]] + k.h * ub[nb[q]]) - w0;
       ub_out[cc * n3 + c] = ub[c] + k.f2 * lu;
       wb_out[cc * n3 + c] = k.f1 * w0;
     }
     const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
     for (int i = 0; i < 3; ++i) {
-      double qr = wt[idx[i][i]] * Dr[i], qi = wt[idx[i][i]] * Di[i];
+      R qr = wt[idx[i][i]] * Dr[i], qi = wt[idx[i][i]] * Di[i];
       for (int j = 0; j < 3; ++j) {
         qr += wt[idx[i][j]] * Dr[j];
         qi += wt[idx[i][j]] * Di[j];
@@ -165,27 +203,30 @@ __global__ void k_adj_step(const double2 *__restrict__ phi, const double2 *__res
 }
 
 // phibar += sum_i D_i^T Q_i,  D_i^T Q(x) = (Q(x - e_i) - Q(x + e_i)) / d
-__global__ void k_adj_divq(double2 *__restrict__ pb, const double *__restrict__ Q, int n, double d) {
+template <typename R>
+__global__ void k_adj_divq(typename V2T<R>::T *__restrict__ pb, const R *__restrict__ Q, int n, R inv_d) {
   const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y, iz = blockIdx.z;
   if (ix >= n || iy >= n) return;
   const int64_t n3 = (int64_t)n * n * n;
   const int64_t c = site(ix, iy, iz, n);
   const int64_t m[3] = {site(wr(ix - 1, n), iy, iz, n), site(ix, wr(iy - 1, n), iz, n), site(ix, iy, wr(iz - 1, n), n)};
   const int64_t p[3] = {site(wr(ix + 1, n), iy, iz, n), site(ix, wr(iy + 1, n), iz, n), site(ix, iy, wr(iz + 1, n), n)};
-  double2 v = pb[c];
+  auto v = pb[c];
   for (int i = 0; i < 3; ++i) {
-    v.x += (Q[(2 * i) * n3 + m[i]] - Q[(2 * i) * n3 + p[i]]) / d;
-    v.y += (Q[(2 * i + 1) * n3 + m[i]] - Q[(2 * i + 1) * n3 + p[i]]) / d;
+    v.x += (Q[(2 * i) * n3 + m[i]] - Q[(2 * i) * n3 + p[i]]) * inv_d;
+    v.y += (Q[(2 * i + 1) * n3 + m[i]] - Q[(2 * i + 1) * n3 + p[i]]) * inv_d;
   }
   pb[c] = v;
 }
 
 // adjoint of the first half drift phi += h pi: pibar += h phibar (u likewise)
-__global__ void k_adj_half_drift(const double2 *pb, double2 *ib, const double *ub, double *wb, int64_t n3, double h) {
+template <typename R>
+__global__ void k_adj_half_drift(const typename V2T<R>::T *pb, typename V2T<R>::T *ib, const R *ub, R *wb, int64_t n3,
+                                 R h) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-    double2 a = ib[s];
-    const double2 b = pb[s];
+    auto a = ib[s];
+    const auto b = pb[s];
     a.x += h * b.x;
     a.y += h * b.y;
     ib[s] = a;
@@ -193,13 +234,17 @@ __global__ void k_adj_half_drift(const double2 *pb, double2 *ib, const double *u
   }
 }
 
-// 12 real inputs of the terminal spectrum: a = tau u, b = u + tau w
-__global__ void k_adj_terminal_in(const double *u, const double *w, int64_t n3, double tau, double *out) {
+// 12 real FP64 inputs of the terminal spectrum: a = tau u, b = u + tau w
+// (the FP32 state carries u as u - cu)
+template <typename R>
+__global__ void k_adj_terminal_in(const R *u, const R *cu, const R *w, int64_t n3, double tau, double *out) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride)
     for (int c = 0; c < 6; ++c) {
-      out[c * n3 + s] = tau * u[c * n3 + s];
-      out[(6 + c) * n3 + s] = u[c * n3 + s] + tau * w[c * n3 + s];
+      double uv = (double)u[c * n3 + s];
+      if (cu) uv -= (double)cu[c * n3 + s];
+      out[c * n3 + s] = tau * uv;
+      out[(6 + c) * n3 + s] = uv + tau * (double)w[c * n3 + s];
     }
 }
 
@@ -261,15 +306,23 @@ __global__ void k_adj_terminal_k(double2 *F, int n, double dwav, double dx6, dou
 }
 
 // ubar = mult (tau ga + gb), wbar = mult tau gb from the Z2D outputs
-__global__ void k_adj_terminal_out(const double *g, int64_t n3, double tau, double *ub, double *wb) {
+template <typename R>
+__global__ void k_adj_terminal_out(const double *g, int64_t n3, double tau, R *ub, R *wb) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const double mult[6] = {1, 2, 1, 2, 2, 1};
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride)
     for (int c = 0; c < 6; ++c) {
       const double ga = g[c * n3 + s], gb = g[(6 + c) * n3 + s];
-      ub[c * n3 + s] = mult[c] * (tau * ga + gb);
-      wb[c * n3 + s] = mult[c] * tau * gb;
+      ub[c * n3 + s] = (R)(mult[c] * (tau * ga + gb));
+      wb[c * n3 + s] = (R)(mult[c] * tau * gb);
     }
+}
+
+// FP32 adjoint fields to complex128 for the caller
+__global__ void k_adj_to_c128(const float2 *src, double2 *dst, int64_t n3) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride)
+    dst[s] = make_double2((double)src[s].x, (double)src[s].y);
 }
 
 int grid_for(int64_t count) {
@@ -298,23 +351,26 @@ StepCoef coef_at(const axg_params &p, double t, double dt, double h) {
     k.dA = k.dB = 0.0;
   }
   k.d = 2 * p.dspa;
+  k.inv_f1 = 1.0 / k.f1;
+  k.inv_d = 1.0 / k.d;
   return k;
 }
 
-}  // namespace
-
-extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half,
-                                   int last_half, int64_t stride, double kmin, double kmax, double *J_out,
-                                   double *dJ_dlambda, double *grad_phi0, double *grad_phidot0, double *ms_forward,
-                                   double *ms_reverse) {
-  if (!ctx || nsteps < 1 || stride < 1 || !(dt > 0) || !(t1 > 0) || !J_out) return AXG_ERR_ARG;
-  if (ctx->p.precision != AXG_PREC_FP64_PLAIN || ctx->p.gw_mode != AXG_GW_UIJ)
-    return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "the adjoint runs on the FP64-plain path with gw_mode UIJ");
+template <typename R>
+int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half, int last_half, int64_t stride,
+                double kmin, double kmax, double *J_out, double *dJ_dlambda, double *grad_phi0, double *grad_phidot0,
+                double *ms_forward, double *ms_reverse) {
+  using V = typename V2T<R>::T;
+  constexpr bool F32 = sizeof(R) == 4;
+  const bool plain = ctx->p.precision == AXG_PREC_FP64_PLAIN;
   const int n = (int)ctx->n;
   const int64_t n3 = ctx->n3, nhalf = (int64_t)n * n * (n / 2 + 1);
-  const size_t state_b = (size_t)n3 * (16 + 16 + 48 + 48);
+  const size_t adj_b = (size_t)n3 * (2 * sizeof(V) + 12 * sizeof(R));  // one adjoint state
+  const size_t ck_b = (size_t)n3 * sizeof(V) * (F32 ? 3 : 2);           // phi (+ its compensation), phi'
   const int64_t nck = nsteps / stride + 1;
-  double *ck = nullptr, *adj = nullptr, *Q = nullptr, *fbuf = nullptr;
+  char *ck = nullptr, *adj = nullptr;
+  R *Q = nullptr;
+  double *fbuf = nullptr;
   int rc = AXG_OK;
   cufftHandle pf = 0, pb = 0;
   bool pfo = false, pbo = false;
@@ -323,9 +379,10 @@ extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t n
   cudaEventCreate(&e1);
   cudaEventCreate(&e2);
   do {
-    if ((rc = axg_alloc(ctx, (void **)&ck, state_b * nck, "adjoint checkpoints"))) break;
-    if ((rc = axg_alloc(ctx, (void **)&adj, state_b * 2, "adjoint state"))) break;
-    if ((rc = axg_alloc(ctx, (void **)&Q, (size_t)n3 * 6 * 8, "adjoint Q"))) break;
+    // nck checkpoints plus the final phi, phi' (restored after the reverse sweep)
+    if ((rc = axg_alloc(ctx, (void **)&ck, ck_b * (nck + 1), "adjoint checkpoints"))) break;
+    if ((rc = axg_alloc(ctx, (void **)&adj, adj_b * 2, "adjoint state"))) break;
+    if ((rc = axg_alloc(ctx, (void **)&Q, (size_t)n3 * 6 * sizeof(R), "adjoint Q"))) break;
     if ((rc = axg_alloc(ctx, (void **)&fbuf, (size_t)12 * n3 * 8 + (size_t)12 * nhalf * 16, "adjoint FFT"))) break;
     int dims[3] = {n, n, n};
     if (cufftPlanMany(&pf, 3, dims, nullptr, 1, (int)n3, nullptr, 1, (int)nhalf, CUFFT_D2Z, 12) != CUFFT_SUCCESS ||
@@ -336,21 +393,22 @@ extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t n
     pfo = pbo = true;
     cufftSetStream(pf, ctx->stream);
     cufftSetStream(pb, ctx->stream);
-    double2 *phi = (double2 *)ctx->phi[ctx->cur], *pi = (double2 *)ctx->phid;
-    double *u = (double *)ctx->u[ctx->cur], *w = (double *)ctx->ud;
+    // the fused paths ping-pong phi and u: always address the current buffers
+    auto cur_phi = [&]() { return (V *)ctx->phi[ctx->cur]; };
+    V *pi = (V *)ctx->phid, *cphi = F32 ? (V *)ctx->cphi : nullptr;
     auto save = [&](int64_t k) {
-      char *dst = (char *)ck + state_b * k;
-      cudaMemcpyAsync(dst, phi, (size_t)n3 * 16, cudaMemcpyDeviceToDevice, ctx->stream);
-      cudaMemcpyAsync(dst + (size_t)n3 * 16, pi, (size_t)n3 * 16, cudaMemcpyDeviceToDevice, ctx->stream);
-      cudaMemcpyAsync(dst + (size_t)n3 * 32, u, (size_t)n3 * 48, cudaMemcpyDeviceToDevice, ctx->stream);
-      cudaMemcpyAsync(dst + (size_t)n3 * 80, w, (size_t)n3 * 48, cudaMemcpyDeviceToDevice, ctx->stream);
+      char *dst = ck + ck_b * k;
+      const size_t fb = (size_t)n3 * sizeof(V);
+      cudaMemcpyAsync(dst, cur_phi(), fb, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(dst + fb, pi, fb, cudaMemcpyDeviceToDevice, ctx->stream);
+      if (F32) cudaMemcpyAsync(dst + 2 * fb, cphi, fb, cudaMemcpyDeviceToDevice, ctx->stream);
     };
     auto load = [&](int64_t k) {
-      const char *src = (const char *)ck + state_b * k;
-      cudaMemcpyAsync(phi, src, (size_t)n3 * 16, cudaMemcpyDeviceToDevice, ctx->stream);
-      cudaMemcpyAsync(pi, src + (size_t)n3 * 16, (size_t)n3 * 16, cudaMemcpyDeviceToDevice, ctx->stream);
-      cudaMemcpyAsync(u, src + (size_t)n3 * 32, (size_t)n3 * 48, cudaMemcpyDeviceToDevice, ctx->stream);
-      cudaMemcpyAsync(w, src + (size_t)n3 * 80, (size_t)n3 * 48, cudaMemcpyDeviceToDevice, ctx->stream);
+      const char *src = ck + ck_b * k;
+      const size_t fb = (size_t)n3 * sizeof(V);
+      cudaMemcpyAsync(cur_phi(), src, fb, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(pi, src + fb, fb, cudaMemcpyDeviceToDevice, ctx->stream);
+      if (F32) cudaMemcpyAsync(cphi, src + 2 * fb, fb, cudaMemcpyDeviceToDevice, ctx->stream);
     };
     // ---------------- forward with checkpoints ----------------
     cudaEventRecord(e0, ctx->stream);
@@ -365,22 +423,28 @@ extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t n
       const double h = (it == nsteps && last_half) ? dt / 2 : dt;
       kt[it] = t;
       kh[it] = h;
-      if ((rc = axg_evo_kick_plain(ctx, t, dt))) break;
-      if ((rc = axg_evo_drift(ctx, h))) break;
+      if (plain) {
+        if ((rc = axg_evo_kick_plain(ctx, t, dt))) break;
+        if ((rc = axg_evo_drift(ctx, h))) break;
+      } else if ((rc = axg_evo_kick_drift(ctx, t, dt, h))) {
+        break;
+      }
       t = t + h;
       if (it % stride == 0) save(it / stride);
     }
     if (rc) break;
+    save(nck);  // final phi, phi'
     const double tau_end = t;
     cudaEventRecord(e1, ctx->stream);
     // ---------------- terminal adjoint ----------------
-    double2 *pb_a = (double2 *)adj, *ib_a = pb_a + n3;
-    double *ub_a = (double *)(ib_a + n3), *wb_a = ub_a + 6 * n3;
-    double2 *pb_b = (double2 *)((char *)adj + state_b), *ib_b = pb_b + n3;
-    double *ub_b = (double *)(ib_b + n3), *wb_b = ub_b + 6 * n3;
+    V *pb_a = (V *)adj, *ib_a = pb_a + n3;
+    R *ub_a = (R *)(ib_a + n3), *wb_a = ub_a + 6 * n3;
+    V *pb_b = (V *)(adj + adj_b), *ib_b = pb_b + n3;
+    R *ub_b = (R *)(ib_b + n3), *wb_b = ub_b + 6 * n3;
     double *fin = fbuf;
     double2 *F = (double2 *)(fbuf + 12 * n3);
-    AXG_LAUNCH(ctx, "adj_terminal_in", k_adj_terminal_in, grid_for(n3), 256, 0, u, w, n3, tau_end, fin);
+    AXG_LAUNCH(ctx, "adj_terminal_in", k_adj_terminal_in<R>, grid_for(n3), 256, 0, (const R *)ctx->u[ctx->cur],
+               F32 ? (const R *)ctx->cu : nullptr, (const R *)ctx->ud, n3, tau_end, fin);
     if (cufftExecD2Z(pf, fin, (cufftDoubleComplex *)F) != CUFFT_SUCCESS) {
       rc = axg_set_error(ctx, AXG_ERR_CUDA, "adjoint D2Z");
       break;
@@ -394,39 +458,53 @@ extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t n
       rc = axg_set_error(ctx, AXG_ERR_CUDA, "adjoint Z2D");
       break;
     }
-    AXG_CUDA_TRY(ctx, cudaMemsetAsync(adj, 0, (size_t)n3 * 32, ctx->stream));  // phibar, pibar = 0
-    AXG_LAUNCH(ctx, "adj_terminal_out", k_adj_terminal_out, grid_for(n3), 256, 0, fin, n3, tau_end, ub_a, wb_a);
+    AXG_CUDA_TRY(ctx, cudaMemsetAsync(adj, 0, (size_t)n3 * 2 * sizeof(V), ctx->stream));  // phibar, pibar = 0
+    AXG_LAUNCH(ctx, "adj_terminal_out", k_adj_terminal_out<R>, grid_for(n3), 256, 0, fin, n3, tau_end, ub_a, wb_a);
     // ---------------- reverse sweep ----------------
     double *dlam = ctx->d_red + 1;
     dim3 blk(32, 8), grd((n + 31) / 32, (n + 7) / 8, n);
     bool a_is_in = true;
+    V *phi = cur_phi();  // the reverse steps phi in place in the final buffer
     for (int64_t it = nsteps; it >= 1 && rc == AXG_OK; --it) {
       const StepCoef kc = coef_at(ctx->p, kt[it], dt, kh[it]);
+      const Coef<R> kr = kc.template as<R>();
       // state after step it -> state before step it (pre-kick)
       if ((it - 1) % stride == 0) {
         load((it - 1) / stride);
       } else {
-        AXG_LAUNCH(ctx, "adj_rev_drift", k_rev_drift, grid_for(n3), 256, 0, phi, pi, u, w, n3, kh[it]);
-        AXG_LAUNCH(ctx, "adj_rev_kick", k_rev_kick, grd, blk, 0, phi, pi, u, w, n, kc);
+        AXG_LAUNCH(ctx, "adj_rev_drift", k_rev_drift<R>, grid_for(n3), 256, 0, phi, cphi, pi, n3, (R)kh[it]);
+        AXG_LAUNCH(ctx, "adj_rev_kick", k_rev_kick<R>, grd, blk, 0, phi, pi, n, kr);
       }
-      double2 *pbi = a_is_in ? pb_a : pb_b, *ibi = a_is_in ? ib_a : ib_b, *pbo_ = a_is_in ? pb_b : pb_a,
-              *ibo = a_is_in ? ib_b : ib_a;
-      double *ubi = a_is_in ? ub_a : ub_b, *wbi = a_is_in ? wb_a : wb_b, *ubo = a_is_in ? ub_b : ub_a,
-             *wbo = a_is_in ? wb_b : wb_a;
-      AXG_LAUNCH(ctx, "adj_step", k_adj_step, grd, blk, 0, phi, pbi, ibi, ubi, wbi, pbo_, ibo, ubo, wbo, Q, n, kc, dlam);
-      AXG_LAUNCH(ctx, "adj_divq", k_adj_divq, grd, blk, 0, pbo_, Q, n, kc.d);
+      V *pbi = a_is_in ? pb_a : pb_b, *ibi = a_is_in ? ib_a : ib_b, *pbo_ = a_is_in ? pb_b : pb_a,
+        *ibo = a_is_in ? ib_b : ib_a;
+      R *ubi = a_is_in ? ub_a : ub_b, *wbi = a_is_in ? wb_a : wb_b, *ubo = a_is_in ? ub_b : ub_a,
+        *wbo = a_is_in ? wb_b : wb_a;
+      AXG_LAUNCH(ctx, "adj_step", k_adj_step<R>, grd, blk, 0, phi, pbi, ibi, ubi, wbi, pbo_, ibo, ubo, wbo, Q, n, kr,
+                 dlam);
+      AXG_LAUNCH(ctx, "adj_divq", k_adj_divq<R>, grd, blk, 0, pbo_, Q, n, kr.inv_d);
       a_is_in = !a_is_in;
     }
     if (rc) break;
-    double2 *pbf = a_is_in ? pb_a : pb_b, *ibf = a_is_in ? ib_a : ib_b;
-    double *ubf = a_is_in ? ub_a : ub_b, *wbf = a_is_in ? wb_a : wb_b;
-    if (first_half) AXG_LAUNCH(ctx, "adj_half_drift", k_adj_half_drift, grid_for(n3), 256, 0, pbf, ibf, ubf, wbf, n3, dt / 2);
+    V *pbf = a_is_in ? pb_a : pb_b, *ibf = a_is_in ? ib_a : ib_b;
+    R *ubf = a_is_in ? ub_a : ub_b, *wbf = a_is_in ? wb_a : wb_b;
+    if (first_half)
+      AXG_LAUNCH(ctx, "adj_half_drift", k_adj_half_drift<R>, grid_for(n3), 256, 0, pbf, ibf, ubf, wbf, n3, (R)(dt / 2));
     cudaEventRecord(e2, ctx->stream);
     double h2[2];
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h2, ctx->d_red, 16, cudaMemcpyDeviceToHost, ctx->stream));
-    if (grad_phi0) AXG_CUDA_TRY(ctx, cudaMemcpyAsync(grad_phi0, pbf, (size_t)n3 * 16, cudaMemcpyDeviceToHost, ctx->stream));
-    if (grad_phidot0)
-      AXG_CUDA_TRY(ctx, cudaMemcpyAsync(grad_phidot0, ibf, (size_t)n3 * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    double *outs[2] = {grad_phi0, grad_phidot0};
+    V *srcs[2] = {pbf, ibf};
+    for (int q = 0; q < 2; ++q) {
+      if (!outs[q]) continue;
+      const void *src = srcs[q];
+      if constexpr (F32) {
+        k_adj_to_c128<<<grid_for(n3), 256, 0, ctx->stream>>>((const float2 *)srcs[q], (double2 *)fbuf, n3);
+        ctx->launches++;
+        src = fbuf;
+      }
+      AXG_CUDA_TRY(ctx, cudaMemcpyAsync(outs[q], src, (size_t)n3 * 16, cudaMemcpyDeviceToHost, ctx->stream));
+      if (F32) AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // fbuf is reused
+    }
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     *J_out = h2[0];
     if (dJ_dlambda) *dJ_dlambda = h2[1];
@@ -435,15 +513,11 @@ extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t n
     cudaEventElapsedTime(&f2, e1, e2);
     if (ms_forward) *ms_forward = f1;
     if (ms_reverse) *ms_reverse = f2;
-    // the context state is left at the end of the forward run, as after axg_leapfrog
-    load(nck - 1);
-    if (nsteps % stride != 0) {
-      // re-run the tail from the last checkpoint to restore the final state exactly
-      for (int64_t it = (nck - 1) * stride + 1; it <= nsteps && rc == AXG_OK; ++it) {
-        rc = axg_evo_kick_plain(ctx, kt[it], dt);
-        if (!rc) rc = axg_evo_drift(ctx, kh[it]);
-      }
-    }
+    // the context state is left at the end of the forward run, as after
+    // axg_leapfrog: u, u' were never stepped back; phi, phi' come back from
+    // the final slot
+    load(nck);
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   } while (0);
   cudaStreamSynchronize(ctx->stream);
   if (pfo) cufftDestroy(pf);
@@ -457,4 +531,20 @@ extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t n
   axg_free(ctx, (void **)&fbuf);
   ctx->flags_valid = false;
   return rc;
+}
+
+}  // namespace
+
+extern "C" int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half,
+                                   int last_half, int64_t stride, double kmin, double kmax, double *J_out,
+                                   double *dJ_dlambda, double *grad_phi0, double *grad_phidot0, double *ms_forward,
+                                   double *ms_reverse) {
+  if (!ctx || nsteps < 1 || stride < 1 || !(dt > 0) || !(t1 > 0) || !J_out) return AXG_ERR_ARG;
+  if (ctx->p.gw_mode != AXG_GW_UIJ)
+    return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "the adjoint needs gw_mode UIJ (J is the u_ij band energy)");
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+    return adjoint_run<float>(ctx, t1, dt, nsteps, first_half, last_half, stride, kmin, kmax, J_out, dJ_dlambda,
+                              grad_phi0, grad_phidot0, ms_forward, ms_reverse);
+  return adjoint_run<double>(ctx, t1, dt, nsteps, first_half, last_half, stride, kmin, kmax, J_out, dJ_dlambda,
+                             grad_phi0, grad_phidot0, ms_forward, ms_reverse);
 }

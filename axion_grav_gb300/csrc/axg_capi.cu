@@ -2,6 +2,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "axg_internal.h"
@@ -81,50 +82,125 @@ constexpr int64_t kChunkBytes = 64ll << 20;  // staging chunk for precision conv
 
 // Copy a complex field between host and device in z-plane chunks, converting
 // precision on the device when the storage is FP32.
+// Creates the copy stream, events and the two staging buffers on first use.
+int xfer_init(axg_ctx *ctx) {
+  if (ctx->xstream) return AXG_OK;
+  for (int b = 0; b < 2; ++b) AXG_TRY(axg_alloc(ctx, &ctx->xstage[b], (size_t)kChunkBytes, "transfer staging"));
+  AXG_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->xstream, cudaStreamNonBlocking));
+  for (int b = 0; b < 2; ++b) {
+    AXG_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->xev_copied[b], cudaEventDisableTiming));
+    AXG_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->xev_done[b], cudaEventDisableTiming));
+  }
+  AXG_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->xev_start, cudaEventDisableTiming));
+  return AXG_OK;
+}
+
+// Chunked transfer with precision conversion through two staging buffers.
+// Upload: the copy stream moves chunk i into stage[i % 2] while the library
+// stream converts chunk i - 1; download: the library stream converts chunk i
+// while the copy stream drains chunk i - 1 to the host.  Returns after the
+// host buffer is no longer touched.
+using XferFn = std::function<cudaError_t(int64_t chunk, void *stage, cudaStream_t s)>;
+int xfer_pipelined(axg_ctx *ctx, bool to_device, int64_t nchunks, const XferFn &copy, const XferFn &convert) {
+  AXG_TRY(xfer_init(ctx));
+  cudaError_t e = cudaEventRecord(ctx->xev_start, ctx->stream);  // earlier work on the library stream
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->xstream, ctx->xev_start, 0);
+  for (int64_t i = 0; i < nchunks && e == cudaSuccess; ++i) {
+    const int b = (int)(i & 1);
+    void *st = ctx->xstage[b];
+    if (to_device) {
+      if (i >= 2) e = cudaStreamWaitEvent(ctx->xstream, ctx->xev_done[b], 0);  // conversion of i-2 read it
+      if (e == cudaSuccess) e = copy(i, st, ctx->xstream);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->xev_copied[b], ctx->xstream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->xev_copied[b], 0);
+      if (e == cudaSuccess) e = convert(i, st, ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->xev_done[b], ctx->stream);
+    } else {
+      if (i >= 2) e = cudaStreamWaitEvent(ctx->stream, ctx->xev_copied[b], 0);  // copy of i-2 drained it
+      if (e == cudaSuccess) e = convert(i, st, ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->xev_done[b], ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->xstream, ctx->xev_done[b], 0);
+      if (e == cudaSuccess) e = copy(i, st, ctx->xstream);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->xev_copied[b], ctx->xstream);
+    }
+  }
+  // the library stream must not run ahead of the last copy (staging reuse)
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->xev_start, ctx->xstream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->xev_start, 0);
+  const cudaError_t s1 = cudaStreamSynchronize(ctx->xstream);
+  const cudaError_t s2 = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = s1 != cudaSuccess ? s1 : s2;
+  if (e != cudaSuccess) return axg_set_error(ctx, AXG_ERR_CUDA, std::string("transfer: ") + cudaGetErrorString(e));
+  return AXG_OK;
+}
+
 int xfer_complex(axg_ctx *ctx, bool to_device, double *host, int64_t plane_stride,
                  int64_t first_plane, void *dev, void *comp) {
   const int64_t n = ctx->n, n2 = n * n;
   const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
   if (plane_stride < n2) return axg_set_error(ctx, AXG_ERR_ARG, "plane_stride < N*N");
   if (first_plane < 0) return axg_set_error(ctx, AXG_ERR_ARG, "first_plane < 0");
-  int64_t zchunk = fp32 ? std::max<int64_t>(1, kChunkBytes / (n2 * 16)) : n;
-  if (zchunk > n) zchunk = n;
-  double2 *stage = nullptr;
-  if (fp32) AXG_TRY(axg_alloc(ctx, (void **)&stage, (size_t)(zchunk * n2 * 16), "staging"));
-  int rc = AXG_OK;
-  for (int64_t z0 = 0; z0 < n && rc == AXG_OK; z0 += zchunk) {
-    const int64_t nz = std::min(zchunk, n - z0);
-    double *h = host + 2 * (first_plane + z0) * plane_stride;
-    double2 *d = fp32 ? stage : (double2 *)dev + z0 * n2;
-    cudaError_t e;
-    if (to_device) {
-      e = cudaMemcpy2DAsync(d, (size_t)(n2 * 16), h, (size_t)(plane_stride * 16), (size_t)(n2 * 16),
-                            (size_t)nz, cudaMemcpyHostToDevice, ctx->stream);
-      if (e == cudaSuccess && fp32) {
-        k_c128_to_f32<<<grid_for(nz * n2), 256, 0, ctx->stream>>>(
-            stage, (float2 *)dev + z0 * n2, comp ? (float2 *)comp + z0 * n2 : nullptr, nz * n2);
-        ctx->launches++;
-        e = cudaGetLastError();
-      }
-    } else {
-      e = cudaSuccess;
-      if (fp32) {
-        k_f32_to_c128<<<grid_for(nz * n2), 256, 0, ctx->stream>>>(
-            (const float2 *)dev + z0 * n2, comp ? (const float2 *)comp + z0 * n2 : nullptr, stage,
-            nz * n2);
-        ctx->launches++;
-        e = cudaGetLastError();
-      }
-      if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(h, (size_t)(plane_stride * 16), d, (size_t)(n2 * 16), (size_t)(n2 * 16),
-                              (size_t)nz, cudaMemcpyDeviceToHost, ctx->stream);
-    }
-    if (e == cudaSuccess && fp32) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) rc = axg_set_error(ctx, AXG_ERR_CUDA, std::string("transfer: ") + cudaGetErrorString(e));
+  if (!fp32) {
+    const cudaError_t e =
+        to_device ? cudaMemcpy2DAsync(dev, (size_t)(n2 * 16), host + 2 * first_plane * plane_stride,
+                                      (size_t)(plane_stride * 16), (size_t)(n2 * 16), (size_t)n,
+                                      cudaMemcpyHostToDevice, ctx->stream)
+                  : cudaMemcpy2DAsync(host + 2 * first_plane * plane_stride, (size_t)(plane_stride * 16), dev,
+                                      (size_t)(n2 * 16), (size_t)(n2 * 16), (size_t)n, cudaMemcpyDeviceToHost,
+                                      ctx->stream);
+    if (e != cudaSuccess) return axg_set_error(ctx, AXG_ERR_CUDA, std::string("transfer: ") + cudaGetErrorString(e));
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return AXG_OK;
   }
-  if (stage) axg_free(ctx, (void **)&stage);
-  if (rc == AXG_OK && !to_device) AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  return rc;
+  // whole z-planes per chunk when a plane fits, else runs of rows
+  const int64_t zchunk = std::max<int64_t>(1, kChunkBytes / (n2 * 16));
+  if (n2 * 16 > kChunkBytes) {
+    const int64_t rows = std::max<int64_t>(1, kChunkBytes / (n * 16));
+    const int64_t per_plane = (n + rows - 1) / rows;
+    return xfer_pipelined(
+        ctx, to_device, n * per_plane,
+        [&](int64_t i, void *st, cudaStream_t s) {
+          const int64_t z = i / per_plane, y0 = (i % per_plane) * rows, ny = std::min(rows, n - y0);
+          double *h = host + 2 * ((first_plane + z) * plane_stride + y0 * n);
+          return to_device ? cudaMemcpyAsync(st, h, (size_t)(ny * n * 16), cudaMemcpyHostToDevice, s)
+                           : cudaMemcpyAsync(h, st, (size_t)(ny * n * 16), cudaMemcpyDeviceToHost, s);
+        },
+        [&](int64_t i, void *st, cudaStream_t s) {
+          const int64_t z = i / per_plane, y0 = (i % per_plane) * rows, ny = std::min(rows, n - y0);
+          const int64_t o = z * n2 + y0 * n, m = ny * n;
+          if (to_device)
+            k_c128_to_f32<<<grid_for(m), 256, 0, s>>>((const double2 *)st, (float2 *)dev + o,
+                                                      comp ? (float2 *)comp + o : nullptr, m);
+          else
+            k_f32_to_c128<<<grid_for(m), 256, 0, s>>>((const float2 *)dev + o,
+                                                      comp ? (const float2 *)comp + o : nullptr, (double2 *)st, m);
+          ctx->launches++;
+          return cudaGetLastError();
+        });
+  }
+  const int64_t nch = (n + zchunk - 1) / zchunk;
+  return xfer_pipelined(
+      ctx, to_device, nch,
+      [&](int64_t i, void *st, cudaStream_t s) {
+        const int64_t z0 = i * zchunk, nz = std::min(zchunk, n - z0);
+        double *h = host + 2 * (first_plane + z0) * plane_stride;
+        return to_device ? cudaMemcpy2DAsync(st, (size_t)(n2 * 16), h, (size_t)(plane_stride * 16),
+                                             (size_t)(n2 * 16), (size_t)nz, cudaMemcpyHostToDevice, s)
+                         : cudaMemcpy2DAsync(h, (size_t)(plane_stride * 16), st, (size_t)(n2 * 16),
+                                             (size_t)(n2 * 16), (size_t)nz, cudaMemcpyDeviceToHost, s);
+      },
+      [&](int64_t i, void *st, cudaStream_t s) {
+        const int64_t z0 = i * zchunk, nz = std::min(zchunk, n - z0);
+        const int64_t o = z0 * n2, m = nz * n2;
+        if (to_device)
+          k_c128_to_f32<<<grid_for(m), 256, 0, s>>>((const double2 *)st, (float2 *)dev + o,
+                                                    comp ? (float2 *)comp + o : nullptr, m);
+        else
+          k_f32_to_c128<<<grid_for(m), 256, 0, s>>>((const float2 *)dev + o,
+                                                    comp ? (const float2 *)comp + o : nullptr, (double2 *)st, m);
+        ctx->launches++;
+        return cudaGetLastError();
+      });
 }
 
 int xfer_real6(axg_ctx *ctx, bool to_device, double *host, void *dev, void *comp) {
@@ -138,35 +214,25 @@ int xfer_real6(axg_ctx *ctx, bool to_device, double *host, void *dev, void *comp
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return AXG_OK;
   }
-  int64_t chunk = kChunkBytes / 8;
-  double *stage = nullptr;
-  AXG_TRY(axg_alloc(ctx, (void **)&stage, (size_t)std::min(chunk, count) * 8, "staging"));
-  int rc = AXG_OK;
-  for (int64_t o = 0; o < count && rc == AXG_OK; o += chunk) {
-    const int64_t m = std::min(chunk, count - o);
-    cudaError_t e = cudaSuccess;
-    if (to_device) {
-      e = cudaMemcpyAsync(stage, host + o, (size_t)m * 8, cudaMemcpyHostToDevice, ctx->stream);
-      if (e == cudaSuccess) {
-        k_r64_to_f32<<<grid_for(m), 256, 0, ctx->stream>>>(stage, (float *)dev + o,
-                                                           comp ? (float *)comp + o : nullptr, m);
+  const int64_t chunk = kChunkBytes / 8;
+  return xfer_pipelined(
+      ctx, to_device, (count + chunk - 1) / chunk,
+      [&](int64_t i, void *st, cudaStream_t s) {
+        const int64_t o = i * chunk, m = std::min(chunk, count - o);
+        return to_device ? cudaMemcpyAsync(st, host + o, (size_t)m * 8, cudaMemcpyHostToDevice, s)
+                         : cudaMemcpyAsync(host + o, st, (size_t)m * 8, cudaMemcpyDeviceToHost, s);
+      },
+      [&](int64_t i, void *st, cudaStream_t s) {
+        const int64_t o = i * chunk, m = std::min(chunk, count - o);
+        if (to_device)
+          k_r64_to_f32<<<grid_for(m), 256, 0, s>>>((const double *)st, (float *)dev + o,
+                                                   comp ? (float *)comp + o : nullptr, m);
+        else
+          k_f32_to_r64<<<grid_for(m), 256, 0, s>>>((const float *)dev + o, comp ? (const float *)comp + o : nullptr,
+                                                   (double *)st, m);
         ctx->launches++;
-        e = cudaGetLastError();
-      }
-    } else {
-      k_f32_to_r64<<<grid_for(m), 256, 0, ctx->stream>>>((const float *)dev + o,
-                                                         comp ? (const float *)comp + o : nullptr,
-                                                         stage, m);
-      ctx->launches++;
-      e = cudaGetLastError();
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(host + o, stage, (size_t)m * 8, cudaMemcpyDeviceToHost, ctx->stream);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) rc = axg_set_error(ctx, AXG_ERR_CUDA, std::string("transfer: ") + cudaGetErrorString(e));
-  }
-  axg_free(ctx, (void **)&stage);
-  return rc;
+        return cudaGetLastError();
+      });
 }
 
 // CRC-32 (IEEE 802.3 polynomial, reflected), table driven.
@@ -445,7 +511,7 @@ int axg_destroy(axg_ctx *ctx) {
   if (!ctx) return AXG_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (void **q : {&ctx->phi[0], &ctx->phi[1], &ctx->phid, &ctx->cphi, &ctx->u[0], &ctx->u[1],
-                   &ctx->ud, &ctx->cu, (void **)&ctx->acc, (void **)&ctx->gsrc,
+                   &ctx->ud, &ctx->cu, (void **)&ctx->acc, (void **)&ctx->gsrc, (void **)&ctx->gw_omega,
                    (void **)&ctx->gsrcF, (void **)&ctx->flags, (void **)&ctx->phase,
                    (void **)&ctx->d_strings, (void **)&ctx->d_walls, (void **)&ctx->spec_mat,
                    (void **)&ctx->spec_largeq0, (void **)&ctx->spec_dq, (void **)&ctx->spec_buf,
@@ -461,6 +527,16 @@ int axg_destroy(axg_ctx *ctx) {
     cudaEventDestroy(pe.second.second);
   }
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->xstream) {
+    cudaStreamSynchronize(ctx->xstream);
+    cudaStreamDestroy(ctx->xstream);
+  }
+  for (int b = 0; b < 2; ++b) {
+    if (ctx->xev_copied[b]) cudaEventDestroy(ctx->xev_copied[b]);
+    if (ctx->xev_done[b]) cudaEventDestroy(ctx->xev_done[b]);
+    axg_free(ctx, &ctx->xstage[b]);
+  }
+  if (ctx->xev_start) cudaEventDestroy(ctx->xev_start);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return AXG_OK;
@@ -567,7 +643,9 @@ int axg_evolve_phidot(axg_ctx *ctx, double t, double dt) {
 
 int axg_leapfrog(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half,
                  int last_half) {
-  if (!valid_ctx(ctx) || nsteps < 0 || !(dt > 0) || !(t1 > 0)) return AXG_ERR_ARG;
+  if (!valid_ctx(ctx) || nsteps < 0 || !(dt != 0) || !std::isfinite(dt) || !(t1 > 0) ||
+      !(t1 + (double)nsteps * dt > 0))
+    return AXG_ERR_ARG;
   double t = t1;
   if (first_half) {
     AXG_TRY(axg_evo_drift(ctx, dt / 2));

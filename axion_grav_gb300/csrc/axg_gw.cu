@@ -5,14 +5,20 @@
 //                    d_i phi = (phi(x+e_i) - phi(x-e_i)) / (2 dx), one pass
 //                    over phi writing 6 x N^3 reals (the reference's arr_dphi
 //                    is never materialised);
-//   2. cuFFT D2Z batched x6: the reference's backward C2C of a real field is
-//                    the conjugate of the forward half spectrum;
-//   3. k_gw_accumulate: one pass over the full spectrum applying, in the
-//                    reference's (i, j) order, the four accumulator updates of
-//                    all six components (grav_waves.f90:239-242), with the
-//                    polarisation tensor of get_comwav_grav (157-191) computed
-//                    in registers.  compat = REF reproduces the cross-wired
-//                    (2,1)/(1,2) updates literally.
+//   2. cuFFT D2Z (R2C for FP32-mixed) batched x6: the reference's backward
+//                    C2C of a real field is the conjugate of the forward half
+//                    spectrum;
+//   3. k_gw_accumulate: one pass over the full spectrum.  Per k the
+//                    polarisation tensor of get_comwav_grav (157-191) is
+//                    formed in registers, the six sources are contracted into
+//                    X+ = sum_ij e+_ij S_ij and X- = sum_ij e-_ij S_ij, and
+//                    the four accumulators of grav_waves.f90:239-242 take
+//                    dw (cos, sin)(k tau) X+-.  compat = REF reproduces the
+//                    cross-wired (2,1)/(1,2) updates through their closed form
+//                    over the six components.  FP64 for the FP64 paths; the
+//                    FP32-mixed path contracts in FP32 (sources, transforms,
+//                    polarisation, sin/cos of the FP64-reduced phase) and
+//                    accumulates in FP64.
 // Spectra: shell histograms in FP64 (grav_waves.f90:257-321), 25 linear bins
 // or log bins; the u_ij path (AXG_GW_UIJ) FFTs w = tau u and w' = u + tau u'
 // (R2C, FP32 for the FP32-mixed path), TT-projects per k and accumulates
@@ -33,8 +39,10 @@ constexpr double kBigHInMstar = 2.1332e-42 / 2.435e18;
 
 __device__ __forceinline__ int kint(int j, int n) { return (j + n / 2) % n - n / 2; }
 
-template <typename V>
-__global__ void k_gw_source(const V *__restrict__ phi, int n, double d, double *__restrict__ src) {
+// FP64 sources in the reference's operation order; division by d = 2 dx is
+// a multiplication by 1/d when d is a power of two (the same single rounding)
+__global__ void k_gw_source(const double2 *__restrict__ phi, int n, double d, double inv_d, int d_pow2,
+                            double *__restrict__ src) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
@@ -49,9 +57,10 @@ __global__ void k_gw_source(const V *__restrict__ phi, int n, double d, double *
     double dr[3], di[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const V pa = phi[a[k]], pb = phi[b[k]];
-      dr[k] = AXD_DIV(AXD_SUB((double)pa.x, (double)pb.x), d);
-      di[k] = AXD_DIV(AXD_SUB((double)pa.y, (double)pb.y), d);
+      const double2 pa = phi[a[k]], pb = phi[b[k]];
+      const double xr = AXD_SUB(pa.x, pb.x), xi = AXD_SUB(pa.y, pb.y);
+      dr[k] = d_pow2 ? AXD_MUL(xr, inv_d) : AXD_DIV(xr, d);
+      di[k] = d_pow2 ? AXD_MUL(xi, inv_d) : AXD_DIV(xi, d);
     }
     int c = 0;
 #pragma unroll
@@ -64,94 +73,196 @@ __global__ void k_gw_source(const V *__restrict__ phi, int n, double d, double *
   }
 }
 
-// complex helpers in the reference's evaluation order
-struct C2 {
-  double r, i;
-};
-__device__ __forceinline__ C2 cmul(C2 a, C2 b) {
-  return {AXD_SUB(AXD_MUL(a.r, b.r), AXD_MUL(a.i, b.i)), AXD_ADD(AXD_MUL(a.r, b.i), AXD_MUL(a.i, b.r))};
-}
-__device__ __forceinline__ C2 cadd(C2 a, C2 b) { return {AXD_ADD(a.r, b.r), AXD_ADD(a.i, b.i)}; }
-__device__ __forceinline__ C2 rmul(double s, C2 a) { return {AXD_MUL(s, a.r), AXD_MUL(s, a.i)}; }
-
-__global__ void k_gw_accumulate(const double2 *__restrict__ srcF, int n, double dwav, double tau,
-                                double dw, int ref_compat, double2 *__restrict__ acc) {
+// FP32 sources from the FP32 field: raw differences, scaled by 2/d^2 once
+__global__ void k_gw_source_f32(const float2 *__restrict__ phi, int n, float scale, float *__restrict__ src) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
-  const int nh = n / 2 + 1;
-  const int64_t nhalf = (int64_t)n * n * nh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
     const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
-    // backward transform of a real field = conj(forward); forward half spectrum
-    // holds kx <= n/2, the rest by Hermitian symmetry F(-k) = conj F(k)
-    int64_t hidx;
+    const int64_t base = iz * n2 + (int64_t)iy * n;
+    const int64_t a[3] = {base + (ix + 1 == n ? 0 : ix + 1), iz * n2 + (int64_t)(iy + 1 == n ? 0 : iy + 1) * n + ix,
+                          (int64_t)(iz + 1 == n ? 0 : iz + 1) * n2 + (int64_t)iy * n + ix};
+    const int64_t b[3] = {base + (ix == 0 ? n - 1 : ix - 1), iz * n2 + (int64_t)(iy == 0 ? n - 1 : iy - 1) * n + ix,
+                          (int64_t)(iz == 0 ? n - 1 : iz - 1) * n2 + (int64_t)iy * n + ix};
+    float dr[3], di[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float2 pa = phi[a[k]], pb = phi[b[k]];
+      dr[k] = pa.x - pb.x;
+      di[k] = pa.y - pb.y;
+    }
+    int c = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j <= i; ++j, ++c) src[c * n3 + s] = scale * (dr[i] * dr[j] + di[i] * di[j]);
+  }
+}
+
+// |k| dwav per k-site (FP64), the phase rate of the FP32 Green accumulation
+__global__ void k_gw_omega(int n, double dwav, double *__restrict__ om) {
+  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    const double kx = (s % n + n / 2) % n - n / 2, ky = ((s / n) % n + n / 2) % n - n / 2,
+                 kz = (s / n2 + n / 2) % n - n / 2;
+    om[s] = sqrt(kx * kx + ky * ky + kz * kz) * dwav;
+  }
+}
+
+// Half-spectrum index of k and whether the Green source is the conjugate of
+// the stored forward value (the backward transform of a real field is
+// conj(forward); the half spectrum holds kx <= n/2, the rest follows from
+// F(-k) = conj F(k)).
+__device__ __forceinline__ int64_t gw_half_index(int ix, int iy, int iz, int n, bool &conj_back) {
+  const int nh = n / 2 + 1;
+  if (ix < nh) {
+    conj_back = true;
+    return ((int64_t)iz * n + iy) * nh + ix;
+  }
+  conj_back = false;
+  const int jx = n - ix, jy = iy == 0 ? 0 : n - iy, jz = iz == 0 ? 0 : n - iz;
+  return ((int64_t)jz * n + jy) * nh + jx;
+}
+
+// get_comwav_grav (grav_waves.f90:157-191): p = (qz c - i s, qz s + i c, -r)
+// for the unit vector q of k, (c, s) its azimuth; e+_ij = p_i p_j, halved on
+// the diagonal, in the component order (1,1),(2,1),(2,2),(3,1),(3,2),(3,3).
+// Divisions are reciprocal multiplies (one rounding more than the reference).
+template <typename R>
+__device__ __forceinline__ bool gw_polarisation(R kx, R ky, R kz, R qq, R pr[6], R pi[6]) {
+  if (!(qq > 0)) return false;
+  const R iq = R(1) / qq;
+  const R qx = kx * iq, qy = ky * iq, qz = kz * iq;
+  const R r = sqrt(qx * qx + qy * qy);
+  R c = 1, sn = 0;
+  if (r > 0) {
+    const R ir = R(1) / r;
+    c = qx * ir;
+    sn = qy * ir;
+  }
+  const R ar[3] = {qz * c, qz * sn, -r}, ai[3] = {-sn, c, 0};
+  int comp = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j, ++comp) {
+      R er = ar[i] * ar[j] - ai[i] * ai[j], ei = ar[i] * ai[j] + ai[i] * ar[j];
+      if (i == j) {
+        er *= R(0.5);
+        ei *= R(0.5);
+      }
+      pr[comp] = er;
+      pi[comp] = ei;
+    }
+  return true;
+}
+
+// X+ = sum e+ S, X- = sum conj(e+) S and the last component's conj(e+) S
+template <typename R, typename V>
+__device__ __forceinline__ void gw_contract(const V *__restrict__ srcF, int64_t nhalf, int64_t hidx, bool conj_back,
+                                            const R pr[6], const R pi[6], R xp[2], R xm[2], R last_m[2]) {
+  xp[0] = xp[1] = xm[0] = xm[1] = 0;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const V f = srcF[c * nhalf + hidx];
+    const R sr = f.x, si = conj_back ? -f.y : f.y;
+    const R a = pr[c] * sr, b = pi[c] * si, e = pr[c] * si, g = pi[c] * sr;
+    xp[0] += a - b;
+    xp[1] += e + g;
+    xm[0] += a + b;
+    xm[1] += e - g;
+    if (c == 5) {
+      last_m[0] = a + b;
+      last_m[1] = e - g;
+    }
+  }
+}
+
+// a11 += w_c X+, a21 += w_s X+, a12 += w_c X-, a22 += w_s X- (INTENDED);
+// REF: per component a21 <- a12 + t21, a12 <- a21 + t12, i.e. after the six
+// components a12 = a12 + w_s X+ + w_c X-, a21 = a12(new) - w_c (last X-).
+__device__ __forceinline__ void gw_update(double2 *__restrict__ acc, int64_t n3, int64_t s, double wc, double ws,
+                                          const double xp[2], const double xm[2], const double lm[2],
+                                          int ref_compat) {
+  double2 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
+  a11.x = fma(wc, xp[0], a11.x);
+  a11.y = fma(wc, xp[1], a11.y);
+  a22.x = fma(ws, xm[0], a22.x);
+  a22.y = fma(ws, xm[1], a22.y);
+  if (ref_compat) {
+    a12.x = fma(wc, xm[0], fma(ws, xp[0], a12.x));
+    a12.y = fma(wc, xm[1], fma(ws, xp[1], a12.y));
+    a21.x = fma(-wc, lm[0], a12.x);
+    a21.y = fma(-wc, lm[1], a12.y);
+  } else {
+    a21.x = fma(ws, xp[0], a21.x);
+    a21.y = fma(ws, xp[1], a21.y);
+    a12.x = fma(wc, xm[0], a12.x);
+    a12.y = fma(wc, xm[1], a12.y);
+  }
+  acc[s] = a11;
+  acc[n3 + s] = a21;
+  acc[2 * n3 + s] = a12;
+  acc[3 * n3 + s] = a22;
+}
+
+__global__ void k_gw_accumulate(const double2 *__restrict__ srcF, int n, double dwav, double tau, double dw,
+                                int ref_compat, double2 *__restrict__ acc) {
+  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
     bool conj_back;
-    if (ix < nh) {
-      hidx = ((int64_t)iz * n + iy) * nh + ix;
-      conj_back = true;
-    } else {
-      const int jx = n - ix, jy = iy == 0 ? 0 : n - iy, jz = iz == 0 ? 0 : n - iz;
-      hidx = ((int64_t)jz * n + jy) * nh + jx;
-      conj_back = false;
+    const int64_t hidx = gw_half_index(ix, iy, iz, n, conj_back);
+    const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
+    const double qq = sqrt(kx * kx + ky * ky + kz * kz);
+    double pr[6], pi[6];
+    if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi)) {
+      // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
+      if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+      continue;
     }
-    // get_comwav_grav (grav_waves.f90:157-191)
-    double qh[3] = {(double)kint(ix, n), (double)kint(iy, n), (double)kint(iz, n)};
-    double qq = AXD_ADD(AXD_MUL(qh[0], qh[0]), AXD_MUL(qh[1], qh[1]));
-    qq = AXD_ADD(qq, AXD_MUL(qh[2], qh[2]));
-    qq = AXD_SQRT(qq);
-    C2 p[3] = {{0, 0}, {0, 0}, {0, 0}};
-    const bool nonzero = qq > 0.0;
-    if (nonzero) {
-      for (int k = 0; k < 3; ++k) qh[k] = AXD_DIV(qh[k], qq);
-      const double r = AXD_SQRT(AXD_ADD(AXD_MUL(qh[0], qh[0]), AXD_MUL(qh[1], qh[1])));
-      double c, sn;
-      if (r > 0.0) {
-        c = AXD_DIV(qh[0], r);
-        sn = AXD_DIV(qh[1], r);
-      } else {
-        c = 1.0;
-        sn = 0.0;
-      }
-      p[0] = {AXD_MUL(qh[2], c), -sn};
-      p[1] = {AXD_MUL(qh[2], sn), c};
-      p[2] = {-r, 0.0};
-    }
-    const double q = AXD_MUL(AXD_MUL(qq, dwav), tau);
     double sq, cq;
-    sincos(q, &sq, &cq);
-    C2 a11 = {acc[s].x, acc[s].y}, a21 = {acc[n3 + s].x, acc[n3 + s].y},
-       a12 = {acc[2 * n3 + s].x, acc[2 * n3 + s].y}, a22 = {acc[3 * n3 + s].x, acc[3 * n3 + s].y};
-    int comp = 0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-      for (int j = 0; j <= i; ++j, ++comp) {
-        C2 pol = {0.0, 0.0};
-        if (nonzero) {
-          pol = cmul(p[i], p[j]);
-          if (i == j) pol = {AXD_DIV(pol.r, 2.0), AXD_DIV(pol.i, 2.0)};
-        }
-        const double2 f = srcF[comp * nhalf + hidx];
-        const C2 S = {f.x, conj_back ? -f.y : f.y};
-        const C2 pp = rmul(dw, pol);
-        const C2 pn = {pp.r, -pp.i};
-        a11 = cadd(a11, cmul(rmul(cq, pp), S));
-        const C2 t21 = cmul(rmul(sq, pp), S);
-        const C2 t12 = cmul(rmul(cq, pn), S);
-        if (ref_compat) {
-          a21 = cadd(a12, t21);
-          a12 = cadd(a21, t12);
-        } else {
-          a21 = cadd(a21, t21);
-          a12 = cadd(a12, t12);
-        }
-        a22 = cadd(a22, cmul(rmul(sq, pn), S));
-      }
+    sincos(qq * dwav * tau, &sq, &cq);
+    double xp[2], xm[2], lm[2];
+    gw_contract<double, double2>(srcF, nhalf, hidx, conj_back, pr, pi, xp, xm, lm);
+    gw_update(acc, n3, s, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+  }
+}
+
+// 2 pi split for the Cody-Waite reduction of the phase (hi + lo = 2 pi to
+// about 1e-32)
+constexpr double kTwoPiHi = 6.283185307179586;
+constexpr double kTwoPiLo = 2.4492935982947064e-16;
+
+__global__ void k_gw_accumulate_f32(const float2 *__restrict__ srcF, const double *__restrict__ om, int n,
+                                    double tau, double dw, int ref_compat, double2 *__restrict__ acc) {
+  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
+    bool conj_back;
+    const int64_t hidx = gw_half_index(ix, iy, iz, n, conj_back);
+    const float kx = (float)kint(ix, n), ky = (float)kint(iy, n), kz = (float)kint(iz, n);
+    const float qq = sqrtf(kx * kx + ky * ky + kz * kz);
+    float pr[6], pi[6];
+    if (!gw_polarisation<float>(kx, ky, kz, qq, pr, pi)) {
+      if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+      continue;
     }
-    acc[s] = make_double2(a11.r, a11.i);
-    acc[n3 + s] = make_double2(a21.r, a21.i);
-    acc[2 * n3 + s] = make_double2(a12.r, a12.i);
-    acc[3 * n3 + s] = make_double2(a22.r, a22.i);
+    // phase |k| dwav tau reduced into [-pi, pi] in FP64, then FP32 sin / cos
+    const double ph = om[s] * tau;
+    const double m = rint(ph * (1.0 / kTwoPiHi));
+    const double red = fma(-m, kTwoPiLo, fma(-m, kTwoPiHi, ph));
+    float sq, cq;
+    sincosf((float)red, &sq, &cq);
+    float xpf[2], xmf[2], lmf[2];
+    gw_contract<float, float2>(srcF, nhalf, hidx, conj_back, pr, pi, xpf, xmf, lmf);
+    const double xp[2] = {xpf[0], xpf[1]}, xm[2] = {xmf[0], xmf[1]}, lm[2] = {lmf[0], lmf[1]};
+    gw_update(acc, n3, s, dw * (double)cq, dw * (double)sq, xp, xm, lm, ref_compat);
   }
 }
 
@@ -348,13 +459,20 @@ int ensure_uij_fft(axg_ctx *ctx) {
 int axg_gw_init(axg_ctx *ctx) {
   const int n = (int)ctx->n;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+  const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
+  const size_t rs = fp32 ? 4 : 8;
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->acc, (size_t)ctx->n3 * 64, "GW accumulators"));
-  AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)ctx->n3 * 6 * 8, "GW sources"));
-  AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrcF, (size_t)nhalf * 6 * 16, "GW source spectra"));
+  AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)ctx->n3 * 6 * rs, "GW sources"));
+  AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrcF, (size_t)nhalf * 6 * 2 * rs, "GW source spectra"));
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->n3 * 64, ctx->stream));
+  if (fp32) {
+    AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_omega, (size_t)ctx->n3 * 8, "GW phase rates"));
+    AXG_LAUNCH(ctx, "gw_omega", k_gw_omega, grid_for(ctx->n3), 256, 0, n, kRefTwoPi / ctx->p.dspa / n,
+               ctx->gw_omega);
+  }
   int dims[3] = {n, n, n};
   AXG_CUFFT_TRY(ctx, cufftPlanMany(&ctx->plan_gsrc, 3, dims, nullptr, 1, (int)ctx->n3, nullptr, 1,
-                                   (int)nhalf, CUFFT_D2Z, 6));
+                                   (int)nhalf, fp32 ? CUFFT_R2C : CUFFT_D2Z, 6));
   ctx->plan_gsrc_ok = true;
   AXG_CUFFT_TRY(ctx, cufftSetStream(ctx->plan_gsrc, ctx->stream));
   return AXG_OK;
@@ -365,18 +483,26 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
   const int n = (int)ctx->n;
   const double d = ctx->p.dspa * 2;
-  if (ctx->p.precision == AXG_PREC_FP32_MIXED)
-    AXG_LAUNCH(ctx, "gw_source_fp32", k_gw_source<float2>, grid_for(ctx->n3), 256, 0,
-               (const float2 *)ctx->phi[ctx->cur], n, d, ctx->gsrc);
-  else
-    AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source<double2>, grid_for(ctx->n3), 256, 0,
-               (const double2 *)ctx->phi[ctx->cur], n, d, ctx->gsrc);
-  AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
   const double dv = ctx->p.dspa * ctx->p.dspa * ctx->p.dspa;
   const double dw = tau * dtau * dv * (ctx->p.sigma_cr * ctx->p.sigma_cr);
   const double dwav = kRefTwoPi / ctx->p.dspa / n;
-  AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate, grid_for(ctx->n3), 256, 0, ctx->gsrcF, n, dwav,
-             tau, dw, ctx->p.compat == AXG_COMPAT_REF ? 1 : 0, ctx->acc);
+  const int ref = ctx->p.compat == AXG_COMPAT_REF ? 1 : 0;
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
+    float *src = (float *)ctx->gsrc;
+    AXG_LAUNCH(ctx, "gw_source_fp32", k_gw_source_f32, grid_for(ctx->n3), 256, 0,
+               (const float2 *)ctx->phi[ctx->cur], n, (float)(2.0 / (d * d)), src);
+    AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_gsrc, src, (cufftComplex *)ctx->gsrcF));
+    AXG_LAUNCH(ctx, "gw_accumulate_fp32", k_gw_accumulate_f32, grid_for(ctx->n3), 256, 0,
+               (const float2 *)ctx->gsrcF, ctx->gw_omega, n, tau, dw, ref, ctx->acc);
+    return AXG_OK;
+  }
+  int ex;
+  const int pow2 = std::frexp(d, &ex) == 0.5;
+  AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source, grid_for(ctx->n3), 256, 0, (const double2 *)ctx->phi[ctx->cur], n,
+             d, 1.0 / d, pow2, ctx->gsrc);
+  AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
+  AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate, grid_for(ctx->n3), 256, 0, ctx->gsrcF, n, dwav, tau, dw, ref,
+             ctx->acc);
   return AXG_OK;
 }
 

@@ -60,6 +60,11 @@ struct axg_ctx {
   int64_t n = 0, n3 = 0;
   int device = 0;
   cudaStream_t stream = nullptr;
+  // host<->device transfers: a copy stream and two staging buffers, so the
+  // copy of one chunk overlaps the precision conversion of the previous one
+  cudaStream_t xstream = nullptr;
+  void *xstage[2] = {nullptr, nullptr};
+  cudaEvent_t xev_copied[2] = {nullptr, nullptr}, xev_done[2] = {nullptr, nullptr}, xev_start = nullptr;
 
   // evolution state; phi[cur] / u[cur] are current (fused paths ping-pong)
   void *phi[2] = {nullptr, nullptr};
@@ -73,8 +78,9 @@ struct axg_ctx {
 
   // Green's-function GW state (grav_waves.f90)
   double2 *acc = nullptr;  // [4][n3]
-  double *gsrc = nullptr;  // [6][n3] real sources S_ij
-  double2 *gsrcF = nullptr;  // [6][n*n*(n/2+1)]
+  double *gsrc = nullptr;  // [6][n3] real sources S_ij (float for FP32-mixed)
+  double2 *gsrcF = nullptr;  // [6][n*n*(n/2+1)] (float2 for FP32-mixed)
+  double *gw_omega = nullptr;  // [n3] |k| dwav per k-site (FP32-mixed Green mode)
   cufftHandle plan_gsrc = 0;
   bool plan_gsrc_ok = false;
 

@@ -158,15 +158,18 @@ def workload_params(ag, n, precision, gw, device=0):
 
 
 def bench_ours(ag, n, precision, gw, steps, warmup, dist, device, t0=2.0, eps=0.25, clocks=False,
-               tune=True):
+               tune=True, tile=None):
     p = workload_params(ag, n, precision, gw, device)
     lat = ag.Lattice(p)
     try:
         lat.ic_gaussian_flat(kcut=2.0 * np.pi / (8 * p.dspa))
         dt, _ = lat.get_dtau(t0, 32.0, eps)
-        tile = None
-        if tune and precision != ag.PREC_FP64_PLAIN:
+        if tile is not None and precision != ag.PREC_FP64_PLAIN:
+            lat.set_tile(tile)
+        elif tune and precision != ag.PREC_FP64_PLAIN:
             tile, _ = lat.autotune(3)
+        else:
+            tile = None
         t = t0
         lat.leapfrog(t, dt, 1, True, False)  # half drift + one step
         t += dt * 1.5
@@ -230,8 +233,19 @@ def bench_e2e(ag, lat, n, nsub, reps, t, dt):
         t += dt * nsub
     per = float(np.median(times[1:]))
     bytes_each = 2 * n ** 3 * 16
+    # one more interval split into its three calls (each returns synchronised)
+    t0 = time.perf_counter()
+    assert lib.axg_upload(lat.handle, dp(h_phi), dp(h_phid), n * n, 0) == 0
+    t1 = time.perf_counter()
+    assert lib.axg_leapfrog(lat.handle, t, dt, nsub, 1, 1) == 0
+    lat.synchronize()
+    t2 = time.perf_counter()
+    assert lib.axg_download(lat.handle, dp(h_phi), dp(h_phid), n * n, 0) == 0
+    t3 = time.perf_counter()
+    split = {"upload_s": t1 - t0, "leapfrog_s": t2 - t1, "download_s": t3 - t2,
+             "upload_gbs": bytes_each / (t1 - t0) / 1e9, "download_gbs": bytes_each / (t3 - t2) / 1e9}
     return {"value": nsub * n ** 3 / per, "unit": UNIT, "h2d_bytes_per_step": bytes_each / nsub,
-            "d2h_bytes_per_step": bytes_each / nsub, "interval_steps": nsub, "s_per_interval": per,
+            "d2h_bytes_per_step": bytes_each / nsub, "interval_steps": nsub, "s_per_interval": per, "split": split,
             "note": "public C-ABI, host-resident complex128 phi and phidot uploaded and downloaded "
                     "once per interval of %d leapfrog steps (pinned host memory); u_ij device-resident" % nsub}
 
@@ -281,28 +295,75 @@ def bench_ensemble(ag, steps, device, sizes=ENSEMBLE_SIZES):
         ens.close()
 
 
-def bench_adjoint(ag, device, n=256, steps=256, stride=64):
-    """Config 4 at reduced length: gradient of J = band-integrated GW energy
-    (k in [m_r/8, m_r/2]) with respect to lambda and the initial fields, by
-    the hand-written adjoint (checkpoint every `stride` steps); its cost
-    against a plain FP64 forward run of the same steps."""
-    p = ag.default_params(ngrid=n, precision=ag.PREC_FP64_PLAIN, gw_mode=ag.GW_UIJ, potential=ag.POT_QUARTIC,
-                          dspa=1.0, sigma_cr=1.0, vev=1.0, seed=1, device=device, **{"lambda": 1.0})
-    t1, dt = 1.0, 0.2
+def bench_adjoint(ag, device, n=256, steps=2000, stride=64, fp64_steps=256):
+    """The 256^3 gradient workload: J = GW energy of u_ij over k in
+    [m_r/8, m_r/2] after `steps` leapfrog steps from tau = 1 (dt = 0.2), its
+    gradient with respect to lambda and the initial fields by the
+    hand-written adjoint (checkpoint every `stride` steps), and the cost of
+    forward + reverse against a plain forward run of the same steps.  FP32-mixed
+    (the workload's precision) at full length; FP64-plain on a shorter run."""
+    out = {"n": n, "stride": stride, "timing": "CUDA events on the library stream"}
+    for name, prec, st in (("fp32_mixed", ag.PREC_FP32_MIXED, steps), ("fp64_plain", ag.PREC_FP64_PLAIN, fp64_steps)):
+        # sigma_cr = 0.005: dt = 0.2 stays inside the leapfrog's stability limit
+        # (dt^2 (12/dx^2 + 6 tau^2 sigma_cr^2) < 4) over the 2000-step run to tau ~ 400
+        p = ag.default_params(ngrid=n, precision=prec, gw_mode=ag.GW_UIJ, potential=ag.POT_QUARTIC,
+                              dspa=1.0, sigma_cr=0.005, vev=1.0, seed=1, device=device, **{"lambda": 1.0})
+        t1, dt = 1.0, 0.2
+        with ag.Lattice(p) as lat:
+            lat.ic_gaussian_flat(kcut=1.0, realisation=0)
+            lat.leapfrog(t1, dt, 4, True, True)  # warm-up (plans, tensor maps, first launches)
+            lat.ic_gaussian_flat(kcut=1.0, realisation=0)
+            lat.synchronize()
+            lat.event_record(0)
+            lat.leapfrog(t1, dt, st, True, True)
+            lat.event_record(1)
+            plain = lat.event_elapsed(0, 1)
+            lat.ic_gaussian_flat(kcut=1.0, realisation=0)
+            J, dl, _, _, mf, mr = lat.adjoint_gw_band(t1, dt, st, stride, 0.125, 0.5, want_grads=False)
+        out[name] = {"steps": st, "J": J, "dJ_dlambda": dl, "ms_forward_step": plain / st,
+                     "ms_forward_with_checkpoints": mf, "ms_reverse": mr, "reverse_vs_forward": mr / plain,
+                     "adjoint_total_vs_forward": (mf + mr) / plain}
+    return out
+
+
+def bench_output_calls(ag, n, device, steps=200, max_fit_cells=2_000_000):
+    """Per-call cost of the output-time routines on the evolved FP32-mixed
+    lattice (host wall clock around each call; every call synchronises):
+    plaquette winding, cell classification, defect fits and sums, field
+    spectrum with window deconvolution, u_ij GW spectra (linear and log
+    bins).  Defect fits are skipped above max_fit_cells string+wall cells."""
+    p = workload_params(ag, n, ag.PREC_FP32_MIXED, ag.GW_UIJ, device)
+    out = {"n": n, "evolved_steps": steps, "timing": "host wall clock, each call synchronises"}
     with ag.Lattice(p) as lat:
-        lat.ic_gaussian_flat(kcut=1.0, realisation=0)
-        lat.leapfrog(t1, dt, 4, True, True)  # warm-up (plans, first launches)
-        lat.ic_gaussian_flat(kcut=1.0, realisation=0)
-        lat.synchronize()
-        lat.event_record(0)
-        lat.leapfrog(t1, dt, steps, True, True)
-        lat.event_record(1)
-        plain = lat.event_elapsed(0, 1)
-        lat.ic_gaussian_flat(kcut=1.0, realisation=0)
-        J, dl, _, _, mf, mr = lat.adjoint_gw_band(t1, dt, steps, stride, 0.125, 0.5, want_grads=False)
-    return {"n": n, "steps": steps, "stride": stride, "J": J, "dJ_dlambda": dl, "ms_plain_forward": plain,
-            "ms_forward_with_checkpoints": mf, "ms_reverse": mr, "cost_vs_forward": (mf + mr) / plain,
-            "precision": "fp64_plain", "timing": "CUDA events on the library stream"}
+        lat.ic_gaussian_flat(kcut=2.0 * np.pi / (8 * p.dspa))
+        dt, _ = lat.get_dtau(2.0, 32.0, 0.25)
+        lat.leapfrog(2.0, dt, steps, True, True)
+        tau = 2.0 + dt * steps
+        out["tau"] = tau
+
+        def timed(name, fn, reps=3):
+            fn()  # first call allocates plans / tables
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                r = fn()
+            out[name] = {"ms": 1e3 * (time.perf_counter() - t0) / reps}
+            return r
+
+        wind = timed("string_winding", lat.string_winding)
+        counts = timed("classify_cells", lambda: lat.classify_cells(7))
+        out["string_winding"]["plaquettes"] = [int(c) for c in wind]
+        out["classify_cells"]["counts"] = [int(c) for c in counts]
+        cells = int(counts[0] + counts[1])
+        if cells <= max_fit_cells:
+            r = timed("id_defects", lambda: lat.id_defects(1, tau), reps=1)
+            out["id_defects"]["fitted_cells"] = cells
+            out["id_defects"]["cells_per_s"] = cells / (out["id_defects"]["ms"] * 1e-3)
+        else:
+            out["id_defects"] = {"skipped": f"{cells} string+wall cells above the {max_fit_cells} cap"}
+        timed("spectrum_estimation", lambda: lat.spectrum_estimation(tau))
+        timed("grav_spec_estimation", lambda: lat.grav_spec_estimation(tau))
+        timed("grav_spec_log", lambda: lat.grav_spec_log(tau))
+    return out
 
 
 def accuracy_fp32(ag, n, steps, device):
@@ -405,7 +466,11 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient cost block")
     ap.add_argument("--no-phi-only", action="store_true", help="skip the phi-only (no u_ij) figures")
-    ap.add_argument("--adjoint-steps", type=int, default=256)
+    ap.add_argument("--no-green", action="store_true", help="skip the Green's-function GW mode step cost")
+    ap.add_argument("--no-output-calls", action="store_true", help="skip the defect / spectrum call timings")
+    ap.add_argument("--tile", type=int, default=None,
+                    help="fused-kernel tile index (axg_tile_info) instead of autotuning the headline arm")
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -428,7 +493,8 @@ def main():
     import axion_grav_gb300 as ag
 
     n = args.n
-    r32 = bench_ours(ag, n, ag.PREC_FP32_MIXED, ag.GW_UIJ, args.steps, args.warmup, dist, local, clocks=True)
+    r32 = bench_ours(ag, n, ag.PREC_FP32_MIXED, ag.GW_UIJ, args.steps, args.warmup, dist, local, clocks=True,
+                     tile=args.tile)
     lat = r32.pop("lat")
     e2e = bench_e2e(ag, lat, n, args.e2e_interval, args.e2e_reps, r32["t"], r32["dt"]) if rank == 0 else None
     lat.close()
@@ -464,6 +530,29 @@ def main():
                 "hbm_frac": (byts / (tms * 1e-3) / 1e9) / peak if tms > 0 else None,
                 "fp32_mixed_speedup": value / v64 / world * world}
 
+    # FP64-fused: the TMA kernel doing the plain path's FP64 operations in the
+    # same order (bit-identical results), one pass per step
+    if fp64 is not None:
+        st64f = max(3, args.steps // 8)
+        rf = bench_ours(ag, n, ag.PREC_FP64_FUSED, ag.GW_UIJ, st64f, args.warmup, dist, local)
+        rf.pop("lat").close()
+        kf = {k: (l, t) for k, l, t in rf["kernels"]}
+        fp64["fused"] = {"value": job_rate(world, sites, st64f, replica_time_ms(rf["ms"], dist)),
+                         "ms_per_step": rf["ms"] / st64f, "steps": st64f, "tile": rf["tile_shape"],
+                         "kernels": {k: {"launches": l, "avg_ms": t / max(l, 1)} for k, (l, t) in kf.items()}}
+
+    green = None
+    if not args.no_green:
+        green = {}
+        for name, prec in (("fp32_mixed", ag.PREC_FP32_MIXED), ("fp64_plain", ag.PREC_FP64_PLAIN)):
+            st = max(3, args.steps // 20)
+            r = bench_ours(ag, n, prec, ag.GW_GREEN, st, args.warmup, dist, local)
+            r.pop("lat").close()
+            kk = {k: (l, t) for k, l, t in r["kernels"]}
+            green[name] = {"ms_per_step": r["ms"] / st, "steps": st,
+                           "value": job_rate(world, sites, st, replica_time_ms(r["ms"], dist)),
+                           "kernels": {k: {"launches": l, "avg_ms": t / max(l, 1)} for k, (l, t) in kk.items()}}
+
     phi_only = None
     if not args.no_phi_only:
         phi_only = {}
@@ -491,6 +580,13 @@ def main():
             accuracy = accuracy_fp32(ag, n, args.accuracy_steps, local)
         except Exception as exc:
             accuracy = {"error": str(exc)}
+
+    output_calls = None
+    if rank == 0 and not args.no_output_calls:
+        try:
+            output_calls = bench_output_calls(ag, n, local)
+        except Exception as exc:
+            output_calls = {"error": str(exc)}
 
     adjoint = None
     if rank == 0 and not args.no_adjoint:
@@ -523,7 +619,7 @@ def main():
                        "tile": r32["tile_shape"]},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r32["launches"],
             "clocks": r32["clocks"], "fp64_plain": fp64, "ensemble": ensemble, "accuracy": accuracy,
-            "adjoint": adjoint, "phi_only": phi_only,
+            "adjoint": adjoint, "phi_only": phi_only, "green": green, "output_calls": output_calls,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

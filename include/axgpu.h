@@ -151,7 +151,10 @@ int axg_symplectic_integration(axg_ctx *ctx, double t1, double t2, double eps_dt
                                int64_t *nsteps_out);
 /* nsteps kick+drift steps of size dt starting at kick time t (fused paths:
  * one pass per step); first_half / last_half apply the half drifts of the DKD
- * scheme before the first / instead of the last full drift. */
+ * scheme before the first / instead of the last full drift.  dt < 0 runs the
+ * same scheme backwards in time (t1 is then the later time; every time of
+ * the run must stay positive): the damped leapfrog is time-reversible, so
+ * leapfrog(t1 + n dt, -dt, n) undoes leapfrog(t1, dt, n) up to rounding. */
 int axg_leapfrog(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half,
                  int last_half);
 
@@ -289,8 +292,11 @@ int axg_launch_count(const axg_ctx *ctx, int64_t *launches);
  * (quartic model, A = lambda/2, B = -lambda v^2/2) and, when the pointers are
  * non-NULL, dJ/dphi and dJ/dphi' of the initial state as complex128 host
  * arrays (d/dRe + i d/dIm).  ms_forward / ms_reverse (may be NULL) give the
- * GPU time of the two sweeps.  FP64-plain contexts with gw_mode UIJ; the
- * context is left at the final state of the forward run. */
+ * GPU time of the two sweeps.  gw_mode UIJ, any precision: the forward run
+ * is the context's own step (FP64-plain, FP64-fused or FP32-mixed) and the
+ * adjoint runs in the same arithmetic (FP32 for FP32-mixed; dJ/dlambda is
+ * accumulated in FP64).  The context is left at the final state of the
+ * forward run. */
 int axg_adjoint_gw_band(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half,
                         int last_half, int64_t stride, double kmin, double kmax, double *J,
                         double *dJ_dlambda, double *grad_phi0, double *grad_phidot0,

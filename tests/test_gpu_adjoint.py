@@ -104,7 +104,49 @@ def test_adjoint_leaves_final_state_of_forward_run():
 
 def test_adjoint_rejects_unsupported_paths():
     p = params(16)
-    p.precision = ag.PREC_FP32_MIXED
+    p.gw_mode = ag.GW_NONE
     with ag.Lattice(p) as lat:
         with pytest.raises(ag.AxgError, match="UNSUPPORTED"):
             lat.adjoint_gw_band(1.5, 0.05, 4, 2, 0.5, 3.0)
+
+
+def _with_precision(p, prec):
+    q = type(p).from_buffer_copy(bytes(p))
+    q.precision = prec
+    return q
+
+
+def test_fp64_fused_adjoint_equals_plain():
+    """The fused FP64 forward is bit-identical to the plain one, so the
+    adjoint built on it gives the same J and gradients."""
+    n = 32
+    st = state(n, 7)
+    a = gpu_adjoint(params(n), st)[0]
+    b = gpu_adjoint(_with_precision(params(n), ag.PREC_FP64_FUSED), st)[0]
+    assert b[0] == pytest.approx(a[0], rel=1e-14)  # J is reduced with atomics: last-bit order effects
+    assert b[1] == pytest.approx(a[1], rel=1e-12)
+    for g, h in ((b[2], a[2]), (b[3], a[3])):
+        assert np.max(np.abs(g - h)) <= 1e-12 * np.max(np.abs(h))
+
+
+def test_fp32_adjoint_against_fp64_adjoint():
+    """FP32-mixed forward and FP32 adjoint arithmetic (dJ/dlambda summed in
+    FP64) against the FP64 adjoint of the same initial state."""
+    n = 32
+    st = state(n, 8)
+    a = gpu_adjoint(params(n), st)[0]
+    b = gpu_adjoint(_with_precision(params(n), ag.PREC_FP32_MIXED), st)[0]
+    assert b[0] == pytest.approx(a[0], rel=1e-4)
+    assert b[1] == pytest.approx(a[1], rel=1e-3)
+    for g, h in ((b[2], a[2]), (b[3], a[3])):
+        assert np.linalg.norm(g - h) <= 1e-3 * np.linalg.norm(h)
+
+
+def test_fp32_adjoint_lambda_against_finite_differences():
+    n, eps = 32, 1e-3
+    st = state(n, 9)
+    p32 = lambda lam: _with_precision(params(n, lam), ag.PREC_FP32_MIXED)
+    (J, dl, *_), _ = gpu_adjoint(p32(1.0), st)
+    (Jp, *_), _ = gpu_adjoint(p32(1.0 + eps), st)
+    (Jm, *_), _ = gpu_adjoint(p32(1.0 - eps), st)
+    assert dl == pytest.approx((Jp - Jm) / (2 * eps), rel=1e-2)

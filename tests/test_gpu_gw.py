@@ -51,6 +51,27 @@ def test_green_accumulators_and_spectrum(compat, precision):
     np.testing.assert_allclose(gpw, pw, rtol=1e-9)
 
 
+@pytest.mark.parametrize("compat", [ag.COMPAT_REF, ag.COMPAT_INTENDED])
+def test_green_fp32_mixed_against_fp64_oracle(compat):
+    """FP32 sources, R2C transforms and contractions with FP64 accumulators:
+    accumulators and the per-bin GW numerator against the FP64 oracle."""
+    n = 32
+    phi, phid = init_state(n, 4)
+    p64 = params(n, ag.PREC_FP64_PLAIN, ag.GW_GREEN, compat=compat)
+    acc = np.zeros((4, n, n, n), np.complex128)
+    nt = axo.symplectic_integration(p64, phi.copy(), phid.copy(), None, None, acc, 2.0, 2.8, 0.4)
+    w, pw, nu, de = axo.grav_spec_estimation(p64, acc)
+    with ag.Lattice(params(n, ag.PREC_FP32_MIXED, ag.GW_GREEN, compat=compat)) as lat:
+        lat.upload(phi, phid)
+        assert lat.symplectic_integration(2.0, 2.8, 0.4) == nt
+        g_acc = lat.download_gw_green()
+        gw_, gpw, gnu, gde = lat.grav_spec_estimation(2.8)
+    assert rel(g_acc, acc) < 1e-4
+    np.testing.assert_array_equal(gde, de)
+    np.testing.assert_allclose(gnu, nu, rtol=1e-3)
+    np.testing.assert_allclose(gpw, pw, rtol=1e-3)
+
+
 def test_green_log_bins():
     n = 16
     phi, phid = init_state(n, 2)
