@@ -378,6 +378,19 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventCreate(&e2);
+  auto cleanup = axg_on_exit([&] {
+    cudaStreamSynchronize(ctx->stream);
+    if (pfo) cufftDestroy(pf);
+    if (pbo) cufftDestroy(pb);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    axg_free(ctx, (void **)&ck);
+    axg_free(ctx, (void **)&adj);
+    axg_free(ctx, (void **)&Q);
+    axg_free(ctx, (void **)&fbuf);
+    ctx->flags_valid = false;
+  });
   do {
     // nck checkpoints plus the final phi, phi' (restored after the reverse sweep)
     if ((rc = axg_alloc(ctx, (void **)&ck, ck_b * (nck + 1), "adjoint checkpoints"))) break;
@@ -519,17 +532,6 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
     load(nck);
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   } while (0);
-  cudaStreamSynchronize(ctx->stream);
-  if (pfo) cufftDestroy(pf);
-  if (pbo) cufftDestroy(pb);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaEventDestroy(e2);
-  axg_free(ctx, (void **)&ck);
-  axg_free(ctx, (void **)&adj);
-  axg_free(ctx, (void **)&Q);
-  axg_free(ctx, (void **)&fbuf);
-  ctx->flags_valid = false;
   return rc;
 }
 

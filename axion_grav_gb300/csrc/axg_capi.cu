@@ -537,6 +537,7 @@ int axg_destroy(axg_ctx *ctx) {
     axg_free(ctx, &ctx->xstage[b]);
   }
   if (ctx->xev_start) cudaEventDestroy(ctx->xev_start);
+  for (auto &e : ctx->bin_cache) axg_free(ctx, (void **)&e.tab);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return AXG_OK;
@@ -589,19 +590,51 @@ int axg_download_uij(axg_ctx *ctx, double *u, double *udot) {
   return AXG_OK;
 }
 
+// The FP32-mixed context keeps each accumulator component as a float-float
+// pair (hi, lo); the host side is always complex128 [4][N^3].
 int axg_upload_gw_green(axg_ctx *ctx, const double *acc) {
   if (!valid_ctx(ctx) || !acc) return AXG_ERR_ARG;
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
-  AXG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->acc, acc, (size_t)ctx->n3 * 64, cudaMemcpyHostToDevice, ctx->stream));
-  AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->p.precision != AXG_PREC_FP32_MIXED) {
+    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->acc, acc, (size_t)ctx->n3 * 64, cudaMemcpyHostToDevice, ctx->stream));
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return AXG_OK;
+  }
+  const size_t total = (size_t)ctx->n3 * 4, chunk = (size_t)1 << 22;  // complex entries
+  std::vector<float4> buf(std::min(chunk, total));
+  float4 *dev = (float4 *)ctx->acc;
+  for (size_t o = 0; o < total; o += chunk) {
+    const size_t m = std::min(chunk, total - o);
+    for (size_t k = 0; k < m; ++k) {
+      const double re = acc[2 * (o + k)], im = acc[2 * (o + k) + 1];
+      const float rh = (float)re, ih = (float)im;
+      buf[k] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+    }
+    AXG_CUDA_TRY(ctx, cudaMemcpy(dev + o, buf.data(), m * sizeof(float4), cudaMemcpyHostToDevice));
+  }
   return AXG_OK;
 }
 
 int axg_download_gw_green(axg_ctx *ctx, double *acc) {
   if (!valid_ctx(ctx) || !acc) return AXG_ERR_ARG;
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
-  AXG_CUDA_TRY(ctx, cudaMemcpyAsync(acc, ctx->acc, (size_t)ctx->n3 * 64, cudaMemcpyDeviceToHost, ctx->stream));
+  if (ctx->p.precision != AXG_PREC_FP32_MIXED) {
+    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(acc, ctx->acc, (size_t)ctx->n3 * 64, cudaMemcpyDeviceToHost, ctx->stream));
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return AXG_OK;
+  }
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  const size_t total = (size_t)ctx->n3 * 4, chunk = (size_t)1 << 22;
+  std::vector<float4> buf(std::min(chunk, total));
+  const float4 *dev = (const float4 *)ctx->acc;
+  for (size_t o = 0; o < total; o += chunk) {
+    const size_t m = std::min(chunk, total - o);
+    AXG_CUDA_TRY(ctx, cudaMemcpy(buf.data(), dev + o, m * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < m; ++k) {
+      acc[2 * (o + k)] = (double)buf[k].x + (double)buf[k].y;
+      acc[2 * (o + k) + 1] = (double)buf[k].z + (double)buf[k].w;
+    }
+  }
   return AXG_OK;
 }
 
@@ -743,6 +776,91 @@ int axg_launch_count(const axg_ctx *ctx, int64_t *launches) {
 // in global x-fastest order, as io_chk writes them; u_ij blocks appended when
 // the context evolves u_ij; CRC-32 of the whole file in path+".crc".
 // ---------------------------------------------------------------------------
+namespace {
+// FP32-mixed sidecar path+".fp32": the raw device state (phi and its Kahan
+// compensation, phi'; u, its compensation and u' when present) so that a
+// resumed FP32 run continues bit for bit; the complex128 file alone fixes
+// only the compensated value phi - c.  Layout: "AXGFP32" NUL, int64 N, int64
+// uij, the arrays, CRC-32 of everything before it.
+struct RawField {
+  void *dev;
+  size_t bytes;
+};
+std::vector<RawField> fp32_fields(axg_ctx *ctx) {
+  const size_t n3 = (size_t)ctx->n3;
+  std::vector<RawField> f = {{ctx->phi[ctx->cur], n3 * 8}, {ctx->cphi, n3 * 8}, {ctx->phid, n3 * 8}};
+  if (ctx->p.gw_mode == AXG_GW_UIJ) {
+    f.push_back({ctx->u[ctx->cur], n3 * 24});
+    f.push_back({ctx->cu, n3 * 24});
+    f.push_back({ctx->ud, n3 * 24});
+  }
+  return f;
+}
+const char kFp32Magic[8] = {'A', 'X', 'G', 'F', 'P', '3', '2', 0};
+
+int write_fp32_sidecar(axg_ctx *ctx, const std::string &path) {
+  FILE *f = std::fopen(path.c_str(), "wb");
+  if (!f) return axg_set_error(ctx, AXG_ERR_IO, "cannot open " + path);
+  const int64_t hdr[2] = {ctx->n, ctx->p.gw_mode == AXG_GW_UIJ ? 1 : 0};
+  uint32_t crc = crc32_update(0, (const unsigned char *)kFp32Magic, 8);
+  crc = crc32_update(crc, (const unsigned char *)hdr, sizeof(hdr));
+  int rc = AXG_OK;
+  if (std::fwrite(kFp32Magic, 1, 8, f) != 8 || std::fwrite(hdr, 1, sizeof(hdr), f) != sizeof(hdr))
+    rc = axg_set_error(ctx, AXG_ERR_IO, "short write");
+  std::vector<unsigned char> buf;
+  for (const RawField &r : fp32_fields(ctx)) {
+    if (rc != AXG_OK) break;
+    buf.resize(r.bytes);
+    if (cudaMemcpy(buf.data(), r.dev, r.bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      rc = axg_set_error(ctx, AXG_ERR_CUDA, "sidecar download");
+      break;
+    }
+    if (std::fwrite(buf.data(), 1, r.bytes, f) != r.bytes) rc = axg_set_error(ctx, AXG_ERR_IO, "short write");
+    crc = crc32_update(crc, buf.data(), r.bytes);
+  }
+  if (rc == AXG_OK && std::fwrite(&crc, 1, 4, f) != 4) rc = axg_set_error(ctx, AXG_ERR_IO, "short write");
+  if (std::fclose(f) != 0 && rc == AXG_OK) rc = axg_set_error(ctx, AXG_ERR_IO, "close failed");
+  return rc;
+}
+
+// 1: restored, 0: no sidecar, < 0: error (a sidecar that exists must verify)
+int read_fp32_sidecar(axg_ctx *ctx, const std::string &path) {
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) return 0;
+  char magic[8];
+  int64_t hdr[2];
+  int rc = AXG_OK;
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kFp32Magic, 8) != 0 ||
+      std::fread(hdr, 1, sizeof(hdr), f) != sizeof(hdr)) {
+    std::fclose(f);
+    return axg_set_error(ctx, AXG_ERR_IO, "FP32 sidecar: bad header");
+  }
+  if (hdr[0] != ctx->n || hdr[1] != (ctx->p.gw_mode == AXG_GW_UIJ ? 1 : 0)) {
+    std::fclose(f);
+    return axg_set_error(ctx, AXG_ERR_IO, "FP32 sidecar: lattice or u_ij mismatch");
+  }
+  uint32_t crc = crc32_update(0, (const unsigned char *)magic, 8);
+  crc = crc32_update(crc, (const unsigned char *)hdr, sizeof(hdr));
+  const std::vector<RawField> fields = fp32_fields(ctx);
+  std::vector<std::vector<unsigned char>> data(fields.size());
+  for (size_t k = 0; k < fields.size() && rc == AXG_OK; ++k) {
+    data[k].resize(fields[k].bytes);
+    if (std::fread(data[k].data(), 1, fields[k].bytes, f) != fields[k].bytes)
+      rc = axg_set_error(ctx, AXG_ERR_IO, "FP32 sidecar too short");
+    else
+      crc = crc32_update(crc, data[k].data(), fields[k].bytes);
+  }
+  uint32_t want = 0;
+  if (rc == AXG_OK && std::fread(&want, 1, 4, f) != 4) rc = axg_set_error(ctx, AXG_ERR_IO, "FP32 sidecar too short");
+  std::fclose(f);
+  if (rc != AXG_OK) return rc;
+  if (want != crc) return axg_set_error(ctx, AXG_ERR_IO, "FP32 sidecar CRC mismatch");
+  for (size_t k = 0; k < fields.size(); ++k)
+    AXG_CUDA_TRY(ctx, cudaMemcpy(fields[k].dev, data[k].data(), fields[k].bytes, cudaMemcpyHostToDevice));
+  return 1;
+}
+}  // namespace
+
 int axg_write_chk(axg_ctx *ctx, const char *path) {
   if (!valid_ctx(ctx) || !path) return AXG_ERR_ARG;
   const int64_t n3 = ctx->n3;
@@ -777,6 +895,10 @@ int axg_write_chk(axg_ctx *ctx, const char *path) {
   if (!c) return axg_set_error(ctx, AXG_ERR_IO, "cannot open " + cpath);
   std::fprintf(c, "%08x %lld\n", crc, (long long)ctx->n);
   std::fclose(c);
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return write_fp32_sidecar(ctx, std::string(path) + ".fp32");
+  }
   return AXG_OK;
 }
 
@@ -823,6 +945,12 @@ int axg_read_chk(axg_ctx *ctx, const char *path) {
   }
   AXG_TRY(axg_upload(ctx, phi.data(), phid.data(), ctx->n * ctx->n, 0));
   if (ctx->p.gw_mode == AXG_GW_UIJ) AXG_TRY(axg_upload_uij(ctx, ub.data(), udb.data()));
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
+    // the raw FP32 state, when its sidecar is there, replaces the converted one
+    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    const int r = read_fp32_sidecar(ctx, std::string(path) + ".fp32");
+    if (r < 0) return r;
+  }
   return AXG_OK;
 }
 

@@ -2,16 +2,27 @@
 //
 // This translation unit is compiled with -fmad=false: every floating-point
 // expression below rounds each operation separately, exactly as IEEE host C
-// does without contraction, and atan2 / sin / cos are the deterministic
-// versions of axg_detmath.h.  Cell flags, counts, plaquette windings and every
-// per-cell fit (position, direction, length, velocity, wall area) are
-// therefore bit-identical to a host evaluation of the same formulas.
+// does without contraction, and the FP64 atan2 / sin / cos are the
+// deterministic versions of axg_detmath.h.  Cell flags, counts, plaquette
+// windings and every per-cell fit (position, direction, length, velocity,
+// wall area) are therefore bit-identical to a host evaluation of the same
+// formulas.  FP32 phases (atan2f) serve only as a filter that decides the
+// cells whose outcome cannot change within their error bound; all other
+// cells go through the FP64 path.
 //
 // Passes (all O(N^3) passes are HBM-streaming, the fits are sparse):
-//   1. phase     : ph[s] = atan2(Im phi, Re phi)                 (8 B / site)
+//   1. phase     : ph[s] = atan2f(Im phi, Re phi), FP32         (4 B / site)
 //   2. classify  : 8 corner phases, sort, largest circular gap -> int8 flags,
-//                  warp-aggregated counts (defects_3d.f90:67-103, 309-349)
-//   3. winding   : three plaquettes per site
+//                  warp-aggregated counts (defects_3d.f90:67-103, 309-349).
+//                  Filtered: the FP32 phases are within 1e-6 of the FP64
+//                  ones, and sorting moves no value by more than that, so a
+//                  cell whose every decision (wall gap against wrap gap,
+//                  largest gap against pi and 7 pi / 4) clears a 2e-5
+//                  margin has the FP64 flags; any other cell is redone from
+//                  phi with the deterministic FP64 atan2, as on the host.
+//   3. winding   : three plaquettes per site, filtered the same way (a
+//                  corner difference within the margin of +-pi is redone in
+//                  FP64)
 //   4. compaction: string and wall cells listed in cell order
 //   5. fits      : one thread per listed cell -- position_string (1001 random
 //                  starts + Nelder-Mead, defects_3d.f90:435-603), string_length
@@ -39,13 +50,24 @@ __device__ __forceinline__ void load_c(const V *a, int64_t s, double &re, double
   im = (double)v.y;
 }
 
+// FP32 phase of each site.  For an FP64 field a component outside the FP32
+// normal range (and not zero) would lose relative precision in conversion:
+// such sites get NaN and every cell touching them is classified in FP64.
 template <typename V>
-__global__ void k_phase(const V *__restrict__ phi, double *__restrict__ ph, int64_t n3) {
+__global__ void k_phase32(const V *__restrict__ phi, float *__restrict__ ph, int64_t n3) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-    double re, im;
-    load_c(phi, s, re, im);
-    ph[s] = axd_atan2(im, re);
+    const V v = phi[s];
+    if constexpr (sizeof(v.x) == 4) {
+      ph[s] = atan2f(v.y, v.x);
+    } else {
+      auto in_range = [](double x) {
+        const long long b = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+        const int e = (int)(b >> 52);
+        return b == 0 || (e >= 1023 - 126 && e <= 1023 + 127);
+      };
+      ph[s] = (in_range(v.x) && in_range(v.y)) ? atan2f((float)v.y, (float)v.x) : __int_as_float(0x7fc00000);
+    }
   }
 }
 
@@ -94,32 +116,112 @@ __device__ __forceinline__ int8_t classify_sorted(const double pht[8], int which
   return flag;
 }
 
-__device__ __forceinline__ void warp_count(unsigned long long *dst, bool pred) {
-  const unsigned b = __ballot_sync(0xffffffffu, pred);
-  if ((threadIdx.x & 31) == 0 && b) atomicAdd(dst, (unsigned long long)__popc(b));
+// Three counters per block: warps tally ballots in registers, the block
+// adds them in shared memory, and one thread adds the block's totals to the
+// global counters (3 global atomics per block instead of 3 per warp pass).
+struct BlockCount3 {
+  unsigned long long c[3] = {0, 0, 0};
+  __device__ __forceinline__ void add(bool a, bool b, bool d) {
+    c[0] += __popc(__ballot_sync(0xffffffffu, a));
+    c[1] += __popc(__ballot_sync(0xffffffffu, b));
+    c[2] += __popc(__ballot_sync(0xffffffffu, d));
+  }
+  __device__ __forceinline__ void flush(unsigned long long *dst) {
+    __shared__ unsigned long long sh[3];
+    if (threadIdx.x < 3) sh[threadIdx.x] = 0;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0)
+      for (int k = 0; k < 3; ++k)
+        if (c[k]) atomicAdd(&sh[k], c[k]);
+    __syncthreads();
+    if (threadIdx.x < 3 && sh[threadIdx.x]) atomicAdd(&dst[threadIdx.x], sh[threadIdx.x]);
+  }
+};
+
+constexpr float kMargin = 2e-5f;  // >> 4 (2 x 1e-6 phase error + FP32 rounding of a gap)
+
+__device__ __forceinline__ void cswapf(float &a, float &b) {
+  const float lo = fminf(a, b), hi = fmaxf(a, b);
+  a = lo;
+  b = hi;
+}
+__device__ __forceinline__ void sort8f(float v[8]) {
+  cswapf(v[0], v[1]); cswapf(v[2], v[3]); cswapf(v[4], v[5]); cswapf(v[6], v[7]);
+  cswapf(v[0], v[2]); cswapf(v[1], v[3]); cswapf(v[4], v[6]); cswapf(v[5], v[7]);
+  cswapf(v[1], v[2]); cswapf(v[5], v[6]); cswapf(v[0], v[4]); cswapf(v[3], v[7]);
+  cswapf(v[1], v[5]); cswapf(v[2], v[6]);
+  cswapf(v[1], v[4]); cswapf(v[3], v[6]);
+  cswapf(v[2], v[4]); cswapf(v[3], v[5]);
+  cswapf(v[3], v[4]);
 }
 
-__global__ void k_classify(const double *__restrict__ ph, int n, int which, int8_t *__restrict__ flags,
-                           unsigned long long *__restrict__ counts) {
+// id_with_phase on FP32 phases; false when a decision lies inside the margin
+__device__ __forceinline__ bool classify_sorted_f(const float p[8], int which, int8_t &flag) {
+  flag = 0;
+  const float t = p[0] - p[7] + (float)kRefTwoPi;
+  float tmax = p[1] - p[0];
+#pragma unroll
+  for (int k = 1; k < 7; ++k) tmax = fmaxf(tmax, p[k + 1] - p[k]);
+  bool sure = true;
+  if (which & AXG_F_ID_WALLS) {
+    sure = fabsf(tmax - t) >= kMargin;
+    if (tmax > t) flag += 2;
+    else tmax = fmaxf(t, tmax);
+  } else {
+    tmax = fmaxf(t, tmax);
+  }
+  if (which & AXG_F_ID_STRINGS) {
+    sure = sure && fabsf(tmax - (float)kStringPhdiff) >= kMargin;
+    if (tmax < (float)kStringPhdiff) flag += 1;
+  }
+  if (which & AXG_F_SPEC_EST) {
+    sure = sure && fabsf(tmax - (float)kRemovalPhdiff) >= kMargin;
+    if (tmax < (float)kRemovalPhdiff) flag += 4;
+  }
+  return sure;
+}
+
+template <typename V>
+__device__ __forceinline__ double phase64(const V *phi, int64_t s) {
+  double re, im;
+  load_c(phi, s, re, im);
+  return axd_atan2(im, re);
+}
+
+template <typename V>
+__global__ void k_classify(const float *__restrict__ ph, const V *__restrict__ phi, int n, int which,
+                           int8_t *__restrict__ flags, unsigned long long *__restrict__ counts) {
   const int64_t n3 = (int64_t)n * n * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  BlockCount3 tally;
   // uniform trip count so every lane reaches the ballots
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n3; base += stride) {
     const int64_t s = base + threadIdx.x;
     int8_t f = 0;
     if (s < n3) {
       const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
-      double v[8];
+      float v[8];
+      bool known = true;
 #pragma unroll
-      for (int c = 0; c < 8; ++c) v[c] = ph[corner(n, ix, iy, iz, c)];
-      sort8(v);
-      f = classify_sorted(v, which);
+      for (int c = 0; c < 8; ++c) {
+        v[c] = ph[corner(n, ix, iy, iz, c)];
+        known = known && !isnan(v[c]);
+      }
+      if (known) {
+        sort8f(v);
+        known = classify_sorted_f(v, which, f);
+      }
+      if (!known) {  // the FP64 classification of the host
+        double d[8];
+        for (int c = 0; c < 8; ++c) d[c] = phase64(phi, corner(n, ix, iy, iz, c));
+        sort8(d);
+        f = classify_sorted(d, which);
+      }
       flags[s] = f;
     }
-    warp_count(&counts[0], (f & 1) != 0);
-    warp_count(&counts[1], (f & 2) != 0);
-    warp_count(&counts[2], (f & 4) != 0);
+    tally.add((f & 1) != 0, (f & 2) != 0, (f & 4) != 0);
   }
+  tally.flush(counts);
 }
 
 __device__ __forceinline__ double wrapd(double d) {
@@ -136,26 +238,51 @@ __device__ __forceinline__ bool pierced(double a, double b, double c, double d) 
   return w > AXD_PI_HI || w < -AXD_PI_HI;
 }
 
-__global__ void k_winding(const double *__restrict__ ph, int n, unsigned long long *__restrict__ counts) {
+// plaquette a-b-c-d on FP32 phases; false when a corner difference lies
+// within the margin of the +-pi wrap or a phase is unknown
+__device__ __forceinline__ bool pierced_f(float a, float b, float c, float d, bool &hit) {
+  const float kPi = (float)AXD_PI_HI;
+  const float ds[4] = {b - a, c - b, d - c, a - d};
+  float w = 0.0f;
+  bool sure = true;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float x = ds[k];
+    sure = sure && fabsf(fabsf(x) - kPi) >= kMargin;  // false for NaN too
+    w += x > kPi ? x - 2 * kPi : (x <= -kPi ? x + 2 * kPi : x);
+  }
+  hit = w > kPi || w < -kPi;
+  return sure;
+}
+
+template <typename V>
+__global__ void k_winding(const float *__restrict__ ph, const V *__restrict__ phi, int n,
+                          unsigned long long *__restrict__ counts) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  BlockCount3 tally;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n3; base += stride) {
     const int64_t s = base + threadIdx.x;
-    bool px = false, py = false, pz = false;
+    bool hit[3] = {false, false, false};
     if (s < n3) {
       const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
       const int x1 = ix + 1 == n ? 0 : ix + 1, y1 = iy + 1 == n ? 0 : iy + 1,
                 z1 = iz + 1 == n ? 0 : iz + 1;
-      auto P = [&](int x, int y, int z) { return ph[((int64_t)z * n + y) * n + x]; };
-      const double c = P(ix, iy, iz);
-      pz = pierced(c, P(x1, iy, iz), P(x1, y1, iz), P(ix, y1, iz));
-      px = pierced(c, P(ix, y1, iz), P(ix, y1, z1), P(ix, iy, z1));
-      py = pierced(c, P(ix, iy, z1), P(x1, iy, z1), P(x1, iy, iz));
+      auto S = [&](int x, int y, int z) { return ((int64_t)z * n + y) * n + x; };
+      // corners of the x, y, z plaquettes (counts[0..2] = px, py, pz)
+      const int64_t q[3][4] = {{S(ix, iy, iz), S(ix, y1, iz), S(ix, y1, z1), S(ix, iy, z1)},
+                               {S(ix, iy, iz), S(ix, iy, z1), S(x1, iy, z1), S(x1, iy, iz)},
+                               {S(ix, iy, iz), S(x1, iy, iz), S(x1, y1, iz), S(ix, y1, iz)}};
+#pragma unroll
+      for (int o = 0; o < 3; ++o) {
+        if (!pierced_f(ph[q[o][0]], ph[q[o][1]], ph[q[o][2]], ph[q[o][3]], hit[o]))
+          hit[o] = pierced(phase64(phi, q[o][0]), phase64(phi, q[o][1]), phase64(phi, q[o][2]),
+                           phase64(phi, q[o][3]));
+      }
     }
-    warp_count(&counts[0], px);
-    warp_count(&counts[1], py);
-    warp_count(&counts[2], pz);
+    tally.add(hit[0], hit[1], hit[2]);
   }
+  tally.flush(counts);
 }
 
 // ---------------- compaction in cell order ----------------
@@ -708,16 +835,15 @@ __device__ void position_wall(const double ph[8], double pos[3], double dir[3], 
 }
 
 template <typename V>
-__global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, const V *__restrict__ phid,
-                                                    const double *__restrict__ ph, int n, double dspa,
-                                                    uint64_t seed, const int64_t *__restrict__ cells,
+__global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, const V *__restrict__ phid, int n,
+                                                    double dspa, uint64_t seed, const int64_t *__restrict__ cells,
                                                     int64_t ncell, double *__restrict__ out) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ncell) return;
   const int64_t s = cells[k];
   const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
   double pc[8];
-  for (int c = 0; c < 8; ++c) pc[c] = ph[corner(n, ix, iy, iz, c)];
+  for (int c = 0; c < 8; ++c) pc[c] = phase64(phi, corner(n, ix, iy, iz, c));
   double pos[3], dir[3], vel[3], gof, l;
   position_string(pc, seed, (uint64_t)s, pos, dir, &gof, &l);
   velocity_string(phi, phid, n, dspa, ix, iy, iz, pos, vel);
@@ -737,15 +863,15 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
   r[12] = -1.0;
 }
 
-__global__ void __launch_bounds__(128) k_wall_fit(const double *__restrict__ ph, int n,
-                                                  const int64_t *__restrict__ cells, int64_t ncell,
-                                                  double *__restrict__ out) {
+template <typename V>
+__global__ void __launch_bounds__(128) k_wall_fit(const V *__restrict__ phi, int n, const int64_t *__restrict__ cells,
+                                                  int64_t ncell, double *__restrict__ out) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ncell) return;
   const int64_t s = cells[k];
   const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
   double pc[8];
-  for (int c = 0; c < 8; ++c) pc[c] = ph[corner(n, ix, iy, iz, c)];
+  for (int c = 0; c < 8; ++c) pc[c] = phase64(phi, corner(n, ix, iy, iz, c));
   double pos[3], dir[3], gof, a;
   position_wall(pc, pos, dir, &gof, &a);
   double *r = out + 10 * k;
@@ -946,7 +1072,7 @@ int grid_for(int64_t count, int per = 256) {
 }
 
 int ensure_scratch(axg_ctx *ctx) {
-  if (!ctx->phase) AXG_TRY(axg_alloc(ctx, (void **)&ctx->phase, (size_t)ctx->n3 * 8, "phase"));
+  if (!ctx->phase) AXG_TRY(axg_alloc(ctx, (void **)&ctx->phase, (size_t)ctx->n3 * 4, "phase"));
   if (!ctx->flags) AXG_TRY(axg_alloc(ctx, (void **)&ctx->flags, (size_t)ctx->n3, "defect flags"));
   return AXG_OK;
 }
@@ -955,10 +1081,10 @@ int compute_phases(axg_ctx *ctx) {
   AXG_TRY(ensure_scratch(ctx));
   const void *phi = ctx->phi[ctx->cur];
   if (ctx->p.precision == AXG_PREC_FP32_MIXED)
-    AXG_LAUNCH(ctx, "defect_phase_fp32", k_phase<float2>, grid_for(ctx->n3), 256, 0,
+    AXG_LAUNCH(ctx, "defect_phase_fp32", k_phase32<float2>, grid_for(ctx->n3), 256, 0,
                (const float2 *)phi, ctx->phase, ctx->n3);
   else
-    AXG_LAUNCH(ctx, "defect_phase_fp64", k_phase<double2>, grid_for(ctx->n3), 256, 0,
+    AXG_LAUNCH(ctx, "defect_phase_fp64", k_phase32<double2>, grid_for(ctx->n3), 256, 0,
                (const double2 *)phi, ctx->phase, ctx->n3);
   return AXG_OK;
 }
@@ -976,6 +1102,11 @@ int group_and_sum(axg_ctx *ctx, double *rows, int width, int gcol, int vcol, int
   int *ib = nullptr;
   double *db = nullptr;
   int rc = AXG_OK;
+  auto cleanup = axg_on_exit([&] {
+    cudaStreamSynchronize(ctx->stream);
+    axg_free(ctx, (void **)&ib);
+    axg_free(ctx, (void **)&db);
+  });
   AXG_TRY(axg_alloc(ctx, (void **)&ib, sizeof(int) * ((size_t)4 * np + 3 * (size_t)ncell + 4), "grouping"));
   do {
     if ((rc = axg_alloc(ctx, (void **)&db, sizeof(double) * ((size_t)np + 4), "group totals"))) break;
@@ -1002,9 +1133,6 @@ int group_and_sum(axg_ctx *ctx, double *rows, int width, int gcol, int vcol, int
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     rc = axg_evo_check_error(ctx);
   } while (0);
-  cudaStreamSynchronize(ctx->stream);
-  axg_free(ctx, (void **)&ib);
-  axg_free(ctx, (void **)&db);
   return rc;
 }
 
@@ -1019,8 +1147,12 @@ double group_threshold(double wid, double hor) {
 int axg_def_classify(axg_ctx *ctx, int which, int64_t counts[3]) {
   AXG_TRY(compute_phases(ctx));
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_cnt, 0, 3 * sizeof(unsigned long long), ctx->stream));
-  AXG_LAUNCH(ctx, "defect_classify", k_classify, grid_for(ctx->n3), 256, 0, ctx->phase, (int)ctx->n,
-             which, ctx->flags, ctx->d_cnt);
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+    AXG_LAUNCH(ctx, "defect_classify", k_classify<float2>, grid_for(ctx->n3), 256, 0, ctx->phase,
+               (const float2 *)ctx->phi[ctx->cur], (int)ctx->n, which, ctx->flags, ctx->d_cnt);
+  else
+    AXG_LAUNCH(ctx, "defect_classify", k_classify<double2>, grid_for(ctx->n3), 256, 0, ctx->phase,
+               (const double2 *)ctx->phi[ctx->cur], (int)ctx->n, which, ctx->flags, ctx->d_cnt);
   unsigned long long h[3];
   AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_cnt, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1035,8 +1167,12 @@ int axg_def_classify(axg_ctx *ctx, int which, int64_t counts[3]) {
 int axg_def_winding(axg_ctx *ctx, int64_t counts[3]) {
   AXG_TRY(compute_phases(ctx));
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_cnt + 3, 0, 3 * sizeof(unsigned long long), ctx->stream));
-  AXG_LAUNCH(ctx, "string_winding", k_winding, grid_for(ctx->n3), 256, 0, ctx->phase, (int)ctx->n,
-             ctx->d_cnt + 3);
+  if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+    AXG_LAUNCH(ctx, "string_winding", k_winding<float2>, grid_for(ctx->n3), 256, 0, ctx->phase,
+               (const float2 *)ctx->phi[ctx->cur], (int)ctx->n, ctx->d_cnt + 3);
+  else
+    AXG_LAUNCH(ctx, "string_winding", k_winding<double2>, grid_for(ctx->n3), 256, 0, ctx->phase,
+               (const double2 *)ctx->phi[ctx->cur], (int)ctx->n, ctx->d_cnt + 3);
   unsigned long long h[3];
   AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_cnt + 3, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1075,16 +1211,21 @@ int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], dou
     if (ns > 0) {
       if (ctx->p.precision == AXG_PREC_FP32_MIXED)
         AXG_LAUNCH(ctx, "string_fit_fp32", k_string_fit<float2>, (unsigned)((ns + 127) / 128), 128, 0,
-                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->phid, ctx->phase, n,
-                   ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings);
+                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->phid, n, ctx->p.dspa,
+                   (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings);
       else
         AXG_LAUNCH(ctx, "string_fit_fp64", k_string_fit<double2>, (unsigned)((ns + 127) / 128), 128, 0,
-                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)ctx->phid, ctx->phase, n,
-                   ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings);
+                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)ctx->phid, n, ctx->p.dspa,
+                   (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings);
     }
-    if (nw > 0)
-      AXG_LAUNCH(ctx, "wall_fit", k_wall_fit, (unsigned)((nw + 127) / 128), 128, 0, ctx->phase, n,
-                 cells + ns, nw, ctx->d_walls);
+    if (nw > 0) {
+      if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+        AXG_LAUNCH(ctx, "wall_fit", k_wall_fit<float2>, (unsigned)((nw + 127) / 128), 128, 0,
+                   (const float2 *)ctx->phi[ctx->cur], n, cells + ns, nw, ctx->d_walls);
+      else
+        AXG_LAUNCH(ctx, "wall_fit", k_wall_fit<double2>, (unsigned)((nw + 127) / 128), 128, 0,
+                   (const double2 *)ctx->phi[ctx->cur], n, cells + ns, nw, ctx->d_walls);
+    }
     AXG_LAUNCH(ctx, "defect_sums", k_defect_sums, 1, 256, 0, ctx->d_strings, ns, ctx->d_walls, nw,
                ctx->d_red);
     double h[6];

@@ -27,6 +27,7 @@
 #include <cmath>
 #include <vector>
 
+#include "axg_binning.h"
 #include "axg_detmath.h"
 #include "axg_internal.h"
 
@@ -99,14 +100,17 @@ __global__ void k_gw_source_f32(const float2 *__restrict__ phi, int n, float sca
   }
 }
 
-// |k| dwav per k-site (FP64), the phase rate of the FP32 Green accumulation
-__global__ void k_gw_omega(int n, double dwav, double *__restrict__ om) {
+// |k| dwav per k-site as a float-float pair, the phase rate of the FP32 Green
+// accumulation
+__global__ void k_gw_omega(int n, double dwav, float2 *__restrict__ om) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
     const double kx = (s % n + n / 2) % n - n / 2, ky = ((s / n) % n + n / 2) % n - n / 2,
                  kz = (s / n2 + n / 2) % n - n / 2;
-    om[s] = sqrt(kx * kx + ky * ky + kz * kz) * dwav;
+    const double w = sqrt(kx * kx + ky * ky + kz * kz) * dwav;
+    const float hi = (float)w;
+    om[s] = make_float2(hi, (float)(w - (double)hi));
   }
 }
 
@@ -232,13 +236,41 @@ __global__ void k_gw_accumulate(const double2 *__restrict__ srcF, int n, double 
   }
 }
 
-// 2 pi split for the Cody-Waite reduction of the phase (hi + lo = 2 pi to
-// about 1e-32)
-constexpr double kTwoPiHi = 6.283185307179586;
-constexpr double kTwoPiLo = 2.4492935982947064e-16;
+// (hi, lo) += x: TwoSum of hi and x, the error folded into lo, then
+// renormalised (Fast2Sum); hi + lo carries about 48 significant bits
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float x) {
+  const float s = hi + x;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (x - bb);
+  const float l = lo + err;
+  hi = s + l;
+  lo = l - (hi - s);
+}
 
-__global__ void k_gw_accumulate_f32(const float2 *__restrict__ srcF, const double *__restrict__ om, int n,
-                                    double tau, double dw, int ref_compat, double2 *__restrict__ acc) {
+// 2 pi = kC1 + kC2 + kC3 with kC1, kC2 of 8 significant bits (Cody-Waite), so
+// m kC1 and m kC2 are exact for |m| < 2^16, i.e. phases below 4e5 rad
+constexpr float kC1 = 6.28125f;
+constexpr float kC2 = 0.0019378662109375f;
+constexpr float kC3 = -2.559031372584286e-06f;
+constexpr float kInv2Pi = 0.15915493667125702f;
+
+// |k| dk tau reduced to about [-pi, pi] (absolute error ~3e-7): the product
+// of the float-float omega and tau keeps its rounding error exactly (fmaf)
+__device__ __forceinline__ float gw_phase(float2 om, float th, float tl) {
+  const float ph = om.x * th;
+  const float pl = fmaf(om.x, th, -ph) + fmaf(om.x, tl, om.y * th);
+  const float m = rintf(ph * kInv2Pi);
+  float r = fmaf(-m, kC1, ph);
+  r = fmaf(-m, kC2, r);
+  r = r + pl;
+  return fmaf(-m, kC3, r);
+}
+
+// FP32-mixed Green accumulation: FP32 sources, polarisation, phase and
+// contraction; the accumulators are float-float pairs (re hi, re lo, im hi,
+// im lo), so no FP64 instruction is issued per k-site.
+__global__ void k_gw_accumulate_f32(const float2 *__restrict__ srcF, const float2 *__restrict__ om, int n, float th,
+                                    float tl, float dw, int ref_compat, float4 *__restrict__ acc) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -253,67 +285,68 @@ __global__ void k_gw_accumulate_f32(const float2 *__restrict__ srcF, const doubl
       if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
       continue;
     }
-    // phase |k| dwav tau reduced into [-pi, pi] in FP64, then FP32 sin / cos
-    const double ph = om[s] * tau;
-    const double m = rint(ph * (1.0 / kTwoPiHi));
-    const double red = fma(-m, kTwoPiLo, fma(-m, kTwoPiHi, ph));
     float sq, cq;
-    sincosf((float)red, &sq, &cq);
-    float xpf[2], xmf[2], lmf[2];
-    gw_contract<float, float2>(srcF, nhalf, hidx, conj_back, pr, pi, xpf, xmf, lmf);
-    const double xp[2] = {xpf[0], xpf[1]}, xm[2] = {xmf[0], xmf[1]}, lm[2] = {lmf[0], lmf[1]};
-    gw_update(acc, n3, s, dw * (double)cq, dw * (double)sq, xp, xm, lm, ref_compat);
+    sincosf(gw_phase(om[s], th, tl), &sq, &cq);
+    float xp[2], xm[2], lm[2];
+    gw_contract<float, float2>(srcF, nhalf, hidx, conj_back, pr, pi, xp, xm, lm);
+    const float wc = dw * cq, ws = dw * sq;
+    float4 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
+    ff_add(a11.x, a11.y, wc * xp[0]);
+    ff_add(a11.z, a11.w, wc * xp[1]);
+    ff_add(a22.x, a22.y, ws * xm[0]);
+    ff_add(a22.z, a22.w, ws * xm[1]);
+    if (ref_compat) {
+      ff_add(a12.x, a12.y, fmaf(wc, xm[0], ws * xp[0]));
+      ff_add(a12.z, a12.w, fmaf(wc, xm[1], ws * xp[1]));
+      a21 = a12;
+      ff_add(a21.x, a21.y, -wc * lm[0]);
+      ff_add(a21.z, a21.w, -wc * lm[1]);
+    } else {
+      ff_add(a21.x, a21.y, ws * xp[0]);
+      ff_add(a21.z, a21.w, ws * xp[1]);
+      ff_add(a12.x, a12.y, wc * xm[0]);
+      ff_add(a12.z, a12.w, wc * xm[1]);
+    }
+    acc[s] = a11;
+    acc[n3 + s] = a21;
+    acc[2 * n3 + s] = a12;
+    acc[3 * n3 + s] = a22;
   }
 }
 
 // ---------------- shell histograms ----------------
 constexpr int kMaxBins = 256;
 
-__device__ __forceinline__ int lin_bin(double q, double dq, int nb) {
-  if (!(q > 0.0)) return -1;
-  const double id = round(AXD_ADD(AXD_DIV(q, dq), 0.5));
-  if (id >= 1 && id <= nb) return (int)id - 1;
-  return -1;
-}
-__device__ __forceinline__ int log_bin(double q, double e0, double ln_ratio, int nb, const double *edges) {
-  if (!(q > 0.0) || q < edges[0] || q > edges[nb]) return -1;
-  int b = (int)floor(log(q / e0) / ln_ratio * nb);
-  if (b >= nb) b = nb - 1;
-  if (b < 0) b = 0;
-  while (b > 0 && q < edges[b]) --b;
-  while (b < nb - 1 && q >= edges[b + 1]) ++b;
-  return b;
+// |A|^2 of one accumulator entry: FP64, or float-float (FP32-mixed)
+__device__ __forceinline__ double acc_norm2(double2 z) { return z.x * z.x + z.y * z.y; }
+__device__ __forceinline__ double acc_norm2(float4 z) {
+  const double re = (double)z.x + (double)z.y, im = (double)z.z + (double)z.w;
+  return re * re + im * im;
 }
 
-// Green accumulators -> numer / denom per bin
-__global__ void k_gw_bin_green(const double2 *__restrict__ acc, int n, double dwav, double dq, int nb,
-                               int logmode, const double *__restrict__ edges, double *__restrict__ numer,
-                               double *__restrict__ denom) {
+// Green accumulators -> numer / denom per bin (bin of |k|^2 from the table)
+template <typename A>
+__global__ void k_gw_bin_green(const A *__restrict__ acc, int n, const int16_t *__restrict__ tab, int nb,
+                               double *__restrict__ numer, double *__restrict__ denom) {
   __shared__ double sn[kMaxBins], sd[kMaxBins];
-  __shared__ double se[kMaxBins + 1];
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sn[b] = sd[b] = 0.0;
-  if (logmode)
-    for (int b = threadIdx.x; b <= nb; b += blockDim.x) se[b] = edges[b];
   __syncthreads();
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
-  const double ln_ratio = logmode ? log(se[nb] / se[0]) : 0.0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-    const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
-    const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
-    double qq = AXD_ADD(AXD_MUL(kx, kx), AXD_MUL(ky, ky));
-    qq = AXD_ADD(qq, AXD_MUL(kz, kz));
-    const double q = AXD_MUL(AXD_SQRT(qq), dwav);
-    const int b = logmode ? log_bin(q, se[0], ln_ratio, nb, se) : lin_bin(q, dq, nb);
-    if (b < 0) continue;
+  // uniform trip count: every lane reaches the warp-aggregated adds
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n3; base += stride) {
+    const int64_t s = base + threadIdx.x;
+    int b = -1;
     double v = 0.0;
+    if (s < n3) {
+      const int kx = kint(s % n, n), ky = kint((s / n) % n, n), kz = kint(s / n2, n);
+      b = tab[kx * kx + ky * ky + kz * kz];
+      if (b >= 0) {
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const double2 z = acc[a * n3 + s];
-      v += z.x * z.x + z.y * z.y;
+        for (int a = 0; a < 4; ++a) v += acc_norm2(acc[a * n3 + s]);
+      }
     }
-    atomicAdd(&sn[b], v);
-    atomicAdd(&sd[b], 1.0);
+    warp_bin_add(sn, sd, b, v, 1.0);
   }
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -332,24 +365,29 @@ __global__ void k_uij_prepare(const R *__restrict__ u, const R *__restrict__ ud,
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-      double uv = (double)u[c * n3 + s];
-      if (cu) uv -= (double)cu[c * n3 + s];
-      const double udv = (double)ud[c * n3 + s];
-      w[c * n3 + s] = (R)(tau * uv);
-      w[(6 + c) * n3 + s] = (R)(uv + tau * udv);
+      // in the precision of the spectrum: FP32 for FP32-mixed (the Kahan
+      // compensation is below FP32 resolution of u; it is applied all the same)
+      R uv = u[c * n3 + s];
+      if (cu) uv -= cu[c * n3 + s];
+      const R t = (R)tau;
+      w[c * n3 + s] = t * uv;
+      w[(6 + c) * n3 + s] = uv + t * ud[c * n3 + s];
     }
   }
 }
 
 // TT power of a complex symmetric 3x3 (components 11,21,22,31,32,33)
-__device__ double tt_power(const double Ur[6], const double Ui[6], const double kh[3]) {
+// |Lambda U|^2 of the TT projection; R = float for FP32 spectra (the shell
+// sums stay FP64)
+template <typename R>
+__device__ R tt_power(const R Ur[6], const R Ui[6], const R kh[3]) {
   const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
-  double P[3][3], Tr[3][3], Ti[3][3], Rr[3][3], Ri[3][3];
+  R P[3][3], Tr[3][3], Ti[3][3], Rr[3][3], Ri[3][3];
   for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < 3; ++b) P[a][b] = (a == b ? 1.0 : 0.0) - kh[a] * kh[b];
+    for (int b = 0; b < 3; ++b) P[a][b] = (a == b ? R(1) : R(0)) - kh[a] * kh[b];
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) {
-      double sr = 0, si = 0;
+      R sr = 0, si = 0;
       for (int c = 0; c < 3; ++c) {
         sr += P[a][c] * Ur[idx[c][b]];
         si += P[a][c] * Ui[idx[c][b]];
@@ -359,7 +397,7 @@ __device__ double tt_power(const double Ur[6], const double Ui[6], const double 
     }
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) {
-      double sr = 0, si = 0;
+      R sr = 0, si = 0;
       for (int c = 0; c < 3; ++c) {
         sr += Tr[a][c] * P[c][b];
         si += Ti[a][c] * P[c][b];
@@ -367,51 +405,55 @@ __device__ double tt_power(const double Ur[6], const double Ui[6], const double 
       Rr[a][b] = sr;
       Ri[a][b] = si;
     }
-  const double trr = Rr[0][0] + Rr[1][1] + Rr[2][2], tri = Ri[0][0] + Ri[1][1] + Ri[2][2];
-  double s = 0;
+  const R trr = Rr[0][0] + Rr[1][1] + Rr[2][2], tri = Ri[0][0] + Ri[1][1] + Ri[2][2];
+  R s = 0;
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) {
-      const double vr = Rr[a][b] - 0.5 * P[a][b] * trr, vi = Ri[a][b] - 0.5 * P[a][b] * tri;
+      const R vr = Rr[a][b] - R(0.5) * P[a][b] * trr, vi = Ri[a][b] - R(0.5) * P[a][b] * tri;
       s += vr * vr + vi * vi;
     }
   return s;
 }
 
 template <typename CV>
-__global__ void k_uij_bin(const CV *__restrict__ F, int n, double dwav, double dv, double dq, int nb,
-                          int logmode, const double *__restrict__ edges, double *__restrict__ numer,
-                          double *__restrict__ denom) {
+__global__ void k_uij_bin(const CV *__restrict__ F, int n, double dwav, double dv, const int16_t *__restrict__ tab,
+                          int nb, double *__restrict__ numer, double *__restrict__ denom) {
   __shared__ double sn[kMaxBins], sd[kMaxBins];
-  __shared__ double se[kMaxBins + 1];
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sn[b] = sd[b] = 0.0;
-  if (logmode)
-    for (int b = threadIdx.x; b <= nb; b += blockDim.x) se[b] = edges[b];
   __syncthreads();
   const int nh = n / 2 + 1;
   const int64_t nhalf = (int64_t)n * n * nh;
-  const double ln_ratio = logmode ? log(se[nb] / se[0]) : 0.0;
+  const double dv2 = dv * dv, dwav2 = dwav * dwav;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
-    const int ix = (int)(h % nh), iy = (int)((h / nh) % n), iz = (int)(h / ((int64_t)nh * n));
-    const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
-    const double qq = sqrt(kx * kx + ky * ky + kz * kz);
-    const double q = qq * dwav;
-    const int b = logmode ? log_bin(q, se[0], ln_ratio, nb, se) : lin_bin(q, dq, nb);
-    if (b < 0) continue;
-    const double kh[3] = {kx / qq, ky / qq, kz / qq};
-    double Ur[6], Ui[6], Dr[6], Di[6];
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nhalf; base += stride) {
+    const int64_t h = base + threadIdx.x;
+    int b = -1;
+    double v = 0.0, wgt = 0.0;
+    if (h < nhalf) {
+      const int ix = (int)(h % nh), iy = (int)((h / nh) % n), iz = (int)(h / ((int64_t)nh * n));
+      const int kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
+      const int k2 = kx * kx + ky * ky + kz * kz;
+      b = tab[k2];
+      if (b >= 0) {
+        // the TT projection in the precision of the spectrum (FP32 for FP32-mixed)
+        using R = decltype(F[0].x);
+        const R iq = R(1) / sqrt((R)k2);
+        const R kh[3] = {(R)kx * iq, (R)ky * iq, (R)kz * iq};
+        R Ur[6], Ui[6], Dr[6], Di[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      const CV a = F[c * nhalf + h], d = F[(6 + c) * nhalf + h];
-      Ur[c] = (double)a.x * dv;
-      Ui[c] = (double)a.y * dv;
-      Dr[c] = (double)d.x * dv;
-      Di[c] = (double)d.y * dv;
+        for (int c = 0; c < 6; ++c) {
+          const CV a = F[c * nhalf + h], d = F[(6 + c) * nhalf + h];
+          Ur[c] = a.x;
+          Ui[c] = a.y;
+          Dr[c] = d.x;
+          Di[c] = d.y;
+        }
+        const double e0 = (double)tt_power<R>(Dr, Di, kh) * dv2, e1 = (double)tt_power<R>(Ur, Ui, kh) * dv2;
+        wgt = (ix == 0 || 2 * ix == n) ? 1.0 : 2.0;  // Hermitian partner of the half spectrum
+        v = wgt * 0.5 * (e0 + (double)k2 * dwav2 * e1);
+      }
     }
-    const double e0 = tt_power(Dr, Di, kh), e1 = tt_power(Ur, Ui, kh);
-    const double wgt = (ix == 0 || 2 * ix == n) ? 1.0 : 2.0;  // Hermitian partner of the half spectrum
-    atomicAdd(&sn[b], wgt * 0.5 * (e0 + q * q * e1));
-    atomicAdd(&sd[b], wgt);
+    warp_bin_add(sn, sd, b, v, wgt);
   }
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -492,8 +534,9 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
     AXG_LAUNCH(ctx, "gw_source_fp32", k_gw_source_f32, grid_for(ctx->n3), 256, 0,
                (const float2 *)ctx->phi[ctx->cur], n, (float)(2.0 / (d * d)), src);
     AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_gsrc, src, (cufftComplex *)ctx->gsrcF));
+    const float th = (float)tau, tl = (float)(tau - (double)th);
     AXG_LAUNCH(ctx, "gw_accumulate_fp32", k_gw_accumulate_f32, grid_for(ctx->n3), 256, 0,
-               (const float2 *)ctx->gsrcF, ctx->gw_omega, n, tau, dw, ref, ctx->acc);
+               (const float2 *)ctx->gsrcF, ctx->gw_omega, n, th, tl, (float)dw, ref, (float4 *)ctx->acc);
     return AXG_OK;
   }
   int ex;
@@ -523,15 +566,18 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
     edges[0] = 0.0;
     for (int k = 1; k <= nb; ++k) edges[k] = edges[k - 1] + dq;
   }
-  // device scratch: numer[nb] denom[nb] edges[nb+1]
-  if ((size_t)(3 * nb + 1) > ctx->red_cap) return axg_set_error(ctx, AXG_ERR_ARG, "too many bins");
-  double *d_num = ctx->d_red, *d_den = ctx->d_red + nb, *d_edge = ctx->d_red + 2 * nb;
+  // device scratch: numer[nb] denom[nb]
+  if ((size_t)(2 * nb) > ctx->red_cap) return axg_set_error(ctx, AXG_ERR_ARG, "too many bins");
+  double *d_num = ctx->d_red, *d_den = ctx->d_red + nb;
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_red, 0, sizeof(double) * 2 * nb, ctx->stream));
-  AXG_CUDA_TRY(ctx, cudaMemcpyAsync(d_edge, edges.data(), sizeof(double) * (nb + 1), cudaMemcpyHostToDevice,
-                                    ctx->stream));
+  const int16_t *tab = nullptr;
+  AXG_TRY(axg_bin_table(ctx, AXG_BIN_GW, n, dwav, dq, nb, log_bins, edges.data(), &tab));
   if (ctx->p.gw_mode == AXG_GW_GREEN) {
-    AXG_LAUNCH(ctx, "gw_bin_green", k_gw_bin_green, 152 * 4, 256, 0, ctx->acc, n, dwav, dq, nb, log_bins,
-               d_edge, d_num, d_den);
+    if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+      AXG_LAUNCH(ctx, "gw_bin_green", k_gw_bin_green<float4>, 152 * 4, 256, 0, (const float4 *)ctx->acc, n, tab, nb,
+                 d_num, d_den);
+    else
+      AXG_LAUNCH(ctx, "gw_bin_green", k_gw_bin_green<double2>, 152 * 4, 256, 0, ctx->acc, n, tab, nb, d_num, d_den);
   } else if (ctx->p.gw_mode == AXG_GW_UIJ) {
     AXG_TRY(ensure_uij_fft(ctx));
     const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
@@ -544,8 +590,7 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
                  (const float *)ctx->u[ctx->cur], (const float *)ctx->ud, (const float *)ctx->cu, ctx->n3,
                  tau, w);
       AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_u, w, (cufftComplex *)F));
-      AXG_LAUNCH(ctx, "uij_bin_fp32", k_uij_bin<float2>, 152 * 4, 256, 0, F, n, dwav, dv, dq, nb, log_bins,
-                 d_edge, d_num, d_den);
+      AXG_LAUNCH(ctx, "uij_bin_fp32", k_uij_bin<float2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
     } else {
       double *w = (double *)ctx->ubuf;
       double2 *F = (double2 *)(w + 12 * ctx->n3);
@@ -553,8 +598,7 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
                  (const double *)ctx->u[ctx->cur], (const double *)ctx->ud, (const double *)nullptr, ctx->n3,
                  tau, w);
       AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_u, w, (cufftDoubleComplex *)F));
-      AXG_LAUNCH(ctx, "uij_bin_fp64", k_uij_bin<double2>, 152 * 4, 256, 0, F, n, dwav, dv, dq, nb, log_bins,
-                 d_edge, d_num, d_den);
+      AXG_LAUNCH(ctx, "uij_bin_fp64", k_uij_bin<double2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
     }
     (void)nhalf;
   } else {

@@ -55,8 +55,17 @@ struct axg_tmaps {
   CUtensorMap pw[4];  // phid, cphi, ud, cu (body boxes; not ping-ponged)
 };
 
+struct axg_bin_cache_entry {
+  int16_t *tab = nullptr;
+  size_t cap = 0;
+  int m = 0, nb = 0;
+  double dwav = 0, dq = 0;
+  std::vector<double> edges;
+};
+
 struct axg_ctx {
   axg_params p{};
+  axg_bin_cache_entry bin_cache[3];  // GW linear, GW log, field spectrum
   int64_t n = 0, n3 = 0;
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -77,16 +86,16 @@ struct axg_ctx {
   size_t elem = 8;  // bytes of one real of the field storage
 
   // Green's-function GW state (grav_waves.f90)
-  double2 *acc = nullptr;  // [4][n3]
+  double2 *acc = nullptr;  // Green accumulators [4][n3]; FP32-mixed: float4 (re hi, re lo, im hi, im lo)  // [4][n3]
   double *gsrc = nullptr;  // [6][n3] real sources S_ij (float for FP32-mixed)
   double2 *gsrcF = nullptr;  // [6][n*n*(n/2+1)] (float2 for FP32-mixed)
-  double *gw_omega = nullptr;  // [n3] |k| dwav per k-site (FP32-mixed Green mode)
+  float2 *gw_omega = nullptr;  // [n3] |k| dwav per k-site as float hi + lo (FP32-mixed Green mode)
   cufftHandle plan_gsrc = 0;
   bool plan_gsrc_ok = false;
 
   // defects
   int8_t *flags = nullptr;  // per cell, bits 1/2/4
-  double *phase = nullptr;  // per site phase scratch
+  float *phase = nullptr;  // per site FP32 phase (filtered classification)
   bool flags_valid = false;
   // fit results of the last id_defects
   double *d_strings = nullptr;
@@ -160,6 +169,18 @@ int axg_set_error(axg_ctx *ctx, int code, const std::string &msg);
     int s_ = (expr);         \
     if (s_ != AXG_OK) return s_; \
   } while (0)
+
+// Runs its function when the scope ends, also on the early returns of the
+// AXG_* macros (scratch buffers, plans and events of multi-step routines).
+template <typename F>
+struct axg_scope_exit {
+  F f;
+  ~axg_scope_exit() { f(); }
+};
+template <typename F>
+axg_scope_exit<F> axg_on_exit(F f) {
+  return axg_scope_exit<F>{f};
+}
 
 // ---------------------------------------------------------------------------
 // kernel launch bookkeeping (per-kernel event timing for the roofline)

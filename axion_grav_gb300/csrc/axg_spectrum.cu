@@ -17,6 +17,7 @@
 #include <cmath>
 #include <vector>
 
+#include "axg_binning.h"
 #include "axg_detmath.h"
 #include "axg_internal.h"
 
@@ -32,6 +33,7 @@ __device__ __forceinline__ int kint(int j, int n) { return (j + n / 2) % n - n /
 template <typename V>
 __global__ void k_spec_degrade(const V *__restrict__ phid, const int8_t *__restrict__ flags, int n, int deg,
                                double inv_deg3, int window, double dv_spa, double2 *__restrict__ out) {
+  // inv_deg3 = 1 / deg^3
   const int m = n / deg;
   const int64_t m3 = (int64_t)m * m * m, n2 = (int64_t)n * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -53,11 +55,13 @@ __global__ void k_spec_degrade(const V *__restrict__ phid, const int8_t *__restr
     if (window)
       out[c] = make_double2(masked ? 0.0 : dv_spa, 0.0);
     else
-      out[c] = masked ? make_double2(0.0, 0.0) : make_double2(sr / inv_deg3, si / inv_deg3);
+      // deg^3 is a power of two: multiplying by its reciprocal is the same
+      // single rounding as the reference's division
+      out[c] = masked ? make_double2(0.0, 0.0) : make_double2(sr * inv_deg3, si * inv_deg3);
   }
 }
 
-__global__ void k_spec_bin(const double2 *__restrict__ F, int m, double dwav, double dq, double dv_spa,
+__global__ void k_spec_bin(const double2 *__restrict__ F, int m, const int16_t *__restrict__ tab, double dv_spa,
                            double dv_wav, int nb, double *__restrict__ conv, double *__restrict__ count) {
   extern __shared__ double sh[];
   double *sc = sh, *sn = sh + nb;
@@ -65,17 +69,21 @@ __global__ void k_spec_bin(const double2 *__restrict__ F, int m, double dwav, do
   __syncthreads();
   const int64_t m3 = (int64_t)m * m * m;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m3; s += stride) {
-    const int ix = (int)(s % m), iy = (int)((s / m) % m), iz = (int)(s / ((int64_t)m * m));
-    const double kx = kint(ix, m), ky = kint(iy, m), kz = kint(iz, m);
-    const double q = __dmul_rn(__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz))), dwav);
-    const double id = round(__dadd_rn(__ddiv_rn(q, dq), 0.5));
-    if (id >= 1 && id <= nb) {
-      const double2 f = F[s];
-      const double re = f.x * dv_spa, im = f.y * dv_spa;
-      atomicAdd(&sc[(int)id - 1], (re * re + im * im) * dv_wav);
-      atomicAdd(&sn[(int)id - 1], 1.0);
+  // uniform trip count: every lane reaches the warp-aggregated adds
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m3; base += stride) {
+    const int64_t s = base + threadIdx.x;
+    int b = -1;
+    double v = 0.0;
+    if (s < m3) {
+      const int kx = kint(s % m, m), ky = kint((s / m) % m, m), kz = kint(s / ((int64_t)m * m), m);
+      b = tab[kx * kx + ky * ky + kz * kz];
+      if (b >= 0) {
+        const double2 f = F[s];
+        const double re = f.x * dv_spa, im = f.y * dv_spa;
+        v = (re * re + im * im) * dv_wav;
+      }
     }
+    warp_bin_add(sc, sn, b, v, 1.0);
   }
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -247,22 +255,20 @@ int pp_inverse(int n, double *ap) {
 
 // estimate_covmat (spectrum.f90:593-641): Gaussian modes with the measured
 // spectrum (Philox stream 16 + iter), sigma per bin of nint(q/dq + 0.5)
-__global__ void k_mc_fill(double2 *F, int m, double dwav, double dq, int nb, const double *sigma, uint64_t seed,
+__global__ void k_mc_fill(double2 *F, int m, const int16_t *__restrict__ tab, const double *sigma, uint64_t seed,
                           uint32_t iter) {
   const int64_t m3 = (int64_t)m * m * m;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m3; s += stride) {
-    const int ix = (int)(s % m), iy = (int)((s / m) % m), iz = (int)(s / ((int64_t)m * m));
-    const double kx = kint(ix, m), ky = kint(iy, m), kz = kint(iz, m);
-    const double q = __dmul_rn(__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz))), dwav);
-    const double id = round(__dadd_rn(__ddiv_rn(q, dq), 0.5));
-    if (id <= nb) {
+    const int kx = kint(s % m, m), ky = kint((s / m) % m, m), kz = kint(s / ((int64_t)m * m), m);
+    const int b = tab[kx * kx + ky * ky + kz * kz];
+    if (b >= 0) {
       const axd_u32x4 r = axd_draw(seed, 16u + iter, 0u, (uint64_t)s);
       const double u1 = axd_u01_open0(r.v[0], r.v[1]), u2 = axd_u01(r.v[2], r.v[3]);
       const double rad = sqrt(-2.0 * log(u1));
       double sn, cs;
       sincos(6.283185307179586 * u2, &sn, &cs);
-      const double sg = sigma[(int)id - 1];
+      const double sg = sigma[b];
       F[s] = make_double2(rad * cs * sg, rad * sn * sg);
     } else {
       F[s] = make_double2(0.0, 0.0);
@@ -377,10 +383,10 @@ int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, d
     // ---- compute_matrix_deconv (spectrum.f90:344-444) ----
     if (fp32)
       AXG_LAUNCH(ctx, "spec_window", k_spec_degrade<float2>, grid_for(m3), 256, 0, (const float2 *)ctx->phid,
-                 ctx->flags, n, deg, (double)deg * deg * deg, 1, dv_spa, ctx->spec_buf);
+                 ctx->flags, n, deg, 1.0 / ((double)deg * deg * deg), 1, dv_spa, ctx->spec_buf);
     else
       AXG_LAUNCH(ctx, "spec_window", k_spec_degrade<double2>, grid_for(m3), 256, 0, (const double2 *)ctx->phid,
-                 ctx->flags, n, deg, (double)deg * deg * deg, 1, dv_spa, ctx->spec_buf);
+                 ctx->flags, n, deg, 1.0 / ((double)deg * deg * deg), 1, dv_spa, ctx->spec_buf);
     AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
                                     (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
     AXG_LAUNCH(ctx, "spec_w2_hist", k_spec_w2_hist, grid_for(m3), 256, 0, ctx->spec_buf, m, h, cnt);
@@ -399,15 +405,17 @@ int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, d
     // ---- compute_conv_spec (spectrum.f90:466-567) ----
     if (fp32)
       AXG_LAUNCH(ctx, "spec_degrade", k_spec_degrade<float2>, grid_for(m3), 256, 0, (const float2 *)ctx->phid,
-                 ctx->flags, n, deg, (double)deg * deg * deg, 0, dv_spa, ctx->spec_buf);
+                 ctx->flags, n, deg, 1.0 / ((double)deg * deg * deg), 0, dv_spa, ctx->spec_buf);
     else
       AXG_LAUNCH(ctx, "spec_degrade", k_spec_degrade<double2>, grid_for(m3), 256, 0, (const double2 *)ctx->phid,
-                 ctx->flags, n, deg, (double)deg * deg * deg, 0, dv_spa, ctx->spec_buf);
+                 ctx->flags, n, deg, 1.0 / ((double)deg * deg * deg), 0, dv_spa, ctx->spec_buf);
     AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
                                     (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
     const double dq = ctx->h_wav[1] - ctx->h_wav[0];
-    AXG_LAUNCH(ctx, "spec_bin", k_spec_bin, 152 * 4, 256, 2 * nb * sizeof(double), ctx->spec_buf, m, dwav, dq,
-               dv_spa, dv_wav, nb, d_conv, d_cnt);
+    const int16_t *tab = nullptr;
+    AXG_TRY(axg_bin_table(ctx, AXG_BIN_SPECTRUM, m, dwav, dq, nb, 0, nullptr, &tab));
+    AXG_LAUNCH(ctx, "spec_bin", k_spec_bin, 152 * 4, 256, 2 * nb * sizeof(double), ctx->spec_buf, m, tab, dv_spa,
+               dv_wav, nb, d_conv, d_cnt);
     std::vector<double> hm(2 * num_cov), hb(2 * nb);
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(hm.data(), mat0, hm.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(hb.data(), d_conv, hb.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -501,21 +509,27 @@ int axg_spec_covariance(axg_ctx *ctx, int min_mc, int max_mc, double tol, double
     sigma[i] = std::sqrt(pwr > 0 ? pwr / 2 : 0.0) / (double)m3;
   }
   double *scr = nullptr;
+  auto cleanup = axg_on_exit([&] {
+    cudaStreamSynchronize(ctx->stream);
+    axg_free(ctx, (void **)&scr);
+  });
   AXG_TRY(axg_alloc(ctx, (void **)&scr, sizeof(double) * (size_t)(3 * nb), "covariance scratch"));
   int rc = AXG_OK, iter;
   double *d_sigma = scr, *d_pow = scr + nb, *d_cnt = scr + 2 * nb;
+  const int16_t *tab = nullptr;
+  AXG_TRY(axg_bin_table(ctx, AXG_BIN_SPECTRUM, m, dwav, dq, nb, 0, nullptr, &tab));
   for (iter = 1; iter <= max_mc && rc == AXG_OK; ++iter) {
     if (iter == 1) AXG_CUDA_TRY(ctx, cudaMemcpyAsync(d_sigma, sigma.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, ctx->stream));
     AXG_CUDA_TRY(ctx, cudaMemsetAsync(d_pow, 0, sizeof(double) * 2 * nb, ctx->stream));
-    AXG_LAUNCH(ctx, "mc_fill", k_mc_fill, grid_for(m3), 256, 0, ctx->spec_buf, m, dwav, dq, nb, d_sigma,
-               (uint64_t)ctx->p.seed, (uint32_t)iter);
+    AXG_LAUNCH(ctx, "mc_fill", k_mc_fill, grid_for(m3), 256, 0, ctx->spec_buf, m, tab, d_sigma, (uint64_t)ctx->p.seed,
+               (uint32_t)iter);
     AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
                                     (cufftDoubleComplex *)ctx->spec_buf, CUFFT_FORWARD));
     AXG_LAUNCH(ctx, "mc_mask", k_mc_mask, grid_for(m3), 256, 0, ctx->spec_buf, ctx->flags, n, deg);
     AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
                                     (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
-    AXG_LAUNCH(ctx, "mc_bin", k_spec_bin, 152 * 4, 256, 2 * nb * sizeof(double), ctx->spec_buf, m, dwav, dq, 1.0,
-               1.0, nb, d_pow, d_cnt);
+    AXG_LAUNCH(ctx, "mc_bin", k_spec_bin, 152 * 4, 256, 2 * nb * sizeof(double), ctx->spec_buf, m, tab, 1.0, 1.0,
+               nb, d_pow, d_cnt);
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(pw0.data(), d_pow, sizeof(double) * nb, cudaMemcpyDeviceToHost, ctx->stream));
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     // pow = mat_deconv pow0 - power (dspmv, beta = 1)
@@ -561,8 +575,6 @@ int axg_spec_covariance(axg_ctx *ctx, int min_mc, int max_mc, double tol, double
     }
     if (diff < tol) break;
   }
-  cudaStreamSynchronize(ctx->stream);
-  axg_free(ctx, (void **)&scr);
   if (rc != AXG_OK) return rc;
   if (iter > max_mc) iter = max_mc + 1;
   for (int ij = 0; ij < num_cov; ++ij) cov[ij] = cov[ij] / iter;

@@ -232,20 +232,27 @@ def bench_e2e(ag, lat, n, nsub, reps, t, dt):
         times.append(time.perf_counter() - t_start)
         t += dt * nsub
     per = float(np.median(times[1:]))
+    per_min = float(np.min(times[1:]))
     bytes_each = 2 * n ** 3 * 16
-    # one more interval split into its three calls (each returns synchronised)
-    t0 = time.perf_counter()
-    assert lib.axg_upload(lat.handle, dp(h_phi), dp(h_phid), n * n, 0) == 0
-    t1 = time.perf_counter()
-    assert lib.axg_leapfrog(lat.handle, t, dt, nsub, 1, 1) == 0
-    lat.synchronize()
-    t2 = time.perf_counter()
-    assert lib.axg_download(lat.handle, dp(h_phi), dp(h_phid), n * n, 0) == 0
-    t3 = time.perf_counter()
-    split = {"upload_s": t1 - t0, "leapfrog_s": t2 - t1, "download_s": t3 - t2,
-             "upload_gbs": bytes_each / (t1 - t0) / 1e9, "download_gbs": bytes_each / (t3 - t2) / 1e9}
+    # three more intervals split into their calls (each returns synchronised); medians
+    parts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        assert lib.axg_upload(lat.handle, dp(h_phi), dp(h_phid), n * n, 0) == 0
+        t1 = time.perf_counter()
+        assert lib.axg_leapfrog(lat.handle, t, dt, nsub, 1, 1) == 0
+        lat.synchronize()
+        t2 = time.perf_counter()
+        assert lib.axg_download(lat.handle, dp(h_phi), dp(h_phid), n * n, 0) == 0
+        t3 = time.perf_counter()
+        parts.append((t1 - t0, t2 - t1, t3 - t2))
+        t += dt * nsub
+    up, lf, dn = (float(np.median([q[i] for q in parts])) for i in range(3))
+    split = {"upload_s": up, "leapfrog_s": lf, "download_s": dn, "upload_gbs": bytes_each / up / 1e9,
+             "download_gbs": bytes_each / dn / 1e9}
     return {"value": nsub * n ** 3 / per, "unit": UNIT, "h2d_bytes_per_step": bytes_each / nsub,
-            "d2h_bytes_per_step": bytes_each / nsub, "interval_steps": nsub, "s_per_interval": per, "split": split,
+            "d2h_bytes_per_step": bytes_each / nsub, "interval_steps": nsub, "s_per_interval": per,
+            "s_per_interval_min": per_min, "split": split,
             "note": "public C-ABI, host-resident complex128 phi and phidot uploaded and downloaded "
                     "once per interval of %d leapfrog steps (pinned host memory); u_ij device-resident" % nsub}
 
@@ -320,9 +327,17 @@ def bench_adjoint(ag, device, n=256, steps=2000, stride=64, fp64_steps=256):
             plain = lat.event_elapsed(0, 1)
             lat.ic_gaussian_flat(kcut=1.0, realisation=0)
             J, dl, _, _, mf, mr = lat.adjoint_gw_band(t1, dt, st, stride, 0.125, 0.5, want_grads=False)
+            # per-kernel breakdown on a shorter run (launch events add overhead)
+            lat.ic_gaussian_flat(kcut=1.0, realisation=0)
+            lat.set_kernel_timing(True)
+            kst = min(st, 256)
+            lat.adjoint_gw_band(t1, dt, kst, stride, 0.125, 0.5, want_grads=False)
+            kt = lat.kernel_timings()
+            lat.set_kernel_timing(False)
         out[name] = {"steps": st, "J": J, "dJ_dlambda": dl, "ms_forward_step": plain / st,
                      "ms_forward_with_checkpoints": mf, "ms_reverse": mr, "reverse_vs_forward": mr / plain,
-                     "adjoint_total_vs_forward": (mf + mr) / plain}
+                     "adjoint_total_vs_forward": (mf + mr) / plain,
+                     "kernels_ms_per_step": {k: round(t / kst, 4) for k, l, t in kt if l > 0}}
     return out
 
 
@@ -343,10 +358,14 @@ def bench_output_calls(ag, n, device, steps=200, max_fit_cells=2_000_000):
 
         def timed(name, fn, reps=3):
             fn()  # first call allocates plans / tables
+            lat.set_kernel_timing(True)
             t0 = time.perf_counter()
             for _ in range(reps):
                 r = fn()
             out[name] = {"ms": 1e3 * (time.perf_counter() - t0) / reps}
+            kt = lat.kernel_timings()
+            lat.set_kernel_timing(False)
+            out[name]["kernels_ms"] = {k: round(t / reps, 3) for k, l, t in kt if l > 0}
             return r
 
         wind = timed("string_winding", lat.string_winding)
@@ -460,7 +479,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--e2e-interval", type=int, default=20)
-    ap.add_argument("--e2e-reps", type=int, default=3)
+    ap.add_argument("--e2e-reps", type=int, default=7)
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy block")
     ap.add_argument("--accuracy-steps", type=int, default=100)

@@ -254,7 +254,10 @@ int axg_field_moments(axg_ctx *ctx, double tau, double out[4]);
 /* ------------------------------------------------------------------ */
 /* io_chk: raw complex128 phi block then phidot block, x fastest, global order
  * (evolve.f90:498-503); plus u_ij blocks when present and a CRC32 sidecar
- * file path+".crc".  write_chk's param.chk is written by axg_write_param_chk. */
+ * file path+".crc".  FP32-mixed contexts also write path+".fp32", the raw
+ * FP32 state with its Kahan compensations and a CRC32, and read it back when
+ * present, so that a resumed run continues bit for bit (a damaged sidecar is
+ * an error).  write_chk's param.chk is written by axg_write_param_chk. */
 int axg_write_chk(axg_ctx *ctx, const char *path);
 int axg_read_chk(axg_ctx *ctx, const char *path);
 /* param.chk "idx tau flag" (evolve.f90:407-421, 445-448). */

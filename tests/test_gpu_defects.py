@@ -26,10 +26,21 @@ def fields(kind, n, seed=0):
         p = params(n, potential=ag.POT_QUARTIC)
         phi, _ = axo.ic_gaussian_flat(p, kcut=0.9, realisation=seed)
         return phi
+    if kind in ("quarter", "half"):
+        # phases on multiples of pi/4 (pi/2): exact gap ties and gaps of exactly
+        # pi, a hair below the reference's truncated pi -- every such cell is
+        # decided by the FP64 fallback of the filtered classification
+        k = rng.integers(0, 8 if kind == "quarter" else 4, (n, n, n))
+        step = np.pi / 4 if kind == "quarter" else np.pi / 2
+        return ((0.5 + rng.random((n, n, n))) * np.exp(1j * step * k)).astype(np.complex128)
+    if kind in ("tiny", "huge"):
+        # components outside the FP32 range: FP32 phases are unknown (NaN)
+        scale = 1e-40 if kind == "tiny" else 1e39
+        return scale * (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n)))
     raise KeyError(kind)
 
 
-@pytest.mark.parametrize("kind", ["random", "strings", "smooth"])
+@pytest.mark.parametrize("kind", ["random", "strings", "smooth", "quarter", "half", "tiny", "huge"])
 @pytest.mark.parametrize("n", [16, 32])
 @pytest.mark.parametrize("which", [7, 1, 5, 3])
 def test_classification_bit_exact(kind, n, which):
@@ -44,18 +55,21 @@ def test_classification_bit_exact(kind, n, which):
     assert np.array_equal(f, ref_flags)
 
 
-def test_classification_fp32_state():
-    """FP32-mixed: classification runs in FP64 on the upcast FP32 snapshot."""
+@pytest.mark.parametrize("kind", ["smooth", "quarter", "random"])
+def test_classification_fp32_state(kind):
+    """FP32-mixed: the flags are those of the FP64 classification of the
+    upcast FP32 snapshot."""
     n = 32
-    phi = fields("smooth", n, 2).astype(np.complex64).astype(np.complex128)
+    phi = fields(kind, n, 2).astype(np.complex64).astype(np.complex128)
     ref_flags, ref_c = axo.classify_cells(params(n), phi, 7, 0)
     with ag.Lattice(params(n, ag.PREC_FP32_MIXED)) as lat:
         lat.upload(phi, np.zeros_like(phi))
         assert np.array_equal(lat.classify_cells(7), ref_c)
         assert np.array_equal(lat.defect_flags(), ref_flags)
+        assert np.array_equal(lat.string_winding(), axo.string_winding(params(n), phi))
 
 
-@pytest.mark.parametrize("kind", ["random", "strings", "smooth"])
+@pytest.mark.parametrize("kind", ["random", "strings", "smooth", "quarter", "half", "tiny"])
 def test_winding_bit_exact(kind):
     n = 32
     phi = fields(kind, n, 7)

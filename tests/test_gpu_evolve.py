@@ -258,6 +258,36 @@ def test_checkpoint_roundtrip_and_crc(tmp_path):
             lat.read_chk(path)
 
 
+def test_fp32_checkpoint_resume_is_bit_exact(tmp_path):
+    """FP32-mixed Mode U: stop, write_chk, read_chk into a fresh context and
+    continue; the result equals the uninterrupted run bit for bit (the .fp32
+    sidecar restores the Kahan compensations), and a damaged sidecar is
+    rejected."""
+    n = 32
+    p = make_params(n, ag.PREC_FP32_MIXED, ag.GW_UIJ)
+    st = random_state(n, 9, 0.2)
+    path = str(tmp_path / "run_fp32.chk")
+    with ag.Lattice(p) as lat:
+        lat.upload(st[0], st[1])
+        lat.upload_uij(st[2], st[3])
+        lat.leapfrog(1.5, 0.02, 7, True, False)
+        lat.write_chk(path)
+        lat.leapfrog(1.64, 0.02, 6, False, True)
+        want = lat.download(), lat.download_uij()
+    with ag.Lattice(p) as lat:
+        lat.read_chk(path)
+        lat.leapfrog(1.64, 0.02, 6, False, True)
+        got = lat.download(), lat.download_uij()
+    for a, b in zip(got[0] + got[1], want[0] + want[1]):
+        assert np.array_equal(a, b)
+    data = bytearray(open(path + ".fp32", "rb").read())
+    data[64] ^= 0x01
+    open(path + ".fp32", "wb").write(bytes(data))
+    with ag.Lattice(p) as lat:
+        with pytest.raises(ag.AxgError, match="CRC"):
+            lat.read_chk(path)
+
+
 def test_kernel_timing_and_launch_count():
     n = 64
     p = make_params(n, ag.PREC_FP32_MIXED, ag.GW_UIJ)
