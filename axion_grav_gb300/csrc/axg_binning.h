@@ -6,8 +6,8 @@
 // same FP64 expressions once per |k|^2 on the host and keeps the table on the
 // device, so a binning kernel does one 2-byte load per k instead of an FP64
 // square root, division and rounding.  Kernels add into shared-memory bins
-// through warp_bin_add: the lanes of a warp that hold the same bin are summed
-// by shuffles and one lane adds the sum.
+// through BinRun: each lane sums a short run of consecutive k-sites privately
+// and adds to the shared bin only when its bin changes.
 #pragma once
 #include <cstdint>
 
@@ -24,28 +24,39 @@ int axg_bin_table(axg_ctx *ctx, int kind, int m, double dwav, double dq, int nb,
                   const double *edges, const int16_t **d_tab);
 
 #ifdef __CUDACC__
-// All 32 lanes must call this (b < 0: nothing to add).
-__device__ __forceinline__ void warp_bin_add(double *sv, double *sw, int b, double v, double w) {
-  const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  unsigned pending = __ballot_sync(full, b >= 0);
-  while (pending) {
-    const int leader = __ffs(pending) - 1;
-    const int b0 = __shfl_sync(full, b, leader);
-    const bool mine = b == b0;
-    double x = mine ? v : 0.0, y = mine ? w : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      x += __shfl_xor_sync(full, x, o);
-      y += __shfl_xor_sync(full, y, o);
-    }
-    if (lane == leader) {
-      atomicAdd(&sv[b0], x);
-      atomicAdd(&sw[b0], y);
-    }
-    pending &= ~__ballot_sync(full, mine);
-  }
-}
+// Per-lane run accumulation: each lane walks kRun consecutive k-sites (along
+// kx, so |k|^2 and the bin change slowly), sums privately and adds to the
+// shared bins only when its bin changes.  FP64 work per site is one add.
+constexpr int kRun = 4;
 
-__device__ __forceinline__ int kint_bin(int j, int n) { return (j + n / 2) % n - n / 2; }
+struct BinRun {
+  int bin = -1;
+  double v = 0.0;
+  unsigned w = 0;  // count (or Hermitian weight sum, <= 2 per site)
+  __device__ __forceinline__ void add(double *sv, double *sw, int b, double val, unsigned wt) {
+    if (b != bin) {
+      flush(sv, sw);
+      bin = b;
+      v = 0.0;
+      w = 0;
+    }
+    if (b >= 0) {
+      v += val;
+      w += wt;
+    }
+  }
+  __device__ __forceinline__ void flush(double *sv, double *sw) {
+    if (bin >= 0 && w) {
+      atomicAdd(&sv[bin], v);
+      atomicAdd(&sw[bin], (double)w);
+    }
+    bin = -1;
+  }
+};
+
+// first site of this lane's run and the stride between runs of one lane
+__device__ __forceinline__ int64_t run_start() {
+  return ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRun;
+}
+__device__ __forceinline__ int64_t run_stride() { return (int64_t)gridDim.x * blockDim.x * kRun; }
 #endif

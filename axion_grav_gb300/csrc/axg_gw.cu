@@ -332,22 +332,20 @@ __global__ void k_gw_bin_green(const A *__restrict__ acc, int n, const int16_t *
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sn[b] = sd[b] = 0.0;
   __syncthreads();
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // uniform trip count: every lane reaches the warp-aggregated adds
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n3; base += stride) {
-    const int64_t s = base + threadIdx.x;
-    int b = -1;
-    double v = 0.0;
-    if (s < n3) {
+  BinRun run;
+  for (int64_t s0 = run_start(); s0 < n3; s0 += run_stride()) {
+    for (int64_t s = s0; s < s0 + kRun && s < n3; ++s) {
       const int kx = kint(s % n, n), ky = kint((s / n) % n, n), kz = kint(s / n2, n);
-      b = tab[kx * kx + ky * ky + kz * kz];
+      const int b = tab[kx * kx + ky * ky + kz * kz];
+      double v = 0.0;
       if (b >= 0) {
 #pragma unroll
         for (int a = 0; a < 4; ++a) v += acc_norm2(acc[a * n3 + s]);
       }
+      run.add(sn, sd, b, v, 1u);
     }
-    warp_bin_add(sn, sd, b, v, 1.0);
   }
+  run.flush(sn, sd);
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     if (sd[b] != 0.0) {
@@ -424,16 +422,15 @@ __global__ void k_uij_bin(const CV *__restrict__ F, int n, double dwav, double d
   const int nh = n / 2 + 1;
   const int64_t nhalf = (int64_t)n * n * nh;
   const double dv2 = dv * dv, dwav2 = dwav * dwav;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nhalf; base += stride) {
-    const int64_t h = base + threadIdx.x;
-    int b = -1;
-    double v = 0.0, wgt = 0.0;
-    if (h < nhalf) {
+  BinRun run;
+  for (int64_t h0 = run_start(); h0 < nhalf; h0 += run_stride()) {
+    for (int64_t h = h0; h < h0 + kRun && h < nhalf; ++h) {
       const int ix = (int)(h % nh), iy = (int)((h / nh) % n), iz = (int)(h / ((int64_t)nh * n));
       const int kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
       const int k2 = kx * kx + ky * ky + kz * kz;
-      b = tab[k2];
+      const int b = tab[k2];
+      double v = 0.0;
+      unsigned wgt = 0;
       if (b >= 0) {
         // the TT projection in the precision of the spectrum (FP32 for FP32-mixed)
         using R = decltype(F[0].x);
@@ -449,12 +446,13 @@ __global__ void k_uij_bin(const CV *__restrict__ F, int n, double dwav, double d
           Di[c] = d.y;
         }
         const double e0 = (double)tt_power<R>(Dr, Di, kh) * dv2, e1 = (double)tt_power<R>(Ur, Ui, kh) * dv2;
-        wgt = (ix == 0 || 2 * ix == n) ? 1.0 : 2.0;  // Hermitian partner of the half spectrum
+        wgt = (ix == 0 || 2 * ix == n) ? 1u : 2u;  // Hermitian partner of the half spectrum
         v = wgt * 0.5 * (e0 + (double)k2 * dwav2 * e1);
       }
+      run.add(sn, sd, b, v, wgt);
     }
-    warp_bin_add(sn, sd, b, v, wgt);
   }
+  run.flush(sn, sd);
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     if (sd[b] != 0.0) {

@@ -68,23 +68,21 @@ __global__ void k_spec_bin(const double2 *__restrict__ F, int m, const int16_t *
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sc[b] = sn[b] = 0.0;
   __syncthreads();
   const int64_t m3 = (int64_t)m * m * m;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // uniform trip count: every lane reaches the warp-aggregated adds
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m3; base += stride) {
-    const int64_t s = base + threadIdx.x;
-    int b = -1;
-    double v = 0.0;
-    if (s < m3) {
+  BinRun run;
+  for (int64_t s0 = run_start(); s0 < m3; s0 += run_stride()) {
+    for (int64_t s = s0; s < s0 + kRun && s < m3; ++s) {
       const int kx = kint(s % m, m), ky = kint((s / m) % m, m), kz = kint(s / ((int64_t)m * m), m);
-      b = tab[kx * kx + ky * ky + kz * kz];
+      const int b = tab[kx * kx + ky * ky + kz * kz];
+      double v = 0.0;
       if (b >= 0) {
         const double2 f = F[s];
         const double re = f.x * dv_spa, im = f.y * dv_spa;
         v = (re * re + im * im) * dv_wav;
       }
+      run.add(sc, sn, b, v, 1u);
     }
-    warp_bin_add(sc, sn, b, v, 1.0);
   }
+  run.flush(sc, sn);
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     if (sn[b] != 0.0) {
@@ -117,12 +115,13 @@ __global__ void k_spec_mat(const double *__restrict__ h, const double *__restric
   const int ij = blockIdx.x;
   const long long lo = range[2 * ij], hi = range[2 * ij + 1];
   const double *tab = mat_spec + (int64_t)ij * (kNumLargeq + 1);
+  const double lq0 = largeq0[ij], idq = 1.0 / dq_spec[ij];  // one division per pair
   double a = 0.0, b = 0.0;
   for (long long iq2 = lo + threadIdx.x; iq2 <= hi; iq2 += blockDim.x) {
     const double c = cnt[iq2];
     if (c == 0.0) continue;
     const double q = sqrt((double)iq2) * dwav;
-    double d = (q - largeq0[ij]) / dq_spec[ij];
+    double d = (q - lq0) * idq;
     const double fl = floor(d);
     double u = 0.0;
     if (fl < kNumLargeq && fl >= 0) {

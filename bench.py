@@ -380,6 +380,23 @@ def bench_output_calls(ag, n, device, steps=200, max_fit_cells=2_000_000):
         else:
             out["id_defects"] = {"skipped": f"{cells} string+wall cells above the {max_fit_cells} cap"}
         timed("spectrum_estimation", lambda: lat.spectrum_estimation(tau))
+        # fit throughput on a 128^3 lattice of the same physics and age
+        p128 = workload_params(ag, 128, ag.PREC_FP32_MIXED, ag.GW_UIJ, device)
+        with ag.Lattice(p128) as small:
+            small.ic_gaussian_flat(kcut=2.0 * np.pi / (8 * p128.dspa))
+            dt128, _ = small.get_dtau(2.0, 32.0, 0.25)
+            nst = int(round((tau - 2.0) / dt128))
+            small.leapfrog(2.0, dt128, nst, True, True)
+            c128 = small.classify_cells(7)
+            small.set_kernel_timing(True)
+            t0 = time.perf_counter()
+            small.id_defects(1, 2.0 + dt128 * nst)
+            ms = 1e3 * (time.perf_counter() - t0)
+            kt = small.kernel_timings()
+            small.set_kernel_timing(False)
+            out["id_defects_128"] = {"ms": ms, "string_cells": int(c128[0]), "wall_cells": int(c128[1]),
+                                     "cells_per_s": float(c128[0] + c128[1]) / (ms * 1e-3),
+                                     "kernels_ms": {k: round(t, 3) for k, l, t in kt if l > 0}}
         timed("grav_spec_estimation", lambda: lat.grav_spec_estimation(tau))
         timed("grav_spec_log", lambda: lat.grav_spec_log(tau))
     return out
