@@ -519,6 +519,7 @@ int axg_destroy(axg_ctx *ctx) {
     axg_free(ctx, q);
   if (ctx->plan_gsrc_ok) cufftDestroy(ctx->plan_gsrc);
   if (ctx->plan_spec_ok) cufftDestroy(ctx->plan_spec);
+  if (ctx->plan_window_ok) cufftDestroy(ctx->plan_window);
   if (ctx->plan_u_ok) cufftDestroy(ctx->plan_u);
   for (auto &e : ctx->user_ev)
     if (e) cudaEventDestroy(e);

@@ -40,7 +40,7 @@ struct KickCoeffs {
 
 // x / d, replaced by the exact multiplication by 1/d when d is a power of two
 __device__ __forceinline__ double div_d(double x, double d, double inv_d, int pow2) {
-  return pow2 ? AXD_MUL(x, inv_d) : AXD_DIV(x, d);
+  return pow2 ? axg_mul_pow2(x, inv_d) : AXD_DIV(x, d);
 }
 
 __global__ void k_drift_fp64(double2 *__restrict__ phi, const double2 *__restrict__ phid,
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) k_kick_fp64(const double2 *__restrict__ p
       for (int j = 0; j <= i; ++j, ++comp) {
         const double *uc = u + comp * n3;
         double src = AXD_ADD(AXD_MUL(dr[i], dr[j]), AXD_MUL(di[i], di[j]));
-        src = AXD_MUL(2.0, src);
+        src = axg_mul_pow2(src, 2.0);
         double lu = AXD_ADD(uc[sx1], uc[sx2]);
         lu = AXD_ADD(lu, uc[sy1]);
         lu = AXD_ADD(lu, uc[sy2]);
@@ -584,7 +584,7 @@ __device__ __forceinline__ bool fused_column(const CUtensorMap *tm_prow, const C
               const double uyp = ty < TY - 1 ? ub[o + TX] : ubt[c * TX + tx];
               const double uzm = ubp[o], uzp = ubn[o];
               double src = AXD_ADD(AXD_MUL(dr[i], dr[j]), AXD_MUL(di[i], di[j]));
-              src = AXD_MUL(2.0, src);
+              src = axg_mul_pow2(src, 2.0);
               double lu = AXD_ADD(uxm, uxp);
               lu = AXD_ADD(lu, uym);
               lu = AXD_ADD(lu, uyp);

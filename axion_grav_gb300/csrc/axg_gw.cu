@@ -60,8 +60,8 @@ __global__ void k_gw_source(const double2 *__restrict__ phi, int n, double d, do
     for (int k = 0; k < 3; ++k) {
       const double2 pa = phi[a[k]], pb = phi[b[k]];
       const double xr = AXD_SUB(pa.x, pb.x), xi = AXD_SUB(pa.y, pb.y);
-      dr[k] = d_pow2 ? AXD_MUL(xr, inv_d) : AXD_DIV(xr, d);
-      di[k] = d_pow2 ? AXD_MUL(xi, inv_d) : AXD_DIV(xi, d);
+      dr[k] = d_pow2 ? axg_mul_pow2(xr, inv_d) : AXD_DIV(xr, d);
+      di[k] = d_pow2 ? axg_mul_pow2(xi, inv_d) : AXD_DIV(xi, d);
     }
     int c = 0;
 #pragma unroll
@@ -69,7 +69,7 @@ __global__ void k_gw_source(const double2 *__restrict__ phi, int n, double d, do
 #pragma unroll
       for (int j = 0; j <= i; ++j, ++c) {
         const double r1 = AXD_ADD(AXD_MUL(dr[i], dr[j]), AXD_MUL(di[i], di[j]));
-        src[c * n3 + s] = AXD_ADD(r1, r1);
+        src[c * n3 + s] = axg_mul_pow2(r1, 2.0);  // == r1 + r1
       }
   }
 }

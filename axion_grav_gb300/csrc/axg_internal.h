@@ -113,6 +113,8 @@ struct axg_ctx {
   double2 *spec_buf = nullptr;  // (N/deg)^3 complex
   cufftHandle plan_spec = 0;
   bool plan_spec_ok = false;
+  cufftHandle plan_window = 0;  // D2Z of the real window (its half spectrum follows the real input in spec_buf)
+  bool plan_window_ok = false;
   int64_t ns_spec = 0;
 
   // GW spectra of u_ij (R2C of 12 fields)
@@ -169,6 +171,22 @@ int axg_set_error(axg_ctx *ctx, int code, const std::string &msg);
     int s_ = (expr);         \
     if (s_ != AXG_OK) return s_; \
   } while (0)
+
+#ifdef __CUDACC__
+// x * f for f = 2^k, bit-identical to the FP64 multiply but on the integer
+// pipe: for a normal x whose product stays normal the product only adds k to
+// the exponent field.  Zero, subnormal, infinite or NaN x, and products that
+// would leave the normal range, take the FP64 multiply.  (GB300 issues FP64
+// at 1/64 of the FP32 rate, so exact power-of-two scalings move off it.)
+__device__ __forceinline__ double axg_mul_pow2(double x, double f) {
+  const long long fb = __double_as_longlong(f);
+  const int k = (int)((fb >> 52) & 0x7ff) - 1023;
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e > 0 && e < 0x7ff && e + k > 0 && e + k < 0x7ff) return __longlong_as_double(b + ((long long)k << 52));
+  return __dmul_rn(x, f);
+}
+#endif
 
 // Runs its function when the scope ends, also on the early returns of the
 // AXG_* macros (scratch buffers, plans and events of multi-step routines).

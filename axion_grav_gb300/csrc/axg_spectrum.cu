@@ -92,18 +92,42 @@ __global__ void k_spec_bin(const double2 *__restrict__ F, int m, const int16_t *
   }
 }
 
-// |W|^2 and mode counts per integer |k|^2
+// the real window of compute_matrix_deconv: dx^3 on unmasked coarse cells
+__global__ void k_spec_window(const int8_t *__restrict__ flags, int n, int deg, double dv_spa,
+                              double *__restrict__ out) {
+  const int m = n / deg;
+  const int64_t m3 = (int64_t)m * m * m, n2 = (int64_t)n * n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < m3; c += stride) {
+    const int ix = (int)(c % m), iy = (int)((c / m) % m), iz = (int)(c / ((int64_t)m * m));
+    bool masked = false;
+    if (flags)
+      for (int z0 = iz * deg; z0 < (iz + 1) * deg && !masked; ++z0)
+        for (int y0 = iy * deg; y0 < (iy + 1) * deg && !masked; ++y0)
+          for (int x0 = ix * deg; x0 < (ix + 1) * deg; ++x0)
+            if (flags[z0 * n2 + (int64_t)y0 * n + x0] & 4) {
+              masked = true;
+              break;
+            }
+    out[c] = masked ? 0.0 : dv_spa;
+  }
+}
+
+// |W|^2 and mode counts per integer |k|^2 from the half spectrum of the real
+// window (|W(-k)| = |W(k)|: interior kx planes count twice)
 __global__ void k_spec_w2_hist(const double2 *__restrict__ W, int m, double *__restrict__ h,
                                double *__restrict__ cnt) {
-  const int64_t m3 = (int64_t)m * m * m;
+  const int mh = m / 2 + 1;
+  const int64_t nhalf = (int64_t)m * m * mh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m3; s += stride) {
-    const int ix = (int)(s % m), iy = (int)((s / m) % m), iz = (int)(s / ((int64_t)m * m));
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nhalf; s += stride) {
+    const int ix = (int)(s % mh), iy = (int)((s / mh) % m), iz = (int)(s / ((int64_t)mh * m));
     const int kx = kint(ix, m), ky = kint(iy, m), kz = kint(iz, m);
     const int iq2 = kx * kx + ky * ky + kz * kz;
+    const double wgt = (ix == 0 || 2 * ix == m) ? 1.0 : 2.0;
     const double2 w = W[s];
-    atomicAdd(&h[iq2], w.x * w.x + w.y * w.y);
-    atomicAdd(&cnt[iq2], 1.0);
+    atomicAdd(&h[iq2], wgt * (w.x * w.x + w.y * w.y));
+    atomicAdd(&cnt[iq2], wgt);
   }
 }
 
@@ -343,10 +367,16 @@ int axg_spec_init(axg_ctx *ctx) {
   AXG_CUDA_TRY(ctx, cudaMemcpy(ctx->spec_largeq0, l0.data(), (size_t)num_cov * 8, cudaMemcpyHostToDevice));
   AXG_CUDA_TRY(ctx, cudaMemcpy(ctx->spec_dq, ctx->h_dq.data(), (size_t)num_cov * 8, cudaMemcpyHostToDevice));
   ctx->ns_spec = m;
-  AXG_TRY(axg_alloc(ctx, (void **)&ctx->spec_buf, (size_t)m * m * m * 16, "spectrum buffer"));
+  // m^3 complex; the window pass uses it as m^3 reals followed by the D2Z
+  // half spectrum m^2 (m/2 + 1), which needs 16 m^2 bytes more
+  AXG_TRY(axg_alloc(ctx, (void **)&ctx->spec_buf, (size_t)m * m * m * 16 + (size_t)m * m * 16 + 256,
+                    "spectrum buffer"));
   AXG_CUFFT_TRY(ctx, cufftPlan3d(&ctx->plan_spec, m, m, m, CUFFT_Z2Z));
   ctx->plan_spec_ok = true;
   AXG_CUFFT_TRY(ctx, cufftSetStream(ctx->plan_spec, ctx->stream));
+  AXG_CUFFT_TRY(ctx, cufftPlan3d(&ctx->plan_window, m, m, m, CUFFT_D2Z));
+  ctx->plan_window_ok = true;
+  AXG_CUFFT_TRY(ctx, cufftSetStream(ctx->plan_window, ctx->stream));
   return AXG_OK;
 }
 
@@ -380,15 +410,13 @@ int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, d
            *d_conv = tat0 + num_cov, *d_cnt = d_conv + nb;
     AXG_CUDA_TRY(ctx, cudaMemsetAsync(scratch, 0, nscr * 8, ctx->stream));
     // ---- compute_matrix_deconv (spectrum.f90:344-444) ----
-    if (fp32)
-      AXG_LAUNCH(ctx, "spec_window", k_spec_degrade<float2>, grid_for(m3), 256, 0, (const float2 *)ctx->phid,
-                 ctx->flags, n, deg, 1.0 / ((double)deg * deg * deg), 1, dv_spa, ctx->spec_buf);
-    else
-      AXG_LAUNCH(ctx, "spec_window", k_spec_degrade<double2>, grid_for(m3), 256, 0, (const double2 *)ctx->phid,
-                 ctx->flags, n, deg, 1.0 / ((double)deg * deg * deg), 1, dv_spa, ctx->spec_buf);
-    AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
-                                    (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
-    AXG_LAUNCH(ctx, "spec_w2_hist", k_spec_w2_hist, grid_for(m3), 256, 0, ctx->spec_buf, m, h, cnt);
+    // the window is real: D2Z half spectrum (|W|^2 is the same for either sign)
+    double *wreal = (double *)ctx->spec_buf;
+    double2 *whalf = (double2 *)(((uintptr_t)(wreal + m3) + 255) & ~(uintptr_t)255);
+    AXG_LAUNCH(ctx, "spec_window", k_spec_window, grid_for(m3), 256, 0, ctx->flags, n, deg, dv_spa, wreal);
+    AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_window, wreal, (cufftDoubleComplex *)whalf));
+    AXG_LAUNCH(ctx, "spec_w2_hist", k_spec_w2_hist, grid_for((int64_t)m * m * (m / 2 + 1)), 256, 0, whalf, m, h,
+               cnt);
     std::vector<long long> hr(2 * (size_t)num_cov);
     for (int ij = 0; ij < num_cov; ++ij) {
       double e = ctx->h_largeq[(size_t)ij * 501 + kNumLargeq] / dwav;

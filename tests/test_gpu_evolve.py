@@ -37,7 +37,7 @@ def run_gpu(p, state, fn):
     return g[0], g[1], gu[0], gu[1], out, launches
 
 
-@pytest.mark.parametrize("n", [12, 16, 32])
+@pytest.mark.parametrize("n", [6, 10, 12, 16, 32])
 @pytest.mark.parametrize("gw", [ag.GW_NONE, ag.GW_UIJ])
 def test_fp64_plain_drift_kick_bit_exact(n, gw):
     p = make_params(n, ag.PREC_FP64_PLAIN, gw)
@@ -56,6 +56,21 @@ def test_fp64_plain_drift_kick_bit_exact(n, gw):
     assert np.array_equal(g_phi, phi) and np.array_equal(g_phid, phid)
     if gw:
         assert np.array_equal(g_u, u) and np.array_equal(g_ud, ud)
+
+
+@pytest.mark.parametrize("dspa", [0.0625, 0.3125, 4.0])
+def test_fp64_plain_spacings_bit_exact(dspa):
+    """d = 2 dx a power of two (1/8, 8: exact exponent shifts on the integer
+    pipe) or not (0.625: FP64 division) -- every case bit-identical to the
+    oracle's IEEE operations."""
+    n = 16
+    p = make_params(n, ag.PREC_FP64_PLAIN, ag.GW_UIJ, dspa=dspa)
+    st = random_state(n, 4, 0.1)
+    phi, phid, u, ud = (a.copy() for a in st)
+    axo.leapfrog(p, phi, phid, u, ud, None, 1.3, 0.01 * dspa, 5, True, True)
+    g_phi, g_phid, g_u, g_ud, _, _ = run_gpu(p, st, lambda lat: lat.leapfrog(1.3, 0.01 * dspa, 5, True, True))
+    assert np.array_equal(g_phi, phi) and np.array_equal(g_phid, phid)
+    assert np.array_equal(g_u, u) and np.array_equal(g_ud, ud)
 
 
 @pytest.mark.parametrize("potential", [ag.POT_REFERENCE, ag.POT_QUARTIC])
