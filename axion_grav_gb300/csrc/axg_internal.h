@@ -178,13 +178,16 @@ int axg_set_error(axg_ctx *ctx, int code, const std::string &msg);
 // the exponent field.  Zero, subnormal, infinite or NaN x, and products that
 // would leave the normal range, take the FP64 multiply.  (GB300 issues FP64
 // at 1/64 of the FP32 rate, so exact power-of-two scalings move off it.)
+// The rare FP64 path is a real call, so that it is branched over instead of
+// being issued predicated-off on every lane.
+static __device__ __noinline__ double axg_mul_pow2_fp64(double x, double f) { return __dmul_rn(x, f); }
 __device__ __forceinline__ double axg_mul_pow2(double x, double f) {
   const long long fb = __double_as_longlong(f);
   const int k = (int)((fb >> 52) & 0x7ff) - 1023;
   const long long b = __double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7ff);
   if (e > 0 && e < 0x7ff && e + k > 0 && e + k < 0x7ff) return __longlong_as_double(b + ((long long)k << 52));
-  return __dmul_rn(x, f);
+  return axg_mul_pow2_fp64(x, f);
 }
 #endif
 
