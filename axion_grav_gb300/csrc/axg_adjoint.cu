@@ -24,7 +24,8 @@
 //              checkpoint every `stride` steps.  u_ij enters the equations
 //              linearly and its adjoint never reads u, so u and u' are not
 //              stepped back (they stay at the final state).  The adjoint step
-//              is two stencil passes (k_adj_step: Laplacians of the adjoint
+//              is two stencil passes (k_adj_step, tiled and z-marching as
+//              k_adj_step_tiled when 32 divides N: Laplacians of the adjoint
 //              momenta, the transposed potential Jacobian, the source
 //              adjoint's Q_i = 2 fs (sum_j wbar_ij D_j phi + wbar_ii D_i phi);
 //              k_adj_divq: phibar += sum_i D_i^T Q_i).  Laplacians are summed
@@ -200,6 +201,110 @@ __global__ void k_adj_step(const typename V2T<R>::T *__restrict__ phi, const typ
   }
   lam_part = warp_sum(lam_part);
   if ((threadIdx.x & 31) == 0 && lam_part != 0.0) atomicAdd(dlam, lam_part);
+}
+
+// The same adjoint step, shared-memory tiled and z-marching: a block owns a
+// TX x TY column of zc planes and keeps a 3-plane ring of (TX+2) x (TY+2)
+// tiles of itil = pibar + h phibar (complex), wtil = wbar + h ubar (six
+// reals) and phi (complex).  Tiles are filled with coalesced loads that form
+// the combinations once per element, so a site costs about 24 scalar loads
+// instead of about 100 scattered ones; the z neighbours come from the ring.
+// The lambda contribution is summed per thread and per warp in R and added
+// with one FP64 atomic per warp.
+template <typename R, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY) k_adj_step_tiled(
+    const typename V2T<R>::T *__restrict__ phi, const typename V2T<R>::T *__restrict__ pb_in,
+    const typename V2T<R>::T *__restrict__ ib_in, const R *__restrict__ ub_in, const R *__restrict__ wb_in,
+    typename V2T<R>::T *__restrict__ pb_out, typename V2T<R>::T *__restrict__ ib_out, R *__restrict__ ub_out,
+    R *__restrict__ wb_out, R *__restrict__ Q, int n, int zc, Coef<R> k, double *__restrict__ dlam) {
+  constexpr int W = TX + 2, H = TY + 2, PLANE = W * H, SLOT = 10 * PLANE;
+  extern __shared__ unsigned char adj_smem[];
+  R *sm = reinterpret_cast<R *>(adj_smem);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int ncx = n / TX;
+  const int x0 = (blockIdx.x % ncx) * TX, y0 = (blockIdx.x / ncx) * TY, z0 = blockIdx.y * zc;
+  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  auto load_plane = [&](int z, int slot) {
+    z = wr(z, n);
+    R *t = sm + slot * SLOT;
+    for (int e = tid; e < PLANE; e += TX * TY) {
+      const int gx = wr(x0 + e % W - 1, n), gy = wr(y0 + e / W - 1, n);
+      const int64_t g = (int64_t)z * n2 + (int64_t)gy * n + gx;
+      const auto a = ib_in[g], b = pb_in[g];
+      t[e] = a.x + k.h * b.x;
+      t[PLANE + e] = a.y + k.h * b.y;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) t[(2 + c) * PLANE + e] = wb_in[c * n3 + g] + k.h * ub_in[c * n3 + g];
+      const auto p = phi[g];
+      t[8 * PLANE + e] = p.x;
+      t[9 * PLANE + e] = p.y;
+    }
+  };
+  load_plane(z0 - 1, 0);
+  load_plane(z0, 1);
+  R lam = 0;
+  const int ci = (ty + 1) * W + (tx + 1);
+  const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
+  for (int kk = 0; kk < zc; ++kk) {
+    const int z = z0 + kk;
+    load_plane(z + 1, (kk + 2) % 3);
+    __syncthreads();
+    const R *tm = sm + (kk % 3) * SLOT, *tc = sm + ((kk + 1) % 3) * SLOT, *tp = sm + ((kk + 2) % 3) * SLOT;
+    const int64_t c = (int64_t)z * n2 + (int64_t)(y0 + ty) * n + (x0 + tx);
+    // Laplacian of itil (differences from the centre)
+    const R i0r = tc[ci], i0i = tc[PLANE + ci];
+    const R lr = (tc[ci - 1] - i0r) + (tc[ci + 1] - i0r) + (tc[ci - W] - i0r) + (tc[ci + W] - i0r) +
+                 (tm[ci] - i0r) + (tp[ci] - i0r);
+    const R li = (tc[PLANE + ci - 1] - i0i) + (tc[PLANE + ci + 1] - i0i) + (tc[PLANE + ci - W] - i0i) +
+                 (tc[PLANE + ci + W] - i0i) + (tm[PLANE + ci] - i0i) + (tp[PLANE + ci] - i0i);
+    const R p0r = tc[8 * PLANE + ci], p0i = tc[9 * PLANE + ci];
+    const R s = p0r * p0r + p0i * p0i, g0 = k.A * s + k.B;
+    const R pd = p0r * i0r + p0i * i0i;
+    const R jr = g0 * i0r + 2 * k.A * p0r * pd + k.D * i0r;
+    const R ji = g0 * i0i + 2 * k.A * p0i * pd - k.D * i0i;
+    const auto pbv = pb_in[c];
+    pb_out[c] = mk<R>(pbv.x + k.f2 * lr + k.f3 * jr, pbv.y + k.f2 * li + k.f3 * ji);
+    ib_out[c] = mk<R>(k.f1 * i0r, k.f1 * i0i);
+    lam += k.f3 * (k.dA * s + k.dB) * pd;
+    // central differences of phi
+    const R Dr[3] = {(tc[8 * PLANE + ci + 1] - tc[8 * PLANE + ci - 1]) * k.inv_d,
+                     (tc[8 * PLANE + ci + W] - tc[8 * PLANE + ci - W]) * k.inv_d,
+                     (tp[8 * PLANE + ci] - tm[8 * PLANE + ci]) * k.inv_d};
+    const R Di[3] = {(tc[9 * PLANE + ci + 1] - tc[9 * PLANE + ci - 1]) * k.inv_d,
+                     (tc[9 * PLANE + ci + W] - tc[9 * PLANE + ci - W]) * k.inv_d,
+                     (tp[9 * PLANE + ci] - tm[9 * PLANE + ci]) * k.inv_d};
+    R wt[6];
+#pragma unroll
+    for (int cc = 0; cc < 6; ++cc) {
+      const R *w = tc + (2 + cc) * PLANE;
+      const R w0 = w[ci];
+      wt[cc] = w0;
+      const R lu = (w[ci - 1] - w0) + (w[ci + 1] - w0) + (w[ci - W] - w0) + (w[ci + W] - w0) +
+                   (tm[(2 + cc) * PLANE + ci] - w0) + (tp[(2 + cc) * PLANE + ci] - w0);
+      ub_out[cc * n3 + c] = ub_in[cc * n3 + c] + k.f2 * lu;
+      wb_out[cc * n3 + c] = k.f1 * w0;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      R qr = wt[idx[i][i]] * Dr[i], qi = wt[idx[i][i]] * Di[i];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        qr += wt[idx[i][j]] * Dr[j];
+        qi += wt[idx[i][j]] * Di[j];
+      }
+      Q[(2 * i) * n3 + c] = 2 * k.fs * qr;
+      Q[(2 * i + 1) * n3 + c] = 2 * k.fs * qi;
+    }
+    __syncthreads();  // the ring slot of plane z - 1 is refilled next
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lam += __shfl_down_sync(0xffffffffu, lam, o);
+  if ((tid & 31) == 0 && lam != R(0)) atomicAdd(dlam, (double)lam);
+}
+
+template <typename R, int TX, int TY>
+constexpr int adj_tiled_smem() {
+  return 3 * 10 * (TX + 2) * (TY + 2) * (int)sizeof(R);
 }
 
 // phibar += sum_i D_i^T Q_i,  D_i^T Q(x) = (Q(x - e_i) - Q(x + e_i)) / d
@@ -476,6 +581,19 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
     // ---------------- reverse sweep ----------------
     double *dlam = ctx->d_red + 1;
     dim3 blk(32, 8), grd((n + 31) / 32, (n + 7) / 8, n);
+    // the tiled step needs N divisible by the 32 x 8 column and the z chunk
+    const int tzc = n % 32 == 0 ? 32 : 16;
+    const bool tiled = n % 32 == 0 && n % tzc == 0;
+    constexpr int tsmem = adj_tiled_smem<R, 32, 8>();
+    const dim3 tgrid((unsigned)((n / 32) * (n / 8)), (unsigned)(tiled ? n / tzc : 1));
+    if (tiled) {
+      static bool attr = false;
+      if (!attr) {
+        AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_adj_step_tiled<R, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               tsmem));
+        attr = true;
+      }
+    }
     bool a_is_in = true;
     V *phi = cur_phi();  // the reverse steps phi in place in the final buffer
     for (int64_t it = nsteps; it >= 1 && rc == AXG_OK; --it) {
@@ -492,8 +610,13 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
         *ibo = a_is_in ? ib_b : ib_a;
       R *ubi = a_is_in ? ub_a : ub_b, *wbi = a_is_in ? wb_a : wb_b, *ubo = a_is_in ? ub_b : ub_a,
         *wbo = a_is_in ? wb_b : wb_a;
-      AXG_LAUNCH(ctx, "adj_step", k_adj_step<R>, grd, blk, 0, phi, pbi, ibi, ubi, wbi, pbo_, ibo, ubo, wbo, Q, n, kr,
-                 dlam);
+      if (tiled) {
+        AXG_LAUNCH(ctx, "adj_step", (k_adj_step_tiled<R, 32, 8>), tgrid, dim3(32, 8), tsmem, phi, pbi, ibi, ubi, wbi,
+                   pbo_, ibo, ubo, wbo, Q, n, tzc, kr, dlam);
+      } else {
+        AXG_LAUNCH(ctx, "adj_step", k_adj_step<R>, grd, blk, 0, phi, pbi, ibi, ubi, wbi, pbo_, ibo, ubo, wbo, Q, n, kr,
+                   dlam);
+      }
       AXG_LAUNCH(ctx, "adj_divq", k_adj_divq<R>, grd, blk, 0, pbo_, Q, n, kr.inv_d);
       a_is_in = !a_is_in;
     }
