@@ -101,7 +101,7 @@ EXPORTED_SYMBOLS = (
     "axg_field_moments_noalloc", "axg_ensemble_create", "axg_ensemble_destroy", "axg_ensemble_last_error",
     "axg_ensemble_size", "axg_ensemble_member", "axg_ensemble_leapfrog", "axg_ensemble_autotune",
     "axg_ensemble_launch_count", "axg_adjoint_gw_band", "axg_spectrum_covariance", "axg_compute_crho_cov",
-    "axg_epsilon", "axg_ensemble_set_tile",
+    "axg_epsilon", "axg_ensemble_set_tile", "axg_ensemble_set_launch_mode", "axg_ensemble_launch_mode",
 )
 
 _lib = None
@@ -179,6 +179,8 @@ def load_library():
         "axg_ensemble_create": ([P(Params), ctypes.c_int32, P(ctypes.c_void_p)], ctypes.c_int),
         "axg_ensemble_destroy": ([ctypes.c_void_p], ctypes.c_int),
         "axg_ensemble_set_tile": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+        "axg_ensemble_set_launch_mode": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+        "axg_ensemble_launch_mode": ([ctypes.c_void_p, P(ctypes.c_int)], ctypes.c_int),
         "axg_ensemble_last_error": ([ctypes.c_void_p], ctypes.c_char_p),
         "axg_ensemble_size": ([ctypes.c_void_p, P(ctypes.c_int32)], ctypes.c_int),
         "axg_ensemble_member": ([ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_void_p)], ctypes.c_int),
@@ -549,6 +551,15 @@ class Ensemble:
 
     def set_tile(self, cfg: int):
         self._check(self.lib.axg_ensemble_set_tile(self._e, cfg))
+
+    def set_launch_mode(self, persistent: bool):
+        """True: resident CTAs walk the work items; False: one CTA per item."""
+        self._check(self.lib.axg_ensemble_set_launch_mode(self._e, int(bool(persistent))))
+
+    def launch_mode(self) -> bool:
+        v = ctypes.c_int()
+        self._check(self.lib.axg_ensemble_launch_mode(self._e, ctypes.byref(v)))
+        return bool(v.value)
 
     def autotune(self, steps=3):
         best = ctypes.c_int()

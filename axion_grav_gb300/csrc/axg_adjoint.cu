@@ -24,15 +24,18 @@
 //              checkpoint every `stride` steps.  u_ij enters the equations
 //              linearly and its adjoint never reads u, so u and u' are not
 //              stepped back (they stay at the final state).  The adjoint step
-//              is two stencil passes (k_adj_step, tiled and z-marching as
-//              k_adj_step_tiled when 32 divides N: Laplacians of the adjoint
-//              momenta, the transposed potential Jacobian, the source
-//              adjoint's Q_i = 2 fs (sum_j wbar_ij D_j phi + wbar_ii D_i phi);
+//              is two stencil passes (k_adj_step; z-marching when 32
+//              divides N, as k_adj_step_roll in FP32 and k_adj_step_tiled
+//              in FP64: Laplacians of the adjoint momenta, the transposed
+//              potential Jacobian, the source adjoint's
+//              Q_i = 2 fs (sum_j wbar_ij D_j phi + wbar_ii D_i phi);
 //              k_adj_divq: phibar += sum_i D_i^T Q_i).  Laplacians are summed
 //              as differences from the centre (exact for smooth fields in
 //              FP32); divisions by f1 and 2 dx are multiplications by
 //              reciprocals computed once per step on the host.
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "axg_internal.h"
@@ -307,6 +310,176 @@ constexpr int adj_tiled_smem() {
   return 3 * 10 * (TX + 2) * (TY + 2) * (int)sizeof(R);
 }
 
+// The adjoint step with the z neighbours in registers: each thread owns one
+// (x, y) column of a TX x TY tile and walks zc planes, holding the
+// combinations (itil, wtil, phi) at z - 1, z and z + 1 in registers.  Only
+// the current plane, with its x and y halo, goes through shared memory, in
+// two slots, so one barrier per plane suffices.  The raw fields of plane
+// z + 2 are loaded into registers before plane z is computed, so their
+// latency overlaps the arithmetic, and the raw centre values double as the
+// additive terms of the outputs (no second load).  The expressions and their
+// order are those of k_adj_step_tiled, so the outputs are bit-identical.
+template <typename R>
+struct AdjRaw {
+  typename V2T<R>::T ib, pb, ph;
+  R wb[6], ub[6];
+};
+
+template <typename R>
+struct AdjCmb {
+  R ir, ii, w[6], pr, pi;
+};
+
+template <typename R, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 2 : 1) k_adj_step_roll(
+    const typename V2T<R>::T *__restrict__ phi, const typename V2T<R>::T *__restrict__ pb_in,
+    const typename V2T<R>::T *__restrict__ ib_in, const R *__restrict__ ub_in, const R *__restrict__ wb_in,
+    typename V2T<R>::T *__restrict__ pb_out, typename V2T<R>::T *__restrict__ ib_out, R *__restrict__ ub_out,
+    R *__restrict__ wb_out, R *__restrict__ Q, int n, int zc, Coef<R> k, double *__restrict__ dlam) {
+  static_assert(TX == 32, "one warp per tile row");
+  static_assert(2 * TY <= 32 && TY >= 3, "halo duties of warps 0-2");
+  constexpr int W = TX + 2, H = TY + 2, PLANE = W * H, SLOT = 10 * PLANE;
+  extern __shared__ unsigned char adj_smem[];
+  R *sm = reinterpret_cast<R *>(adj_smem);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int ncx = n / TX;
+  const int x0 = (blockIdx.x % ncx) * TX, y0 = (blockIdx.x / ncx) * TY, z0 = blockIdx.y * zc;
+  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int64_t own = (int64_t)(y0 + ty) * n + (x0 + tx);
+  // halo duty: warp 0 the row y0 - 1, warp 1 the row y0 + TY, warp 2 (lanes
+  // below 2 TY) the columns x0 - 1 and x0 + TX; the corners are never read
+  int64_t hoff = -1;
+  int hsi = 0;
+  if (ty == 0) {
+    hoff = (int64_t)wr(y0 - 1, n) * n + x0 + tx;
+    hsi = tx + 1;
+  } else if (ty == 1) {
+    hoff = (int64_t)wr(y0 + TY, n) * n + x0 + tx;
+    hsi = (TY + 1) * W + tx + 1;
+  } else if (ty == 2 && tx < 2 * TY) {
+    const int r = tx % TY;
+    const bool lo = tx < TY;
+    hoff = (int64_t)(y0 + r) * n + wr(lo ? x0 - 1 : x0 + TX, n);
+    hsi = (r + 1) * W + (lo ? 0 : TX + 1);
+  }
+  const bool halo = hoff >= 0;
+  auto load = [&](int z, int64_t off, AdjRaw<R> &r) {
+    const int64_t g = (int64_t)wr(z, n) * n2 + off;
+    r.ib = ib_in[g];
+    r.pb = pb_in[g];
+    r.ph = phi[g];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      r.wb[c] = wb_in[c * n3 + g];
+      r.ub[c] = ub_in[c * n3 + g];
+    }
+  };
+  auto combine = [&](const AdjRaw<R> &r) {
+    AdjCmb<R> m;
+    m.ir = r.ib.x + k.h * r.pb.x;
+    m.ii = r.ib.y + k.h * r.pb.y;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) m.w[c] = r.wb[c] + k.h * r.ub[c];
+    m.pr = r.ph.x;
+    m.pi = r.ph.y;
+    return m;
+  };
+  auto store = [&](R *slot, int si, const AdjCmb<R> &m) {
+    slot[si] = m.ir;
+    slot[PLANE + si] = m.ii;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) slot[(2 + c) * PLANE + si] = m.w[c];
+    slot[8 * PLANE + si] = m.pr;
+    slot[9 * PLANE + si] = m.pi;
+  };
+  const int ci = (ty + 1) * W + (tx + 1);
+  AdjRaw<R> rn, rh;
+  load(z0 - 1, own, rn);
+  AdjCmb<R> prev = combine(rn);
+  load(z0, own, rn);
+  AdjCmb<R> cur = combine(rn);
+  R pbc[2] = {rn.pb.x, rn.pb.y}, ubc[6];  // raw centre values of plane z
+#pragma unroll
+  for (int c = 0; c < 6; ++c) ubc[c] = rn.ub[c];
+  store(sm, ci, cur);
+  if (halo) {
+    load(z0, hoff, rh);
+    store(sm, hsi, combine(rh));
+  }
+  load(z0 + 1, own, rn);
+  if (halo && zc > 1) load(z0 + 1, hoff, rh);
+  R lam = 0;
+  const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
+  for (int kk = 0; kk < zc; ++kk) {
+    const int z = z0 + kk;
+    __syncthreads();  // plane z is complete in slot kk & 1; the other slot is free
+    const AdjCmb<R> next = combine(rn);
+    R pbn[2] = {rn.pb.x, rn.pb.y}, ubn[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) ubn[c] = rn.ub[c];
+    if (kk + 1 < zc) {
+      R *tn = sm + ((kk + 1) & 1) * SLOT;
+      store(tn, ci, next);
+      if (halo) store(tn, hsi, combine(rh));
+      load(z + 2, own, rn);  // prefetch: `next` of plane z + 1
+      if (halo && kk + 2 < zc) load(z + 2, hoff, rh);
+    }
+    const R *tc = sm + (kk & 1) * SLOT;
+    const int64_t c = (int64_t)z * n2 + own;
+    const R i0r = cur.ir, i0i = cur.ii;
+    const R lr = (tc[ci - 1] - i0r) + (tc[ci + 1] - i0r) + (tc[ci - W] - i0r) + (tc[ci + W] - i0r) +
+                 (prev.ir - i0r) + (next.ir - i0r);
+    const R li = (tc[PLANE + ci - 1] - i0i) + (tc[PLANE + ci + 1] - i0i) + (tc[PLANE + ci - W] - i0i) +
+                 (tc[PLANE + ci + W] - i0i) + (prev.ii - i0i) + (next.ii - i0i);
+    const R p0r = cur.pr, p0i = cur.pi;
+    const R s = p0r * p0r + p0i * p0i, g0 = k.A * s + k.B;
+    const R pd = p0r * i0r + p0i * i0i;
+    const R jr = g0 * i0r + 2 * k.A * p0r * pd + k.D * i0r;
+    const R ji = g0 * i0i + 2 * k.A * p0i * pd - k.D * i0i;
+    pb_out[c] = mk<R>(pbc[0] + k.f2 * lr + k.f3 * jr, pbc[1] + k.f2 * li + k.f3 * ji);
+    ib_out[c] = mk<R>(k.f1 * i0r, k.f1 * i0i);
+    lam += k.f3 * (k.dA * s + k.dB) * pd;
+    const R Dr[3] = {(tc[8 * PLANE + ci + 1] - tc[8 * PLANE + ci - 1]) * k.inv_d,
+                     (tc[8 * PLANE + ci + W] - tc[8 * PLANE + ci - W]) * k.inv_d, (next.pr - prev.pr) * k.inv_d};
+    const R Di[3] = {(tc[9 * PLANE + ci + 1] - tc[9 * PLANE + ci - 1]) * k.inv_d,
+                     (tc[9 * PLANE + ci + W] - tc[9 * PLANE + ci - W]) * k.inv_d, (next.pi - prev.pi) * k.inv_d};
+#pragma unroll
+    for (int cc = 0; cc < 6; ++cc) {
+      const R *w = tc + (2 + cc) * PLANE;
+      const R w0 = cur.w[cc];
+      const R lu = (w[ci - 1] - w0) + (w[ci + 1] - w0) + (w[ci - W] - w0) + (w[ci + W] - w0) + (prev.w[cc] - w0) +
+                   (next.w[cc] - w0);
+      ub_out[cc * n3 + c] = ubc[cc] + k.f2 * lu;
+      wb_out[cc * n3 + c] = k.f1 * w0;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      R qr = cur.w[idx[i][i]] * Dr[i], qi = cur.w[idx[i][i]] * Di[i];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        qr += cur.w[idx[i][j]] * Dr[j];
+        qi += cur.w[idx[i][j]] * Di[j];
+      }
+      Q[(2 * i) * n3 + c] = 2 * k.fs * qr;
+      Q[(2 * i + 1) * n3 + c] = 2 * k.fs * qi;
+    }
+    prev = cur;
+    cur = next;
+    pbc[0] = pbn[0];
+    pbc[1] = pbn[1];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) ubc[q] = ubn[q];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lam += __shfl_down_sync(0xffffffffu, lam, o);
+  if (((ty * TX + tx) & 31) == 0 && lam != R(0)) atomicAdd(dlam, (double)lam);
+}
+
+template <typename R, int TX, int TY>
+constexpr int adj_roll_smem() {
+  return 2 * 10 * (TX + 2) * (TY + 2) * (int)sizeof(R);
+}
+
 // phibar += sum_i D_i^T Q_i,  D_i^T Q(x) = (Q(x - e_i) - Q(x + e_i)) / d
 template <typename R>
 __global__ void k_adj_divq(typename V2T<R>::T *__restrict__ pb, const R *__restrict__ Q, int n, R inv_d) {
@@ -461,6 +634,23 @@ StepCoef coef_at(const axg_params &p, double t, double dt, double h) {
   return k;
 }
 
+// Which adjoint-step kernel runs.  All three give bit-identical adjoint
+// fields (the lambda sum differs in its last bits: the plain kernel sums in
+// FP64 per site).  AXG_ADJOINT_STEP_KERNEL = plain | ring | roll overrides
+// the choice, for the tests that compare them.
+enum class AdjKernel { plain, ring, roll };
+
+AdjKernel adj_kernel_choice(int n, bool f32) {
+  const bool tiled = n % 32 == 0;
+  AdjKernel k = !tiled ? AdjKernel::plain : (f32 ? AdjKernel::roll : AdjKernel::ring);
+  if (const char *v = std::getenv("AXG_ADJOINT_STEP_KERNEL")) {
+    if (!std::strcmp(v, "plain")) k = AdjKernel::plain;
+    else if (tiled && !std::strcmp(v, "ring")) k = AdjKernel::ring;
+    else if (tiled && !std::strcmp(v, "roll")) k = AdjKernel::roll;
+  }
+  return k;
+}
+
 template <typename R>
 int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_half, int last_half, int64_t stride,
                 double kmin, double kmax, double *J_out, double *dJ_dlambda, double *grad_phi0, double *grad_phidot0,
@@ -581,16 +771,20 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
     // ---------------- reverse sweep ----------------
     double *dlam = ctx->d_red + 1;
     dim3 blk(32, 8), grd((n + 31) / 32, (n + 7) / 8, n);
-    // the tiled step needs N divisible by the 32 x 8 column and the z chunk
-    const int tzc = n % 32 == 0 ? 32 : 16;
-    const bool tiled = n % 32 == 0 && n % tzc == 0;
-    constexpr int tsmem = adj_tiled_smem<R, 32, 8>();
-    const dim3 tgrid((unsigned)((n / 32) * (n / 8)), (unsigned)(tiled ? n / tzc : 1));
-    if (tiled) {
+    // the tiled steps need N divisible by the 32 x 8 column and the z chunk;
+    // FP32 rolls the z neighbours through registers, FP64 (twice the
+    // registers per value) keeps the 3-plane ring
+    const int tzc = 32;
+    const AdjKernel kind = adj_kernel_choice(n, F32);
+    constexpr int tsmem = adj_tiled_smem<R, 32, 8>(), rsmem = adj_roll_smem<R, 32, 8>();
+    const dim3 tgrid((unsigned)((n / 32) * (n / 8)), (unsigned)(kind != AdjKernel::plain ? n / tzc : 1));
+    {
       static bool attr = false;
       if (!attr) {
         AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_adj_step_tiled<R, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                tsmem));
+        AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_adj_step_roll<R, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               rsmem));
         attr = true;
       }
     }
@@ -610,7 +804,10 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
         *ibo = a_is_in ? ib_b : ib_a;
       R *ubi = a_is_in ? ub_a : ub_b, *wbi = a_is_in ? wb_a : wb_b, *ubo = a_is_in ? ub_b : ub_a,
         *wbo = a_is_in ? wb_b : wb_a;
-      if (tiled) {
+      if (kind == AdjKernel::roll) {
+        AXG_LAUNCH(ctx, "adj_step", (k_adj_step_roll<R, 32, 8>), tgrid, dim3(32, 8), rsmem, phi, pbi, ibi, ubi, wbi,
+                   pbo_, ibo, ubo, wbo, Q, n, tzc, kr, dlam);
+      } else if (kind == AdjKernel::ring) {
         AXG_LAUNCH(ctx, "adj_step", (k_adj_step_tiled<R, 32, 8>), tgrid, dim3(32, 8), tsmem, phi, pbi, ibi, ubi, wbi,
                    pbo_, ibo, ubo, wbo, Q, n, tzc, kr, dlam);
       } else {

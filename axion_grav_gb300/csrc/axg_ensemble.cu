@@ -2,13 +2,14 @@
 //
 // An ensemble owns M member contexts (each a full axg_ctx: IC, defects,
 // spectra and transfers go through the member handle) on one shared stream.
-// The leapfrog of all members runs as one persistent launch per step
-// (k_fused_batch in axg_evolve.cu): work items are (member, column, z-chunk),
+// The leapfrog of all members runs as one launch per step (k_fused_batch in
+// axg_evolve.cu): work items are (member, column, z-chunk),
 // coefficients come from a device table, and the whole step sequence of an
 // interval -- coefficient upload, first half drifts, nsteps batched steps --
 // is captured once into a CUDA graph and replayed for later intervals with
-// the same shape.  The tile shape is shared by all members and chosen by
-// axg_ensemble_autotune.
+// the same shape.  The tile shape is shared by all members; it and the
+// launch mode (resident CTAs walking the items, or one CTA per item) are
+// chosen by axg_ensemble_autotune.
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -28,6 +29,7 @@ struct axg_ensemble {
   int *d_err = nullptr;
   long long total_items = 0;
   int cfg = -1;
+  bool persistent = false;
   int cur = 0;
   bool fp32 = true, uij = false;
   double dspa = 1.0;
@@ -132,7 +134,7 @@ int enqueue_interval(axg_ensemble *e, double dt, int64_t nsteps, int first_half,
   }
   for (int64_t s = 0; s < nsteps; ++s) {
     const int rc = axg_evo_batch_step(e->m[0], e->stream, e->d_mem, (int)e->m.size(), e->total_items, cur, e->d_coef,
-                                      (int)s, e->cfg, e->d_err, e->fp32, e->uij, e->dspa);
+                                      (int)s, e->cfg, e->d_err, e->fp32, e->uij, e->dspa, e->persistent);
     if (count) e->launches++;
     if (rc != AXG_OK) return ens_error(e, rc, e->m[0]->err);
     cur = 1 - cur;
@@ -311,6 +313,21 @@ int axg_ensemble_set_tile(axg_ensemble *e, int cfg) {
   return build_descriptors(e, cfg);
 }
 
+int axg_ensemble_set_launch_mode(axg_ensemble *e, int persistent) {
+  if (!e) return AXG_ERR_ARG;
+  if (e->persistent != (persistent != 0)) {
+    e->persistent = persistent != 0;
+    clear_graphs(e);  // captured launches carry the grid
+  }
+  return AXG_OK;
+}
+
+int axg_ensemble_launch_mode(const axg_ensemble *e, int *persistent) {
+  if (!e || !persistent) return AXG_ERR_ARG;
+  *persistent = e->persistent ? 1 : 0;
+  return AXG_OK;
+}
+
 int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *best_ms) {
   if (!e || steps < 1) return AXG_ERR_ARG;
   // snapshot everything a step modifies
@@ -341,7 +358,9 @@ int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *bes
     cudaMemcpyAsync(b.copy, b.src, b.bytes, cudaMemcpyDeviceToDevice, e->stream);
   }
   const int cur0 = e->cur, cfg0 = e->cfg;
+  const bool mode0 = e->persistent;
   int best = -1;
+  bool best_mode = mode0;
   double bt = 1e300;
   cudaEvent_t a, z;
   cudaEventCreate(&a);
@@ -349,20 +368,24 @@ int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *bes
   for (int cfg = 0; rc == AXG_OK && cfg < axg_evo_tile_count(); ++cfg) {
     if (!tile_ok_all(e, cfg)) continue;
     if ((rc = build_descriptors(e, cfg)) != AXG_OK) break;
-    if ((rc = axg_ensemble_leapfrog(e, 10.0, 1e-3, 1, 0, 0, 0)) != AXG_OK) break;  // warm-up
-    cudaEventRecord(a, e->stream);
-    rc = axg_ensemble_leapfrog(e, 10.0, 1e-3, steps, 0, 0, 0);
-    cudaEventRecord(z, e->stream);
-    cudaEventSynchronize(z);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, a, z);
-    if (rc == AXG_OK && ms / steps < bt) {
-      bt = ms / steps;
-      best = cfg;
+    for (int mode = 0; rc == AXG_OK && mode < 2; ++mode) {
+      e->persistent = mode == 1;
+      if ((rc = axg_ensemble_leapfrog(e, 10.0, 1e-3, 1, 0, 0, 0)) != AXG_OK) break;  // warm-up
+      cudaEventRecord(a, e->stream);
+      rc = axg_ensemble_leapfrog(e, 10.0, 1e-3, steps, 0, 0, 0);
+      cudaEventRecord(z, e->stream);
+      cudaEventSynchronize(z);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, z);
+      if (rc == AXG_OK && ms / steps < bt) {
+        bt = ms / steps;
+        best = cfg;
+        best_mode = e->persistent;
+      }
+      e->cur = cur0;
+      for (auto *c : e->m) c->cur = cur0;
+      for (auto &b : bufs) cudaMemcpyAsync(b.src, b.copy, b.bytes, cudaMemcpyDeviceToDevice, e->stream);
     }
-    e->cur = cur0;
-    for (auto *c : e->m) c->cur = cur0;
-    for (auto &b : bufs) cudaMemcpyAsync(b.src, b.copy, b.bytes, cudaMemcpyDeviceToDevice, e->stream);
   }
   cudaStreamSynchronize(e->stream);
   cudaEventDestroy(a);
@@ -370,6 +393,7 @@ int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *bes
   for (auto &b : bufs)
     if (b.copy) cudaFree(b.copy);
   const int chosen = (rc == AXG_OK && best >= 0) ? best : cfg0;
+  e->persistent = (rc == AXG_OK && best >= 0) ? best_mode : mode0;
   const int rc2 = build_descriptors(e, chosen);
   if (rc != AXG_OK) return rc;
   AXG_TRY(rc2);

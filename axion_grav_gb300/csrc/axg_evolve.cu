@@ -650,10 +650,11 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
 }
 
 // ------------------------------------------------------------------------
-// persistent batched kernel: ensembles of lattices of uneven sizes in one
-// launch.  Work items are (member, column, z-chunk) in member order, columns
-// fastest; each CTA walks the items with a grid stride, re-using its TMA
-// ring (stage phases continue through `gplane`).  Per-step coefficients come
+// batched kernel: ensembles of lattices of uneven sizes in one launch.  Work
+// items are (member, column, z-chunk) in member order, columns fastest.  Each
+// CTA walks the items with a grid stride, re-using its TMA ring (stage phases
+// continue through `gplane`); launched with one CTA per item the loop runs
+// once and the hardware scheduler balances the SMs.  Per-step coefficients come
 // from device memory so the whole step sequence can be graph-captured once.
 // ------------------------------------------------------------------------
 template <typename R, int TX, int TY, bool UIJ, bool PW>
@@ -1024,7 +1025,7 @@ int axg_evo_check_error(axg_ctx *ctx) {
 namespace {
 template <typename R, int TX, int TY, bool UIJ, bool PW>
 int launch_batch_t(axg_ctx *ctx, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem, long long total,
-                   int cur, const axg_ens_coef *d_coef, int step, int zc, double dspa, int *d_err) {
+                   int cur, const axg_ens_coef *d_coef, int step, int zc, double dspa, int *d_err, bool persistent) {
   constexpr int smem = fused_smem_bytes<R, TX, TY, UIJ, PW>();
   static bool attr_set = false;
   if (!attr_set) {
@@ -1037,7 +1038,9 @@ int launch_batch_t(axg_ctx *ctx, cudaStream_t stream, const axg_ens_member_dev *
                                                                   TX * TY, smem));
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  long long grid = (long long)std::max(per_sm, 1) * std::max(sms, 1);
+  // persistent: resident CTAs walk the items with a grid stride; otherwise
+  // one CTA per item and the hardware scheduler balances the SMs
+  long long grid = persistent ? (long long)std::max(per_sm, 1) * std::max(sms, 1) : total;
   if (grid > total) grid = total;
   k_fused_batch<R, TX, TY, UIJ, PW><<<(unsigned)grid, dim3(TX, TY), smem, stream>>>(d_mem, nmem, total, cur,
                                                                                    d_coef, step, zc, dspa, d_err);
@@ -1049,11 +1052,11 @@ int launch_batch_t(axg_ctx *ctx, cudaStream_t stream, const axg_ens_member_dev *
 
 int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem,
                        long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,
-                       int *d_err, bool fp32, bool uij, double dspa) {
+                       int *d_err, bool fp32, bool uij, double dspa, bool persistent) {
   const axg_tile_cfg t = kTiles[cfg];
 #define AXG_BATCH(R, TY_, U, PW_)                                                                         \
   return launch_batch_t<R, 32, TY_, U, PW_>(any, stream, d_mem, nmem, total_items, cur, d_coef, step, t.zc, dspa, \
-                                            d_err)
+                                            d_err, persistent)
 #define AXG_BATCH_TY(R, U)                        \
   if (t.pw) {                                     \
     if (t.ty == 8) AXG_BATCH(R, 8, U, true);      \

@@ -241,10 +241,11 @@ axg_tile_cfg axg_evo_tile(int i);
 int axg_evo_tile_supported(const axg_ctx *ctx, int i);
 int axg_evo_default_tile(const axg_ctx *ctx);
 int axg_evo_build_tmaps(axg_ctx *ctx, int cfg);
-// one persistent launch over every member's columns (ensemble.cu drives it)
+// one launch over every member's columns (ensemble.cu drives it); persistent
+// = resident CTAs walk the items, else one CTA per item
 int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem,
                        long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,
-                       int *d_err, bool fp32, bool uij, double dspa);
+                       int *d_err, bool fp32, bool uij, double dspa, bool persistent);
 
 // kick coefficients (axg_capi.cu) -- evolve.f90:291-305
 void axg_kick_coeffs(const axg_params *p, double t, double dt, double f[4], double pot[4]);

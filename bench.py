@@ -262,7 +262,7 @@ ENSEMBLE_SIZES = [(64, 32), (128, 32), (160, 24), (192, 8)]  # (N, members): 96 
 
 def bench_ensemble(ag, steps, device, sizes=ENSEMBLE_SIZES):
     """Config 3: 96 seeded realisations of uneven sizes stepped together, one
-    persistent launch per step, intervals replayed from a CUDA graph."""
+    launch per step, intervals replayed from a CUDA graph."""
     ps = []
     for n, cnt in sizes:
         for r in range(cnt):
@@ -301,6 +301,7 @@ def bench_ensemble(ag, steps, device, sizes=ENSEMBLE_SIZES):
                 "value": sites * nsteps / wall, "unit": UNIT, "ms_per_step": 1e3 * wall / nsteps,
                 "steps": nsteps, "intervals": 4, "graph": True, "launches": launches,
                 "batched_launches_per_step": 1, "tile": ens.members[0].tiles()[best],
+                "launch_mode": "persistent CTAs" if ens.launch_mode() else "one CTA per work item",
                 "setup_s": setup_s, "string_length_sample": float(np.mean(xi)),
                 "timing": "host wall clock around graph replays of kick+drift steps (each call synchronises)"}
     finally:

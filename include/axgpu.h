@@ -326,11 +326,17 @@ int axg_ensemble_member(axg_ensemble *e, int32_t i, axg_ctx **member);
  * graph that later intervals of that shape replay. */
 int axg_ensemble_leapfrog(axg_ensemble *e, double t1, double dt, int64_t nsteps, int first_half,
                           int last_half, int use_graph);
-/* choose the tile shape shared by all members (state restored) */
+/* choose the tile shape shared by all members and the launch mode (state
+ * restored) */
 int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *best_ms_per_step);
 /* fixes the tile shape (axg_tile_info index) of the batched kernel; it must
  * fit every member */
 int axg_ensemble_set_tile(axg_ensemble *e, int cfg);
+/* launch mode of the batched kernel: persistent = 1 runs one resident set of
+ * CTAs that walk the (member, column, z-chunk) items with a grid stride;
+ * persistent = 0 launches one CTA per item.  Results are identical. */
+int axg_ensemble_set_launch_mode(axg_ensemble *e, int persistent);
+int axg_ensemble_launch_mode(const axg_ensemble *e, int *persistent);
 int axg_ensemble_launch_count(const axg_ensemble *e, int64_t *launches);
 
 /* ------------------------------------------------------------------ */

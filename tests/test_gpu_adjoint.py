@@ -150,3 +150,28 @@ def test_fp32_adjoint_lambda_against_finite_differences():
     (Jp, *_), _ = gpu_adjoint(p32(1.0 + eps), st)
     (Jm, *_), _ = gpu_adjoint(p32(1.0 - eps), st)
     assert dl == pytest.approx((Jp - Jm) / (2 * eps), rel=1e-2)
+
+
+@pytest.mark.parametrize("precision", [ag.PREC_FP32_MIXED, ag.PREC_FP64_PLAIN])
+@pytest.mark.parametrize("n", [32, 64])
+def test_adjoint_step_kernels_agree(monkeypatch, precision, n):
+    """The plain global stencil, the 3-plane shared-memory ring and the
+    register-rolling z-march give bit-identical gradients.  dJ/dlambda is
+    summed per site in FP64 by the plain kernel, per warp in the arithmetic
+    type by the tiled ones, and J and dJ/dlambda go through FP64 atomics."""
+    st = state(n, 10)
+    p = _with_precision(params(n), precision)
+    out = {}
+    for kind in ("plain", "ring", "roll"):
+        monkeypatch.setenv("AXG_ADJOINT_STEP_KERNEL", kind)
+        out[kind] = gpu_adjoint(p, st, nsteps=9, stride=4)[0]
+    monkeypatch.delenv("AXG_ADJOINT_STEP_KERNEL")
+    ref = out["plain"]
+    assert np.isfinite(ref[0]) and np.all(np.isfinite(ref[2]))
+    for kind in ("ring", "roll"):
+        got = out[kind]
+        assert got[0] == pytest.approx(ref[0], rel=1e-13), kind  # J: atomics, last-bit order effects
+        assert got[1] == pytest.approx(ref[1], rel=1e-5 if precision == ag.PREC_FP32_MIXED else 1e-12), kind
+        assert np.array_equal(got[2], ref[2]) and np.array_equal(got[3], ref[3]), kind
+    # ring and roll sum the same per-warp values; only the FP64 atomics' order differs
+    assert out["roll"][1] == pytest.approx(out["ring"][1], rel=1e-13)

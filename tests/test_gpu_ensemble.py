@@ -1,5 +1,5 @@
-"""Batched ensembles of uneven lattices (one persistent launch per step,
-graph-captured intervals) reproduce single-lattice runs bit for bit."""
+"""Batched ensembles of uneven lattices (one launch per step, graph-captured
+intervals) reproduce single-lattice runs bit for bit."""
 import numpy as np
 import pytest
 
@@ -50,9 +50,11 @@ def test_ensemble_matches_single_runs(use_graph):
         assert np.array_equal(gu, u) and np.array_equal(gud, ud), i
 
 
-def test_ensemble_every_tile_matches_single_runs():
+@pytest.mark.parametrize("persistent", [False, True])
+def test_ensemble_every_tile_matches_single_runs(persistent):
     """The batched kernel on every tile shape that fits all members, with the
-    pointwise fields in registers or in the TMA ring."""
+    pointwise fields in registers or in the TMA ring, launched with one CTA
+    per work item or as resident CTAs walking the items."""
     sizes = [32, 64, 96]
     ps = [member_params(n, 200 + i) for i, n in enumerate(sizes)]
     dt, t0, nsteps = 0.02, 1.6, 6
@@ -65,6 +67,8 @@ def test_ensemble_every_tile_matches_single_runs():
                 ens.set_tile(cfg)
             except ag.AxgError:
                 continue
+            ens.set_launch_mode(persistent)
+            assert ens.launch_mode() == persistent
             for i, m in enumerate(ens.members):
                 m.ic_gaussian_flat(1.5, 200 + i)
             ens.leapfrog(t0, dt, nsteps, True, True, use_graph=True)
