@@ -25,9 +25,10 @@
 //              linearly and its adjoint never reads u, so u and u' are not
 //              stepped back (they stay at the final state).  The adjoint step
 //              is two stencil passes (k_adj_step; z-marching when 32
-//              divides N, as k_adj_step_roll in FP32 and k_adj_step_tiled
-//              in FP64: Laplacians of the adjoint momenta, the transposed
-//              potential Jacobian, the source adjoint's
+//              divides N, as k_adj_step_roll in FP32, which also fuses the
+//              backward re-step of phi, and k_adj_step_tiled in FP64:
+//              Laplacians of the adjoint momenta, the transposed potential
+//              Jacobian, the source adjoint's
 //              Q_i = 2 fs (sum_j wbar_ij D_j phi + wbar_ii D_i phi);
 //              k_adj_divq: phibar += sum_i D_i^T Q_i).  Laplacians are summed
 //              as differences from the centre (exact for smooth fields in
@@ -80,6 +81,35 @@ struct StepCoef {
   }
 };
 
+// Pinned arithmetic: every operation rounds once, in the order written.  The
+// adjoint-step variants below (plain stencil, shared-memory ring, register
+// roll, and the roll with the backward re-step fused in) share the point
+// formulas that follow, so they give the same bits whatever contractions the
+// compiler would otherwise pick in each kernel.
+__device__ __forceinline__ float pmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double pmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float padd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double padd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float pfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double pfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// adjoint of the drift: x + h y (pibar + h phibar, wbar + h ubar)
+template <typename R>
+__device__ __forceinline__ R dcomb(R x, R y, R h) {
+  return pfma(h, y, x);
+}
+
+template <typename R>
+__device__ __forceinline__ R mod2(R a, R b) {
+  return pfma(a, a, pmul(b, b));
+}
+
+// central difference (a - b) / (2 dx)
+template <typename R>
+__device__ __forceinline__ R cdiff(R a, R b, R inv_d) {
+  return pmul(padd(a, -b), inv_d);
+}
+
 __device__ __forceinline__ void kahan_sub(float &x, float &c, float dec) {
   const float y = -dec - c;
   const float t = x + y;
@@ -87,7 +117,64 @@ __device__ __forceinline__ void kahan_sub(float &x, float &c, float dec) {
   x = t;
 }
 
-// backward drift: phi -= h pi (FP32: Kahan-compensated like the forward drift)
+// backward drift of one component: phi -= h pi (FP32: Kahan-compensated like
+// the forward drift)
+__device__ __forceinline__ void rev_drift1(float &x, float &c, float h, float b) { kahan_sub(x, c, pmul(h, b)); }
+__device__ __forceinline__ void rev_drift1(double &x, double &, double h, double b) { x = pfma(-h, b, x); }
+
+// backward kick at one site: pi = (pi+ - f2 L phi - f3 g(phi)) / f1
+template <typename R>
+__device__ __forceinline__ typename V2T<R>::T rev_kick1(typename V2T<R>::T pv, R lr, R li, R p0r, R p0i,
+                                                        const Coef<R> &k) {
+  const R g0 = pfma(k.A, mod2(p0r, p0i), k.B);
+  const R gr = padd(pfma(g0, p0r, pmul(k.D, p0r)), k.C), gi = pfma(g0, p0i, -pmul(k.D, p0i));
+  return mk<R>(pmul(pfma(-k.f3, gr, pfma(-k.f2, lr, pv.x)), k.inv_f1),
+               pmul(pfma(-k.f3, gi, pfma(-k.f2, li, pv.y)), k.inv_f1));
+}
+
+// adjoint of the kick at one site, without the D^T Q part of phibar: from
+// itil at the site (i0), its Laplacian (l), phi (p0) and phibar+ (pb):
+// phibar, pibar and the site's dJ/dlambda term
+template <typename R>
+struct AdjOut {
+  typename V2T<R>::T pb, ib;
+  R lam;
+};
+
+template <typename R>
+__device__ __forceinline__ AdjOut<R> adj_point(R i0r, R i0i, R lr, R li, R p0r, R p0i, R pbr, R pbi,
+                                               const Coef<R> &k) {
+  const R s = mod2(p0r, p0i), g0 = pfma(k.A, s, k.B);
+  const R pd = pfma(p0r, i0r, pmul(p0i, i0i));
+  const R a2 = pmul(R(2), k.A);
+  const R jr = pfma(k.D, i0r, pfma(g0, i0r, pmul(pmul(a2, p0r), pd)));
+  const R ji = pfma(-k.D, i0i, pfma(g0, i0i, pmul(pmul(a2, p0i), pd)));
+  AdjOut<R> o;
+  o.pb = mk<R>(pfma(k.f3, jr, pfma(k.f2, lr, pbr)), pfma(k.f3, ji, pfma(k.f2, li, pbi)));
+  o.ib = mk<R>(pmul(k.f1, i0r), pmul(k.f1, i0i));
+  o.lam = pmul(pmul(k.f3, pfma(k.dA, s, k.dB)), pd);
+  return o;
+}
+
+// the source adjoint Q_i = 2 fs (sum_j wtil_ij D_j phi + wtil_ii D_i phi)
+template <typename R>
+__device__ __forceinline__ void adj_q(const R wt[6], const R Dr[3], const R Di[3], R fs, R q[6]) {
+  const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
+  const R fs2 = pmul(R(2), fs);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    R qr = pmul(wt[idx[i][i]], Dr[i]), qi = pmul(wt[idx[i][i]], Di[i]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      qr = pfma(wt[idx[i][j]], Dr[j], qr);
+      qi = pfma(wt[idx[i][j]], Di[j], qi);
+    }
+    q[2 * i] = pmul(fs2, qr);
+    q[2 * i + 1] = pmul(fs2, qi);
+  }
+}
+
+// backward drift: phi -= h pi
 template <typename R>
 __global__ void k_rev_drift(typename V2T<R>::T *phi, typename V2T<R>::T *cphi, const typename V2T<R>::T *pi,
                             int64_t n3, R h) {
@@ -95,15 +182,11 @@ __global__ void k_rev_drift(typename V2T<R>::T *phi, typename V2T<R>::T *cphi, c
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
     auto a = phi[s];
     const auto b = pi[s];
-    if constexpr (sizeof(R) == 4) {
-      float2 c = cphi[s];
-      kahan_sub(a.x, c.x, h * b.x);
-      kahan_sub(a.y, c.y, h * b.y);
-      cphi[s] = c;
-    } else {
-      a.x -= h * b.x;
-      a.y -= h * b.y;
-    }
+    typename V2T<R>::T c = mk<R>(0, 0);
+    if constexpr (sizeof(R) == 4) c = cphi[s];
+    rev_drift1(a.x, c.x, h, b.x);
+    rev_drift1(a.y, c.y, h, b.y);
+    if constexpr (sizeof(R) == 4) cphi[s] = c;
     phi[s] = a;
   }
 }
@@ -118,18 +201,14 @@ __global__ void k_rev_kick(const typename V2T<R>::T *__restrict__ phi, typename 
   const int64_t nb[6] = {site(wr(ix - 1, n), iy, iz, n), site(wr(ix + 1, n), iy, iz, n), site(ix, wr(iy - 1, n), iz, n),
                          site(ix, wr(iy + 1, n), iz, n), site(ix, iy, wr(iz - 1, n), n), site(ix, iy, wr(iz + 1, n), n)};
   const auto p0 = phi[c];
-  R lr = 0, li = 0;
-  for (int q = 0; q < 6; ++q) {
+  // Laplacian as differences from the centre, summed x-, x+, y-, y+, z-, z+
+  R lr = phi[nb[0]].x - p0.x, li = phi[nb[0]].y - p0.y;
+  for (int q = 1; q < 6; ++q) {
     const auto v = phi[nb[q]];
-    lr += v.x - p0.x;
-    li += v.y - p0.y;
+    lr = lr + (v.x - p0.x);
+    li = li + (v.y - p0.y);
   }
-  const R s = p0.x * p0.x + p0.y * p0.y, g0 = k.A * s + k.B;
-  const R gr = g0 * p0.x + k.D * p0.x + k.C, gi = g0 * p0.y - k.D * p0.y;
-  auto v = pi[c];
-  v.x = (v.x - k.f2 * lr - k.f3 * gr) * k.inv_f1;
-  v.y = (v.y - k.f2 * li - k.f3 * gi) * k.inv_f1;
-  pi[c] = v;
+  pi[c] = rev_kick1<R>(pi[c], lr, li, p0.x, p0.y, k);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -138,7 +217,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // Adjoint of one kick+drift at the pre-kick state phi (in: adjoint after the
-// step; out: adjoint before it, except the D^T Q part of phibar).
+// step; out: adjoint before it, except the D^T Q part of phibar).  dJ/dlambda
+// is summed per site in FP64 here.
 template <typename R>
 __global__ void k_adj_step(const typename V2T<R>::T *__restrict__ phi, const typename V2T<R>::T *__restrict__ pb_in,
                            const typename V2T<R>::T *__restrict__ ib_in, const R *__restrict__ ub_in,
@@ -153,54 +233,45 @@ __global__ void k_adj_step(const typename V2T<R>::T *__restrict__ phi, const typ
     const int64_t nb[6] = {site(wr(ix - 1, n), iy, iz, n), site(wr(ix + 1, n), iy, iz, n),
                            site(ix, wr(iy - 1, n), iz, n), site(ix, wr(iy + 1, n), iz, n),
                            site(ix, iy, wr(iz - 1, n), n), site(ix, iy, wr(iz + 1, n), n)};
-    // pibar_t = pibar+ + h phibar+ (adjoint of the drift), at the site and its neighbours
+    // itil = pibar+ + h phibar+ at the site and its neighbours
     auto it = [&](int64_t q) {
       const auto a = ib_in[q], b = pb_in[q];
-      return mk<R>(a.x + k.h * b.x, a.y + k.h * b.y);
+      return mk<R>(dcomb(a.x, b.x, k.h), dcomb(a.y, b.y, k.h));
     };
     const auto i0 = it(c);
-    R lr = 0, li = 0;
-    for (int q = 0; q < 6; ++q) {
+    const auto v0 = it(nb[0]);
+    R lr = v0.x - i0.x, li = v0.y - i0.y;
+    for (int q = 1; q < 6; ++q) {
       const auto v = it(nb[q]);
-      lr += v.x - i0.x;
-      li += v.y - i0.y;
+      lr = lr + (v.x - i0.x);
+      li = li + (v.y - i0.y);
     }
     const auto p0 = phi[c];
-    const R s = p0.x * p0.x + p0.y * p0.y, g0 = k.A * s + k.B;
-    const R pd = p0.x * i0.x + p0.y * i0.y;
-    const R jr = g0 * i0.x + 2 * k.A * p0.x * pd + k.D * i0.x;
-    const R ji = g0 * i0.y + 2 * k.A * p0.y * pd - k.D * i0.y;
     const auto pbv = pb_in[c];
-    pb_out[c] = mk<R>(pbv.x + k.f2 * lr + k.f3 * jr, pbv.y + k.f2 * li + k.f3 * ji);
-    ib_out[c] = mk<R>(k.f1 * i0.x, k.f1 * i0.y);
-    lam_part = (double)k.f3 * ((double)k.dA * (double)s + (double)k.dB) * (double)pd;
-    // u_ij: wbar_t = wbar+ + h ubar+
+    const AdjOut<R> o = adj_point<R>(i0.x, i0.y, lr, li, p0.x, p0.y, pbv.x, pbv.y, k);
+    pb_out[c] = o.pb;
+    ib_out[c] = o.ib;
+    const R s = p0.x * p0.x + p0.y * p0.y;
+    lam_part = (double)k.f3 * ((double)k.dA * (double)s + (double)k.dB) * ((double)p0.x * i0.x + (double)p0.y * i0.y);
     R Dr[3], Di[3];
     for (int q = 0; q < 3; ++q) {
       const auto a = phi[nb[2 * q + 1]], b = phi[nb[2 * q]];
-      Dr[q] = (a.x - b.x) * k.inv_d;
-      Di[q] = (a.y - b.y) * k.inv_d;
+      Dr[q] = cdiff(a.x, b.x, k.inv_d);
+      Di[q] = cdiff(a.y, b.y, k.inv_d);
     }
     R wt[6];
     for (int cc = 0; cc < 6; ++cc) {
       const R *wb = wb_in + cc * n3, *ub = ub_in + cc * n3;
-      const R w0 = wb[c] + k.h * ub[c];
+      const R w0 = dcomb(wb[c], ub[c], k.h);
       wt[cc] = w0;
-      R lu = 0;
-      for (int q = 0; q < 6; ++q) lu += (wb[nb[q]] + k.h * ub[nb[q]]) - w0;
-      ub_out[cc * n3 + c] = ub[c] + k.f2 * lu;
-      wb_out[cc * n3 + c] = k.f1 * w0;
+      R lu = dcomb(wb[nb[0]], ub[nb[0]], k.h) - w0;
+      for (int q = 1; q < 6; ++q) lu = lu + (dcomb(wb[nb[q]], ub[nb[q]], k.h) - w0);
+      ub_out[cc * n3 + c] = pfma(k.f2, lu, ub[c]);
+      wb_out[cc * n3 + c] = pmul(k.f1, w0);
     }
-    const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
-    for (int i = 0; i < 3; ++i) {
-      R qr = wt[idx[i][i]] * Dr[i], qi = wt[idx[i][i]] * Di[i];
-      for (int j = 0; j < 3; ++j) {
-        qr += wt[idx[i][j]] * Dr[j];
-        qi += wt[idx[i][j]] * Di[j];
-      }
-      Q[(2 * i) * n3 + c] = 2 * k.fs * qr;
-      Q[(2 * i + 1) * n3 + c] = 2 * k.fs * qi;
-    }
+    R q[6];
+    adj_q(wt, Dr, Di, k.fs, q);
+    for (int i = 0; i < 6; ++i) Q[i * n3 + c] = q[i];
   }
   lam_part = warp_sum(lam_part);
   if ((threadIdx.x & 31) == 0 && lam_part != 0.0) atomicAdd(dlam, lam_part);
@@ -234,10 +305,10 @@ __global__ void __launch_bounds__(TX *TY) k_adj_step_tiled(
       const int gx = wr(x0 + e % W - 1, n), gy = wr(y0 + e / W - 1, n);
       const int64_t g = (int64_t)z * n2 + (int64_t)gy * n + gx;
       const auto a = ib_in[g], b = pb_in[g];
-      t[e] = a.x + k.h * b.x;
-      t[PLANE + e] = a.y + k.h * b.y;
+      t[e] = dcomb(a.x, b.x, k.h);
+      t[PLANE + e] = dcomb(a.y, b.y, k.h);
 #pragma unroll
-      for (int c = 0; c < 6; ++c) t[(2 + c) * PLANE + e] = wb_in[c * n3 + g] + k.h * ub_in[c * n3 + g];
+      for (int c = 0; c < 6; ++c) t[(2 + c) * PLANE + e] = dcomb(wb_in[c * n3 + g], ub_in[c * n3 + g], k.h);
       const auto p = phi[g];
       t[8 * PLANE + e] = p.x;
       t[9 * PLANE + e] = p.y;
@@ -247,7 +318,6 @@ __global__ void __launch_bounds__(TX *TY) k_adj_step_tiled(
   load_plane(z0, 1);
   R lam = 0;
   const int ci = (ty + 1) * W + (tx + 1);
-  const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
   for (int kk = 0; kk < zc; ++kk) {
     const int z = z0 + kk;
     load_plane(z + 1, (kk + 2) % 3);
@@ -261,21 +331,18 @@ __global__ void __launch_bounds__(TX *TY) k_adj_step_tiled(
     const R li = (tc[PLANE + ci - 1] - i0i) + (tc[PLANE + ci + 1] - i0i) + (tc[PLANE + ci - W] - i0i) +
                  (tc[PLANE + ci + W] - i0i) + (tm[PLANE + ci] - i0i) + (tp[PLANE + ci] - i0i);
     const R p0r = tc[8 * PLANE + ci], p0i = tc[9 * PLANE + ci];
-    const R s = p0r * p0r + p0i * p0i, g0 = k.A * s + k.B;
-    const R pd = p0r * i0r + p0i * i0i;
-    const R jr = g0 * i0r + 2 * k.A * p0r * pd + k.D * i0r;
-    const R ji = g0 * i0i + 2 * k.A * p0i * pd - k.D * i0i;
     const auto pbv = pb_in[c];
-    pb_out[c] = mk<R>(pbv.x + k.f2 * lr + k.f3 * jr, pbv.y + k.f2 * li + k.f3 * ji);
-    ib_out[c] = mk<R>(k.f1 * i0r, k.f1 * i0i);
-    lam += k.f3 * (k.dA * s + k.dB) * pd;
+    const AdjOut<R> o = adj_point<R>(i0r, i0i, lr, li, p0r, p0i, pbv.x, pbv.y, k);
+    pb_out[c] = o.pb;
+    ib_out[c] = o.ib;
+    lam = padd(lam, o.lam);
     // central differences of phi
-    const R Dr[3] = {(tc[8 * PLANE + ci + 1] - tc[8 * PLANE + ci - 1]) * k.inv_d,
-                     (tc[8 * PLANE + ci + W] - tc[8 * PLANE + ci - W]) * k.inv_d,
-                     (tp[8 * PLANE + ci] - tm[8 * PLANE + ci]) * k.inv_d};
-    const R Di[3] = {(tc[9 * PLANE + ci + 1] - tc[9 * PLANE + ci - 1]) * k.inv_d,
-                     (tc[9 * PLANE + ci + W] - tc[9 * PLANE + ci - W]) * k.inv_d,
-                     (tp[9 * PLANE + ci] - tm[9 * PLANE + ci]) * k.inv_d};
+    const R Dr[3] = {cdiff(tc[8 * PLANE + ci + 1], tc[8 * PLANE + ci - 1], k.inv_d),
+                     cdiff(tc[8 * PLANE + ci + W], tc[8 * PLANE + ci - W], k.inv_d),
+                     cdiff(tp[8 * PLANE + ci], tm[8 * PLANE + ci], k.inv_d)};
+    const R Di[3] = {cdiff(tc[9 * PLANE + ci + 1], tc[9 * PLANE + ci - 1], k.inv_d),
+                     cdiff(tc[9 * PLANE + ci + W], tc[9 * PLANE + ci - W], k.inv_d),
+                     cdiff(tp[9 * PLANE + ci], tm[9 * PLANE + ci], k.inv_d)};
     R wt[6];
 #pragma unroll
     for (int cc = 0; cc < 6; ++cc) {
@@ -284,20 +351,13 @@ __global__ void __launch_bounds__(TX *TY) k_adj_step_tiled(
       wt[cc] = w0;
       const R lu = (w[ci - 1] - w0) + (w[ci + 1] - w0) + (w[ci - W] - w0) + (w[ci + W] - w0) +
                    (tm[(2 + cc) * PLANE + ci] - w0) + (tp[(2 + cc) * PLANE + ci] - w0);
-      ub_out[cc * n3 + c] = ub_in[cc * n3 + c] + k.f2 * lu;
-      wb_out[cc * n3 + c] = k.f1 * w0;
+      ub_out[cc * n3 + c] = pfma(k.f2, lu, ub_in[cc * n3 + c]);
+      wb_out[cc * n3 + c] = pmul(k.f1, w0);
     }
+    R q[6];
+    adj_q(wt, Dr, Di, k.fs, q);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      R qr = wt[idx[i][i]] * Dr[i], qi = wt[idx[i][i]] * Di[i];
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        qr += wt[idx[i][j]] * Dr[j];
-        qi += wt[idx[i][j]] * Di[j];
-      }
-      Q[(2 * i) * n3 + c] = 2 * k.fs * qr;
-      Q[(2 * i + 1) * n3 + c] = 2 * k.fs * qi;
-    }
+    for (int i = 0; i < 6; ++i) Q[i * n3 + c] = q[i];
     __syncthreads();  // the ring slot of plane z - 1 is refilled next
   }
 #pragma unroll
@@ -317,12 +377,20 @@ constexpr int adj_tiled_smem() {
 // two slots, so one barrier per plane suffices.  The raw fields of plane
 // z + 2 are loaded into registers before plane z is computed, so their
 // latency overlaps the arithmetic, and the raw centre values double as the
-// additive terms of the outputs (no second load).  The expressions and their
-// order are those of k_adj_step_tiled, so the outputs are bit-identical.
-template <typename R>
+// additive terms of the outputs (no second load).
+//
+// REV fuses the backward re-step of phi into the same pass: the kernel reads
+// the state after the step (phi+, its FP32 compensation, pi+), drifts phi
+// back at every stencil point, kicks pi back at the centre, and writes phi,
+// its compensation and pi to the other buffers; the adjoint step then uses
+// that phi.  Per site this saves the write and two re-reads of phi, and two
+// launches.  The point formulas are those of k_rev_drift, k_rev_kick and
+// k_adj_step, so every variant gives the same bits.
+template <typename R, bool REV>
 struct AdjRaw {
   typename V2T<R>::T ib, pb, ph;
   R wb[6], ub[6];
+  typename V2T<R>::T cph, pv;  // REV: compensation of phi+ (FP32) and pi+
 };
 
 template <typename R>
@@ -330,14 +398,25 @@ struct AdjCmb {
   R ir, ii, w[6], pr, pi;
 };
 
-template <typename R, int TX, int TY>
+// centre values a plane carries to its outputs
+template <typename R>
+struct AdjCentre {
+  R pb[2], ub[6];
+  R pv[2], c[2];  // REV: pi+ and the updated compensation of phi
+};
+
+template <typename R, int TX, int TY, bool REV>
 __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 2 : 1) k_adj_step_roll(
     const typename V2T<R>::T *__restrict__ phi, const typename V2T<R>::T *__restrict__ pb_in,
     const typename V2T<R>::T *__restrict__ ib_in, const R *__restrict__ ub_in, const R *__restrict__ wb_in,
     typename V2T<R>::T *__restrict__ pb_out, typename V2T<R>::T *__restrict__ ib_out, R *__restrict__ ub_out,
-    R *__restrict__ wb_out, R *__restrict__ Q, int n, int zc, Coef<R> k, double *__restrict__ dlam) {
+    R *__restrict__ wb_out, R *__restrict__ Q, int n, int zc, Coef<R> k, double *__restrict__ dlam,
+    const typename V2T<R>::T *__restrict__ cphi_in, const typename V2T<R>::T *__restrict__ pi_in,
+    typename V2T<R>::T *__restrict__ phi_out, typename V2T<R>::T *__restrict__ cphi_out,
+    typename V2T<R>::T *__restrict__ pi_out) {
   static_assert(TX == 32, "one warp per tile row");
   static_assert(2 * TY <= 32 && TY >= 3, "halo duties of warps 0-2");
+  constexpr bool F32 = sizeof(R) == 4;
   constexpr int W = TX + 2, H = TY + 2, PLANE = W * H, SLOT = 10 * PLANE;
   extern __shared__ unsigned char adj_smem[];
   R *sm = reinterpret_cast<R *>(adj_smem);
@@ -363,7 +442,7 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 2 : 1) k_adj_step_rol
     hsi = (r + 1) * W + (lo ? 0 : TX + 1);
   }
   const bool halo = hoff >= 0;
-  auto load = [&](int z, int64_t off, AdjRaw<R> &r) {
+  auto load = [&](int z, int64_t off, AdjRaw<R, REV> &r) {
     const int64_t g = (int64_t)wr(z, n) * n2 + off;
     r.ib = ib_in[g];
     r.pb = pb_in[g];
@@ -373,16 +452,43 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 2 : 1) k_adj_step_rol
       r.wb[c] = wb_in[c * n3 + g];
       r.ub[c] = ub_in[c * n3 + g];
     }
+    if constexpr (REV) {
+      if constexpr (F32) r.cph = cphi_in[g];
+      r.pv = pi_in[g];
+    }
   };
-  auto combine = [&](const AdjRaw<R> &r) {
+  // combined values of a point; REV drifts phi back first (cnew receives the
+  // updated compensation)
+  auto combine = [&](const AdjRaw<R, REV> &r, R *cnew) {
     AdjCmb<R> m;
-    m.ir = r.ib.x + k.h * r.pb.x;
-    m.ii = r.ib.y + k.h * r.pb.y;
+    m.ir = dcomb(r.ib.x, r.pb.x, k.h);
+    m.ii = dcomb(r.ib.y, r.pb.y, k.h);
 #pragma unroll
-    for (int c = 0; c < 6; ++c) m.w[c] = r.wb[c] + k.h * r.ub[c];
+    for (int c = 0; c < 6; ++c) m.w[c] = dcomb(r.wb[c], r.ub[c], k.h);
     m.pr = r.ph.x;
     m.pi = r.ph.y;
+    if constexpr (REV) {
+      R cx = 0, cy = 0;
+      if constexpr (F32) {
+        cx = r.cph.x;
+        cy = r.cph.y;
+      }
+      rev_drift1(m.pr, cx, k.h, r.pv.x);
+      rev_drift1(m.pi, cy, k.h, r.pv.y);
+      cnew[0] = cx;
+      cnew[1] = cy;
+    }
     return m;
+  };
+  auto centre = [&](const AdjRaw<R, REV> &r, AdjCentre<R> &o) {
+    o.pb[0] = r.pb.x;
+    o.pb[1] = r.pb.y;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) o.ub[c] = r.ub[c];
+    if constexpr (REV) {
+      o.pv[0] = r.pv.x;
+      o.pv[1] = r.pv.y;
+    }
   };
   auto store = [&](R *slot, int si, const AdjCmb<R> &m) {
     slot[si] = m.ir;
@@ -393,82 +499,75 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 2 : 1) k_adj_step_rol
     slot[9 * PLANE + si] = m.pi;
   };
   const int ci = (ty + 1) * W + (tx + 1);
-  AdjRaw<R> rn, rh;
+  AdjRaw<R, REV> rn, rh;
+  R cdummy[2];
+  AdjCentre<R> oc, on;
   load(z0 - 1, own, rn);
-  AdjCmb<R> prev = combine(rn);
+  AdjCmb<R> prev = combine(rn, cdummy);
   load(z0, own, rn);
-  AdjCmb<R> cur = combine(rn);
-  R pbc[2] = {rn.pb.x, rn.pb.y}, ubc[6];  // raw centre values of plane z
-#pragma unroll
-  for (int c = 0; c < 6; ++c) ubc[c] = rn.ub[c];
+  AdjCmb<R> cur = combine(rn, oc.c);
+  centre(rn, oc);
   store(sm, ci, cur);
   if (halo) {
     load(z0, hoff, rh);
-    store(sm, hsi, combine(rh));
+    store(sm, hsi, combine(rh, cdummy));
   }
   load(z0 + 1, own, rn);
   if (halo && zc > 1) load(z0 + 1, hoff, rh);
   R lam = 0;
-  const int idx[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
   for (int kk = 0; kk < zc; ++kk) {
     const int z = z0 + kk;
     __syncthreads();  // plane z is complete in slot kk & 1; the other slot is free
-    const AdjCmb<R> next = combine(rn);
-    R pbn[2] = {rn.pb.x, rn.pb.y}, ubn[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) ubn[c] = rn.ub[c];
+    const AdjCmb<R> next = combine(rn, on.c);
+    centre(rn, on);
     if (kk + 1 < zc) {
       R *tn = sm + ((kk + 1) & 1) * SLOT;
       store(tn, ci, next);
-      if (halo) store(tn, hsi, combine(rh));
+      if (halo) store(tn, hsi, combine(rh, cdummy));
       load(z + 2, own, rn);  // prefetch: `next` of plane z + 1
       if (halo && kk + 2 < zc) load(z + 2, hoff, rh);
     }
     const R *tc = sm + (kk & 1) * SLOT;
     const int64_t c = (int64_t)z * n2 + own;
+    const R p0r = cur.pr, p0i = cur.pi;
+    if constexpr (REV) {
+      const R lpr = (tc[8 * PLANE + ci - 1] - p0r) + (tc[8 * PLANE + ci + 1] - p0r) + (tc[8 * PLANE + ci - W] - p0r) +
+                    (tc[8 * PLANE + ci + W] - p0r) + (prev.pr - p0r) + (next.pr - p0r);
+      const R lpi = (tc[9 * PLANE + ci - 1] - p0i) + (tc[9 * PLANE + ci + 1] - p0i) + (tc[9 * PLANE + ci - W] - p0i) +
+                    (tc[9 * PLANE + ci + W] - p0i) + (prev.pi - p0i) + (next.pi - p0i);
+      pi_out[c] = rev_kick1<R>(mk<R>(oc.pv[0], oc.pv[1]), lpr, lpi, p0r, p0i, k);
+      phi_out[c] = mk<R>(p0r, p0i);
+      if constexpr (F32) cphi_out[c] = mk<R>(oc.c[0], oc.c[1]);
+    }
     const R i0r = cur.ir, i0i = cur.ii;
     const R lr = (tc[ci - 1] - i0r) + (tc[ci + 1] - i0r) + (tc[ci - W] - i0r) + (tc[ci + W] - i0r) +
                  (prev.ir - i0r) + (next.ir - i0r);
     const R li = (tc[PLANE + ci - 1] - i0i) + (tc[PLANE + ci + 1] - i0i) + (tc[PLANE + ci - W] - i0i) +
                  (tc[PLANE + ci + W] - i0i) + (prev.ii - i0i) + (next.ii - i0i);
-    const R p0r = cur.pr, p0i = cur.pi;
-    const R s = p0r * p0r + p0i * p0i, g0 = k.A * s + k.B;
-    const R pd = p0r * i0r + p0i * i0i;
-    const R jr = g0 * i0r + 2 * k.A * p0r * pd + k.D * i0r;
-    const R ji = g0 * i0i + 2 * k.A * p0i * pd - k.D * i0i;
-    pb_out[c] = mk<R>(pbc[0] + k.f2 * lr + k.f3 * jr, pbc[1] + k.f2 * li + k.f3 * ji);
-    ib_out[c] = mk<R>(k.f1 * i0r, k.f1 * i0i);
-    lam += k.f3 * (k.dA * s + k.dB) * pd;
-    const R Dr[3] = {(tc[8 * PLANE + ci + 1] - tc[8 * PLANE + ci - 1]) * k.inv_d,
-                     (tc[8 * PLANE + ci + W] - tc[8 * PLANE + ci - W]) * k.inv_d, (next.pr - prev.pr) * k.inv_d};
-    const R Di[3] = {(tc[9 * PLANE + ci + 1] - tc[9 * PLANE + ci - 1]) * k.inv_d,
-                     (tc[9 * PLANE + ci + W] - tc[9 * PLANE + ci - W]) * k.inv_d, (next.pi - prev.pi) * k.inv_d};
+    const AdjOut<R> o = adj_point<R>(i0r, i0i, lr, li, p0r, p0i, oc.pb[0], oc.pb[1], k);
+    pb_out[c] = o.pb;
+    ib_out[c] = o.ib;
+    lam = padd(lam, o.lam);
+    const R Dr[3] = {cdiff(tc[8 * PLANE + ci + 1], tc[8 * PLANE + ci - 1], k.inv_d),
+                     cdiff(tc[8 * PLANE + ci + W], tc[8 * PLANE + ci - W], k.inv_d), cdiff(next.pr, prev.pr, k.inv_d)};
+    const R Di[3] = {cdiff(tc[9 * PLANE + ci + 1], tc[9 * PLANE + ci - 1], k.inv_d),
+                     cdiff(tc[9 * PLANE + ci + W], tc[9 * PLANE + ci - W], k.inv_d), cdiff(next.pi, prev.pi, k.inv_d)};
 #pragma unroll
     for (int cc = 0; cc < 6; ++cc) {
       const R *w = tc + (2 + cc) * PLANE;
       const R w0 = cur.w[cc];
       const R lu = (w[ci - 1] - w0) + (w[ci + 1] - w0) + (w[ci - W] - w0) + (w[ci + W] - w0) + (prev.w[cc] - w0) +
                    (next.w[cc] - w0);
-      ub_out[cc * n3 + c] = ubc[cc] + k.f2 * lu;
-      wb_out[cc * n3 + c] = k.f1 * w0;
+      ub_out[cc * n3 + c] = pfma(k.f2, lu, oc.ub[cc]);
+      wb_out[cc * n3 + c] = pmul(k.f1, w0);
     }
+    R q[6];
+    adj_q(cur.w, Dr, Di, k.fs, q);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      R qr = cur.w[idx[i][i]] * Dr[i], qi = cur.w[idx[i][i]] * Di[i];
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        qr += cur.w[idx[i][j]] * Dr[j];
-        qi += cur.w[idx[i][j]] * Di[j];
-      }
-      Q[(2 * i) * n3 + c] = 2 * k.fs * qr;
-      Q[(2 * i + 1) * n3 + c] = 2 * k.fs * qi;
-    }
+    for (int i = 0; i < 6; ++i) Q[i * n3 + c] = q[i];
     prev = cur;
     cur = next;
-    pbc[0] = pbn[0];
-    pbc[1] = pbn[1];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) ubc[q] = ubn[q];
+    oc = on;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) lam += __shfl_down_sync(0xffffffffu, lam, o);
@@ -663,7 +762,7 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
   const size_t adj_b = (size_t)n3 * (2 * sizeof(V) + 12 * sizeof(R));  // one adjoint state
   const size_t ck_b = (size_t)n3 * sizeof(V) * (F32 ? 3 : 2);           // phi (+ its compensation), phi'
   const int64_t nck = nsteps / stride + 1;
-  char *ck = nullptr, *adj = nullptr;
+  char *ck = nullptr, *adj = nullptr, *spare = nullptr;
   R *Q = nullptr;
   double *fbuf = nullptr;
   int rc = AXG_OK;
@@ -684,6 +783,7 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
     axg_free(ctx, (void **)&adj);
     axg_free(ctx, (void **)&Q);
     axg_free(ctx, (void **)&fbuf);
+    axg_free(ctx, (void **)&spare);
     ctx->flags_valid = false;
   });
   do {
@@ -711,13 +811,14 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
       cudaMemcpyAsync(dst + fb, pi, fb, cudaMemcpyDeviceToDevice, ctx->stream);
       if (F32) cudaMemcpyAsync(dst + 2 * fb, cphi, fb, cudaMemcpyDeviceToDevice, ctx->stream);
     };
-    auto load = [&](int64_t k) {
+    auto load_to = [&](int64_t k, V *dphi, V *dpi, V *dcphi) {
       const char *src = ck + ck_b * k;
       const size_t fb = (size_t)n3 * sizeof(V);
-      cudaMemcpyAsync(cur_phi(), src, fb, cudaMemcpyDeviceToDevice, ctx->stream);
-      cudaMemcpyAsync(pi, src + fb, fb, cudaMemcpyDeviceToDevice, ctx->stream);
-      if (F32) cudaMemcpyAsync(cphi, src + 2 * fb, fb, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(dphi, src, fb, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(dpi, src + fb, fb, cudaMemcpyDeviceToDevice, ctx->stream);
+      if (F32) cudaMemcpyAsync(dcphi, src + 2 * fb, fb, cudaMemcpyDeviceToDevice, ctx->stream);
     };
+    auto load = [&](int64_t k) { load_to(k, cur_phi(), pi, cphi); };
     // ---------------- forward with checkpoints ----------------
     cudaEventRecord(e0, ctx->stream);
     double t = t1;
@@ -783,18 +884,35 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
       if (!attr) {
         AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_adj_step_tiled<R, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                tsmem));
-        AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_adj_step_roll<R, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               rsmem));
+        AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_adj_step_roll<R, 32, 8, false>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, rsmem));
+        AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_adj_step_roll<R, 32, 8, true>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, rsmem));
         attr = true;
       }
     }
+    // The roll kernel steps phi back inside the adjoint step and so cannot
+    // work in place: phi, its compensation and pi ping-pong between the
+    // context's buffers (slot 0) and spares.
+    V *rphi[2] = {cur_phi(), nullptr}, *rcphi[2] = {cphi, nullptr}, *rpi[2] = {pi, nullptr};
+    int rs = 0;
+    if (kind == AdjKernel::roll) {
+      if ((rc = axg_alloc(ctx, (void **)&spare, (size_t)n3 * sizeof(V) * 3, "adjoint re-step buffers"))) break;
+      rphi[1] = (V *)spare;
+      rpi[1] = rphi[1] + n3;
+      rcphi[1] = F32 ? rpi[1] + n3 : nullptr;
+    }
     bool a_is_in = true;
-    V *phi = cur_phi();  // the reverse steps phi in place in the final buffer
+    V *phi = cur_phi();  // the plain and ring paths step phi back in place in the final buffer
     for (int64_t it = nsteps; it >= 1 && rc == AXG_OK; --it) {
       const StepCoef kc = coef_at(ctx->p, kt[it], dt, kh[it]);
       const Coef<R> kr = kc.template as<R>();
-      // state after step it -> state before step it (pre-kick)
-      if ((it - 1) % stride == 0) {
+      // state after step it -> state before step it (pre-kick); the
+      // checkpoints re-anchor it every `stride` steps
+      const bool anchor = (it - 1) % stride == 0;
+      if (kind == AdjKernel::roll) {
+        if (anchor) load_to((it - 1) / stride, rphi[rs], rpi[rs], rcphi[rs]);
+      } else if (anchor) {
         load((it - 1) / stride);
       } else {
         AXG_LAUNCH(ctx, "adj_rev_drift", k_rev_drift<R>, grid_for(n3), 256, 0, phi, cphi, pi, n3, (R)kh[it]);
@@ -805,8 +923,16 @@ int adjoint_run(axg_ctx *ctx, double t1, double dt, int64_t nsteps, int first_ha
       R *ubi = a_is_in ? ub_a : ub_b, *wbi = a_is_in ? wb_a : wb_b, *ubo = a_is_in ? ub_b : ub_a,
         *wbo = a_is_in ? wb_b : wb_a;
       if (kind == AdjKernel::roll) {
-        AXG_LAUNCH(ctx, "adj_step", (k_adj_step_roll<R, 32, 8>), tgrid, dim3(32, 8), rsmem, phi, pbi, ibi, ubi, wbi,
-                   pbo_, ibo, ubo, wbo, Q, n, tzc, kr, dlam);
+        if (anchor) {
+          AXG_LAUNCH(ctx, "adj_step", (k_adj_step_roll<R, 32, 8, false>), tgrid, dim3(32, 8), rsmem, rphi[rs], pbi,
+                     ibi, ubi, wbi, pbo_, ibo, ubo, wbo, Q, n, tzc, kr, dlam, nullptr, nullptr, nullptr, nullptr,
+                     nullptr);
+        } else {
+          AXG_LAUNCH(ctx, "adj_step_rev", (k_adj_step_roll<R, 32, 8, true>), tgrid, dim3(32, 8), rsmem, rphi[rs], pbi,
+                     ibi, ubi, wbi, pbo_, ibo, ubo, wbo, Q, n, tzc, kr, dlam, rcphi[rs], rpi[rs], rphi[1 - rs],
+                     rcphi[1 - rs], rpi[1 - rs]);
+          rs = 1 - rs;
+        }
       } else if (kind == AdjKernel::ring) {
         AXG_LAUNCH(ctx, "adj_step", (k_adj_step_tiled<R, 32, 8>), tgrid, dim3(32, 8), tsmem, phi, pbi, ibi, ubi, wbi,
                    pbo_, ibo, ubo, wbo, Q, n, tzc, kr, dlam);

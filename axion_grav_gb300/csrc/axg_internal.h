@@ -25,8 +25,9 @@ struct axg_tile_cfg {
 };
 
 // Device-side descriptor of one ensemble member (tensor maps of both
-// ping-pong buffers plus the field pointers); 64-byte aligned for TMA.
-struct alignas(64) axg_ens_member_dev {
+// ping-pong buffers plus the field pointers); it takes the alignment of its
+// tensor maps, as TMA requires.
+struct axg_ens_member_dev {
   CUtensorMap tm[2][6];  // [buffer][phi_row, phi_body, phi_halo, u_row, u_body, u_halo]
   CUtensorMap pw[4];     // pointwise planes: phid, cphi, ud, cu
   void *phi[2], *phid, *cphi, *u[2], *ud, *cu;
@@ -34,6 +35,7 @@ struct alignas(64) axg_ens_member_dev {
   int32_t n, ncols;
   long long item_begin;  // first work item (column x z-chunk) of this member
 };
+static_assert(alignof(axg_ens_member_dev) >= 64, "tensor maps in device memory need 64-byte alignment");
 
 // Per-step coefficients of the batched kick + drift (read by the kernel
 // from device memory so a captured step graph can be replayed).

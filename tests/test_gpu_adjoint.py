@@ -156,16 +156,22 @@ def test_fp32_adjoint_lambda_against_finite_differences():
 @pytest.mark.parametrize("n", [32, 64])
 def test_adjoint_step_kernels_agree(monkeypatch, precision, n):
     """The plain global stencil, the 3-plane shared-memory ring and the
-    register-rolling z-march give bit-identical gradients.  dJ/dlambda is
-    summed per site in FP64 by the plain kernel, per warp in the arithmetic
-    type by the tiled ones, and J and dJ/dlambda go through FP64 atomics."""
+    register-rolling z-march (which also fuses the backward re-step of phi)
+    give bit-identical gradients.  dJ/dlambda is summed per site in FP64 by
+    the plain kernel, per warp in the arithmetic type by the tiled ones, and
+    J and dJ/dlambda go through FP64 atomics."""
     st = state(n, 10)
     p = _with_precision(params(n), precision)
-    out = {}
+    out, fin = {}, {}
     for kind in ("plain", "ring", "roll"):
         monkeypatch.setenv("AXG_ADJOINT_STEP_KERNEL", kind)
-        out[kind] = gpu_adjoint(p, st, nsteps=9, stride=4)[0]
+        out[kind], fin[kind] = gpu_adjoint(p, st, nsteps=9, stride=4)
     monkeypatch.delenv("AXG_ADJOINT_STEP_KERNEL")
+    # the roll path ping-pongs phi through spare buffers: the context is left
+    # at the end of the forward run all the same
+    for kind in ("ring", "roll"):
+        for a, b in zip(fin[kind][0] + fin[kind][1], fin["plain"][0] + fin["plain"][1]):
+            assert np.array_equal(a, b), kind
     ref = out["plain"]
     assert np.isfinite(ref[0]) and np.all(np.isfinite(ref[2]))
     for kind in ("ring", "roll"):
