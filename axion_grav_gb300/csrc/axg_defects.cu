@@ -24,8 +24,9 @@
 //                  corner difference within the margin of +-pi is redone in
 //                  FP64)
 //   4. compaction: string and wall cells listed in cell order
-//   5. fits      : one thread per listed cell -- position_string (1001 random
-//                  starts + Nelder-Mead, defects_3d.f90:435-603), string_length
+//   5. fits      : string cells lane-scheduled from a counter -- the search
+//                  of position_string (1001 random starts, screened in FP32,
+//                  + Nelder-Mead, defects_3d.f90:435-603), string_length
 //                  (1027-1056), velocity_string (605-692), position_wall
 //                  (1058-1233)
 //   6. sums      : add_string_length / add_wall_area without grouping
@@ -453,99 +454,293 @@ __device__ __forceinline__ bool out_of_box(const double t[4]) {
   return false;
 }
 
-// defects_3d.f90:435-603
-__device__ void position_string(const double ph[8], uint64_t seed, uint64_t cell, double pos[3],
-                                double dir[3], double *gof, double *sl) {
-  const double chi2max = 8 * kRefPi * kRefPi, tol = 0.05;
+// Start point i of the random search (defects_3d.f90:463-470): four
+// uniforms from two Philox draws, mapped onto the parameter box.
+__device__ __forceinline__ void string_start(uint64_t seed, uint64_t cell, int i, double t[4]) {
   const double max_s[4] = {1.0, kRefPi, sqrt(3.0) / 2, kRefPi};
   const double min_s[4] = {-1.0, -kRefPi, 0.0, -kRefPi};
-  double p_s[5][4], chi2_s[5], c_s[4], t_s[4], s_s[4], chi2, chi2s;
-  for (int a = 0; a < 5; ++a) {
-    chi2_s[a] = 0.0;
-    for (int k = 0; k < 4; ++k) p_s[a][k] = 0.0;
+  double x[4];
+  for (int k = 0; k < 4; k += 2) {
+    const int j = i * 4 + k;
+    const axd_u32x4 r = axd_draw(seed, 3u, (uint32_t)(j >> 1), cell);
+    x[k] = axd_u01(r.v[0], r.v[1]);
+    x[k + 1] = axd_u01(r.v[2], r.v[3]);
   }
-  int n0 = -1;
-  for (int i = 0; i <= kMaxIter; ++i) {
-    double x[4];
-    for (int k = 0; k < 4; k += 2) {
-      const int j = i * 4 + k;
-      const axd_u32x4 r = axd_draw(seed, 3u, (uint32_t)(j >> 1), cell);
-      x[k] = axd_u01(r.v[0], r.v[1]);
-      x[k + 1] = axd_u01(r.v[2], r.v[3]);
+  for (int k = 0; k < 4; ++k) t[k] = max_s[k] * x[k] + min_s[k] * (1 - x[k]);
+}
+
+// A lower bound of calc_chi2_string(ph, t) from an FP32 evaluation, or -inf
+// where the FP32 value cannot be bounded (a corner too close to the string
+// axis for its angle to be resolved, or a phase difference within the error
+// of the +-pi wrap).  Error budget, all generous:
+//   du, dv: angles and radius rounded to FP32, sqrt(1 - mu^2) from an FP64
+//           product, CUDA sincosf (2 ulp), products and sums of terms below
+//           2.4 in magnitude: |error| <= kDuv = 4e-6;
+//   angle : atan2f (3 ulp of pi) plus the rotation of (du, dv) by an error
+//           of kDuv at radius r: e = kAng + 2 kDuv / (r - 2 kDuv);
+//   phase : FP32 rounding of ph, of the difference and of the wrap
+//           constants, within kPh = 2e-6;
+//   chi2  : a = <d^2> moves by at most (2 pi + E) E, b^2 = <d>^2 by at most
+//           (2 pi + E + 2e-6)(E + 2e-6), FP32 summation by below 2e-5;
+// and the total is doubled, plus 1e-4.
+__device__ float chi2_string_lower(const float phf[8], const double t[4]) {
+  constexpr float kDuv = 4e-6f, kAng = 2e-6f, kPh = 2e-6f;
+  constexpr float kPiF = (float)kRefPi, kTwoPiF = (float)kRefTwoPi;
+  const float mu = (float)t[0], ph = (float)t[1], rad = (float)t[2], ang = (float)t[3];
+  float s4, c4, sp, cp;
+  sincosf(ang, &s4, &c4);
+  sincosf(ph, &sp, &cp);
+  // 1 - mu^2 is formed in FP64: for |mu| near 1 the FP32 rounding of mu
+  // alone would move sqrt(1 - mu^2) by up to 5e-4
+  const float u0 = rad * c4, v0 = rad * s4, sm = sqrtf((float)((1.0 - t[0]) * (1.0 + t[0])));
+  float a = 0.0f, b = 0.0f, E = 0.0f;
+  for (int iz = 0; iz <= 1; ++iz) {
+    const float z = iz - 0.5f;
+    for (int iy = 0; iy <= 1; ++iy) {
+      const float y = iy - 0.5f;
+      for (int ix = 0; ix <= 1; ++ix) {
+        const float x = ix - 0.5f;
+        const int i = (iz * 2 + iy) * 2 + ix;
+        const float du = -u0 + mu * (x * cp + y * sp) - z * sm;
+        const float dv = -v0 - x * sp + y * cp;
+        const float r = sqrtf(du * du + dv * dv);
+        if (!(r > 8 * kDuv)) return -INFINITY;
+        const float e = kAng + kPh + 2 * kDuv / (r - 2 * kDuv);
+        float d = phf[i] - atan2f(dv, du);
+        if (!(fabsf(fabsf(d) - kPiF) > e + kPh)) return -INFINITY;
+        if (d >= kPiF)
+          d = d - kTwoPiF;
+        else if (d < -kPiF)
+          d = d + kTwoPiF;
+        a = a + d * d;
+        b = b + d;
+        E = fmaxf(E, e);
+      }
     }
-    for (int k = 0; k < 4; ++k) t_s[k] = max_s[k] * x[k] + min_s[k] * (1 - x[k]);
-    chi2 = calc_chi2_string(ph, t_s);
-    if (n0 <= 0) {
-      n0 = n0 + 1;
-      chi2_s[n0] = chi2;
-      for (int k = 0; k < 4; ++k) p_s[n0][k] = t_s[k];
+  }
+  a = a / 8;
+  b = b / 8;
+  const float tp = (float)kRefTwoPi;
+  const float bound = 2 * ((tp + E) * E + (tp + E + 2e-6f) * (E + 2e-6f) + 2e-5f) + 1e-4f;
+  return (a - b * b) - bound;
+}
+
+// defects_3d.f90:435-603, as a per-lane state machine.
+//
+// The fit of one string cell is a random search over 1001 starts followed by
+// a Nelder-Mead simplex of up to 1000 iterations (tol 0.05 on chi2).  In
+// evolved fields about two thirds of the string cells never reach the
+// tolerance and run all 1000 iterations.  Written as one loop per thread,
+// a warp ran its slowest cell's iteration count, and the expansion,
+// contraction and shrink branches one after another.  Here each lane holds
+// the search state of one cell and advances it to its next chi2
+// evaluation; every pass of the scheduling loop makes at most one chi2
+// evaluation per lane, at a lane-specific point, so the 8 atan2 of the
+// evaluations run on all active lanes together.  A lane whose cell is done
+// writes the cell's results and takes the next cell from a global counter.
+//
+// The random search keeps kNumSimp + 1 of the starts, in the order drawn.
+// Once that set is full, a start changes it only if its chi2 is at most the
+// value in the last slot.  That value can rise (the first two starts are
+// kept unsorted, defects_3d.f90:471-476, and a larger early value moves up
+// the list), but never above the largest value kept at any earlier time.
+// The starts are therefore screened with FP32 lower bounds
+// (chi2_string_lower) against the largest kept value; only the starts that
+// pass are evaluated exactly, in draw order.  A screened-out start has an
+// exact chi2 above any threshold the sequential search could have compared
+// it with.  Every chi2 that enters a decision or the kept state is the FP64
+// value, so the fit is bit-identical to the sequential search.
+struct StringSearch {
+  double p_s[5][4], chi2_s[5], c_s[4], t_s[4], s_s[4], chi2;
+  int n0, i, it, stage;
+  bool expand;
+};
+
+enum : int {
+  kSearch = 0,
+  kNmStart,
+  kNmReflect,
+  kNmSecondPrep,
+  kNmSecond,
+  kShrink1,  // kShrink1 .. kShrink1 + kNumSimp - 1: shrink vertices 1..kNumSimp
+  kNmSort = kShrink1 + kNumSimp,
+  kFinished
+};
+
+__device__ __forceinline__ void search_init(StringSearch &S) {
+  for (int a = 0; a < 5; ++a) {
+    S.chi2_s[a] = 0.0;
+    for (int k = 0; k < 4; ++k) S.p_s[a][k] = 0.0;
+  }
+  S.n0 = -1;
+  S.i = 0;
+  S.it = 0;
+  S.stage = kSearch;
+  S.expand = false;
+  S.chi2 = 0.0;
+}
+
+// the random-search bookkeeping of one exactly evaluated start (t_s, chi2)
+__device__ __forceinline__ void search_insert(StringSearch &S, double chi2) {
+  if (S.n0 <= 0) {
+    S.n0 = S.n0 + 1;
+    S.chi2_s[S.n0] = chi2;
+    for (int k = 0; k < 4; ++k) S.p_s[S.n0][k] = S.t_s[k];
+    return;
+  }
+  if (S.n0 < kNumSimp || chi2 <= S.chi2_s[S.n0]) {
+    S.n0 = S.n0 + 1 < kNumSimp ? S.n0 + 1 : kNumSimp;
+    int i0 = S.n0;
+    while (chi2 <= S.chi2_s[i0 - 1]) {
+      if (i0 <= kNumSimp) {
+        S.chi2_s[i0] = S.chi2_s[i0 - 1];
+        for (int k = 0; k < 4; ++k) S.p_s[i0][k] = S.p_s[i0 - 1][k];
+      }
+      i0 = i0 - 1;
+      if (i0 == 0) break;
+    }
+    S.chi2_s[i0] = chi2;
+    for (int k = 0; k < 4; ++k) S.p_s[i0][k] = S.t_s[k];
+  }
+}
+
+// the expansion / contraction decision with the second point's chi2
+__device__ __forceinline__ void search_second(StringSearch &S, double chi2s) {
+  if (S.expand) {
+    if (S.chi2 <= chi2s) {
+      S.chi2_s[kNumSimp] = S.chi2;
+      for (int k = 0; k < 4; ++k) S.p_s[kNumSimp][k] = S.t_s[k];
+    } else {
+      S.chi2_s[kNumSimp] = chi2s;
+      for (int k = 0; k < 4; ++k) S.p_s[kNumSimp][k] = S.s_s[k];
+    }
+    S.stage = kNmSort;
+  } else if (chi2s <= S.chi2_s[kNumSimp]) {
+    S.chi2_s[kNumSimp] = chi2s;
+    for (int k = 0; k < 4; ++k) S.p_s[kNumSimp][k] = S.s_s[k];
+    S.stage = kNmSort;
+  } else {
+    S.stage = kShrink1;
+  }
+}
+
+// Advance S to its next chi2 evaluation; true with the point in P, false
+// when the lane has none this pass (screening budget spent, or finished).
+__device__ bool search_prepare(StringSearch &S, const float phf[8], uint64_t seed, uint64_t cell, double P[4]) {
+  const double chi2max = 8 * kRefPi * kRefPi, tol = 0.05;
+  for (;;) {
+    if (S.stage == kSearch) {
+      if (S.i > kMaxIter) {
+        S.stage = kNmStart;
+        continue;
+      }
+      if (S.n0 < kNumSimp) {  // filling the kept set: no screen
+        string_start(seed, cell, S.i, S.t_s);
+        for (int k = 0; k < 4; ++k) P[k] = S.t_s[k];
+        return true;
+      }
+      double thr = S.chi2_s[0];
+      for (int k = 1; k <= kNumSimp; ++k) thr = S.chi2_s[k] > thr ? S.chi2_s[k] : thr;
+      for (int k = 0; k <= kNumSimp; ++k)
+        if (S.chi2_s[k] != S.chi2_s[k]) thr = INFINITY;
+      for (int cnt = 0; cnt < 32 && S.i <= kMaxIter; ++cnt) {
+        string_start(seed, cell, S.i, S.t_s);
+        if (!((double)chi2_string_lower(phf, S.t_s) > thr)) {
+          for (int k = 0; k < 4; ++k) P[k] = S.t_s[k];
+          return true;
+        }
+        S.i = S.i + 1;
+      }
+      if (S.i > kMaxIter) {
+        S.stage = kNmStart;
+        continue;
+      }
+      return false;
+    }
+    if (S.stage == kNmStart) {
+      if (!(S.chi2_s[0] > tol && S.it < kMaxIter)) {
+        S.stage = kFinished;
+        return false;
+      }
+      S.it = S.it + 1;
+      for (int k = 0; k < 4; ++k) S.c_s[k] = 0.0;
+      for (int i0 = 0; i0 < kNumSimp; ++i0)
+        for (int k = 0; k < 4; ++k) S.c_s[k] = S.c_s[k] + S.p_s[i0][k];
+      for (int k = 0; k < 4; ++k) S.c_s[k] = S.c_s[k] / kNumSimp;
+      for (int k = 0; k < 4; ++k) S.t_s[k] = 2 * S.c_s[k] - S.p_s[kNumSimp][k];
+      if (out_of_box(S.t_s)) {
+        S.chi2 = chi2max;
+        S.stage = kNmSecondPrep;
+        continue;
+      }
+      for (int k = 0; k < 4; ++k) P[k] = S.t_s[k];
+      S.stage = kNmReflect;
+      return true;
+    }
+    if (S.stage == kNmSecondPrep) {
+      S.expand = S.chi2 < S.chi2_s[kNumSimp];
+      if (S.expand)
+        for (int k = 0; k < 4; ++k) S.s_s[k] = 3 * S.c_s[k] - 4 * S.p_s[kNumSimp][k];
+      else
+        for (int k = 0; k < 4; ++k) S.s_s[k] = 1.5 * S.c_s[k] - 0.5 * S.p_s[kNumSimp][k];
+      if (out_of_box(S.s_s)) {
+        search_second(S, chi2max);
+        continue;
+      }
+      for (int k = 0; k < 4; ++k) P[k] = S.s_s[k];
+      S.stage = kNmSecond;
+      return true;
+    }
+    if (S.stage == kNmSort) {
+      for (int i0 = kNumSimp - 1; i0 >= 0; --i0)
+        for (int m = 0; m <= i0; ++m)
+          if (S.chi2_s[m] > S.chi2_s[m + 1]) {
+            for (int k = 0; k < 4; ++k) {
+              const double tt = S.p_s[m][k];
+              S.p_s[m][k] = S.p_s[m + 1][k];
+              S.p_s[m + 1][k] = tt;
+            }
+            const double c = S.chi2_s[m];
+            S.chi2_s[m] = S.chi2_s[m + 1];
+            S.chi2_s[m + 1] = c;
+          }
+      S.stage = kNmStart;
       continue;
     }
-    if (n0 < kNumSimp || chi2 <= chi2_s[n0]) {
-      n0 = n0 + 1 < kNumSimp ? n0 + 1 : kNumSimp;
-      int i0 = n0;
-      while (chi2 <= chi2_s[i0 - 1]) {
-        if (i0 <= kNumSimp) {
-          chi2_s[i0] = chi2_s[i0 - 1];
-          for (int k = 0; k < 4; ++k) p_s[i0][k] = p_s[i0 - 1][k];
-        }
-        i0 = i0 - 1;
-        if (i0 == 0) break;
-      }
-      chi2_s[i0] = chi2;
-      for (int k = 0; k < 4; ++k) p_s[i0][k] = t_s[k];
+    if (S.stage >= kShrink1 && S.stage < kNmSort) {  // shrink towards the best vertex
+      const int j = S.stage - kShrink1 + 1;
+      for (int k = 0; k < 4; ++k) S.p_s[j][k] = 0.5 * (S.p_s[j][k] + S.p_s[0][k]);
+      for (int k = 0; k < 4; ++k) P[k] = S.p_s[j][k];
+      return true;
     }
+    return false;  // kFinished
   }
-  int it = 0;
-  while (chi2_s[0] > tol && it < kMaxIter) {
-    it = it + 1;
-    for (int k = 0; k < 4; ++k) c_s[k] = 0.0;
-    for (int i0 = 0; i0 < kNumSimp; ++i0)
-      for (int k = 0; k < 4; ++k) c_s[k] = c_s[k] + p_s[i0][k];
-    for (int k = 0; k < 4; ++k) c_s[k] = c_s[k] / kNumSimp;
-    for (int k = 0; k < 4; ++k) t_s[k] = 2 * c_s[k] - p_s[kNumSimp][k];
-    chi2 = out_of_box(t_s) ? chi2max : calc_chi2_string(ph, t_s);
-    if (chi2 < chi2_s[kNumSimp]) {
-      for (int k = 0; k < 4; ++k) s_s[k] = 3 * c_s[k] - 4 * p_s[kNumSimp][k];
-      chi2s = out_of_box(s_s) ? chi2max : calc_chi2_string(ph, s_s);
-      if (chi2 <= chi2s) {
-        chi2_s[kNumSimp] = chi2;
-        for (int k = 0; k < 4; ++k) p_s[kNumSimp][k] = t_s[k];
-      } else {
-        chi2_s[kNumSimp] = chi2s;
-        for (int k = 0; k < 4; ++k) p_s[kNumSimp][k] = s_s[k];
-      }
-    } else {
-      for (int k = 0; k < 4; ++k) s_s[k] = 1.5 * c_s[k] - 0.5 * p_s[kNumSimp][k];
-      chi2s = out_of_box(s_s) ? chi2max : calc_chi2_string(ph, s_s);
-      if (chi2s <= chi2_s[kNumSimp]) {
-        chi2_s[kNumSimp] = chi2s;
-        for (int k = 0; k < 4; ++k) p_s[kNumSimp][k] = s_s[k];
-      } else {
-        for (int i0 = 1; i0 <= kNumSimp; ++i0) {
-          for (int k = 0; k < 4; ++k) p_s[i0][k] = 0.5 * (p_s[i0][k] + p_s[0][k]);
-          chi2_s[i0] = calc_chi2_string(ph, p_s[i0]);
-        }
-      }
-    }
-    for (int i0 = kNumSimp - 1; i0 >= 0; --i0)
-      for (int m = 0; m <= i0; ++m)
-        if (chi2_s[m] > chi2_s[m + 1]) {
-          for (int k = 0; k < 4; ++k) {
-            const double tt = p_s[m][k];
-            p_s[m][k] = p_s[m + 1][k];
-            p_s[m + 1][k] = tt;
-          }
-          const double c = chi2_s[m];
-          chi2_s[m] = chi2_s[m + 1];
-          chi2_s[m + 1] = c;
-        }
+}
+
+// S takes the chi2 of the point search_prepare returned
+__device__ void search_consume(StringSearch &S, double v) {
+  if (S.stage == kSearch) {
+    search_insert(S, v);
+    S.i = S.i + 1;
+  } else if (S.stage == kNmReflect) {
+    S.chi2 = v;
+    S.stage = kNmSecondPrep;
+  } else if (S.stage == kNmSecond) {
+    search_second(S, v);
+  } else {
+    const int j = S.stage - kShrink1 + 1;
+    S.chi2_s[j] = v;
+    S.stage = j < kNumSimp ? S.stage + 1 : kNmSort;
   }
-  const double mu = p_s[0][0], phi = p_s[0][1];
+}
+
+// position, direction, goodness of fit and length from the best vertex
+__device__ void string_result(const StringSearch &S, double pos[3], double dir[3], double *gof, double *sl) {
+  const double mu = S.p_s[0][0], phi = S.p_s[0][1];
   double s4, c4, sp, cp;
-  axd_sincos(p_s[0][3], &s4, &c4);
-  const double u0 = p_s[0][2] * c4, v0 = p_s[0][2] * s4;
-  chi2 = chi2_s[0];
+  axd_sincos(S.p_s[0][3], &s4, &c4);
+  const double u0 = S.p_s[0][2] * c4, v0 = S.p_s[0][2] * s4;
+  const double chi2 = S.chi2_s[0];
   axd_sincos(phi, &sp, &cp);
   const double sq = sqrt(1.0 - mu * mu);
   dir[0] = sq * cp;
@@ -834,33 +1029,61 @@ __device__ void position_wall(const double ph[8], double pos[3], double dir[3], 
   *wa = area;
 }
 
+// String fits, lane-scheduled: each lane takes cells from *next (zero at
+// launch) and advances its search one chi2 evaluation per pass (see
+// search_prepare); the grid is sized to the resident CTAs.
 template <typename V>
 __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, const V *__restrict__ phid, int n,
                                                     double dspa, uint64_t seed, const int64_t *__restrict__ cells,
-                                                    int64_t ncell, double *__restrict__ out) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= ncell) return;
-  const int64_t s = cells[k];
-  const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
+                                                    int64_t ncell, double *__restrict__ out,
+                                                    unsigned long long *__restrict__ next) {
+  StringSearch S;
   double pc[8];
-  for (int c = 0; c < 8; ++c) pc[c] = phase64(phi, corner(n, ix, iy, iz, c));
-  double pos[3], dir[3], vel[3], gof, l;
-  position_string(pc, seed, (uint64_t)s, pos, dir, &gof, &l);
-  velocity_string(phi, phid, n, dspa, ix, iy, iz, pos, vel);
-  double *r = out + 13 * k;
-  r[0] = pos[0] + ix + 0.5;
-  r[1] = pos[1] + iy + 0.5;
-  r[2] = pos[2] + iz + 0.5;
-  r[3] = dir[0];
-  r[4] = dir[1];
-  r[5] = dir[2];
-  r[6] = vel[0];
-  r[7] = vel[1];
-  r[8] = vel[2];
-  r[9] = gof;
-  r[10] = l;
-  r[11] = (double)s;
-  r[12] = -1.0;
+  float phf[8];
+  int64_t k = -1, s = 0;
+  auto fetch = [&]() {
+    k = (int64_t)atomicAdd(next, 1ull);
+    if (k >= ncell) {
+      k = -1;
+      return;
+    }
+    s = cells[k];
+    const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
+    for (int c = 0; c < 8; ++c) {
+      pc[c] = phase64(phi, corner(n, ix, iy, iz, c));
+      phf[c] = (float)pc[c];
+    }
+    search_init(S);
+  };
+  fetch();
+  for (;;) {
+    if (k >= 0 && S.stage == kFinished) {
+      const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
+      double pos[3], dir[3], vel[3], gof, l;
+      string_result(S, pos, dir, &gof, &l);
+      velocity_string(phi, phid, n, dspa, ix, iy, iz, pos, vel);
+      double *r = out + 13 * k;
+      r[0] = pos[0] + ix + 0.5;
+      r[1] = pos[1] + iy + 0.5;
+      r[2] = pos[2] + iz + 0.5;
+      r[3] = dir[0];
+      r[4] = dir[1];
+      r[5] = dir[2];
+      r[6] = vel[0];
+      r[7] = vel[1];
+      r[8] = vel[2];
+      r[9] = gof;
+      r[10] = l;
+      r[11] = (double)s;
+      r[12] = -1.0;
+      fetch();
+    }
+    if (__all_sync(0xffffffffu, k < 0)) break;
+    double P[4];
+    const bool need = k >= 0 && search_prepare(S, phf, seed, (uint64_t)s, P);
+    __syncwarp();
+    if (need) search_consume(S, calc_chi2_string(pc, P));
+  }
 }
 
 template <typename V>
@@ -1209,14 +1432,24 @@ int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], dou
                cells, cells + ns);
     const int n = (int)ctx->n;
     if (ns > 0) {
-      if (ctx->p.precision == AXG_PREC_FP32_MIXED)
-        AXG_LAUNCH(ctx, "string_fit_fp32", k_string_fit<float2>, (unsigned)((ns + 127) / 128), 128, 0,
+      // resident CTAs only: lanes take cells from a counter (d_cnt[8])
+      const bool f32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
+      int per_sm = 0, sms = 0;
+      AXG_CUDA_TRY(ctx, f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_string_fit<float2>, 128, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_string_fit<double2>, 128, 0));
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+      int64_t grid = (int64_t)std::max(per_sm, 1) * std::max(sms, 1);
+      grid = std::min<int64_t>(grid, (ns + 127) / 128);
+      unsigned long long *next = ctx->d_cnt + 8;
+      AXG_CUDA_TRY(ctx, cudaMemsetAsync(next, 0, sizeof(unsigned long long), ctx->stream));
+      if (f32)
+        AXG_LAUNCH(ctx, "string_fit_fp32", k_string_fit<float2>, (unsigned)grid, 128, 0,
                    (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->phid, n, ctx->p.dspa,
-                   (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings);
+                   (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
       else
-        AXG_LAUNCH(ctx, "string_fit_fp64", k_string_fit<double2>, (unsigned)((ns + 127) / 128), 128, 0,
+        AXG_LAUNCH(ctx, "string_fit_fp64", k_string_fit<double2>, (unsigned)grid, 128, 0,
                    (const double2 *)ctx->phi[ctx->cur], (const double2 *)ctx->phid, n, ctx->p.dspa,
-                   (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings);
+                   (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
     }
     if (nw > 0) {
       if (ctx->p.precision == AXG_PREC_FP32_MIXED)
