@@ -391,8 +391,85 @@ __global__ void k_compact(const int8_t *__restrict__ flags, int64_t n3, const in
 }
 
 // ---------------- per-cell fits ----------------
-// defects_3d.f90:385-433
-__device__ double calc_chi2_string(const double ph[8], const double pr[4]) {
+// atan(k/8) as hi + lo (axd_atan_tab_hi / axd_atan_tab_lo), k = 0..8, in
+// shared memory: the string-fit kernel indexes it per lane
+struct AtanTab {
+  double hi[9], lo[9], c[9];  // c[k] = k / 8
+};
+
+__device__ __forceinline__ void atan_tab_fill(AtanTab &t) {
+  for (int k = threadIdx.x; k < 9; k += blockDim.x) {
+    t.hi[k] = axd_atan_tab_hi(k);
+    t.lo[k] = axd_atan_tab_lo(k);
+    t.c[k] = (double)k * 0.125;
+  }
+}
+
+// FP64 comparisons issue on the FP64 pipe, at 1/64 of the FP32 rate on
+// GB300; these give the same answers from the bit patterns on the integer
+// pipe.  dkey orders non-NaN doubles as signed integers (-0 below +0, which
+// no comparison below can meet: it compares with nonzero constants or
+// between magnitudes).
+__device__ __forceinline__ long long dkey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool is_nan_bits(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool is_zero_bits(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) == 0;
+}
+
+// axd_atan2 with the branches turned into selects: the same IEEE operations
+// on the same operands, so the same bits, but no control flow, which lets
+// the compiler overlap the eight corner evaluations of a chi2 (their
+// divisions and polynomial chains are independent).
+__device__ __forceinline__ double atan2_sel(double y, double x, const AtanTab &tab) {
+  const double ax = axd_fabs(x), ay = axd_fabs(y);
+  // magnitudes: their bit patterns order as integers (a NaN case is replaced
+  // by the last select)
+  const bool swap = __double_as_longlong(ay) > __double_as_longlong(ax);
+  const double num = swap ? ax : ay, den = swap ? ay : ax;
+  const double t = AXD_DIV(num, den);
+  int k = (int)AXD_ADD(AXD_MUL(t, 8.0), 0.5);
+  k = k < 0 ? 0 : (k > 8 ? 8 : k);  // only NaN t (both zero or both infinite) can leave 0..8
+  const double c = tab.c[k];
+  const double r = AXD_DIV(AXD_SUB(t, c), AXD_FMA(t, c, 1.0));
+  const double r2 = AXD_MUL(r, r);
+  double p = -0.06666666666666667;
+  p = AXD_FMA(p, r2, 0.07692307692307693);
+  p = AXD_FMA(p, r2, -0.09090909090909091);
+  p = AXD_FMA(p, r2, 0.1111111111111111);
+  p = AXD_FMA(p, r2, -0.14285714285714285);
+  p = AXD_FMA(p, r2, 0.2);
+  p = AXD_FMA(p, r2, -0.3333333333333333);
+  const double atr = AXD_FMA(AXD_MUL(r, r2), p, r);
+  const double hi = tab.hi[k], lo = AXD_ADD(tab.lo[k], atr);
+  const bool sgnx = axd_signbit(x);
+  // swap: pi/2 - (hi + lo), and pi minus that for x < 0; no swap and x < 0:
+  // pi - (hi + lo); otherwise hi + lo
+  const double A = AXD_ADD(AXD_SUB(swap ? AXD_PIO2_HI : AXD_PI_HI, hi), AXD_SUB(swap ? AXD_PIO2_LO : AXD_PI_LO, lo));
+  const double B = AXD_ADD(hi, lo);
+  const double C = AXD_ADD(AXD_SUB(AXD_PI_HI, A), AXD_PI_LO);
+  double a = swap ? (sgnx ? C : A) : (sgnx ? A : B);
+  a = axd_copysign(a, y);
+  const double on_x = sgnx ? axd_copysign(AXD_ADD(AXD_PI_HI, AXD_PI_LO), y) : y;  // ay == 0
+  const double on_y = axd_copysign(AXD_ADD(AXD_PIO2_HI, AXD_PIO2_LO), y);         // ax == 0
+  a = is_zero_bits(ax) ? on_y : a;
+  a = is_zero_bits(ay) ? on_x : a;
+  return (is_nan_bits(x) || is_nan_bits(y)) ? AXD_ADD(x, y) : a;
+}
+
+// defects_3d.f90:385-433.  The corner offsets are +-1/2, so x cos(phi) and
+// the like are exact halvings of one product; they are formed once, and the
+// sums that do not depend on every corner coordinate are shared.  Every
+// value, and the order of every rounding, is that of the plain
+// per-corner loop
+//   du = -u0 + cm (x cp + y sp) - z sm,  dv = -v0 - x sp + y cp,
+//   d = ph - atan2(dv, du) wrapped into [-pi, pi),
+// so the result is bit-identical to it.
+__device__ double calc_chi2_string(const double ph[8], const double pr[4], const AtanTab &tab) {
   const double mu = pr[0], phi = pr[1];
   double s4, c4, sp, cp;
   axd_sincos(pr[3], &s4, &c4);
@@ -401,28 +478,39 @@ __device__ double calc_chi2_string(const double ph[8], const double pr[4]) {
   const double cm = mu;
   const double sm = sqrt(1.0 - mu * mu);
   axd_sincos(phi, &sp, &cp);
-  double a = 0.0, b = 0.0;
-  for (int iz = 0; iz <= 1; ++iz) {
-    const double z = iz - 0.5;
-    for (int iy = 0; iy <= 1; ++iy) {
-      const double y = iy - 0.5;
-      for (int ix = 0; ix <= 1; ++ix) {
-        const double x = ix - 0.5;
-        const int i = (iz * 2 + iy) * 2 + ix;
-        const double du = -u0 + cm * (x * cp + y * sp) - z * sm;
-        const double dv = -v0 - x * sp + y * cp;
-        double d = ph[i] - axd_atan2(dv, du);
-        if (d >= kRefPi)
-          d = d - kRefTwoPi;
-        else if (d < -kRefPi)
-          d = d + kRefTwoPi;
-        a = a + d * d;
-        b = b + d;
-      }
+  const double hcp = 0.5 * cp, hsp = 0.5 * sp, hsm = 0.5 * sm;  // x cp etc. for x = +1/2
+  double T[4], Wv[2];
+  for (int iy = 0; iy <= 1; ++iy)
+    for (int ix = 0; ix <= 1; ++ix) {
+      const double xcp = ix ? hcp : -hcp, ysp = iy ? hsp : -hsp;
+      T[iy * 2 + ix] = -u0 + cm * (xcp + ysp);
     }
+  for (int ix = 0; ix <= 1; ++ix) Wv[ix] = -v0 - (ix ? hsp : -hsp);
+  double d[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int ix = i & 1, iy = (i >> 1) & 1, iz = i >> 2;
+    const double du = T[iy * 2 + ix] - (iz ? hsm : -hsm);
+    const double dv = Wv[ix] + (iy ? hcp : -hcp);
+    d[i] = ph[i] - atan2_sel(dv, du, tab);
   }
-  a = a / 8;
-  b = b / 8;
+  // d >= pi and d < -pi from the integer keys; a NaN d takes one of the
+  // branches and stays the same NaN, as in the FP64 comparisons
+  const long long kp = dkey(kRefPi), km = dkey(-kRefPi);
+  double a = 0.0, b = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    double e = d[i];
+    const long long ke = dkey(e);
+    if (ke >= kp)
+      e = e - kRefTwoPi;
+    else if (ke < km)
+      e = e + kRefTwoPi;
+    a = a + e * e;
+    b = b + e;
+  }
+  a = a * 0.125;  // exact: the same value as a / 8
+  b = b * 0.125;
   return a - b * b;
 }
 
@@ -666,7 +754,8 @@ __device__ bool search_prepare(StringSearch &S, const float phf[8], uint64_t see
       for (int k = 0; k < 4; ++k) S.c_s[k] = 0.0;
       for (int i0 = 0; i0 < kNumSimp; ++i0)
         for (int k = 0; k < 4; ++k) S.c_s[k] = S.c_s[k] + S.p_s[i0][k];
-      for (int k = 0; k < 4; ++k) S.c_s[k] = S.c_s[k] / kNumSimp;
+      static_assert(kNumSimp == 4, "the centroid scaling below is 1 / kNumSimp");
+      for (int k = 0; k < 4; ++k) S.c_s[k] = S.c_s[k] * 0.25;  // exact: the same value as / kNumSimp
       for (int k = 0; k < 4; ++k) S.t_s[k] = 2 * S.c_s[k] - S.p_s[kNumSimp][k];
       if (out_of_box(S.t_s)) {
         S.chi2 = chi2max;
@@ -1037,6 +1126,9 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
                                                     double dspa, uint64_t seed, const int64_t *__restrict__ cells,
                                                     int64_t ncell, double *__restrict__ out,
                                                     unsigned long long *__restrict__ next) {
+  __shared__ AtanTab tab;
+  atan_tab_fill(tab);
+  __syncthreads();
   StringSearch S;
   double pc[8];
   float phf[8];
@@ -1082,7 +1174,7 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
     double P[4];
     const bool need = k >= 0 && search_prepare(S, phf, seed, (uint64_t)s, P);
     __syncwarp();
-    if (need) search_consume(S, calc_chi2_string(pc, P));
+    if (need) search_consume(S, calc_chi2_string(pc, P, tab));
   }
 }
 
