@@ -25,6 +25,7 @@
 // 1/2 sum_ij (|W'_TT|^2 + k^2 |W_TT|^2), the continuum-equivalent of the
 // Green's-function numerator.
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "axg_binning.h"
@@ -211,8 +212,36 @@ __device__ __forceinline__ void gw_update(double2 *__restrict__ acc, int64_t n3,
   acc[3 * n3 + s] = a22;
 }
 
-__global__ void k_gw_accumulate(const double2 *__restrict__ srcF, int n, double dwav, double tau, double dw,
-                                int ref_compat, double2 *__restrict__ acc) {
+// The polarisation tensor and phase rate |k| dwav of every half-spectrum k,
+// [13][nhalf]: e+ real parts, e+ imaginary parts, rate.  They depend on k
+// only; GB300 issues FP64 at 1/64 of the FP32 rate, and forming them takes
+// about half of the per-k FP64 work of a Green step, so the FP64 path reads
+// them (104 B per half-spectrum k) instead.  For -k the polarisation vector
+// is the conjugate (q and its azimuth change sign), so e+(-k) = conj e+(k)
+// (exactly: the negations are exact and the products keep their operands).
+__global__ void k_gw_pol_table(int n, double dwav, double *__restrict__ tab) {
+  const int nh = n / 2 + 1;
+  const int64_t nhalf = (int64_t)n * n * nh;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
+    const int ix = (int)(h % nh), iy = (int)((h / nh) % n), iz = (int)(h / ((int64_t)nh * n));
+    const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
+    const double qq = sqrt(kx * kx + ky * ky + kz * kz);
+    double pr[6], pi[6];
+    if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi))
+      for (int c = 0; c < 6; ++c) pr[c] = pi[c] = 0.0;
+    for (int c = 0; c < 6; ++c) {
+      tab[c * nhalf + h] = pr[c];
+      tab[(6 + c) * nhalf + h] = pi[c];
+    }
+    tab[12 * nhalf + h] = qq * dwav;
+  }
+}
+
+// TABLE: polarisation and rate from k_gw_pol_table; otherwise formed here
+template <bool TABLE>
+__global__ void k_gw_accumulate(const double2 *__restrict__ srcF, const double *__restrict__ tab, int n, double dwav,
+                                double tau, double dw, int ref_compat, double2 *__restrict__ acc) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -220,16 +249,33 @@ __global__ void k_gw_accumulate(const double2 *__restrict__ srcF, int n, double 
     const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
     bool conj_back;
     const int64_t hidx = gw_half_index(ix, iy, iz, n, conj_back);
-    const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
-    const double qq = sqrt(kx * kx + ky * ky + kz * kz);
-    double pr[6], pi[6];
-    if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi)) {
-      // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
-      if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
-      continue;
+    double pr[6], pi[6], rate;
+    // The stored entry is k's (conj_back) or -k's.  A Nyquist y or z index
+    // maps to itself, so there the entry is not -k's: form those directly.
+    if (TABLE && (conj_back || (iy != n / 2 && iz != n / 2))) {
+      rate = tab[12 * nhalf + hidx];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        pr[c] = tab[c * nhalf + hidx];
+        const double v = tab[(6 + c) * nhalf + hidx];
+        pi[c] = conj_back ? v : -v;
+      }
+      if (!(rate > 0)) {
+        // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
+        if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+        continue;
+      }
+    } else {
+      const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
+      const double qq = sqrt(kx * kx + ky * ky + kz * kz);
+      if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi)) {
+        if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+        continue;
+      }
+      rate = qq * dwav;
     }
     double sq, cq;
-    sincos(qq * dwav * tau, &sq, &cq);
+    sincos(rate * tau, &sq, &cq);
     double xp[2], xm[2], lm[2];
     gw_contract<double, double2>(srcF, nhalf, hidx, conj_back, pr, pi, xp, xm, lm);
     gw_update(acc, n3, s, dw * cq, dw * sq, xp, xm, lm, ref_compat);
@@ -509,6 +555,21 @@ int axg_gw_init(axg_ctx *ctx) {
     AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_omega, (size_t)ctx->n3 * 8, "GW phase rates"));
     AXG_LAUNCH(ctx, "gw_omega", k_gw_omega, grid_for(ctx->n3), 256, 0, n, kRefTwoPi / ctx->p.dspa / n,
                ctx->gw_omega);
+  } else {
+    // The FP64 polarisation table (13 doubles per half-spectrum k) when it
+    // takes at most an eighth of the device memory (512^3: 7 GB); otherwise
+    // the accumulation forms the polarisation per step.
+    // AXG_GW_POL_TABLE=0 forces the per-step form (tests compare the two).
+    size_t freeb = 0, total = 0;
+    cudaMemGetInfo(&freeb, &total);
+    const size_t tb = (size_t)nhalf * 13 * 8;
+    const char *env = std::getenv("AXG_GW_POL_TABLE");
+    const bool want = !(env && env[0] == '0');
+    if (want && tb <= total / 8) {
+      AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_pol, tb, "GW polarisation table"));
+      AXG_LAUNCH(ctx, "gw_pol_table", k_gw_pol_table, grid_for(nhalf), 256, 0, n, kRefTwoPi / ctx->p.dspa / n,
+                 ctx->gw_pol);
+    }
   }
   int dims[3] = {n, n, n};
   AXG_CUFFT_TRY(ctx, cufftPlanMany(&ctx->plan_gsrc, 3, dims, nullptr, 1, (int)ctx->n3, nullptr, 1,
@@ -542,8 +603,12 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source, grid_for(ctx->n3), 256, 0, (const double2 *)ctx->phi[ctx->cur], n,
              d, 1.0 / d, pow2, ctx->gsrc);
   AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
-  AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate, grid_for(ctx->n3), 256, 0, ctx->gsrcF, n, dwav, tau, dw, ref,
-             ctx->acc);
+  if (ctx->gw_pol)
+    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate<true>, grid_for(ctx->n3), 256, 0, ctx->gsrcF, ctx->gw_pol, n,
+               dwav, tau, dw, ref, ctx->acc);
+  else
+    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate<false>, grid_for(ctx->n3), 256, 0, ctx->gsrcF, nullptr, n,
+               dwav, tau, dw, ref, ctx->acc);
   return AXG_OK;
 }
 

@@ -92,6 +92,7 @@ struct axg_ctx {
   double *gsrc = nullptr;  // [6][n3] real sources S_ij (float for FP32-mixed)
   double2 *gsrcF = nullptr;  // [6][n*n*(n/2+1)] (float2 for FP32-mixed)
   float2 *gw_omega = nullptr;  // [n3] |k| dwav per k-site as float hi + lo (FP32-mixed Green mode)
+  double *gw_pol = nullptr;    // [13][n*n*(n/2+1)] e+ real, e+ imag, |k| dwav (FP64 Green mode), or null
   cufftHandle plan_gsrc = 0;
   bool plan_gsrc_ok = false;
 

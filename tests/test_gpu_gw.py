@@ -52,6 +52,26 @@ def test_green_accumulators_and_spectrum(compat, precision):
 
 
 @pytest.mark.parametrize("compat", [ag.COMPAT_REF, ag.COMPAT_INTENDED])
+@pytest.mark.parametrize("n", [16, 18])
+def test_green_polarisation_table_matches_per_step_form(monkeypatch, compat, n):
+    """FP64 Green accumulation with the precomputed polarisation table
+    (conjugated for the k outside the stored half spectrum) equals the
+    per-step form bit for bit."""
+    phi, phid = init_state(n)
+    p = params(n, ag.PREC_FP64_PLAIN, ag.GW_GREEN, compat=compat)
+    out = {}
+    for table in ("1", "0"):
+        monkeypatch.setenv("AXG_GW_POL_TABLE", table)
+        with ag.Lattice(p) as lat:
+            lat.upload(phi, phid)
+            lat.symplectic_integration(2.0, 2.4, 0.4)
+            out[table] = lat.download_gw_green()
+    monkeypatch.delenv("AXG_GW_POL_TABLE")
+    assert np.any(out["1"] != 0)
+    assert np.array_equal(out["1"], out["0"])
+
+
+@pytest.mark.parametrize("compat", [ag.COMPAT_REF, ag.COMPAT_INTENDED])
 def test_green_fp32_mixed_against_fp64_oracle(compat):
     """FP32 sources, R2C transforms and contractions with FP64 accumulators:
     accumulators and the per-bin GW numerator against the FP64 oracle."""
