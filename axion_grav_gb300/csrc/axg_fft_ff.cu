@@ -1,0 +1,338 @@
+// axg_fft_ff.cu -- 3-D real-to-complex FFTs at FP64 accuracy in float-float
+// arithmetic.
+//
+// GB300 issues FP64 at 1/64 of its FP32 rate, and an FP64 FFT is bound by
+// it: cuFFT's 512^3 D2Z takes about 15.5 ms, while moving its bytes takes
+// about 1 ms.  Here every value is a float-float pair (hi + lo, about 48
+// significant bits) and the butterflies run on the FP32 pipes:
+//   ff add : Dekker's two-sum of the high parts, low parts added, one
+//            renormalisation (error below 2^-47 (|a| + |b|));
+//   ff mul : complex products as two-term dot products: the exact high
+//            products through FMAs, their two-sum, the cross terms of the
+//            low parts, left unnormalised for the add that follows;
+// all through the round-once intrinsics (__fadd_rn, __fmul_rn, __fmaf_rn),
+// which the compiler never contracts.  The input doubles are split into
+// float-float on load and the output is hi + lo in double, so the transform
+// agrees with an FP64 FFT to about 1e-13 of the spectrum's largest value.
+//
+// Layout and convention are cuFFT's: batched D2Z, in [batch][n][n][n] reals,
+// out [batch][n][n][n/2+1] complex, forward (exp(-2 pi i k x / n)),
+// unnormalised; and in-place Z2Z of one [n][n][n] volume in either
+// direction (the complex row pass replaces the real one).  Three passes,
+// each one read and one write of the spectrum (the output buffer holds the
+// float-float intermediate):
+//   rows    : per x-row, the n reals as n/2 complex points z[m] = x[2m] +
+//             i x[2m+1], an n/2-point FFT, and the split of Z into the n/2+1
+//             outputs X[k] = E[k] + W_n^k O[k];
+//   y, z    : n-point FFTs along y and along z, 8 adjacent kx columns per
+//             CTA so every row of the tile is one 128-byte segment.
+// Each FFT is radix-2 decimation in time in shared memory (bit-reversed
+// load, natural-order result), twiddles W_n^k from a float-float table made
+// on the host in FP64.  Powers of two from 16 to 1024.
+#include <cmath>
+#include <cstdlib>
+#include <vector>
+
+#include "axg_internal.h"
+
+namespace {
+
+struct F2 {
+  float h, l;
+};
+
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float v = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ F2 f2_neg(F2 a) { return {-a.h, -a.l}; }
+
+__device__ __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_add(a, f2_neg(b)); }
+
+__device__ __forceinline__ F2 f2_half(F2 a) { return {__fmul_rn(a.h, 0.5f), __fmul_rn(a.l, 0.5f)}; }  // exact
+
+// complex float-float in a float4: (re.h, re.l, im.h, im.l)
+__device__ __forceinline__ F2 re(float4 v) { return {v.x, v.y}; }
+__device__ __forceinline__ F2 im(float4 v) { return {v.z, v.w}; }
+__device__ __forceinline__ float4 cx(F2 r, F2 i) { return make_float4(r.h, r.l, i.h, i.l); }
+__device__ __forceinline__ float4 c_add(float4 a, float4 b) { return cx(f2_add(re(a), re(b)), f2_add(im(a), im(b))); }
+__device__ __forceinline__ float4 c_sub(float4 a, float4 b) { return cx(f2_sub(re(a), re(b)), f2_sub(im(a), im(b))); }
+// a.b + s c.d as an unnormalised float-float (s = +-1): the exact high
+// products through FMAs, their two-sum, and the cross terms of the low
+// parts; the add that consumes it renormalises.
+__device__ __forceinline__ F2 f2_dot2(F2 a, F2 b, F2 c, F2 d, float sg) {
+  const float p1 = __fmul_rn(a.h, b.h), p2 = __fmul_rn(sg * c.h, d.h);
+  const float s = __fadd_rn(p1, p2), v = __fsub_rn(s, p1);
+  const float e0 = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v));
+  const float e1 = __fmaf_rn(a.h, b.h, -p1), e2 = __fmaf_rn(sg * c.h, d.h, -p2);
+  float t = __fmul_rn(sg * c.l, d.h);
+  t = __fmaf_rn(sg * c.h, d.l, t);
+  t = __fmaf_rn(a.l, b.h, t);
+  t = __fmaf_rn(a.h, b.l, t);
+  return {s, __fadd_rn(__fadd_rn(e0, __fadd_rn(e1, e2)), t)};
+}
+
+__device__ __forceinline__ float4 c_mul(float4 a, float4 b) {
+  return cx(f2_dot2(re(a), re(b), im(a), im(b), -1.f), f2_dot2(re(a), im(b), im(a), re(b), 1.f));
+}
+__device__ __forceinline__ float4 c_conj(float4 a) { return make_float4(a.x, a.y, -a.z, -a.w); }
+
+__device__ __forceinline__ F2 f2_from(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+
+__device__ __forceinline__ double f2_to(F2 a) { return (double)a.h + (double)a.l; }
+
+__device__ __forceinline__ int brev(int j, int bits) { return (int)(__brev((unsigned)j) >> (32 - bits)); }
+
+constexpr int kLines = 8;   // lines per CTA
+constexpr int kThreads = 256;
+
+template <int L>
+__host__ __device__ constexpr int log2c() {
+  return L <= 1 ? 0 : 1 + log2c<L / 2>();
+}
+
+// In-place L-point forward FFTs of kLines interleaved lines in shared memory
+// (element i of line b at s[i * kLines + b]), input bit-reversed.  The
+// twiddle of stage h for butterfly m is W_L^(m L / 2h) = tw[m (L / 2h) ts],
+// tw being the W_(L ts)^k table.
+template <int L, bool INV = false>
+__device__ __forceinline__ void fft_lines(float4 *s, const float4 *tw, int ts) {
+  for (int h = 1; h < L; h <<= 1) {
+    const int step = (L / (2 * h)) * ts;
+    for (int idx = threadIdx.x; idx < kLines * (L / 2); idx += kThreads) {
+      const int b = idx % kLines, q = idx / kLines;
+      const int m = q & (h - 1), i0 = ((q - m) << 1) + m, i1 = i0 + h;
+      const float4 x0 = s[i0 * kLines + b], x1 = s[i1 * kLines + b];
+      const float4 w = INV ? c_conj(tw[m * step]) : tw[m * step];  // inverse: exp(+2 pi i k / L)
+      const float4 t = h == 1 ? x1 : c_mul(w, x1);
+      s[i0 * kLines + b] = c_add(x0, t);
+      s[i1 * kLines + b] = c_sub(x0, t);
+    }
+    __syncthreads();
+  }
+}
+
+// Row pass: kLines rows of N = 2M reals -> M + 1 complex each (float-float).
+template <int M>
+__global__ void __launch_bounds__(kThreads) k_ff_rows(const double *__restrict__ in, float4 *__restrict__ out,
+                                                      int64_t rows, const float4 *__restrict__ tw) {
+  constexpr int N = 2 * M, NH = M + 1, LB = log2c<M>();
+  extern __shared__ float4 ff_sm[];
+  float4 *s = ff_sm, *tws = ff_sm + M * kLines;
+  for (int k = threadIdx.x; k < M; k += kThreads) tws[k] = tw[k];  // W_N^k, k < N / 2
+  const int64_t r0 = (int64_t)blockIdx.x * kLines;
+  for (int idx = threadIdx.x; idx < kLines * M; idx += kThreads) {
+    const int r = idx / M, m = idx % M;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (r0 + r < rows) {
+      const double2 x = reinterpret_cast<const double2 *>(in + (r0 + r) * N)[m];
+      v = cx(f2_from(x.x), f2_from(x.y));
+    }
+    s[brev(m, LB) * kLines + r] = v;
+  }
+  __syncthreads();
+  fft_lines<M>(s, tws, 2);  // W_M^j = W_N^(2j)
+  // X[k] = E[k] + W_N^k O[k], E = (Z[k] + conj Z[M-k]) / 2, O = (Z[k] - conj Z[M-k]) / 2i
+  for (int idx = threadIdx.x; idx < kLines * NH; idx += kThreads) {
+    const int r = idx / NH, k = idx % NH;
+    if (r0 + r >= rows) continue;
+    const float4 zk = s[(k % M) * kLines + r], zm = c_conj(s[((M - k) % M) * kLines + r]);
+    const float4 e = c_add(zk, zm), d = c_sub(zk, zm);
+    const float4 E = cx(f2_half(re(e)), f2_half(im(e)));
+    const float4 O = cx(f2_half(im(d)), f2_neg(f2_half(re(d))));
+    const float4 X = k == M ? c_sub(E, O) : c_add(E, k == 0 ? O : c_mul(tws[k], O));
+    out[(r0 + r) * NH + k] = X;
+  }
+}
+
+// Complex row pass: kLines contiguous rows of L complex doubles -> L
+// float-float points each, transformed in place of the input.
+template <int L, bool INV>
+__global__ void __launch_bounds__(kThreads) k_ff_rows_c2c(double2 *__restrict__ data, int64_t rows,
+                                                          const float4 *__restrict__ tw) {
+  constexpr int LB = log2c<L>();
+  extern __shared__ float4 ff_sm[];
+  float4 *s = ff_sm, *tws = ff_sm + L * kLines;
+  for (int k = threadIdx.x; k < L / 2; k += kThreads) tws[k] = tw[k];
+  const int64_t r0 = (int64_t)blockIdx.x * kLines;
+  for (int idx = threadIdx.x; idx < kLines * L; idx += kThreads) {
+    const int r = idx / L, j = idx % L;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (r0 + r < rows) {
+      const double2 x = data[(r0 + r) * L + j];
+      v = cx(f2_from(x.x), f2_from(x.y));
+    }
+    s[brev(j, LB) * kLines + r] = v;
+  }
+  __syncthreads();
+  fft_lines<L, INV>(s, tws, 1);
+  float4 *out = reinterpret_cast<float4 *>(data);
+  for (int idx = threadIdx.x; idx < kLines * L; idx += kThreads) {
+    const int r = idx / L, j = idx % L;
+    if (r0 + r < rows) out[(r0 + r) * L + j] = s[j * kLines + r];
+  }
+}
+
+// Column pass: L-point FFTs along an axis of the half spectrum for kLines
+// adjacent kx.  Line (o, kx): element j at (o / ninner) shi + (o % ninner)
+// slo + j sj + kx.  The last pass writes the double2 result in place.
+template <int L, bool INV = false>
+__global__ void __launch_bounds__(kThreads) k_ff_cols(float4 *__restrict__ data, int nh, int ninner, int64_t shi,
+                                                      int64_t slo, int64_t sj, const float4 *__restrict__ tw,
+                                                      int last) {
+  constexpr int LB = log2c<L>();
+  extern __shared__ float4 ff_sm[];
+  float4 *s = ff_sm, *tws = ff_sm + L * kLines;
+  for (int k = threadIdx.x; k < L / 2; k += kThreads) tws[k] = tw[k];  // W_L^k
+  const int nkb = (nh + kLines - 1) / kLines;
+  const int o = blockIdx.x / nkb, kx0 = (blockIdx.x % nkb) * kLines;
+  const int64_t base = (int64_t)(o / ninner) * shi + (int64_t)(o % ninner) * slo + kx0;
+  for (int idx = threadIdx.x; idx < kLines * L; idx += kThreads) {
+    const int c = idx % kLines, j = idx / kLines;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (kx0 + c < nh) v = data[base + j * sj + c];
+    s[brev(j, LB) * kLines + c] = v;
+  }
+  __syncthreads();
+  fft_lines<L, INV>(s, tws, 1);
+  for (int idx = threadIdx.x; idx < kLines * L; idx += kThreads) {
+    const int c = idx % kLines, j = idx / kLines;
+    if (kx0 + c >= nh) continue;
+    const float4 v = s[j * kLines + c];
+    if (last)
+      reinterpret_cast<double2 *>(data)[base + j * sj + c] = make_double2(f2_to(re(v)), f2_to(im(v)));
+    else
+      data[base + j * sj + c] = v;
+  }
+}
+
+template <int L>
+int set_smem(axg_ctx *ctx) {
+  AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ff_cols<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)((L * kLines + L / 2) * sizeof(float4))));
+  AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ff_rows<L / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)((L / 2 * kLines + L / 2) * sizeof(float4))));
+  return AXG_OK;
+}
+
+template <int L, bool INV>
+int z2z_t(axg_ctx *ctx, double2 *data, const float4 *tw) {
+  static bool attr = false;
+  const size_t sm = (L * kLines + L / 2) * sizeof(float4);
+  if (!attr) {
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ff_rows_c2c<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sm));
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ff_cols<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    attr = true;
+  }
+  constexpr int n = L;
+  const int64_t rows = (int64_t)n * n, plane = (int64_t)n * n, vol = plane * n;
+  float4 *f = reinterpret_cast<float4 *>(data);
+  AXG_LAUNCH(ctx, "fft_ff_rows_c2c", (k_ff_rows_c2c<L, INV>), (unsigned)((rows + kLines - 1) / kLines), kThreads, sm,
+             data, rows, tw);
+  const int nkb = n / kLines;
+  AXG_LAUNCH(ctx, "fft_ff_y", (k_ff_cols<L, INV>), (unsigned)((int64_t)n * nkb), kThreads, sm, f, n, n, vol, plane,
+             (int64_t)n, tw, 0);
+  AXG_LAUNCH(ctx, "fft_ff_z", (k_ff_cols<L, INV>), (unsigned)((int64_t)n * nkb), kThreads, sm, f, n, n, vol,
+             (int64_t)n, plane, tw, 1);
+  return AXG_OK;
+}
+
+template <int L>
+int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 *tw) {
+  static bool attr = false;
+  if (!attr) {
+    AXG_TRY(set_smem<L>(ctx));
+    attr = true;
+  }
+  constexpr int n = L, nh = L / 2 + 1;
+  const int64_t rows = (int64_t)batch * n * n;
+  float4 *f = reinterpret_cast<float4 *>(out);
+  AXG_LAUNCH(ctx, "fft_ff_rows", k_ff_rows<L / 2>, (unsigned)((rows + kLines - 1) / kLines), kThreads,
+             (L / 2 * kLines + L / 2) * sizeof(float4), in, f, rows, tw);
+  const int nkb = (nh + kLines - 1) / kLines;
+  const size_t sm = (L * kLines + L / 2) * sizeof(float4);
+  const int64_t plane = (int64_t)n * nh, vol = plane * n;
+  // y: lines (field, z); z: lines (field, y)
+  AXG_LAUNCH(ctx, "fft_ff_y", k_ff_cols<L>, (unsigned)((int64_t)batch * n * nkb), kThreads, sm, f, nh, n, vol,
+             plane, (int64_t)nh, tw, 0);
+  AXG_LAUNCH(ctx, "fft_ff_z", k_ff_cols<L>, (unsigned)((int64_t)batch * n * nkb), kThreads, sm, f, nh, n, vol,
+             (int64_t)nh, plane, tw, 1);
+  return AXG_OK;
+}
+
+}  // namespace
+
+bool axg_ff_fft_supported(int n) { return n >= 16 && n <= 1024 && (n & (n - 1)) == 0; }
+
+bool axg_ff_use(int n) {
+  const char *env = std::getenv("AXG_FFT_FF");
+  return axg_ff_fft_supported(n) && !(env && env[0] == '0');
+}
+
+namespace {
+int ensure_twiddles(axg_ctx *ctx, int n) {
+  if (ctx->ff_tw_n != n) {
+    axg_free(ctx, (void **)&ctx->ff_tw);
+    ctx->ff_tw_n = 0;
+    // W_n^k = exp(-2 pi i k / n), k < n / 2, split into float-float on the host
+    std::vector<float> h((size_t)n / 2 * 4);
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int k = 0; k < n / 2; ++k) {
+      const double c = std::cos(two_pi * k / n), s = -std::sin(two_pi * k / n);
+      const float ch = (float)c, sh = (float)s;
+      h[4 * k + 0] = ch;
+      h[4 * k + 1] = (float)(c - (double)ch);
+      h[4 * k + 2] = sh;
+      h[4 * k + 3] = (float)(s - (double)sh);
+    }
+    AXG_TRY(axg_alloc(ctx, (void **)&ctx->ff_tw, h.size() * sizeof(float), "FFT twiddles"));
+    AXG_CUDA_TRY(ctx, cudaMemcpy(ctx->ff_tw, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    ctx->ff_tw_n = n;
+  }
+  return AXG_OK;
+}
+}  // namespace
+
+int axg_ff_z2z(axg_ctx *ctx, double2 *data, int n, int inverse) {
+  if (!axg_ff_fft_supported(n)) return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
+  AXG_TRY(ensure_twiddles(ctx, n));
+  const float4 *tw = reinterpret_cast<const float4 *>(ctx->ff_tw);
+#define AXG_FF_Z2Z(L) \
+  case L: return inverse ? z2z_t<L, true>(ctx, data, tw) : z2z_t<L, false>(ctx, data, tw);
+  switch (n) {
+    AXG_FF_Z2Z(16)
+    AXG_FF_Z2Z(32)
+    AXG_FF_Z2Z(64)
+    AXG_FF_Z2Z(128)
+    AXG_FF_Z2Z(256)
+    AXG_FF_Z2Z(512)
+    AXG_FF_Z2Z(1024)
+    default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
+  }
+#undef AXG_FF_Z2Z
+}
+
+int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch) {
+  if (!axg_ff_fft_supported(n)) return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
+  AXG_TRY(ensure_twiddles(ctx, n));
+  const float4 *tw = reinterpret_cast<const float4 *>(ctx->ff_tw);
+  switch (n) {
+    case 16: return d2z_t<16>(ctx, in, out, batch, tw);
+    case 32: return d2z_t<32>(ctx, in, out, batch, tw);
+    case 64: return d2z_t<64>(ctx, in, out, batch, tw);
+    case 128: return d2z_t<128>(ctx, in, out, batch, tw);
+    case 256: return d2z_t<256>(ctx, in, out, batch, tw);
+    case 512: return d2z_t<512>(ctx, in, out, batch, tw);
+    case 1024: return d2z_t<1024>(ctx, in, out, batch, tw);
+    default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
+  }
+}

@@ -602,7 +602,13 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   const int pow2 = std::frexp(d, &ex) == 0.5;
   AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source, grid_for(ctx->n3), 256, 0, (const double2 *)ctx->phi[ctx->cur], n,
              d, 1.0 / d, pow2, ctx->gsrc);
-  AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
+  // the six source transforms: float-float for power-of-two N (FP64
+  // accuracy on the FP32 pipes), else cuFFT
+  if (axg_ff_use(n)) {
+    AXG_TRY(axg_ff_d2z(ctx, ctx->gsrc, ctx->gsrcF, n, 6));
+  } else {
+    AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
+  }
   if (ctx->gw_pol)
     AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate<true>, grid_for(ctx->n3), 256, 0, ctx->gsrcF, ctx->gw_pol, n,
                dwav, tau, dw, ref, ctx->acc);
@@ -660,7 +666,10 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
       AXG_LAUNCH(ctx, "uij_prepare_fp64", (k_uij_prepare<double2, double>), grid_for(ctx->n3), 256, 0,
                  (const double *)ctx->u[ctx->cur], (const double *)ctx->ud, (const double *)nullptr, ctx->n3,
                  tau, w);
-      AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_u, w, (cufftDoubleComplex *)F));
+      if (axg_ff_use(n))
+        AXG_TRY(axg_ff_d2z(ctx, w, F, n, 12));
+      else
+        AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_u, w, (cufftDoubleComplex *)F));
       AXG_LAUNCH(ctx, "uij_bin_fp64", k_uij_bin<double2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
     }
     (void)nhalf;

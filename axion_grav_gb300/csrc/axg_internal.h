@@ -93,6 +93,8 @@ struct axg_ctx {
   double2 *gsrcF = nullptr;  // [6][n*n*(n/2+1)] (float2 for FP32-mixed)
   float2 *gw_omega = nullptr;  // [n3] |k| dwav per k-site as float hi + lo (FP32-mixed Green mode)
   double *gw_pol = nullptr;    // [13][n*n*(n/2+1)] e+ real, e+ imag, |k| dwav (FP64 Green mode), or null
+  float *ff_tw = nullptr;      // float-float FFT twiddles W_n^k, k < n/2 (axg_fft_ff.cu)
+  int ff_tw_n = 0;
   cufftHandle plan_gsrc = 0;
   bool plan_gsrc_ok = false;
 
@@ -246,6 +248,14 @@ int axg_evo_default_tile(const axg_ctx *ctx);
 int axg_evo_build_tmaps(axg_ctx *ctx, int cfg);
 // one launch over every member's columns (ensemble.cu drives it); persistent
 // = resident CTAs walk the items, else one CTA per item
+// 3-D batched D2Z at FP64 accuracy in float-float arithmetic (axg_fft_ff.cu):
+// cuFFT's layout and convention, n a power of two in [16, 1024]
+// (axg_ff_use: supported, and not switched off by AXG_FFT_FF=0, which the
+// tests use to compare with cuFFT)
+bool axg_ff_fft_supported(int n);
+bool axg_ff_use(int n);
+int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch);
+int axg_ff_z2z(axg_ctx *ctx, double2 *data, int n, int inverse);  // in place, one n^3 volume
 int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem,
                        long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,
                        int *d_err, bool fp32, bool uij, double dspa, bool persistent);

@@ -414,7 +414,10 @@ int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, d
     double *wreal = (double *)ctx->spec_buf;
     double2 *whalf = (double2 *)(((uintptr_t)(wreal + m3) + 255) & ~(uintptr_t)255);
     AXG_LAUNCH(ctx, "spec_window", k_spec_window, grid_for(m3), 256, 0, ctx->flags, n, deg, dv_spa, wreal);
-    AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_window, wreal, (cufftDoubleComplex *)whalf));
+    if (axg_ff_use(m))
+      AXG_TRY(axg_ff_d2z(ctx, wreal, whalf, m, 1));
+    else
+      AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_window, wreal, (cufftDoubleComplex *)whalf));
     AXG_LAUNCH(ctx, "spec_w2_hist", k_spec_w2_hist, grid_for((int64_t)m * m * (m / 2 + 1)), 256, 0, whalf, m, h,
                cnt);
     std::vector<long long> hr(2 * (size_t)num_cov);
@@ -436,8 +439,11 @@ int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, d
     else
       AXG_LAUNCH(ctx, "spec_degrade", k_spec_degrade<double2>, grid_for(m3), 256, 0, (const double2 *)ctx->phid,
                  ctx->flags, n, deg, 1.0 / ((double)deg * deg * deg), 0, dv_spa, ctx->spec_buf);
-    AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
-                                    (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
+    if (axg_ff_use(m))
+      AXG_TRY(axg_ff_z2z(ctx, (double2 *)ctx->spec_buf, m, 1));
+    else
+      AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
+                                      (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
     const double dq = ctx->h_wav[1] - ctx->h_wav[0];
     const int16_t *tab = nullptr;
     AXG_TRY(axg_bin_table(ctx, AXG_BIN_SPECTRUM, m, dwav, dq, nb, 0, nullptr, &tab));
@@ -545,16 +551,23 @@ int axg_spec_covariance(axg_ctx *ctx, int min_mc, int max_mc, double tol, double
   double *d_sigma = scr, *d_pow = scr + nb, *d_cnt = scr + 2 * nb;
   const int16_t *tab = nullptr;
   AXG_TRY(axg_bin_table(ctx, AXG_BIN_SPECTRUM, m, dwav, dq, nb, 0, nullptr, &tab));
+  const bool ff = axg_ff_use(m);  // float-float transforms (FP64 accuracy on the FP32 pipes)
   for (iter = 1; iter <= max_mc && rc == AXG_OK; ++iter) {
     if (iter == 1) AXG_CUDA_TRY(ctx, cudaMemcpyAsync(d_sigma, sigma.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, ctx->stream));
     AXG_CUDA_TRY(ctx, cudaMemsetAsync(d_pow, 0, sizeof(double) * 2 * nb, ctx->stream));
     AXG_LAUNCH(ctx, "mc_fill", k_mc_fill, grid_for(m3), 256, 0, ctx->spec_buf, m, tab, d_sigma, (uint64_t)ctx->p.seed,
                (uint32_t)iter);
-    AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
-                                    (cufftDoubleComplex *)ctx->spec_buf, CUFFT_FORWARD));
+    if (ff)
+      AXG_TRY(axg_ff_z2z(ctx, (double2 *)ctx->spec_buf, m, 0));
+    else
+      AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
+                                      (cufftDoubleComplex *)ctx->spec_buf, CUFFT_FORWARD));
     AXG_LAUNCH(ctx, "mc_mask", k_mc_mask, grid_for(m3), 256, 0, ctx->spec_buf, ctx->flags, n, deg);
-    AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
-                                    (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
+    if (ff)
+      AXG_TRY(axg_ff_z2z(ctx, (double2 *)ctx->spec_buf, m, 1));
+    else
+      AXG_CUFFT_TRY(ctx, cufftExecZ2Z(ctx->plan_spec, (cufftDoubleComplex *)ctx->spec_buf,
+                                      (cufftDoubleComplex *)ctx->spec_buf, CUFFT_INVERSE));
     AXG_LAUNCH(ctx, "mc_bin", k_spec_bin, 152 * 4, 256, 2 * nb * sizeof(double), ctx->spec_buf, m, tab, 1.0, 1.0,
                nb, d_pow, d_cnt);
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(pw0.data(), d_pow, sizeof(double) * nb, cudaMemcpyDeviceToHost, ctx->stream));

@@ -71,6 +71,24 @@ def test_green_polarisation_table_matches_per_step_form(monkeypatch, compat, n):
     assert np.array_equal(out["1"], out["0"])
 
 
+@pytest.mark.parametrize("n", [16, 32, 64, 128])
+def test_green_float_float_fft_matches_cufft(monkeypatch, n):
+    """The FP64 Green path transforms its sources with the float-float D2Z
+    for power-of-two N: its accumulators agree with the cuFFT FP64 path to
+    about 1e-13 of their largest value."""
+    phi, phid = init_state(n)
+    p = params(n, ag.PREC_FP64_PLAIN, ag.GW_GREEN, compat=ag.COMPAT_INTENDED)
+    out = {}
+    for ff in ("1", "0"):
+        monkeypatch.setenv("AXG_FFT_FF", ff)
+        with ag.Lattice(p) as lat:
+            lat.upload(phi, phid)
+            lat.symplectic_integration(2.0, 2.4, 0.4)
+            out[ff] = lat.download_gw_green()
+    monkeypatch.delenv("AXG_FFT_FF")
+    assert rel(out["1"], out["0"]) < 1e-12
+
+
 @pytest.mark.parametrize("compat", [ag.COMPAT_REF, ag.COMPAT_INTENDED])
 def test_green_fp32_mixed_against_fp64_oracle(compat):
     """FP32 sources, R2C transforms and contractions with FP64 accumulators:

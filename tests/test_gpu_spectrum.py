@@ -76,3 +76,28 @@ def test_spectrum_covariance_matches_oracle(n, deg):
     np.testing.assert_allclose(gcov, cov, rtol=1e-7, atol=1e-9 * scale)
     assert grho == pytest.approx(rho, rel=1e-6)
     assert gdrho == pytest.approx(drho, rel=1e-6)
+
+
+@pytest.mark.parametrize("n,deg", [(64, 0), (64, 1)])
+def test_float_float_transforms_match_cufft(monkeypatch, n, deg):
+    """Window D2Z, field Z2Z and the covariance's forward / inverse Z2Z run
+    in float-float for power-of-two sizes: spectrum and covariance agree with
+    the cuFFT FP64 transforms to ~1e-12."""
+    phi, phid = state(n, 7 + deg)
+    p = params(n, degrade_spec=deg)
+    out = {}
+    for ff in ("1", "0"):
+        monkeypatch.setenv("AXG_FFT_FF", ff)
+        with ag.Lattice(p) as lat:
+            lat.upload(phi, phid)
+            lat.classify_cells(7)
+            w, pw, cv, ct = lat.spectrum_estimation(3.0)
+            cov, it = lat.spectrum_covariance(4, 4, 0.05)
+            out[ff] = (pw, cv, ct, cov, it)
+    monkeypatch.delenv("AXG_FFT_FF")
+    a, b = out["1"], out["0"]
+    np.testing.assert_array_equal(a[2], b[2])
+    np.testing.assert_allclose(a[1], b[1], rtol=1e-12)
+    np.testing.assert_allclose(a[0], b[0], rtol=1e-10, atol=1e-12 * np.max(np.abs(b[0])))
+    assert a[4] == b[4]
+    np.testing.assert_allclose(a[3], b[3], rtol=1e-8, atol=1e-10 * np.max(np.abs(b[3])))
