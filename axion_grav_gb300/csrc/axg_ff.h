@@ -1,0 +1,56 @@
+// axg_ff.h -- float-float arithmetic for FP64-accuracy work on the FP32
+// pipes (GB300 issues FP64 at 1/64 of its FP32 rate).
+//
+// A value is an unevaluated sum hi + lo of two floats, about 48 significant
+// bits.  Every operation goes through the round-once intrinsics
+// (__fadd_rn, __fmul_rn, __fmaf_rn), which the compiler never contracts, so
+// the error-free transformations below stay exact:
+//   f2_add  : Dekker's two-sum of the high parts, the low parts added, one
+//             renormalisation (error below 2^-47 (|a| + |b|));
+//   f2_dot2 : a b + s c d (s = +-1) as a two-term dot product: the exact
+//             high products through FMAs, their two-sum and the low-part
+//             cross terms, left unnormalised for the add that consumes it.
+#ifndef AXG_FF_H
+#define AXG_FF_H
+
+#include <cuda_runtime.h>
+
+struct F2 {
+  float h, l;
+};
+
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float v = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ F2 f2_neg(F2 a) { return {-a.h, -a.l}; }
+
+__device__ __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_add(a, f2_neg(b)); }
+
+__device__ __forceinline__ F2 f2_dot2(F2 a, F2 b, F2 c, F2 d, float sg) {
+  const float p1 = __fmul_rn(a.h, b.h), p2 = __fmul_rn(sg * c.h, d.h);
+  const float s = __fadd_rn(p1, p2), v = __fsub_rn(s, p1);
+  const float e0 = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v));
+  const float e1 = __fmaf_rn(a.h, b.h, -p1), e2 = __fmaf_rn(sg * c.h, d.h, -p2);
+  float t = __fmul_rn(sg * c.l, d.h);
+  t = __fmaf_rn(sg * c.h, d.l, t);
+  t = __fmaf_rn(a.l, b.h, t);
+  t = __fmaf_rn(a.h, b.l, t);
+  return {s, __fadd_rn(__fadd_rn(e0, __fadd_rn(e1, e2)), t)};
+}
+
+__device__ __forceinline__ F2 f2_half(F2 a) { return {__fmul_rn(a.h, 0.5f), __fmul_rn(a.l, 0.5f)}; }  // exact
+
+__device__ __forceinline__ F2 f2_from(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+
+__device__ __forceinline__ double f2_to(F2 a) { return (double)a.h + (double)a.l; }
+
+#endif  // AXG_FF_H

@@ -1,19 +1,13 @@
-// axg_fft_ff.cu -- 3-D real-to-complex FFTs at FP64 accuracy in float-float
-// arithmetic.
+// axg_fft_ff.cu -- 3-D FFTs at FP64 accuracy in float-float arithmetic.
 //
 // GB300 issues FP64 at 1/64 of its FP32 rate, and an FP64 FFT is bound by
 // it: cuFFT's 512^3 D2Z takes about 15.5 ms, while moving its bytes takes
-// about 1 ms.  Here every value is a float-float pair (hi + lo, about 48
-// significant bits) and the butterflies run on the FP32 pipes:
-//   ff add : Dekker's two-sum of the high parts, low parts added, one
-//            renormalisation (error below 2^-47 (|a| + |b|));
-//   ff mul : complex products as two-term dot products: the exact high
-//            products through FMAs, their two-sum, the cross terms of the
-//            low parts, left unnormalised for the add that follows;
-// all through the round-once intrinsics (__fadd_rn, __fmul_rn, __fmaf_rn),
-// which the compiler never contracts.  The input doubles are split into
-// float-float on load and the output is hi + lo in double, so the transform
-// agrees with an FP64 FFT to about 1e-13 of the spectrum's largest value.
+// about 1 ms.  Here every value is a float-float pair (axg_ff.h) and the
+// butterflies run on the FP32 pipes; complex twiddle products are two f2_dot2
+// terms.  The input doubles are split into float-float on load and the
+// output is hi + lo in double (or stays float-float for a consumer that
+// reads it so), so the transform agrees with an FP64 FFT to about 1e-13 of
+// the spectrum's largest value.
 //
 // Layout and convention are cuFFT's: batched D2Z, in [batch][n][n][n] reals,
 // out [batch][n][n][n/2+1] complex, forward (exp(-2 pi i k x / n)),
@@ -33,28 +27,10 @@
 #include <cstdlib>
 #include <vector>
 
+#include "axg_ff.h"
 #include "axg_internal.h"
 
 namespace {
-
-struct F2 {
-  float h, l;
-};
-
-__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
-  const float s = __fadd_rn(a.h, b.h);
-  const float v = __fsub_rn(s, a.h);
-  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
-  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
-  const float h = __fadd_rn(s, e);
-  return {h, __fsub_rn(e, __fsub_rn(h, s))};
-}
-
-__device__ __forceinline__ F2 f2_neg(F2 a) { return {-a.h, -a.l}; }
-
-__device__ __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_add(a, f2_neg(b)); }
-
-__device__ __forceinline__ F2 f2_half(F2 a) { return {__fmul_rn(a.h, 0.5f), __fmul_rn(a.l, 0.5f)}; }  // exact
 
 // complex float-float in a float4: (re.h, re.l, im.h, im.l)
 __device__ __forceinline__ F2 re(float4 v) { return {v.x, v.y}; }
@@ -62,32 +38,11 @@ __device__ __forceinline__ F2 im(float4 v) { return {v.z, v.w}; }
 __device__ __forceinline__ float4 cx(F2 r, F2 i) { return make_float4(r.h, r.l, i.h, i.l); }
 __device__ __forceinline__ float4 c_add(float4 a, float4 b) { return cx(f2_add(re(a), re(b)), f2_add(im(a), im(b))); }
 __device__ __forceinline__ float4 c_sub(float4 a, float4 b) { return cx(f2_sub(re(a), re(b)), f2_sub(im(a), im(b))); }
-// a.b + s c.d as an unnormalised float-float (s = +-1): the exact high
-// products through FMAs, their two-sum, and the cross terms of the low
-// parts; the add that consumes it renormalises.
-__device__ __forceinline__ F2 f2_dot2(F2 a, F2 b, F2 c, F2 d, float sg) {
-  const float p1 = __fmul_rn(a.h, b.h), p2 = __fmul_rn(sg * c.h, d.h);
-  const float s = __fadd_rn(p1, p2), v = __fsub_rn(s, p1);
-  const float e0 = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v));
-  const float e1 = __fmaf_rn(a.h, b.h, -p1), e2 = __fmaf_rn(sg * c.h, d.h, -p2);
-  float t = __fmul_rn(sg * c.l, d.h);
-  t = __fmaf_rn(sg * c.h, d.l, t);
-  t = __fmaf_rn(a.l, b.h, t);
-  t = __fmaf_rn(a.h, b.l, t);
-  return {s, __fadd_rn(__fadd_rn(e0, __fadd_rn(e1, e2)), t)};
-}
 
 __device__ __forceinline__ float4 c_mul(float4 a, float4 b) {
   return cx(f2_dot2(re(a), re(b), im(a), im(b), -1.f), f2_dot2(re(a), im(b), im(a), re(b), 1.f));
 }
 __device__ __forceinline__ float4 c_conj(float4 a) { return make_float4(a.x, a.y, -a.z, -a.w); }
-
-__device__ __forceinline__ F2 f2_from(double x) {
-  const float h = __double2float_rn(x);
-  return {h, __double2float_rn(x - (double)h)};
-}
-
-__device__ __forceinline__ double f2_to(F2 a) { return (double)a.h + (double)a.l; }
 
 __device__ __forceinline__ int brev(int j, int bits) { return (int)(__brev((unsigned)j) >> (32 - bits)); }
 
@@ -247,7 +202,7 @@ int z2z_t(axg_ctx *ctx, double2 *data, const float4 *tw) {
 }
 
 template <int L>
-int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 *tw) {
+int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 *tw, bool keep_ff) {
   static bool attr = false;
   if (!attr) {
     AXG_TRY(set_smem<L>(ctx));
@@ -265,7 +220,7 @@ int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 
   AXG_LAUNCH(ctx, "fft_ff_y", k_ff_cols<L>, (unsigned)((int64_t)batch * n * nkb), kThreads, sm, f, nh, n, vol,
              plane, (int64_t)nh, tw, 0);
   AXG_LAUNCH(ctx, "fft_ff_z", k_ff_cols<L>, (unsigned)((int64_t)batch * n * nkb), kThreads, sm, f, nh, n, vol,
-             (int64_t)nh, plane, tw, 1);
+             (int64_t)nh, plane, tw, keep_ff ? 0 : 1);
   return AXG_OK;
 }
 
@@ -321,18 +276,18 @@ int axg_ff_z2z(axg_ctx *ctx, double2 *data, int n, int inverse) {
 #undef AXG_FF_Z2Z
 }
 
-int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch) {
+int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch, bool keep_ff) {
   if (!axg_ff_fft_supported(n)) return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
   AXG_TRY(ensure_twiddles(ctx, n));
   const float4 *tw = reinterpret_cast<const float4 *>(ctx->ff_tw);
   switch (n) {
-    case 16: return d2z_t<16>(ctx, in, out, batch, tw);
-    case 32: return d2z_t<32>(ctx, in, out, batch, tw);
-    case 64: return d2z_t<64>(ctx, in, out, batch, tw);
-    case 128: return d2z_t<128>(ctx, in, out, batch, tw);
-    case 256: return d2z_t<256>(ctx, in, out, batch, tw);
-    case 512: return d2z_t<512>(ctx, in, out, batch, tw);
-    case 1024: return d2z_t<1024>(ctx, in, out, batch, tw);
+    case 16: return d2z_t<16>(ctx, in, out, batch, tw, keep_ff);
+    case 32: return d2z_t<32>(ctx, in, out, batch, tw, keep_ff);
+    case 64: return d2z_t<64>(ctx, in, out, batch, tw, keep_ff);
+    case 128: return d2z_t<128>(ctx, in, out, batch, tw, keep_ff);
+    case 256: return d2z_t<256>(ctx, in, out, batch, tw, keep_ff);
+    case 512: return d2z_t<512>(ctx, in, out, batch, tw, keep_ff);
+    case 1024: return d2z_t<1024>(ctx, in, out, batch, tw, keep_ff);
     default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
   }
 }

@@ -30,6 +30,7 @@
 
 #include "axg_binning.h"
 #include "axg_detmath.h"
+#include "axg_ff.h"
 #include "axg_internal.h"
 
 namespace {
@@ -212,14 +213,20 @@ __device__ __forceinline__ void gw_update(double2 *__restrict__ acc, int64_t n3,
   acc[3 * n3 + s] = a22;
 }
 
-// The polarisation tensor and phase rate |k| dwav of every half-spectrum k,
-// [13][nhalf]: e+ real parts, e+ imaginary parts, rate.  They depend on k
-// only; GB300 issues FP64 at 1/64 of the FP32 rate, and forming them takes
-// about half of the per-k FP64 work of a Green step, so the FP64 path reads
-// them (104 B per half-spectrum k) instead.  For -k the polarisation vector
-// is the conjugate (q and its azimuth change sign), so e+(-k) = conj e+(k)
-// (exactly: the negations are exact and the products keep their operands).
-__global__ void k_gw_pol_table(int n, double dwav, double *__restrict__ tab) {
+// The polarisation tensor and phase rate |k| dwav of every half-spectrum k:
+// e+ real and imaginary parts as float-float pairs, [12][nhalf] float2, then
+// the rates, [nhalf] double (104 B per half-spectrum k).  They depend on k
+// only; GB300 issues FP64 at 1/64 of the FP32 rate, and forming them took
+// about half of the per-k FP64 work of a Green step.  For -k the
+// polarisation vector is the conjugate (q and its azimuth change sign), so
+// e+(-k) = conj e+(k) exactly: the negations are exact and the products
+// keep their operands.
+__device__ __forceinline__ float2 f2_pack(double x) {
+  const F2 v = f2_from(x);
+  return make_float2(v.h, v.l);
+}
+
+__global__ void k_gw_pol_table(int n, double dwav, float2 *__restrict__ pol, double *__restrict__ rate) {
   const int nh = n / 2 + 1;
   const int64_t nhalf = (int64_t)n * n * nh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -231,17 +238,16 @@ __global__ void k_gw_pol_table(int n, double dwav, double *__restrict__ tab) {
     if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi))
       for (int c = 0; c < 6; ++c) pr[c] = pi[c] = 0.0;
     for (int c = 0; c < 6; ++c) {
-      tab[c * nhalf + h] = pr[c];
-      tab[(6 + c) * nhalf + h] = pi[c];
+      pol[c * nhalf + h] = f2_pack(pr[c]);
+      pol[(6 + c) * nhalf + h] = f2_pack(pi[c]);
     }
-    tab[12 * nhalf + h] = qq * dwav;
+    rate[h] = qq * dwav;
   }
 }
 
-// TABLE: polarisation and rate from k_gw_pol_table; otherwise formed here
-template <bool TABLE>
-__global__ void k_gw_accumulate(const double2 *__restrict__ srcF, const double *__restrict__ tab, int n, double dwav,
-                                double tau, double dw, int ref_compat, double2 *__restrict__ acc) {
+// Green accumulation with the polarisation formed per k in FP64 (no table)
+__global__ void k_gw_accumulate(const double2 *__restrict__ srcF, int n, double dwav, double tau, double dw,
+                                int ref_compat, double2 *__restrict__ acc) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -249,35 +255,97 @@ __global__ void k_gw_accumulate(const double2 *__restrict__ srcF, const double *
     const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
     bool conj_back;
     const int64_t hidx = gw_half_index(ix, iy, iz, n, conj_back);
-    double pr[6], pi[6], rate;
+    const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
+    const double qq = sqrt(kx * kx + ky * ky + kz * kz);
+    double pr[6], pi[6];
+    if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi)) {
+      // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
+      if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+      continue;
+    }
+    double sq, cq;
+    sincos(qq * dwav * tau, &sq, &cq);
+    double xp[2], xm[2], lm[2];
+    gw_contract<double, double2>(srcF, nhalf, hidx, conj_back, pr, pi, xp, xm, lm);
+    gw_update(acc, n3, s, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+  }
+}
+
+// A source spectrum value as float-float: from the float-float transform
+// (float4: re hi, re lo, im hi, im lo) or from an FP64 one.
+__device__ __forceinline__ void src_ff(float4 v, F2 &r, F2 &i) {
+  r = {v.x, v.y};
+  i = {v.z, v.w};
+}
+__device__ __forceinline__ void src_ff(double2 v, F2 &r, F2 &i) {
+  r = f2_from(v.x);
+  i = f2_from(v.y);
+}
+
+// Green accumulation with the polarisation table: the contraction
+// X+- = sum e+- S runs in float-float on the FP32 pipes (four f2_dot2 per
+// component), the phase sin / cos and the accumulator updates in FP64.
+template <typename SRC>
+__global__ void k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *__restrict__ pol,
+                                    const double *__restrict__ rates, int n, double dwav, double tau, double dw,
+                                    int ref_compat, double2 *__restrict__ acc) {
+  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
+    const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
+    bool conj_back;
+    const int64_t hidx = gw_half_index(ix, iy, iz, n, conj_back);
+    F2 er[6], ei[6];
+    double rate;
     // The stored entry is k's (conj_back) or -k's.  A Nyquist y or z index
     // maps to itself, so there the entry is not -k's: form those directly.
-    if (TABLE && (conj_back || (iy != n / 2 && iz != n / 2))) {
-      rate = tab[12 * nhalf + hidx];
+    if (conj_back || (iy != n / 2 && iz != n / 2)) {
+      rate = rates[hidx];
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        pr[c] = tab[c * nhalf + hidx];
-        const double v = tab[(6 + c) * nhalf + hidx];
-        pi[c] = conj_back ? v : -v;
-      }
-      if (!(rate > 0)) {
-        // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
-        if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
-        continue;
+        const float2 a = pol[c * nhalf + hidx], b = pol[(6 + c) * nhalf + hidx];
+        er[c] = {a.x, a.y};
+        ei[c] = conj_back ? F2{b.x, b.y} : F2{-b.x, -b.y};
       }
     } else {
       const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
       const double qq = sqrt(kx * kx + ky * ky + kz * kz);
-      if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi)) {
-        if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
-        continue;
+      double pr[6], pi[6];
+      if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi))
+        for (int c = 0; c < 6; ++c) pr[c] = pi[c] = 0.0;
+      for (int c = 0; c < 6; ++c) {
+        er[c] = f2_from(pr[c]);
+        ei[c] = f2_from(pi[c]);
       }
       rate = qq * dwav;
     }
+    if (!(rate > 0)) {
+      // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
+      if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+      continue;
+    }
     double sq, cq;
     sincos(rate * tau, &sq, &cq);
-    double xp[2], xm[2], lm[2];
-    gw_contract<double, double2>(srcF, nhalf, hidx, conj_back, pr, pi, xp, xm, lm);
+    F2 p0 = {0.f, 0.f}, p1 = p0, m0 = p0, m1 = p0, l0 = p0, l1 = p0;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      F2 sr, si;
+      src_ff(srcF[c * nhalf + hidx], sr, si);
+      if (conj_back) si = f2_neg(si);
+      // a = er sr, b = ei si, e = er si, g = ei sr: X+ += (a - b, e + g), X- += (a + b, e - g)
+      const F2 t0 = f2_dot2(er[c], sr, ei[c], si, -1.f), t1 = f2_dot2(er[c], si, ei[c], sr, 1.f);
+      const F2 t2 = f2_dot2(er[c], sr, ei[c], si, 1.f), t3 = f2_dot2(er[c], si, ei[c], sr, -1.f);
+      p0 = f2_add(p0, t0);
+      p1 = f2_add(p1, t1);
+      m0 = f2_add(m0, t2);
+      m1 = f2_add(m1, t3);
+      if (c == 5) {
+        l0 = t2;
+        l1 = t3;
+      }
+    }
+    const double xp[2] = {f2_to(p0), f2_to(p1)}, xm[2] = {f2_to(m0), f2_to(m1)}, lm[2] = {f2_to(l0), f2_to(l1)};
     gw_update(acc, n3, s, dw * cq, dw * sq, xp, xm, lm, ref_compat);
   }
 }
@@ -568,7 +636,7 @@ int axg_gw_init(axg_ctx *ctx) {
     if (want && tb <= total / 8) {
       AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_pol, tb, "GW polarisation table"));
       AXG_LAUNCH(ctx, "gw_pol_table", k_gw_pol_table, grid_for(nhalf), 256, 0, n, kRefTwoPi / ctx->p.dspa / n,
-                 ctx->gw_pol);
+                 reinterpret_cast<float2 *>(ctx->gw_pol), ctx->gw_pol + 12 * nhalf);
     }
   }
   int dims[3] = {n, n, n};
@@ -603,18 +671,25 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source, grid_for(ctx->n3), 256, 0, (const double2 *)ctx->phi[ctx->cur], n,
              d, 1.0 / d, pow2, ctx->gsrc);
   // the six source transforms: float-float for power-of-two N (FP64
-  // accuracy on the FP32 pipes), else cuFFT
-  if (axg_ff_use(n)) {
-    AXG_TRY(axg_ff_d2z(ctx, ctx->gsrc, ctx->gsrcF, n, 6));
-  } else {
-    AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
-  }
-  if (ctx->gw_pol)
-    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate<true>, grid_for(ctx->n3), 256, 0, ctx->gsrcF, ctx->gw_pol, n,
-               dwav, tau, dw, ref, ctx->acc);
+  // accuracy on the FP32 pipes; kept as float-float pairs when the
+  // float-float contraction reads them), else cuFFT
+  const bool ff = axg_ff_use(n), tab = ctx->gw_pol != nullptr;
+  if (ff)
+    AXG_TRY(axg_ff_d2z(ctx, ctx->gsrc, ctx->gsrcF, n, 6, tab));
   else
-    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate<false>, grid_for(ctx->n3), 256, 0, ctx->gsrcF, nullptr, n,
-               dwav, tau, dw, ref, ctx->acc);
+    AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
+  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+  if (tab && ff)
+    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate_tab<float4>, grid_for(ctx->n3), 256, 0,
+               reinterpret_cast<const float4 *>(ctx->gsrcF), reinterpret_cast<const float2 *>(ctx->gw_pol),
+               ctx->gw_pol + 12 * nhalf, n, dwav, tau, dw, ref, ctx->acc);
+  else if (tab)
+    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate_tab<double2>, grid_for(ctx->n3), 256, 0,
+               (const double2 *)ctx->gsrcF, reinterpret_cast<const float2 *>(ctx->gw_pol), ctx->gw_pol + 12 * nhalf,
+               n, dwav, tau, dw, ref, ctx->acc);
+  else
+    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate, grid_for(ctx->n3), 256, 0, ctx->gsrcF, n, dwav, tau, dw, ref,
+               ctx->acc);
   return AXG_OK;
 }
 

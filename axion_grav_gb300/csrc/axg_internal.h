@@ -92,7 +92,8 @@ struct axg_ctx {
   double *gsrc = nullptr;  // [6][n3] real sources S_ij (float for FP32-mixed)
   double2 *gsrcF = nullptr;  // [6][n*n*(n/2+1)] (float2 for FP32-mixed)
   float2 *gw_omega = nullptr;  // [n3] |k| dwav per k-site as float hi + lo (FP32-mixed Green mode)
-  double *gw_pol = nullptr;    // [13][n*n*(n/2+1)] e+ real, e+ imag, |k| dwav (FP64 Green mode), or null
+  double *gw_pol = nullptr;    // FP64 Green mode: [12][n*n*(n/2+1)] float2 e+ (re, im as float-float), then
+                               // [n*n*(n/2+1)] double |k| dwav; or null
   float *ff_tw = nullptr;      // float-float FFT twiddles W_n^k, k < n/2 (axg_fft_ff.cu)
   int ff_tw_n = 0;
   cufftHandle plan_gsrc = 0;
@@ -254,7 +255,9 @@ int axg_evo_build_tmaps(axg_ctx *ctx, int cfg);
 // tests use to compare with cuFFT)
 bool axg_ff_fft_supported(int n);
 bool axg_ff_use(int n);
-int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch);
+// keep_ff: the output stays float-float, (re hi, re lo, im hi, im lo) per
+// complex value in the same 16 bytes, for a consumer that reads it so
+int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch, bool keep_ff = false);
 int axg_ff_z2z(axg_ctx *ctx, double2 *data, int n, int inverse);  // in place, one n^3 volume
 int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem,
                        long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,

@@ -55,8 +55,8 @@ def test_green_accumulators_and_spectrum(compat, precision):
 @pytest.mark.parametrize("n", [16, 18])
 def test_green_polarisation_table_matches_per_step_form(monkeypatch, compat, n):
     """FP64 Green accumulation with the precomputed polarisation table
-    (conjugated for the k outside the stored half spectrum) equals the
-    per-step form bit for bit."""
+    (conjugated for the k outside the stored half spectrum) and the
+    float-float contraction agrees with the per-step FP64 form to ~1e-13."""
     phi, phid = init_state(n)
     p = params(n, ag.PREC_FP64_PLAIN, ag.GW_GREEN, compat=compat)
     out = {}
@@ -68,7 +68,7 @@ def test_green_polarisation_table_matches_per_step_form(monkeypatch, compat, n):
             out[table] = lat.download_gw_green()
     monkeypatch.delenv("AXG_GW_POL_TABLE")
     assert np.any(out["1"] != 0)
-    assert np.array_equal(out["1"], out["0"])
+    assert rel(out["1"], out["0"]) < 1e-12
 
 
 @pytest.mark.parametrize("n", [16, 32, 64, 128])
