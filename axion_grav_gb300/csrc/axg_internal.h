@@ -250,7 +250,7 @@ int axg_evo_build_tmaps(axg_ctx *ctx, int cfg);
 // one launch over every member's columns (ensemble.cu drives it); persistent
 // = resident CTAs walk the items, else one CTA per item
 // 3-D batched D2Z at FP64 accuracy in float-float arithmetic (axg_fft_ff.cu):
-// cuFFT's layout and convention, n a power of two in [16, 1024]
+// cuFFT's layout and convention, n a power of two in [16, 512]
 // (axg_ff_use: supported, and not switched off by AXG_FFT_FF=0, which the
 // tests use to compare with cuFFT)
 bool axg_ff_fft_supported(int n);
