@@ -442,7 +442,7 @@ def accuracy_fp32(ag, n, steps, device):
     return out
 
 
-def cpu_oracle_rate(n, steps, threads=None):
+def cpu_oracle_rate(n, steps, threads=None, warmup=1):
     """FP64 CPU restatement of evolve.f90 (phi + six u_ij), all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import axo
@@ -457,8 +457,11 @@ def cpu_oracle_rate(n, steps, threads=None):
     u = np.zeros((6, n, n, n))
     ud = np.zeros((6, n, n, n))
     dt, _ = axo.get_dtau(p, 2.0, 32.0, 0.25)
-    axo.leapfrog(p, phi, phid, u, ud, None, 2.0, dt, 1, True, False)  # warm-up
+    axo.leapfrog(p, phi, phid, u, ud, None, 2.0, dt, 1, True, False)  # opens the DKD sequence (warm-up)
     t = 2.0 + 1.5 * dt
+    for _ in range(max(0, warmup - 1)):
+        axo.leapfrog(p, phi, phid, u, ud, None, t, dt, 1, False, False)
+        t += dt
     times = []
     for _ in range(steps):
         t0 = time.perf_counter()
@@ -475,10 +478,11 @@ def run_reference(args):
         return
     n = args.n
     steps = max(1, args.steps)
-    rate, per, cores = cpu_oracle_rate(n, steps)
-    sample = f"{steps} leapfrog steps (phi + 6 u_ij, FP64) of the {n}^3 lattice after 1 warm-up step"
+    warm = max(1, args.warmup)
+    rate, per, cores = cpu_oracle_rate(n, steps, warmup=warm)
+    sample = f"{steps} leapfrog steps (phi + 6 u_ij, FP64) of the {n}^3 lattice after {warm} warm-up steps"
     line = {
-        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{n}^3 lattice leapfrog of phi + 6 u_ij (one site-update = one kick+drift of all "
