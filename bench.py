@@ -167,7 +167,12 @@ def bench_ours(ag, n, precision, gw, steps, warmup, dist, device, t0=2.0, eps=0.
         if tile is not None and precision != ag.PREC_FP64_PLAIN:
             lat.set_tile(tile)
         elif tune and precision != ag.PREC_FP64_PLAIN:
-            tile, _ = lat.autotune(3)
+            try:
+                tile, _ = lat.autotune(3)
+            except ag.AxgError:
+                # the tuner snapshots the state; without room for it the
+                # library's default shape runs
+                tile = None
         else:
             tile = None
         t = t0
