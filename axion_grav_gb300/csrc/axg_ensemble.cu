@@ -200,8 +200,10 @@ int axg_ensemble_create(const axg_params *members, int32_t count, axg_ensemble *
     } else {
       cudaMemset(e->d_err, 0, 64);
       int cfg = -1;
-      for (int k = 0; k < axg_evo_tile_count() && cfg < 0; ++k)
-        if (tile_ok_all(e, k)) cfg = k;
+      for (int k = 0; k < axg_evo_tile_count() && cfg < 0; ++k) {
+        const int c = axg_evo_tile_preference(e->fp32, k);
+        if (tile_ok_all(e, c)) cfg = c;
+      }
       if (cfg < 0) rc = axg_set_error(nullptr, AXG_ERR_UNSUPPORTED, "no fused tile fits every member");
       else if ((rc = build_descriptors(e, cfg)) != AXG_OK) axg_set_error(nullptr, rc, e->err);
     }

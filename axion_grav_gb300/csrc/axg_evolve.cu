@@ -887,13 +887,26 @@ int axg_evo_tile_supported(const axg_ctx *ctx, int i) {
 }
 
 int axg_evo_default_tile(const axg_ctx *ctx) {
-  // preferred order; first supported wins
-  const int pref_fp32[] = {0, 1, 2, 3, 4, 5, 6};
-  const int pref_fp64[] = {1, 3, 5, 0, 2, 4, 6};
-  const int *pref = ctx->p.precision == AXG_PREC_FP32_MIXED ? pref_fp32 : pref_fp64;
-  for (int i = 0; i < kNumTiles; ++i)
-    if (axg_evo_tile_supported(ctx, pref[i])) return pref[i];
+  // the first supported shape in the preference order
+  const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
+  for (int i = 0; i < kNumTiles; ++i) {
+    const int cfg = axg_evo_tile_preference(fp32, i);
+    if (axg_evo_tile_supported(ctx, cfg)) return cfg;
+  }
   return -1;
+}
+
+// Preferred order for a context that was not autotuned.  FP32: the shapes
+// with the pointwise fields in the TMA ring first (the autotuner's picks at
+// 256^3 to 1024^3); FP64 is bound by the FP64 pipe and nearly indifferent
+// to the shape.
+int axg_evo_tile_preference(bool fp32, int rank) {
+  if (rank < 0 || rank >= kNumTiles) return -1;
+  static const int pref_fp32[] = {8, 11, 10, 7, 9, 1, 0, 3, 2, 5, 4, 6};
+  static const int pref_fp64[] = {7, 1, 3, 5, 8, 9, 10, 11, 0, 2, 4, 6};
+  static_assert(sizeof(pref_fp32) / sizeof(int) == kNumTiles && sizeof(pref_fp64) / sizeof(int) == kNumTiles,
+                "one entry per tile shape");
+  return fp32 ? pref_fp32[rank] : pref_fp64[rank];
 }
 
 int axg_evo_drift(axg_ctx *ctx, double h) {

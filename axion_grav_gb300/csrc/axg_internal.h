@@ -246,6 +246,7 @@ int axg_evo_tile_count();
 axg_tile_cfg axg_evo_tile(int i);
 int axg_evo_tile_supported(const axg_ctx *ctx, int i);
 int axg_evo_default_tile(const axg_ctx *ctx);
+int axg_evo_tile_preference(bool fp32, int rank);  // tile index of the rank-th preferred shape
 int axg_evo_build_tmaps(axg_ctx *ctx, int cfg);
 // one launch over every member's columns (ensemble.cu drives it); persistent
 // = resident CTAs walk the items, else one CTA per item
