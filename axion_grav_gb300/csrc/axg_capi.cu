@@ -596,7 +596,7 @@ int axg_download_uij(axg_ctx *ctx, double *u, double *udot) {
 int axg_upload_gw_green(axg_ctx *ctx, const double *acc) {
   if (!valid_ctx(ctx) || !acc) return AXG_ERR_ARG;
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
-  if (ctx->p.precision != AXG_PREC_FP32_MIXED) {
+  if (!ctx->acc_ff) {
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->acc, acc, (size_t)ctx->n3 * 64, cudaMemcpyHostToDevice, ctx->stream));
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return AXG_OK;
@@ -619,7 +619,7 @@ int axg_upload_gw_green(axg_ctx *ctx, const double *acc) {
 int axg_download_gw_green(axg_ctx *ctx, double *acc) {
   if (!valid_ctx(ctx) || !acc) return AXG_ERR_ARG;
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
-  if (ctx->p.precision != AXG_PREC_FP32_MIXED) {
+  if (!ctx->acc_ff) {
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(acc, ctx->acc, (size_t)ctx->n3 * 64, cudaMemcpyDeviceToHost, ctx->stream));
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return AXG_OK;

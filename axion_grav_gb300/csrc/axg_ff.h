@@ -9,7 +9,8 @@
 //             renormalisation (error below 2^-47 (|a| + |b|));
 //   f2_dot2 : a b + s c d (s = +-1) as a two-term dot product: the exact
 //             high products through FMAs, their two-sum and the low-part
-//             cross terms, left unnormalised for the add that consumes it.
+//             cross terms, left unnormalised for the add that consumes it;
+//   f2_mul  : a b likewise, unnormalised.
 #ifndef AXG_FF_H
 #define AXG_FF_H
 
@@ -42,6 +43,16 @@ __device__ __forceinline__ F2 f2_dot2(F2 a, F2 b, F2 c, F2 d, float sg) {
   t = __fmaf_rn(a.l, b.h, t);
   t = __fmaf_rn(a.h, b.l, t);
   return {s, __fadd_rn(__fadd_rn(e0, __fadd_rn(e1, e2)), t)};
+}
+
+// a b, unnormalised (the exact high product through an FMA plus the cross
+// terms of the low parts)
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return {p, e};
 }
 
 __device__ __forceinline__ F2 f2_half(F2 a) { return {__fmul_rn(a.h, 0.5f), __fmul_rn(a.l, 0.5f)}; }  // exact

@@ -282,13 +282,70 @@ __device__ __forceinline__ void src_ff(double2 v, F2 &r, F2 &i) {
   i = f2_from(v.y);
 }
 
+// sin and cos of x (|x| < 1e6) as float-float pairs.  x is reduced by pi/2
+// in FP64 with the three-part Cody-Waite constant of axd_sincos (6 FP64
+// operations), the remainder |r| <= pi/4 is split into float-float, and the
+// Taylor series of sin (to r^17) and cos (to r^16) run by Horner in
+// float-float on the FP32 pipes; the first omitted terms are below 1e-16.
+// The coefficients are (-1)^k / n! as float-float pairs.
+__device__ __forceinline__ void ff_sincos(double x, F2 &sn, F2 &cs) {
+  const double kf = rint(x * AXD_TWO_OVER_PI);
+  double rd = fma(-kf, AXD_CW_P1, x);
+  rd = fma(-kf, AXD_CW_P2, rd);
+  rd = fma(-kf, AXD_CW_P3, rd);
+  const int q = (int)(long long)kf & 3;
+  const F2 r = f2_from(rd);
+  const F2 r2 = f2_add(f2_mul(r, r), F2{0.f, 0.f});
+  constexpr float ks[9][2] = {{1.0f, 0.0f},
+                              {-0.1666666716337204f, 4.967053879312289e-09f},
+                              {0.008333333767950535f, -4.34617203337595e-10f},
+                              {-0.00019841270113829523f, 2.725596874933456e-12f},
+                              {2.7557318844628753e-06f, 3.793571224297229e-14f},
+                              {-2.5052107943679403e-08f, -4.4176230446483665e-16f},
+                              {1.6059044372074283e-10f, -5.352526511562726e-18f},
+                              {-7.647163609812713e-13f, -1.2200710471178288e-20f},
+                              {2.8114573589663704e-15f, -1.0462084739763658e-22f}};
+  constexpr float kc[9][2] = {{1.0f, 0.0f},
+                              {-0.5f, 0.0f},
+                              {0.0416666679084301f, -1.2417634698280722e-09f},
+                              {-0.0013888889225199819f, 3.3631094437103215e-11f},
+                              {2.4801587642286904e-05f, -3.40699609366682e-13f},
+                              {-2.755731998149713e-07f, 7.575112209051195e-15f},
+                              {2.0876755879584152e-09f, 1.1082839147459852e-16f},
+                              {-1.147074536050896e-11f, -2.372207689231238e-19f},
+                              {4.7794772561329454e-14f, 7.62544404448643e-22f}};
+  F2 ps = {ks[8][0], ks[8][1]}, pc = {kc[8][0], kc[8][1]};
+#pragma unroll
+  for (int k = 7; k >= 0; --k) {
+    ps = f2_add(f2_mul(ps, r2), F2{ks[k][0], ks[k][1]});
+    pc = f2_add(f2_mul(pc, r2), F2{kc[k][0], kc[k][1]});
+  }
+  const F2 s0 = f2_add(f2_mul(ps, r), F2{0.f, 0.f});  // sin r
+  const F2 c0 = pc;                                   // cos r
+  // x = q pi / 2 + r
+  sn = (q & 1) ? c0 : s0;
+  cs = (q & 1) ? s0 : c0;
+  if (q == 2 || q == 3) sn = f2_neg(sn);
+  if (q == 1 || q == 2) cs = f2_neg(cs);
+}
+
+// acc += w x for float-float complex values (float4: re hi, re lo, im hi, im lo)
+__device__ __forceinline__ void ff_axpy(float4 &a, F2 w, F2 xr, F2 xi) {
+  const F2 r = f2_add(F2{a.x, a.y}, f2_mul(w, xr)), i = f2_add(F2{a.z, a.w}, f2_mul(w, xi));
+  a = make_float4(r.h, r.l, i.h, i.l);
+}
+
 // Green accumulation with the polarisation table: the contraction
 // X+- = sum e+- S runs in float-float on the FP32 pipes (four f2_dot2 per
 // component), the phase sin / cos and the accumulator updates in FP64.
-template <typename SRC>
+//
+// ACCFF: the accumulators are float-float (float4) as in the FP32-mixed path,
+// the phase sin / cos are float-float (ff_sincos) and the updates run in
+// float-float, so a k-site issues about ten FP64 operations.
+template <typename SRC, bool ACCFF>
 __global__ void k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *__restrict__ pol,
                                     const double *__restrict__ rates, int n, double dwav, double tau, double dw,
-                                    int ref_compat, double2 *__restrict__ acc) {
+                                    float dw_hi, float dw_lo, int ref_compat, void *__restrict__ accp) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -322,11 +379,17 @@ __global__ void k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *
     }
     if (!(rate > 0)) {
       // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
-      if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+      if (ref_compat) {
+        if constexpr (ACCFF) {
+          float4 *acc = static_cast<float4 *>(accp);
+          acc[n3 + s] = acc[2 * n3 + s];
+        } else {
+          double2 *acc = static_cast<double2 *>(accp);
+          acc[n3 + s] = acc[2 * n3 + s];
+        }
+      }
       continue;
     }
-    double sq, cq;
-    sincos(rate * tau, &sq, &cq);
     F2 p0 = {0.f, 0.f}, p1 = p0, m0 = p0, m1 = p0, l0 = p0, l1 = p0;
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -345,8 +408,35 @@ __global__ void k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *
         l1 = t3;
       }
     }
-    const double xp[2] = {f2_to(p0), f2_to(p1)}, xm[2] = {f2_to(m0), f2_to(m1)}, lm[2] = {f2_to(l0), f2_to(l1)};
-    gw_update(acc, n3, s, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+    if constexpr (ACCFF) {
+      F2 sq, cq;
+      ff_sincos(rate * tau, sq, cq);
+      const F2 dwf = {dw_hi, dw_lo};
+      const F2 wc = f2_add(f2_mul(dwf, cq), F2{0.f, 0.f}), ws = f2_add(f2_mul(dwf, sq), F2{0.f, 0.f});
+      float4 *acc = static_cast<float4 *>(accp);
+      float4 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
+      ff_axpy(a11, wc, p0, p1);
+      ff_axpy(a22, ws, m0, m1);
+      if (ref_compat) {
+        // a12 += ws X+ + wc X-, then a21 = a12 - wc (last X-)
+        ff_axpy(a12, ws, p0, p1);
+        ff_axpy(a12, wc, m0, m1);
+        a21 = a12;
+        ff_axpy(a21, f2_neg(wc), l0, l1);
+      } else {
+        ff_axpy(a21, ws, p0, p1);
+        ff_axpy(a12, wc, m0, m1);
+      }
+      acc[s] = a11;
+      acc[n3 + s] = a21;
+      acc[2 * n3 + s] = a12;
+      acc[3 * n3 + s] = a22;
+    } else {
+      double sq, cq;
+      sincos(rate * tau, &sq, &cq);
+      const double xp[2] = {f2_to(p0), f2_to(p1)}, xm[2] = {f2_to(m0), f2_to(m1)}, lm[2] = {f2_to(l0), f2_to(l1)};
+      gw_update(static_cast<double2 *>(accp), n3, s, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+    }
   }
 }
 
@@ -639,6 +729,10 @@ int axg_gw_init(axg_ctx *ctx) {
                  reinterpret_cast<float2 *>(ctx->gw_pol), ctx->gw_pol + 12 * nhalf);
     }
   }
+  // float-float accumulators where the transforms are float-float too: the
+  // whole Green accumulation then stays on the FP32 pipes but for the phase
+  // reduction
+  ctx->acc_ff = fp32 || (ctx->gw_pol != nullptr && axg_ff_use(n));
   int dims[3] = {n, n, n};
   AXG_CUFFT_TRY(ctx, cufftPlanMany(&ctx->plan_gsrc, 3, dims, nullptr, 1, (int)ctx->n3, nullptr, 1,
                                    (int)nhalf, fp32 ? CUFFT_R2C : CUFFT_D2Z, 6));
@@ -679,14 +773,23 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   else
     AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
-  if (tab && ff)
-    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate_tab<float4>, grid_for(ctx->n3), 256, 0,
-               reinterpret_cast<const float4 *>(ctx->gsrcF), reinterpret_cast<const float2 *>(ctx->gw_pol),
-               ctx->gw_pol + 12 * nhalf, n, dwav, tau, dw, ref, ctx->acc);
+  const float dw_hi = (float)dw, dw_lo = (float)(dw - (double)dw_hi);
+  const float2 *pol = reinterpret_cast<const float2 *>(ctx->gw_pol);
+  const double *rates = ctx->gw_pol + 12 * nhalf;
+  if (tab && ff && ctx->acc_ff)
+    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<float4, true>), grid_for(ctx->n3), 256, 0,
+               reinterpret_cast<const float4 *>(ctx->gsrcF), pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref,
+               (void *)ctx->acc);
+  else if (tab && ff)
+    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<float4, false>), grid_for(ctx->n3), 256, 0,
+               reinterpret_cast<const float4 *>(ctx->gsrcF), pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref,
+               (void *)ctx->acc);
+  else if (tab && ctx->acc_ff)
+    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<double2, true>), grid_for(ctx->n3), 256, 0,
+               (const double2 *)ctx->gsrcF, pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref, (void *)ctx->acc);
   else if (tab)
-    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate_tab<double2>, grid_for(ctx->n3), 256, 0,
-               (const double2 *)ctx->gsrcF, reinterpret_cast<const float2 *>(ctx->gw_pol), ctx->gw_pol + 12 * nhalf,
-               n, dwav, tau, dw, ref, ctx->acc);
+    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<double2, false>), grid_for(ctx->n3), 256, 0,
+               (const double2 *)ctx->gsrcF, pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref, (void *)ctx->acc);
   else
     AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate, grid_for(ctx->n3), 256, 0, ctx->gsrcF, n, dwav, tau, dw, ref,
                ctx->acc);
@@ -717,7 +820,7 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
   const int16_t *tab = nullptr;
   AXG_TRY(axg_bin_table(ctx, AXG_BIN_GW, n, dwav, dq, nb, log_bins, edges.data(), &tab));
   if (ctx->p.gw_mode == AXG_GW_GREEN) {
-    if (ctx->p.precision == AXG_PREC_FP32_MIXED)
+    if (ctx->acc_ff)
       AXG_LAUNCH(ctx, "gw_bin_green", k_gw_bin_green<float4>, 152 * 4, 256, 0, (const float4 *)ctx->acc, n, tab, nb,
                  d_num, d_den);
     else

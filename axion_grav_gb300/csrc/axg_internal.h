@@ -94,6 +94,8 @@ struct axg_ctx {
   float2 *gw_omega = nullptr;  // [n3] |k| dwav per k-site as float hi + lo (FP32-mixed Green mode)
   double *gw_pol = nullptr;    // FP64 Green mode: [12][n*n*(n/2+1)] float2 e+ (re, im as float-float), then
                                // [n*n*(n/2+1)] double |k| dwav; or null
+  bool acc_ff = false;         // Green accumulators are float-float float4 (FP32-mixed, and the FP64 paths
+                               // on the float-float transforms), else double2
   float *ff_tw = nullptr;      // float-float FFT twiddles W_n^k, k < n/2 (axg_fft_ff.cu)
   int ff_tw_n = 0;
   cufftHandle plan_gsrc = 0;
