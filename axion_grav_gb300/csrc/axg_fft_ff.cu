@@ -20,9 +20,9 @@
 //             outputs X[k] = E[k] + W_n^k O[k];
 //   y, z    : n-point FFTs along y and along z, 8 adjacent kx columns per
 //             CTA so every row of the tile is one 128-byte segment.
-// Each FFT is radix-2 decimation in time in shared memory (bit-reversed
-// load, natural-order result), twiddles W_n^k from a float-float table made
-// on the host in FP64.  Powers of two from 16 to 512.
+// Each FFT is decimation in time in shared memory (bit-reversed load,
+// natural-order result), radix-2 stages fused in pairs in registers,
+// twiddles W_n^k from a float-float table made on the host in FP64.  Powers of two from 16 to 512.
 #include <cmath>
 #include <cstdlib>
 #include <vector>
@@ -54,19 +54,60 @@ __host__ __device__ constexpr int log2c() {
   return L <= 1 ? 0 : 1 + log2c<L / 2>();
 }
 
-// In-place L-point forward FFTs of kLines interleaved lines in shared memory
+// In-place L-point FFTs of kLines interleaved lines in shared memory
 // (element i of line b at s[i * kLines + b]), input bit-reversed.  The
-// twiddle of stage h for butterfly m is W_L^(m L / 2h) = tw[m (L / 2h) ts],
-// tw being the W_(L ts)^k table.
+// radix-2 stages are taken in pairs (h, 2h): a thread holds the four
+// elements m, m + h, m + 2h, m + 3h of a 4h-group in registers and applies
+//   stage h : (a, b), (c, d) with W = W_2h^m,
+//   stage 2h: (a, c) with V = W_4h^m, (b, d) with V W_4h^h = -i V (+i V
+//             for the inverse),
+// so a pair of stages is one shared-memory round trip and one barrier; the
+// first pair (h = 1) needs no twiddle at all.  An odd stage count ends with
+// a radix-2 stage.  Twiddle W_L^k = tw[k ts], tw being the W_(L ts)^k table;
+// INV conjugates them (exp(+2 pi i k / L)).
+__device__ __forceinline__ float4 c_mul_mi(float4 a, bool inv) {  // a (-i), or a (+i) for the inverse
+  return inv ? make_float4(-a.z, -a.w, a.x, a.y) : make_float4(a.z, a.w, -a.x, -a.y);
+}
+
 template <int L, bool INV = false>
 __device__ __forceinline__ void fft_lines(float4 *s, const float4 *tw, int ts) {
-  for (int h = 1; h < L; h <<= 1) {
+  int h = 1;
+  for (; 4 * h <= L; h <<= 2) {
+    for (int idx = threadIdx.x; idx < kLines * (L / 4); idx += kThreads) {
+      const int b = idx % kLines, u = idx / kLines;
+      const int m = u & (h - 1), i0 = ((u - m) << 2) + m;
+      float4 x0 = s[i0 * kLines + b], x1 = s[(i0 + h) * kLines + b], x2 = s[(i0 + 2 * h) * kLines + b],
+             x3 = s[(i0 + 3 * h) * kLines + b];
+      if (h > 1) {
+        float4 w = tw[m * (L / (2 * h)) * ts];
+        if (INV) w = c_conj(w);
+        x1 = c_mul(w, x1);
+        x3 = c_mul(w, x3);
+      }
+      const float4 a1 = c_add(x0, x1), b1 = c_sub(x0, x1), c1 = c_add(x2, x3), d1 = c_sub(x2, x3);
+      float4 vc = c1, vd = d1;
+      if (h > 1) {
+        float4 v = tw[m * (L / (4 * h)) * ts];
+        if (INV) v = c_conj(v);
+        vc = c_mul(v, c1);
+        vd = c_mul(v, d1);
+      }
+      vd = c_mul_mi(vd, INV);
+      s[i0 * kLines + b] = c_add(a1, vc);
+      s[(i0 + 2 * h) * kLines + b] = c_sub(a1, vc);
+      s[(i0 + h) * kLines + b] = c_add(b1, vd);
+      s[(i0 + 3 * h) * kLines + b] = c_sub(b1, vd);
+    }
+    __syncthreads();
+  }
+  if (h < L) {  // one radix-2 stage left (h = L / 2)
     const int step = (L / (2 * h)) * ts;
     for (int idx = threadIdx.x; idx < kLines * (L / 2); idx += kThreads) {
       const int b = idx % kLines, q = idx / kLines;
       const int m = q & (h - 1), i0 = ((q - m) << 1) + m, i1 = i0 + h;
       const float4 x0 = s[i0 * kLines + b], x1 = s[i1 * kLines + b];
-      const float4 w = INV ? c_conj(tw[m * step]) : tw[m * step];  // inverse: exp(+2 pi i k / L)
+      float4 w = tw[m * step];
+      if (INV) w = c_conj(w);
       const float4 t = h == 1 ? x1 : c_mul(w, x1);
       s[i0 * kLines + b] = c_add(x0, t);
       s[i1 * kLines + b] = c_sub(x0, t);
