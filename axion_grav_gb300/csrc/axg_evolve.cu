@@ -17,6 +17,7 @@
 #include <cudaTypedefs.h>
 
 #include <cmath>
+#include <cstdlib>
 
 #include "axg_detmath.h"
 #include "axg_internal.h"
@@ -334,6 +335,118 @@ __device__ __forceinline__ void tma_phi(uint32_t dst, const CUtensorMap *m, int 
     tma_load_4d(dst, m, 0, x, y, z, bar);  // (re|im, x, y, z) doubles
 }
 
+// ---- per-site arithmetic of the fused step, shared by the TMA kernels and
+// the plain stencil kernel so every launch shape gives the same bits.  The
+// FP32 forms pin their fused multiply-adds with round-once intrinsics; the
+// FP64 forms use the reference's unfused operations in its order.
+
+// phi kick + drift at one site from its 7-point stencil; pd, cp: phi' and
+// the compensation of phi at the site (cp unused in FP64)
+__device__ __forceinline__ void site_phi(const FusedParams<float> &P, float2 c0, float2 xm, float2 xp, float2 ym,
+                                         float2 yp, float2 zm, float2 zp, float2 pd, float2 &cp, float2 &pdn,
+                                         float2 &pn) {
+  // difference-form Laplacian, Kahan drift
+  const float lr = ((xm.x - c0.x) + (xp.x - c0.x)) + ((ym.x - c0.x) + (yp.x - c0.x)) + ((zm.x - c0.x) + (zp.x - c0.x));
+  const float li = ((xm.y - c0.y) + (xp.y - c0.y)) + ((ym.y - c0.y) + (yp.y - c0.y)) + ((zm.y - c0.y) + (zp.y - c0.y));
+  const float s2 = __fmaf_rn(c0.x, c0.x, __fmul_rn(c0.y, c0.y));
+  const float g = __fmaf_rn(P.A, s2, P.B);
+  const float vr = __fadd_rn(__fmaf_rn(g, c0.x, __fmul_rn(P.D, c0.x)), P.C);
+  const float vi = __fmaf_rn(g, c0.y, -__fmul_rn(P.D, c0.y));
+  pdn.x = __fmaf_rn(P.f3, vr, __fmaf_rn(P.f2, lr, __fmul_rn(P.f1, pd.x)));
+  pdn.y = __fmaf_rn(P.f3, vi, __fmaf_rn(P.f2, li, __fmul_rn(P.f1, pd.y)));
+  pn = c0;
+  kahan_add(pn.x, cp.x, __fmul_rn(P.dtd, pdn.x));
+  kahan_add(pn.y, cp.y, __fmul_rn(P.dtd, pdn.y));
+}
+
+__device__ __forceinline__ void site_phi(const FusedParams<double> &P, double2 c0, double2 xm, double2 xp,
+                                         double2 ym, double2 yp, double2 zm, double2 zp, double2 pd, double2 &,
+                                         double2 &pdn, double2 &pn) {
+  double lr = AXD_ADD(xm.x, xp.x);
+  lr = AXD_ADD(lr, ym.x);
+  lr = AXD_ADD(lr, yp.x);
+  lr = AXD_ADD(lr, zm.x);
+  lr = AXD_ADD(lr, zp.x);
+  lr = AXD_SUB(lr, AXD_MUL(6.0, c0.x));
+  double li = AXD_ADD(xm.y, xp.y);
+  li = AXD_ADD(li, ym.y);
+  li = AXD_ADD(li, yp.y);
+  li = AXD_ADD(li, zm.y);
+  li = AXD_ADD(li, zp.y);
+  li = AXD_SUB(li, AXD_MUL(6.0, c0.y));
+  const double s2 = AXD_ADD(AXD_MUL(c0.x, c0.x), AXD_MUL(c0.y, c0.y));
+  const double g = AXD_ADD(AXD_MUL(P.A, s2), P.B);
+  double vr = AXD_MUL(g, c0.x), vi = AXD_MUL(g, c0.y);
+  if (P.D != 0.0) {
+    vr = AXD_ADD(vr, AXD_MUL(P.D, c0.x));
+    vi = AXD_SUB(vi, AXD_MUL(P.D, c0.y));
+  }
+  vr = AXD_ADD(vr, P.C);
+  double pr = AXD_ADD(AXD_MUL(P.f1, pd.x), AXD_MUL(P.f2, lr));
+  pr = AXD_ADD(pr, AXD_MUL(P.f3, vr));
+  double pi_ = AXD_ADD(AXD_MUL(P.f1, pd.y), AXD_MUL(P.f2, li));
+  pi_ = AXD_ADD(pi_, AXD_MUL(P.f3, vi));
+  pdn = make_double2(pr, pi_);
+  pn = make_double2(AXD_ADD(c0.x, AXD_MUL(P.dtd, pr)), AXD_ADD(c0.y, AXD_MUL(P.dtd, pi_)));
+}
+
+// the six sources S_c (c = (1,1),(2,1),(2,2),(3,1),(3,2),(3,3)) at one site
+// from the phi differences; FP32: raw differences (1 / (2dx)^2 and the
+// factor 2 are folded into fsc); FP64: the reference's (d_i phi)(d_j phi)*
+// with d = 2 dx and the factor 2
+__device__ __forceinline__ void site_sources(const FusedParams<float> &, float2 xm, float2 xp, float2 ym, float2 yp,
+                                             float2 zm, float2 zp, float S[6]) {
+  const float gxr = xp.x - xm.x, gxi = xp.y - xm.y;
+  const float gyr = yp.x - ym.x, gyi = yp.y - ym.y;
+  const float gzr = zp.x - zm.x, gzi = zp.y - zm.y;
+  S[0] = __fmaf_rn(gxr, gxr, __fmul_rn(gxi, gxi));
+  S[1] = __fmaf_rn(gyr, gxr, __fmul_rn(gyi, gxi));
+  S[2] = __fmaf_rn(gyr, gyr, __fmul_rn(gyi, gyi));
+  S[3] = __fmaf_rn(gzr, gxr, __fmul_rn(gzi, gxi));
+  S[4] = __fmaf_rn(gzr, gyr, __fmul_rn(gzi, gyi));
+  S[5] = __fmaf_rn(gzr, gzr, __fmul_rn(gzi, gzi));
+}
+
+__device__ __forceinline__ void site_sources(const FusedParams<double> &P, double2 xm, double2 xp, double2 ym,
+                                             double2 yp, double2 zm, double2 zp, double S[6]) {
+  double dr[3], di[3];
+  dr[0] = div_d(AXD_SUB(xp.x, xm.x), P.d, P.inv_d, P.d_pow2);
+  di[0] = div_d(AXD_SUB(xp.y, xm.y), P.d, P.inv_d, P.d_pow2);
+  dr[1] = div_d(AXD_SUB(yp.x, ym.x), P.d, P.inv_d, P.d_pow2);
+  di[1] = div_d(AXD_SUB(yp.y, ym.y), P.d, P.inv_d, P.d_pow2);
+  dr[2] = div_d(AXD_SUB(zp.x, zm.x), P.d, P.inv_d, P.d_pow2);
+  di[2] = div_d(AXD_SUB(zp.y, zm.y), P.d, P.inv_d, P.d_pow2);
+  int c = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j, ++c) S[c] = axg_mul_pow2(AXD_ADD(AXD_MUL(dr[i], dr[j]), AXD_MUL(di[i], di[j])), 2.0);
+}
+
+// one u_ij component: kick with source S, drift (FP32: Kahan with cc)
+__device__ __forceinline__ void site_u(const FusedParams<float> &P, float S, float uc, float uxm, float uxp,
+                                       float uym, float uyp, float uzm, float uzp, float udv, float &cc, float &udn,
+                                       float &un) {
+  const float lu = ((uxm - uc) + (uxp - uc)) + ((uym - uc) + (uyp - uc)) + ((uzm - uc) + (uzp - uc));
+  udn = __fmaf_rn(P.fsc, S, __fmaf_rn(P.f2, lu, __fmul_rn(P.f1, udv)));
+  un = uc;
+  kahan_add(un, cc, __fmul_rn(P.dtd, udn));
+}
+
+__device__ __forceinline__ void site_u(const FusedParams<double> &P, double S, double uc, double uxm, double uxp,
+                                       double uym, double uyp, double uzm, double uzp, double udv, double &,
+                                       double &udn, double &un) {
+  double lu = AXD_ADD(uxm, uxp);
+  lu = AXD_ADD(lu, uym);
+  lu = AXD_ADD(lu, uyp);
+  lu = AXD_ADD(lu, uzm);
+  lu = AXD_ADD(lu, uzp);
+  lu = AXD_SUB(lu, AXD_MUL(6.0, uc));
+  double v = AXD_ADD(AXD_MUL(P.f1, udv), AXD_MUL(P.f2, lu));
+  udn = AXD_ADD(v, AXD_MUL(P.fsc, S));
+  un = AXD_ADD(uc, AXD_MUL(P.dtd, udn));
+}
+
 // One TX x TY column of zc planes starting at (x0, y0, z0): stage the
 // stencil planes by TMA, compute kick + drift, store.  `gplane` counts the
 // planes this CTA has staged so far, so stage indices and mbarrier phases
@@ -471,132 +584,35 @@ __device__ __forceinline__ bool fused_column(const CUtensorMap *tm_prow, const C
       const V zm = reinterpret_cast<const V *>(sp + L::phi_main)[(ty + 1) * TX + tx];
       const V zp = reinterpret_cast<const V *>(sn + L::phi_main)[(ty + 1) * TX + tx];
 
-      if constexpr (sizeof(R) == 4) {
-        // ---- FP32-mixed: difference-form Laplacian, Kahan drift ----
-        const float lr = ((xm.x - c0.x) + (xp.x - c0.x)) + ((ym.x - c0.x) + (yp.x - c0.x)) +
-                         ((zm.x - c0.x) + (zp.x - c0.x));
-        const float li = ((xm.y - c0.y) + (xp.y - c0.y)) + ((ym.y - c0.y) + (yp.y - c0.y)) +
-                         ((zm.y - c0.y) + (zp.y - c0.y));
-        const float s2 = c0.x * c0.x + c0.y * c0.y;
-        const float g = P.A * s2 + P.B;
-        const float vr = g * c0.x + P.D * c0.x + P.C;
-        const float vi = g * c0.y - P.D * c0.y;
-        V pdn;
-        pdn.x = P.f1 * pd.x + P.f2 * lr + P.f3 * vr;
-        pdn.y = P.f1 * pd.y + P.f2 * li + P.f3 * vi;
-        V pn = c0;
-        kahan_add(pn.x, cp.x, P.dtd * pdn.x);
-        kahan_add(pn.y, cp.y, P.dtd * pdn.y);
-        P.phid[s] = pdn;
-        P.cphi[s] = cp;
-        P.phi_out[s] = pn;
-        if constexpr (UIJ) {
-          const float gxr = xp.x - xm.x, gxi = xp.y - xm.y;
-          const float gyr = yp.x - ym.x, gyi = yp.y - ym.y;
-          const float gzr = zp.x - zm.x, gzi = zp.y - zm.y;
-          float S[6];
-          S[0] = gxr * gxr + gxi * gxi;
-          S[1] = gyr * gxr + gyi * gxi;
-          S[2] = gyr * gyr + gyi * gyi;
-          S[3] = gzr * gxr + gzi * gxi;
-          S[4] = gzr * gyr + gzi * gyi;
-          S[5] = gzr * gzr + gzi * gzi;
-          const float *ub = reinterpret_cast<const float *>(sc + L::u_body);
-          const float *ut = reinterpret_cast<const float *>(sc + L::u_top);
-          const float *ubt = reinterpret_cast<const float *>(sc + L::u_bot);
-          const float *uhl = reinterpret_cast<const float *>(sc + L::u_hl);
-          const float *uhr = reinterpret_cast<const float *>(sc + L::u_hr);
-          const float *ubp = reinterpret_cast<const float *>(sp + L::u_body);
-          const float *ubn = reinterpret_cast<const float *>(sn + L::u_body);
+      V pdn, pn;
+      site_phi(P, c0, xm, xp, ym, yp, zm, zp, pd, cp, pdn, pn);
+      P.phid[s] = pdn;
+      if constexpr (sizeof(R) == 4) P.cphi[s] = cp;
+      P.phi_out[s] = pn;
+      if constexpr (UIJ) {
+        R S[6];
+        site_sources(P, xm, xp, ym, yp, zm, zp, S);
+        const R *ub = reinterpret_cast<const R *>(sc + L::u_body);
+        const R *ut = reinterpret_cast<const R *>(sc + L::u_top);
+        const R *ubt = reinterpret_cast<const R *>(sc + L::u_bot);
+        const R *uhl = reinterpret_cast<const R *>(sc + L::u_hl);
+        const R *uhr = reinterpret_cast<const R *>(sc + L::u_hr);
+        const R *ubp = reinterpret_cast<const R *>(sp + L::u_body);
+        const R *ubn = reinterpret_cast<const R *>(sn + L::u_body);
 #pragma unroll
-          for (int c = 0; c < 6; ++c) {
-            const int o = (c * TY + ty) * TX + tx;
-            const float uc = ub[o];
-            const float uxm = tx > 0 ? ub[o - 1] : uhl[(c * TY + ty) * L::UHW + L::UHW - 1];
-            const float uxp = tx < TX - 1 ? ub[o + 1] : uhr[(c * TY + ty) * L::UHW];
-            const float uym = ty > 0 ? ub[o - TX] : ut[c * TX + tx];
-            const float uyp = ty < TY - 1 ? ub[o + TX] : ubt[c * TX + tx];
-            const float uzm = ubp[o], uzp = ubn[o];
-            const float lu = ((uxm - uc) + (uxp - uc)) + ((uym - uc) + (uyp - uc)) +
-                             ((uzm - uc) + (uzp - uc));
-            const float udn = P.f1 * udv[c] + P.f2 * lu + P.fsc * S[c];
-            float un = uc, cc = cuv[c];
-            kahan_add(un, cc, P.dtd * udn);
-            P.ud[c * P.n3 + s] = udn;
-            P.cu[c * P.n3 + s] = cc;
-            P.u_out[c * P.n3 + s] = un;
-          }
-        }
-      } else {
-        // ---- FP64-fused: same operations and order as the plain kernels ----
-        double lr = AXD_ADD(xm.x, xp.x);
-        lr = AXD_ADD(lr, ym.x);
-        lr = AXD_ADD(lr, yp.x);
-        lr = AXD_ADD(lr, zm.x);
-        lr = AXD_ADD(lr, zp.x);
-        lr = AXD_SUB(lr, AXD_MUL(6.0, c0.x));
-        double li = AXD_ADD(xm.y, xp.y);
-        li = AXD_ADD(li, ym.y);
-        li = AXD_ADD(li, yp.y);
-        li = AXD_ADD(li, zm.y);
-        li = AXD_ADD(li, zp.y);
-        li = AXD_SUB(li, AXD_MUL(6.0, c0.y));
-        const double s2 = AXD_ADD(AXD_MUL(c0.x, c0.x), AXD_MUL(c0.y, c0.y));
-        const double g = AXD_ADD(AXD_MUL(P.A, s2), P.B);
-        double vr = AXD_MUL(g, c0.x), vi = AXD_MUL(g, c0.y);
-        if (P.D != 0.0) {
-          vr = AXD_ADD(vr, AXD_MUL(P.D, c0.x));
-          vi = AXD_SUB(vi, AXD_MUL(P.D, c0.y));
-        }
-        vr = AXD_ADD(vr, P.C);
-        double pr = AXD_ADD(AXD_MUL(P.f1, pd.x), AXD_MUL(P.f2, lr));
-        pr = AXD_ADD(pr, AXD_MUL(P.f3, vr));
-        double pi_ = AXD_ADD(AXD_MUL(P.f1, pd.y), AXD_MUL(P.f2, li));
-        pi_ = AXD_ADD(pi_, AXD_MUL(P.f3, vi));
-        P.phid[s] = make_double2(pr, pi_);
-        P.phi_out[s] =
-            make_double2(AXD_ADD(c0.x, AXD_MUL(P.dtd, pr)), AXD_ADD(c0.y, AXD_MUL(P.dtd, pi_)));
-        if constexpr (UIJ) {
-          double dr[3], di[3];
-          dr[0] = div_d(AXD_SUB(xp.x, xm.x), P.d, P.inv_d, P.d_pow2);
-          di[0] = div_d(AXD_SUB(xp.y, xm.y), P.d, P.inv_d, P.d_pow2);
-          dr[1] = div_d(AXD_SUB(yp.x, ym.x), P.d, P.inv_d, P.d_pow2);
-          di[1] = div_d(AXD_SUB(yp.y, ym.y), P.d, P.inv_d, P.d_pow2);
-          dr[2] = div_d(AXD_SUB(zp.x, zm.x), P.d, P.inv_d, P.d_pow2);
-          di[2] = div_d(AXD_SUB(zp.y, zm.y), P.d, P.inv_d, P.d_pow2);
-          const double *ub = reinterpret_cast<const double *>(sc + L::u_body);
-          const double *ut = reinterpret_cast<const double *>(sc + L::u_top);
-          const double *ubt = reinterpret_cast<const double *>(sc + L::u_bot);
-          const double *uhl = reinterpret_cast<const double *>(sc + L::u_hl);
-          const double *uhr = reinterpret_cast<const double *>(sc + L::u_hr);
-          const double *ubp = reinterpret_cast<const double *>(sp + L::u_body);
-          const double *ubn = reinterpret_cast<const double *>(sn + L::u_body);
-          int c = 0;
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-#pragma unroll
-            for (int j = 0; j <= i; ++j, ++c) {
-              const int o = (c * TY + ty) * TX + tx;
-              const double uc = ub[o];
-              const double uxm = tx > 0 ? ub[o - 1] : uhl[(c * TY + ty) * L::UHW + L::UHW - 1];
-              const double uxp = tx < TX - 1 ? ub[o + 1] : uhr[(c * TY + ty) * L::UHW];
-              const double uym = ty > 0 ? ub[o - TX] : ut[c * TX + tx];
-              const double uyp = ty < TY - 1 ? ub[o + TX] : ubt[c * TX + tx];
-              const double uzm = ubp[o], uzp = ubn[o];
-              double src = AXD_ADD(AXD_MUL(dr[i], dr[j]), AXD_MUL(di[i], di[j]));
-              src = axg_mul_pow2(src, 2.0);
-              double lu = AXD_ADD(uxm, uxp);
-              lu = AXD_ADD(lu, uym);
-              lu = AXD_ADD(lu, uyp);
-              lu = AXD_ADD(lu, uzm);
-              lu = AXD_ADD(lu, uzp);
-              lu = AXD_SUB(lu, AXD_MUL(6.0, uc));
-              double v = AXD_ADD(AXD_MUL(P.f1, udv[c]), AXD_MUL(P.f2, lu));
-              v = AXD_ADD(v, AXD_MUL(P.fsc, src));
-              P.ud[c * P.n3 + s] = v;
-              P.u_out[c * P.n3 + s] = AXD_ADD(uc, AXD_MUL(P.dtd, v));
-            }
-          }
+        for (int c = 0; c < 6; ++c) {
+          const int o = (c * TY + ty) * TX + tx;
+          const R uc = ub[o];
+          const R uxm = tx > 0 ? ub[o - 1] : uhl[(c * TY + ty) * L::UHW + L::UHW - 1];
+          const R uxp = tx < TX - 1 ? ub[o + 1] : uhr[(c * TY + ty) * L::UHW];
+          const R uym = ty > 0 ? ub[o - TX] : ut[c * TX + tx];
+          const R uyp = ty < TY - 1 ? ub[o + TX] : ubt[c * TX + tx];
+          const R uzm = ubp[o], uzp = ubn[o];
+          R cc = sizeof(R) == 4 ? cuv[c] : R(0), udn, un;
+          site_u(P, S[c], uc, uxm, uxp, uym, uyp, uzm, uzp, udv[c], cc, udn, un);
+          P.ud[c * P.n3 + s] = udn;
+          if constexpr (sizeof(R) == 4) P.cu[c * P.n3 + s] = cc;
+          P.u_out[c * P.n3 + s] = un;
         }
       }
     }
@@ -711,6 +727,52 @@ __global__ void __launch_bounds__(TX *TY, (sizeof(R) == 4 && TX * TY <= 256 ? 2 
                                           (col % ncx) * TX, (col / ncx) * TY, chunk * zc, smem, bars, gplane, pwsmem,
                                           bars + kStages, gpw))
       return;
+  }
+}
+
+// ------------------------------------------------------------------------
+// The fused step as a plain stencil kernel: one thread per site, the stencil
+// read from global memory (through L1 / L2).  It serves lattices that no TMA
+// tile shape fits (N not a multiple of 32) and runs the same per-site
+// arithmetic as the tiled kernels, so it gives the same bits.
+// ------------------------------------------------------------------------
+template <typename R, bool UIJ>
+__global__ void __launch_bounds__(256) k_fused_plain(const typename V2<R>::T *__restrict__ phi_in,
+                                                     const R *__restrict__ u_in, FusedParams<R> P) {
+  using V = typename V2<R>::T;
+  const int n = P.n;
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y, iz = blockIdx.z;
+  if (ix >= n || iy >= n) return;
+  const int64_t n2 = (int64_t)n * n;
+  const int xm1 = ix == 0 ? n - 1 : ix - 1, xp1 = ix + 1 == n ? 0 : ix + 1;
+  const int ym1 = iy == 0 ? n - 1 : iy - 1, yp1 = iy + 1 == n ? 0 : iy + 1;
+  const int zm1 = iz == 0 ? n - 1 : iz - 1, zp1 = iz + 1 == n ? 0 : iz + 1;
+  const int64_t row = (int64_t)iz * n2 + (int64_t)iy * n;
+  const int64_t s = row + ix, sxm = row + xm1, sxp = row + xp1;
+  const int64_t sym = (int64_t)iz * n2 + (int64_t)ym1 * n + ix, syp = (int64_t)iz * n2 + (int64_t)yp1 * n + ix;
+  const int64_t szm = (int64_t)zm1 * n2 + (int64_t)iy * n + ix, szp = (int64_t)zp1 * n2 + (int64_t)iy * n + ix;
+  const V c0 = phi_in[s], xm = phi_in[sxm], xp = phi_in[sxp], ym = phi_in[sym], yp = phi_in[syp], zm = phi_in[szm],
+          zp = phi_in[szp];
+  const V pd = P.phid[s];
+  V cp{};
+  if constexpr (sizeof(R) == 4) cp = P.cphi[s];
+  V pdn, pn;
+  site_phi(P, c0, xm, xp, ym, yp, zm, zp, pd, cp, pdn, pn);
+  P.phid[s] = pdn;
+  if constexpr (sizeof(R) == 4) P.cphi[s] = cp;
+  P.phi_out[s] = pn;
+  if constexpr (UIJ) {
+    R S[6];
+    site_sources(P, xm, xp, ym, yp, zm, zp, S);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const R *u = u_in + c * P.n3;
+      R cc = sizeof(R) == 4 ? P.cu[c * P.n3 + s] : R(0), udn, un;
+      site_u(P, S[c], u[s], u[sxm], u[sxp], u[sym], u[syp], u[szm], u[szp], P.ud[c * P.n3 + s], cc, udn, un);
+      P.ud[c * P.n3 + s] = udn;
+      if constexpr (sizeof(R) == 4) P.cu[c * P.n3 + s] = cc;
+      P.u_out[c * P.n3 + s] = un;
+    }
   }
 }
 
@@ -950,15 +1012,17 @@ int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd) {
   if (ctx->p.precision == AXG_PREC_FP64_PLAIN)
     return axg_set_error(ctx, AXG_ERR_STATE, "fused step requested on the FP64-plain path");
   int cfg = ctx->tile_cfg >= 0 ? ctx->tile_cfg : axg_evo_default_tile(ctx);
-  if (cfg < 0 || !axg_evo_tile_supported(ctx, cfg))
-    return axg_set_error(ctx, AXG_ERR_UNSUPPORTED,
-                         "lattice size has no supported fused tile (N must be a multiple of 32)");
-  AXG_TRY(build_tmaps(ctx, cfg));
+  // no TMA tile shape fits (N not a multiple of 32): the plain stencil
+  // kernel; AXG_FUSED_PLAIN=1 selects it for any N (tests compare the two)
+  const char *pe = std::getenv("AXG_FUSED_PLAIN");
+  const bool plain = cfg < 0 || !axg_evo_tile_supported(ctx, cfg) || (pe && pe[0] == '1');
+  if (!plain) AXG_TRY(build_tmaps(ctx, cfg));
   double f[4], pot[4];
   axg_kick_coeffs(&ctx->p, t, dt, f, pot);
   const bool uij = ctx->p.gw_mode == AXG_GW_UIJ;
   const int b = ctx->cur, o = 1 - b;
-  const axg_tile_cfg tc = kTiles[cfg];
+  const axg_tile_cfg tc = plain ? axg_tile_cfg{32, 8, 1, 0} : kTiles[cfg];
+  const dim3 pblock(32, 8), pgrid((unsigned)((ctx->n + 31) / 32), (unsigned)((ctx->n + 7) / 8), (unsigned)ctx->n);
   if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
     FusedParams<float> P;
     P.phi_out = (float2 *)ctx->phi[o];
@@ -984,7 +1048,13 @@ int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd) {
     P.inv_d = 1.0 / P.d;
     P.d_pow2 = 0;
     P.err = ctx->d_err;
-    if (uij) AXG_TRY((launch_fused_cfg<float, true>(ctx, P, cfg, "fused_kd_fp32_uij")));
+    if (plain && uij)
+      AXG_LAUNCH(ctx, "fused_kd_fp32_uij_plain", (k_fused_plain<float, true>), pgrid, pblock, 0,
+                 (const float2 *)ctx->phi[b], (const float *)ctx->u[b], P);
+    else if (plain)
+      AXG_LAUNCH(ctx, "fused_kd_fp32_phi_plain", (k_fused_plain<float, false>), pgrid, pblock, 0,
+                 (const float2 *)ctx->phi[b], (const float *)ctx->u[b], P);
+    else if (uij) AXG_TRY((launch_fused_cfg<float, true>(ctx, P, cfg, "fused_kd_fp32_uij")));
     else AXG_TRY((launch_fused_cfg<float, false>(ctx, P, cfg, "fused_kd_fp32_phi")));
   } else {
     FusedParams<double> P;
@@ -1011,7 +1081,13 @@ int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd) {
     P.d_pow2 = std::frexp(P.d, &ex) == 0.5;
     P.inv_d = 1.0 / P.d;
     P.err = ctx->d_err;
-    if (uij) AXG_TRY((launch_fused_cfg<double, true>(ctx, P, cfg, "fused_kd_fp64_uij")));
+    if (plain && uij)
+      AXG_LAUNCH(ctx, "fused_kd_fp64_uij_plain", (k_fused_plain<double, true>), pgrid, pblock, 0,
+                 (const double2 *)ctx->phi[b], (const double *)ctx->u[b], P);
+    else if (plain)
+      AXG_LAUNCH(ctx, "fused_kd_fp64_phi_plain", (k_fused_plain<double, false>), pgrid, pblock, 0,
+                 (const double2 *)ctx->phi[b], (const double *)ctx->u[b], P);
+    else if (uij) AXG_TRY((launch_fused_cfg<double, true>(ctx, P, cfg, "fused_kd_fp64_uij")));
     else AXG_TRY((launch_fused_cfg<double, false>(ctx, P, cfg, "fused_kd_fp64_phi")));
   }
   ctx->cur = o;

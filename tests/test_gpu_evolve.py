@@ -149,7 +149,54 @@ def test_fp32_mixed_identical_on_all_tiles(gw):
     assert tested >= 4 and pw >= 2
 
 
-@pytest.mark.parametrize("n", [32, 64])
+@pytest.mark.parametrize("n", [24, 48])
+@pytest.mark.parametrize("gw", [ag.GW_NONE, ag.GW_UIJ])
+def test_fp64_fused_plain_kernel_bit_exact(n, gw):
+    """N not a multiple of 32 has no TMA tile: the plain stencil kernel runs
+    the fused step with the same operations, bit for bit."""
+    p = make_params(n, ag.PREC_FP64_FUSED, gw)
+    st = random_state(n, 5, 0.05)
+    phi, phid, u, ud = (a.copy() for a in st)
+    axo.leapfrog(p, phi, phid, u if gw else None, ud, None, 1.5, 0.02, 5, True, True)
+
+    def fn(lat):
+        lat.set_kernel_timing(True)
+        lat.leapfrog(1.5, 0.02, 5, True, True)
+        lat.synchronize()
+        return dict((k, l) for k, l, _ in lat.kernel_timings())
+    g_phi, g_phid, g_u, g_ud, kt, _ = run_gpu(p, st, fn)
+    assert kt.get("fused_kd_fp64_%s_plain" % ("uij" if gw else "phi"), 0) == 5
+    assert np.array_equal(g_phi, phi) and np.array_equal(g_phid, phid)
+    if gw:
+        assert np.array_equal(g_u, u) and np.array_equal(g_ud, ud)
+
+
+@pytest.mark.parametrize("prec", [ag.PREC_FP32_MIXED, ag.PREC_FP64_FUSED])
+@pytest.mark.parametrize("gw", [ag.GW_NONE, ag.GW_UIJ])
+def test_plain_kernel_identical_to_tma_tiles(prec, gw, monkeypatch):
+    """AXG_FUSED_PLAIN=1 forces the plain stencil kernel at N = 64; its
+    per-site arithmetic is the tiled kernels' own, so the bits agree."""
+    n = 64
+    p = make_params(n, prec, gw)
+    st = random_state(n, 6, 0.05)
+    run = lambda lat: lat.leapfrog(1.5, 0.02, 6, True, True)
+    ref = run_gpu(p, st, run)
+    monkeypatch.setenv("AXG_FUSED_PLAIN", "1")
+
+    def fn(lat):
+        lat.set_kernel_timing(True)
+        run(lat)
+        lat.synchronize()
+        return dict((k, l) for k, l, _ in lat.kernel_timings())
+    out = run_gpu(p, st, fn)
+    name = "fused_kd_%s_%s_plain" % ("fp32" if prec == ag.PREC_FP32_MIXED else "fp64", "uij" if gw else "phi")
+    assert out[4].get(name, 0) == 6
+    for a, b in zip(out[:4], ref[:4]):
+        if a is not None:
+            assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("n", [32, 48, 64])
 def test_fp32_mixed_matches_fp64_oracle(n):
     """FP32 fields and stencil with Kahan drift: tolerance against FP64."""
     p64 = make_params(n, ag.PREC_FP64_PLAIN, ag.GW_UIJ)
@@ -335,7 +382,9 @@ def test_autotune_restores_state():
 def test_bad_params_raise():
     with pytest.raises(ag.AxgError):
         ag.Lattice(make_params(15, ag.PREC_FP64_PLAIN))
-    p = make_params(48, ag.PREC_FP32_MIXED)  # not a multiple of 32: no fused tile
+    p = make_params(48, ag.PREC_FP32_MIXED)  # not a multiple of 32: no TMA tile to select
     with ag.Lattice(p) as lat:
         with pytest.raises(ag.AxgError, match="UNSUPPORTED"):
-            lat.leapfrog(1.0, 0.01, 1)
+            lat.set_tile(0)
+        with pytest.raises(ag.AxgError, match="UNSUPPORTED"):
+            lat.autotune(1)
