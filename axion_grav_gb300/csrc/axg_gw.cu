@@ -342,31 +342,122 @@ __device__ __forceinline__ void ff_axpy(float4 &a, F2 w, F2 xr, F2 xi) {
 // ACCFF: the accumulators are float-float (float4) as in the FP32-mixed path,
 // the phase sin / cos are float-float (ff_sincos) and the updates run in
 // float-float, so a k-site issues about ten FP64 operations.
+// The contraction of one k-site from float-float polarisation parts er, ei
+// and the stored source spectrum entry h: p = X+, m = X-, l = the last
+// component's X-.  neg_si: the stored entry is S(k)'s conjugate (k in the
+// stored half), so its imaginary part changes sign.
+template <typename SRC>
+__device__ __forceinline__ void ff_contract(const SRC *__restrict__ srcF, int64_t nhalf, int64_t h, const F2 er[6],
+                                            const F2 ei[6], bool neg_si, F2 &p0, F2 &p1, F2 &m0, F2 &m1, F2 &l0,
+                                            F2 &l1) {
+  p0 = p1 = m0 = m1 = l0 = l1 = F2{0.f, 0.f};
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    F2 sr, si;
+    src_ff(srcF[c * nhalf + h], sr, si);
+    if (neg_si) si = f2_neg(si);
+    // a = er sr, b = ei si, e = er si, g = ei sr: X+ += (a - b, e + g), X- += (a + b, e - g)
+    const F2 t0 = f2_dot2(er[c], sr, ei[c], si, -1.f), t1 = f2_dot2(er[c], si, ei[c], sr, 1.f);
+    const F2 t2 = f2_dot2(er[c], sr, ei[c], si, 1.f), t3 = f2_dot2(er[c], si, ei[c], sr, -1.f);
+    p0 = f2_add(p0, t0);
+    p1 = f2_add(p1, t1);
+    m0 = f2_add(m0, t2);
+    m1 = f2_add(m1, t3);
+    if (c == 5) {
+      l0 = t2;
+      l1 = t3;
+    }
+  }
+}
+
+// float-float accumulators at site s: a11 += wc X+, a22 += ws X-, and a12,
+// a21 as in gw_update
+__device__ __forceinline__ void ff_update(float4 *__restrict__ acc, int64_t n3, int64_t s, F2 wc, F2 ws, F2 p0,
+                                          F2 p1, F2 m0, F2 m1, F2 l0, F2 l1, int ref_compat) {
+  float4 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
+  ff_axpy(a11, wc, p0, p1);
+  ff_axpy(a22, ws, m0, m1);
+  if (ref_compat) {
+    // a12 += ws X+ + wc X-, then a21 = a12 - wc (last X-)
+    ff_axpy(a12, ws, p0, p1);
+    ff_axpy(a12, wc, m0, m1);
+    a21 = a12;
+    ff_axpy(a21, f2_neg(wc), l0, l1);
+  } else {
+    ff_axpy(a21, ws, p0, p1);
+    ff_axpy(a12, wc, m0, m1);
+  }
+  acc[s] = a11;
+  acc[n3 + s] = a21;
+  acc[2 * n3 + s] = a12;
+  acc[3 * n3 + s] = a22;
+}
+
+// Full-array index of the site whose wave vector indices negate those of
+// half-spectrum entry (hx, hy, hz), 0 < hx < n/2.
+__device__ __forceinline__ int64_t gw_mirror_site(int hx, int hy, int hz, int n) {
+  return ((int64_t)(hz == 0 ? 0 : n - hz) * n + (hy == 0 ? 0 : n - hy)) * n + (n - hx);
+}
+
+// Green accumulation with the polarisation table: the contraction
+// X+- = sum e+- S runs in float-float on the FP32 pipes (four f2_dot2 per
+// component), the phase sin / cos and the accumulator updates in FP64.
+//
+// ACCFF: the accumulators are float-float (float4) as in the FP32-mixed path,
+// the phase sin / cos are float-float (ff_sincos) and the updates run in
+// float-float, so a k-site issues about ten FP64 operations.
+//
+// One thread per stored half-spectrum entry h = (hx, hy, hz) updates the site
+// k itself and, for 0 < hx < n/2, the site of -k in the other half.  There
+// S(-k) = conj S(k) (real sources) and e+(-k) = conj e+(k), so X+-(-k) =
+// conj X+-(k): the negations are exact, so the mirrored site gets the bits a
+// contraction of its own would give, and the table entry, the six source
+// values and the phase are read and formed once for the pair.  When hy or hz
+// is the Nyquist index n/2 the mirrored site's wave vector index maps to
+// itself (kint(n/2) = -n/2) and is not -k: its polarisation is formed
+// directly.  |k|, and so the phase, is the same at both sites.
 template <typename SRC, bool ACCFF>
 __global__ void k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *__restrict__ pol,
                                     const double *__restrict__ rates, int n, double dwav, double tau, double dw,
                                     float dw_hi, float dw_lo, int ref_compat, void *__restrict__ accp) {
-  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
-  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+  const int nh = n / 2 + 1;
+  const int64_t n3 = (int64_t)n * n * n;
+  const int64_t nhalf = (int64_t)n * n * nh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-    const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
-    bool conj_back;
-    const int64_t hidx = gw_half_index(ix, iy, iz, n, conj_back);
-    F2 er[6], ei[6];
-    double rate;
-    // The stored entry is k's (conj_back) or -k's.  A Nyquist y or z index
-    // maps to itself, so there the entry is not -k's: form those directly.
-    if (conj_back || (iy != n / 2 && iz != n / 2)) {
-      rate = rates[hidx];
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const float2 a = pol[c * nhalf + hidx], b = pol[(6 + c) * nhalf + hidx];
-        er[c] = {a.x, a.y};
-        ei[c] = conj_back ? F2{b.x, b.y} : F2{-b.x, -b.y};
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
+    const int hx = (int)(h % nh), hy = (int)((h / nh) % n), hz = (int)(h / ((int64_t)nh * n));
+    const int64_t s1 = ((int64_t)hz * n + hy) * n + hx;
+    const bool mirror = hx > 0 && hx < n / 2;
+    const double rate = rates[h];
+    if (!(rate > 0)) {
+      // k = 0 (h = 0, no mirror): every e_ij is 0; the cross-wired REF
+      // updates still copy a12 into a21
+      if (ref_compat) {
+        if constexpr (ACCFF) {
+          float4 *acc = static_cast<float4 *>(accp);
+          acc[n3 + s1] = acc[2 * n3 + s1];
+        } else {
+          double2 *acc = static_cast<double2 *>(accp);
+          acc[n3 + s1] = acc[2 * n3 + s1];
+        }
       }
-    } else {
-      const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
+      continue;
+    }
+    F2 er[6], ei[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const float2 a = pol[c * nhalf + h], b = pol[(6 + c) * nhalf + h];
+      er[c] = {a.x, a.y};
+      ei[c] = {b.x, b.y};
+    }
+    F2 p0, p1, m0, m1, l0, l1;
+    ff_contract(srcF, nhalf, h, er, ei, true, p0, p1, m0, m1, l0, l1);
+    // the mirrored site's own contraction on a Nyquist y or z row
+    const bool nyq = mirror && (hy == n / 2 || hz == n / 2);
+    F2 q0, q1, r0, r1, v0, v1;
+    if (nyq) {
+      const int jx = n - hx, jy = hy == 0 ? 0 : n - hy, jz = hz == 0 ? 0 : n - hz;
+      const double kx = kint(jx, n), ky = kint(jy, n), kz = kint(jz, n);
       const double qq = sqrt(kx * kx + ky * ky + kz * kz);
       double pr[6], pi[6];
       if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi))
@@ -375,67 +466,31 @@ __global__ void k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *
         er[c] = f2_from(pr[c]);
         ei[c] = f2_from(pi[c]);
       }
-      rate = qq * dwav;
+      ff_contract(srcF, nhalf, h, er, ei, false, q0, q1, r0, r1, v0, v1);
+    } else {
+      q0 = p0, q1 = f2_neg(p1), r0 = m0, r1 = f2_neg(m1), v0 = l0, v1 = f2_neg(l1);
     }
-    if (!(rate > 0)) {
-      // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
-      if (ref_compat) {
-        if constexpr (ACCFF) {
-          float4 *acc = static_cast<float4 *>(accp);
-          acc[n3 + s] = acc[2 * n3 + s];
-        } else {
-          double2 *acc = static_cast<double2 *>(accp);
-          acc[n3 + s] = acc[2 * n3 + s];
-        }
-      }
-      continue;
-    }
-    F2 p0 = {0.f, 0.f}, p1 = p0, m0 = p0, m1 = p0, l0 = p0, l1 = p0;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      F2 sr, si;
-      src_ff(srcF[c * nhalf + hidx], sr, si);
-      if (conj_back) si = f2_neg(si);
-      // a = er sr, b = ei si, e = er si, g = ei sr: X+ += (a - b, e + g), X- += (a + b, e - g)
-      const F2 t0 = f2_dot2(er[c], sr, ei[c], si, -1.f), t1 = f2_dot2(er[c], si, ei[c], sr, 1.f);
-      const F2 t2 = f2_dot2(er[c], sr, ei[c], si, 1.f), t3 = f2_dot2(er[c], si, ei[c], sr, -1.f);
-      p0 = f2_add(p0, t0);
-      p1 = f2_add(p1, t1);
-      m0 = f2_add(m0, t2);
-      m1 = f2_add(m1, t3);
-      if (c == 5) {
-        l0 = t2;
-        l1 = t3;
-      }
-    }
+    const int64_t s2 = mirror ? gw_mirror_site(hx, hy, hz, n) : -1;
     if constexpr (ACCFF) {
       F2 sq, cq;
       ff_sincos(rate * tau, sq, cq);
       const F2 dwf = {dw_hi, dw_lo};
       const F2 wc = f2_add(f2_mul(dwf, cq), F2{0.f, 0.f}), ws = f2_add(f2_mul(dwf, sq), F2{0.f, 0.f});
       float4 *acc = static_cast<float4 *>(accp);
-      float4 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
-      ff_axpy(a11, wc, p0, p1);
-      ff_axpy(a22, ws, m0, m1);
-      if (ref_compat) {
-        // a12 += ws X+ + wc X-, then a21 = a12 - wc (last X-)
-        ff_axpy(a12, ws, p0, p1);
-        ff_axpy(a12, wc, m0, m1);
-        a21 = a12;
-        ff_axpy(a21, f2_neg(wc), l0, l1);
-      } else {
-        ff_axpy(a21, ws, p0, p1);
-        ff_axpy(a12, wc, m0, m1);
-      }
-      acc[s] = a11;
-      acc[n3 + s] = a21;
-      acc[2 * n3 + s] = a12;
-      acc[3 * n3 + s] = a22;
+      ff_update(acc, n3, s1, wc, ws, p0, p1, m0, m1, l0, l1, ref_compat);
+      if (mirror) ff_update(acc, n3, s2, wc, ws, q0, q1, r0, r1, v0, v1, ref_compat);
     } else {
       double sq, cq;
       sincos(rate * tau, &sq, &cq);
-      const double xp[2] = {f2_to(p0), f2_to(p1)}, xm[2] = {f2_to(m0), f2_to(m1)}, lm[2] = {f2_to(l0), f2_to(l1)};
-      gw_update(static_cast<double2 *>(accp), n3, s, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+      double2 *acc = static_cast<double2 *>(accp);
+      {
+        const double xp[2] = {f2_to(p0), f2_to(p1)}, xm[2] = {f2_to(m0), f2_to(m1)}, lm[2] = {f2_to(l0), f2_to(l1)};
+        gw_update(acc, n3, s1, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+      }
+      if (mirror) {
+        const double xp[2] = {f2_to(q0), f2_to(q1)}, xm[2] = {f2_to(r0), f2_to(r1)}, lm[2] = {f2_to(v0), f2_to(v1)};
+        gw_update(acc, n3, s2, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+      }
     }
   }
 }
@@ -470,51 +525,74 @@ __device__ __forceinline__ float gw_phase(float2 om, float th, float tl) {
   return fmaf(-m, kC3, r);
 }
 
+// float-float accumulators at site s from FP32 X+, X- and the weights
+__device__ __forceinline__ void f32_update(float4 *__restrict__ acc, int64_t n3, int64_t s, float wc, float ws,
+                                           const float xp[2], const float xm[2], const float lm[2], int ref_compat) {
+  float4 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
+  ff_add(a11.x, a11.y, wc * xp[0]);
+  ff_add(a11.z, a11.w, wc * xp[1]);
+  ff_add(a22.x, a22.y, ws * xm[0]);
+  ff_add(a22.z, a22.w, ws * xm[1]);
+  if (ref_compat) {
+    ff_add(a12.x, a12.y, fmaf(wc, xm[0], ws * xp[0]));
+    ff_add(a12.z, a12.w, fmaf(wc, xm[1], ws * xp[1]));
+    a21 = a12;
+    ff_add(a21.x, a21.y, -wc * lm[0]);
+    ff_add(a21.z, a21.w, -wc * lm[1]);
+  } else {
+    ff_add(a21.x, a21.y, ws * xp[0]);
+    ff_add(a21.z, a21.w, ws * xp[1]);
+    ff_add(a12.x, a12.y, wc * xm[0]);
+    ff_add(a12.z, a12.w, wc * xm[1]);
+  }
+  acc[s] = a11;
+  acc[n3 + s] = a21;
+  acc[2 * n3 + s] = a12;
+  acc[3 * n3 + s] = a22;
+}
+
 // FP32-mixed Green accumulation: FP32 sources, polarisation, phase and
 // contraction; the accumulators are float-float pairs (re hi, re lo, im hi,
-// im lo), so no FP64 instruction is issued per k-site.
+// im lo), so no FP64 instruction is issued per k-site.  One thread per stored
+// half-spectrum entry updates k and, for 0 < hx < n/2, -k (the conjugate
+// contraction; formed directly on Nyquist y / z rows), as in
+// k_gw_accumulate_tab.
 __global__ void k_gw_accumulate_f32(const float2 *__restrict__ srcF, const float2 *__restrict__ om, int n, float th,
                                     float tl, float dw, int ref_compat, float4 *__restrict__ acc) {
-  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
-  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+  const int nh = n / 2 + 1;
+  const int64_t n3 = (int64_t)n * n * n;
+  const int64_t nhalf = (int64_t)n * n * nh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-    const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
-    bool conj_back;
-    const int64_t hidx = gw_half_index(ix, iy, iz, n, conj_back);
-    const float kx = (float)kint(ix, n), ky = (float)kint(iy, n), kz = (float)kint(iz, n);
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
+    const int hx = (int)(h % nh), hy = (int)((h / nh) % n), hz = (int)(h / ((int64_t)nh * n));
+    const int64_t s1 = ((int64_t)hz * n + hy) * n + hx;
+    const bool mirror = hx > 0 && hx < n / 2;
+    const float kx = (float)kint(hx, n), ky = (float)kint(hy, n), kz = (float)kint(hz, n);
     const float qq = sqrtf(kx * kx + ky * ky + kz * kz);
     float pr[6], pi[6];
     if (!gw_polarisation<float>(kx, ky, kz, qq, pr, pi)) {
-      if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+      if (ref_compat) acc[n3 + s1] = acc[2 * n3 + s1];  // k = 0 (h = 0, no mirror)
       continue;
     }
     float sq, cq;
-    sincosf(gw_phase(om[s], th, tl), &sq, &cq);
-    float xp[2], xm[2], lm[2];
-    gw_contract<float, float2>(srcF, nhalf, hidx, conj_back, pr, pi, xp, xm, lm);
+    sincosf(gw_phase(om[s1], th, tl), &sq, &cq);
     const float wc = dw * cq, ws = dw * sq;
-    float4 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
-    ff_add(a11.x, a11.y, wc * xp[0]);
-    ff_add(a11.z, a11.w, wc * xp[1]);
-    ff_add(a22.x, a22.y, ws * xm[0]);
-    ff_add(a22.z, a22.w, ws * xm[1]);
-    if (ref_compat) {
-      ff_add(a12.x, a12.y, fmaf(wc, xm[0], ws * xp[0]));
-      ff_add(a12.z, a12.w, fmaf(wc, xm[1], ws * xp[1]));
-      a21 = a12;
-      ff_add(a21.x, a21.y, -wc * lm[0]);
-      ff_add(a21.z, a21.w, -wc * lm[1]);
+    float xp[2], xm[2], lm[2];
+    gw_contract<float, float2>(srcF, nhalf, h, true, pr, pi, xp, xm, lm);
+    f32_update(acc, n3, s1, wc, ws, xp, xm, lm, ref_compat);
+    if (!mirror) continue;
+    const int64_t s2 = gw_mirror_site(hx, hy, hz, n);
+    if (hy == n / 2 || hz == n / 2) {
+      const int jx = n - hx, jy = hy == 0 ? 0 : n - hy, jz = hz == 0 ? 0 : n - hz;
+      const float jkx = (float)kint(jx, n), jky = (float)kint(jy, n), jkz = (float)kint(jz, n);
+      gw_polarisation<float>(jkx, jky, jkz, sqrtf(jkx * jkx + jky * jky + jkz * jkz), pr, pi);
+      gw_contract<float, float2>(srcF, nhalf, h, false, pr, pi, xp, xm, lm);
     } else {
-      ff_add(a21.x, a21.y, ws * xp[0]);
-      ff_add(a21.z, a21.w, ws * xp[1]);
-      ff_add(a12.x, a12.y, wc * xm[0]);
-      ff_add(a12.z, a12.w, wc * xm[1]);
+      xp[1] = -xp[1];
+      xm[1] = -xm[1];
+      lm[1] = -lm[1];
     }
-    acc[s] = a11;
-    acc[n3 + s] = a21;
-    acc[2 * n3 + s] = a12;
-    acc[3 * n3 + s] = a22;
+    f32_update(acc, n3, s2, wc, ws, xp, xm, lm, ref_compat);
   }
 }
 
@@ -750,13 +828,14 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   const double dw = tau * dtau * dv * (ctx->p.sigma_cr * ctx->p.sigma_cr);
   const double dwav = kRefTwoPi / ctx->p.dspa / n;
   const int ref = ctx->p.compat == AXG_COMPAT_REF ? 1 : 0;
+  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
     float *src = (float *)ctx->gsrc;
     AXG_LAUNCH(ctx, "gw_source_fp32", k_gw_source_f32, grid_for(ctx->n3), 256, 0,
                (const float2 *)ctx->phi[ctx->cur], n, (float)(2.0 / (d * d)), src);
     AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_gsrc, src, (cufftComplex *)ctx->gsrcF));
     const float th = (float)tau, tl = (float)(tau - (double)th);
-    AXG_LAUNCH(ctx, "gw_accumulate_fp32", k_gw_accumulate_f32, grid_for(ctx->n3), 256, 0,
+    AXG_LAUNCH(ctx, "gw_accumulate_fp32", k_gw_accumulate_f32, grid_for(nhalf), 256, 0,
                (const float2 *)ctx->gsrcF, ctx->gw_omega, n, th, tl, (float)dw, ref, (float4 *)ctx->acc);
     return AXG_OK;
   }
@@ -772,23 +851,22 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
     AXG_TRY(axg_ff_d2z(ctx, ctx->gsrc, ctx->gsrcF, n, 6, tab));
   else
     AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
-  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   const float dw_hi = (float)dw, dw_lo = (float)(dw - (double)dw_hi);
   const float2 *pol = reinterpret_cast<const float2 *>(ctx->gw_pol);
   const double *rates = ctx->gw_pol + 12 * nhalf;
   if (tab && ff && ctx->acc_ff)
-    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<float4, true>), grid_for(ctx->n3), 256, 0,
+    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<float4, true>), grid_for(nhalf), 256, 0,
                reinterpret_cast<const float4 *>(ctx->gsrcF), pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref,
                (void *)ctx->acc);
   else if (tab && ff)
-    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<float4, false>), grid_for(ctx->n3), 256, 0,
+    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<float4, false>), grid_for(nhalf), 256, 0,
                reinterpret_cast<const float4 *>(ctx->gsrcF), pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref,
                (void *)ctx->acc);
   else if (tab && ctx->acc_ff)
-    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<double2, true>), grid_for(ctx->n3), 256, 0,
+    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<double2, true>), grid_for(nhalf), 256, 0,
                (const double2 *)ctx->gsrcF, pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref, (void *)ctx->acc);
   else if (tab)
-    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<double2, false>), grid_for(ctx->n3), 256, 0,
+    AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<double2, false>), grid_for(nhalf), 256, 0,
                (const double2 *)ctx->gsrcF, pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref, (void *)ctx->acc);
   else
     AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate, grid_for(ctx->n3), 256, 0, ctx->gsrcF, n, dwav, tau, dw, ref,

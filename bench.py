@@ -255,6 +255,26 @@ def bench_e2e(ag, lat, n, nsub, reps, t, dt):
     up, lf, dn = (float(np.median([q[i] for q in parts])) for i in range(3))
     split = {"upload_s": up, "leapfrog_s": lf, "download_s": dn, "upload_gbs": bytes_each / up / 1e9,
              "download_gbs": bytes_each / dn / 1e9}
+    # the host link on its own: a plain pinned copy of phi's host buffer each
+    # way (best of 3, CUDA events); upload + steps + download cannot beat
+    # bytes / link rate + the device-side steps
+    d_tmp = torch.empty(shape, dtype=torch.float64, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    link = {}
+    for name, dst, src in (("h2d_gbs", d_tmp, h_phi), ("d2h_gbs", h_phi, d_tmp)):
+        best = 1e30
+        for _ in range(3):
+            ev[0].record()
+            dst.copy_(src, non_blocking=True)
+            ev[1].record()
+            ev[1].synchronize()
+            best = min(best, ev[0].elapsed_time(ev[1]) * 1e-3)
+        link[name] = bytes_each / 2 / best / 1e9
+    del d_tmp
+    bound = bytes_each / (link["h2d_gbs"] * 1e9) + lf + bytes_each / (link["d2h_gbs"] * 1e9)
+    split["link"] = link
+    split["interval_bound_s"] = bound
+    split["frac_of_link_bound"] = bound / per
     return {"value": nsub * n ** 3 / per, "unit": UNIT, "h2d_bytes_per_step": bytes_each / nsub,
             "d2h_bytes_per_step": bytes_each / nsub, "interval_steps": nsub, "s_per_interval": per,
             "s_per_interval_min": per_min, "split": split,
