@@ -265,6 +265,248 @@ int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 
   return AXG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// FP32 transform of the six Green's-function sources, the source computation
+// fused into the row pass.  The FP32-mixed Green step needs the forward
+// transforms of S_ij = (2 / d^2) (dr_i dr_j + di_i di_j), d_i the raw
+// central differences of phi: the row kernel forms S_ij for its rows from
+// phi (the stencil rows come through L1 / L2) and runs the real-to-half x
+// transform of all six at once, so the real sources never reach HBM; the y
+// and z passes are the column passes above in complex float.  Output as
+// cuFFT's R2C: [6][n][n][n/2+1] complex float.  Twiddles are the high parts
+// of the float-float table, i.e. W_n^k rounded to float.
+
+__device__ __forceinline__ float2 f_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 f_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 f_mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 f_conj(float2 a) { return make_float2(a.x, -a.y); }
+
+// In-register DFTs of 2, 4 and 8 points, natural order in and out; INV uses
+// exp(+2 pi i / R).  The 8-point one is two 4-point DFTs of the even and odd
+// inputs joined with W_8^k = exp(-+ 2 pi i k / 8).
+template <bool INV>
+__device__ __forceinline__ float2 f_mul_w4(float2 a) {  // a W_4 = a (-i), inverse a (+i)
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+constexpr float kRs2 = 0.70710678118654752440f;  // 1 / sqrt 2
+template <bool INV>
+__device__ __forceinline__ float2 f_mul_w8(float2 a) {  // a W_8: (1 -+ i) / sqrt 2
+  return INV ? make_float2((a.x - a.y) * kRs2, (a.x + a.y) * kRs2) : make_float2((a.x + a.y) * kRs2, (a.y - a.x) * kRs2);
+}
+template <bool INV>
+__device__ __forceinline__ float2 f_mul_w8_3(float2 a) {  // a W_8^3: (-1 -+ i) / sqrt 2
+  return INV ? make_float2((-a.x - a.y) * kRs2, (a.x - a.y) * kRs2)
+             : make_float2((a.y - a.x) * kRs2, (-a.x - a.y) * kRs2);
+}
+template <bool INV>
+__device__ __forceinline__ void f_dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3) {
+  const float2 a = f_add(x0, x2), b = f_sub(x0, x2), c = f_add(x1, x3), d = f_mul_w4<INV>(f_sub(x1, x3));
+  x0 = f_add(a, c);
+  x1 = f_add(b, d);
+  x2 = f_sub(a, c);
+  x3 = f_sub(b, d);
+}
+template <int R, bool INV>
+__device__ __forceinline__ void f_dft(float2 *v) {
+  if constexpr (R == 2) {
+    const float2 t = v[0];
+    v[0] = f_add(t, v[1]);
+    v[1] = f_sub(t, v[1]);
+  } else if constexpr (R == 4) {
+    f_dft4<INV>(v[0], v[1], v[2], v[3]);
+  } else {
+    float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    f_dft4<INV>(e0, e1, e2, e3);
+    f_dft4<INV>(o0, o1, o2, o3);
+    o1 = f_mul_w8<INV>(o1);
+    o2 = f_mul_w4<INV>(o2);
+    o3 = f_mul_w8_3<INV>(o3);
+    v[0] = f_add(e0, o0);
+    v[4] = f_sub(e0, o0);
+    v[1] = f_add(e1, o1);
+    v[5] = f_sub(e1, o1);
+    v[2] = f_add(e2, o2);
+    v[6] = f_sub(e2, o2);
+    v[3] = f_add(e3, o3);
+    v[7] = f_sub(e3, o3);
+  }
+}
+
+// Stockham autosort FFT of L points, L / 8 threads per line, 8 values per
+// thread in registers.  Pass (R, NS), NS the product of the earlier radices:
+// iteration jj < L / R reads x[jj + r L / R], multiplies input r by
+// W_(NS R)^(r (jj mod NS)), takes the R-point DFT and writes output r to
+// (jj / NS) NS R + jj mod NS + r NS.  Radix 8 while 8 divides what is left,
+// then one radix-4 or radix-2 pass; a thread runs 8 / R iterations per pass.
+// Input and output are in natural order.  Between passes the values go
+// through shared memory, element i of the line at line[pad(i) * ls]
+// (pad(i) = i + i / 8 keeps the radix-8 strides off a single bank); the last
+// pass hands its outputs to `store`.  tw[k] = W_(L ts)^k, k < L ts.
+__device__ __forceinline__ int fpad(int i) { return i + (i >> 3); }
+
+template <int L, int NS, bool INV, typename Store>
+__device__ __forceinline__ void f_stockham(float2 v[8], int j, float2 *line, int ls, const float2 *tw, int ts,
+                                           Store store) {
+  constexpr int REM = L / NS, R = REM >= 8 ? 8 : REM, NI = 8 / R, T = L / 8;
+#pragma unroll
+  for (int q = 0; q < NI; ++q) {
+    const int jj = j + q * T;
+    if constexpr (NS > 1) {
+      const int k = jj & (NS - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        float2 w = tw[r * k * (L / (NS * R)) * ts];
+        if (INV) w = f_conj(w);
+        v[q * R + r] = f_mul(v[q * R + r], w);
+      }
+    }
+    f_dft<R, INV>(&v[q * R]);
+  }
+  if constexpr (NS * R == L) {
+#pragma unroll
+    for (int q = 0; q < NI; ++q) {
+      const int jj = j + q * T;
+#pragma unroll
+      for (int r = 0; r < R; ++r) store(jj + r * NS, v[q * R + r]);  // last pass: NS = L / R, jj < NS
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < NI; ++q) {
+      const int jj = j + q * T, d = (jj / NS) * NS * R + (jj & (NS - 1));
+#pragma unroll
+      for (int r = 0; r < R; ++r) line[fpad(d + r * NS) * ls] = v[q * R + r];
+    }
+    __syncthreads();
+    constexpr int NS2 = NS * R, R2 = L / NS2 >= 8 ? 8 : L / NS2;
+#pragma unroll
+    for (int q = 0; q < 8 / R2; ++q)
+#pragma unroll
+      for (int r = 0; r < R2; ++r) v[q * R2 + r] = line[fpad(j + q * T + r * (L / R2)) * ls];
+    __syncthreads();
+    f_stockham<L, NS2, INV>(v, j, line, ls, tw, ts, store);
+  }
+}
+
+constexpr int kSrcRows = 2;  // x-rows per CTA of the source row pass (6 x 2 lines)
+
+// Row pass with the sources, for rows (y, z) = row0 .. row0 + kSrcRows - 1
+// of the N = 2M lattice.  Line c kSrcRows + r holds source c of row r
+// packed as M complex points z[m] = S(2m) + i S(2m + 1); an M-point FFT per
+// line (M / 8 threads each), then X[k] = E[k] + W_N^k O[k] for k <= M.
+template <int M>
+__global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 *__restrict__ phi, float scale,
+                                                                   float2 *__restrict__ out,
+                                                                   const float4 *__restrict__ twff) {
+  constexpr int N = 2 * M, NH = M + 1, NL = 6 * kSrcRows, T = M / 8, LP = M + M / 8;
+  __shared__ float2 s[NL * LP];
+  __shared__ float2 tw[N];  // W_N^k, k < N
+  for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    const float4 w = twff[k];
+    tw[k] = make_float2(w.x, w.z);
+    tw[k + M] = make_float2(-w.x, -w.z);
+  }
+  const int64_t row0 = (int64_t)blockIdx.x * kSrcRows, nhalf = (int64_t)N * N * NH;
+  for (int idx = threadIdx.x; idx < kSrcRows * M; idx += blockDim.x) {
+    const int r = idx / M, m = idx % M;
+    const int64_t row = row0 + r;
+    const int y = (int)(row % N), z = (int)(row / N), x0 = 2 * m;
+    const float2 *prow = phi + row * N;
+    const float4 c01 = *reinterpret_cast<const float4 *>(prow + x0);  // phi(x0), phi(x0 + 1)
+    const float2 xm = prow[x0 == 0 ? N - 1 : x0 - 1], xp = prow[x0 + 2 == N ? 0 : x0 + 2];
+    const int64_t ym = (int64_t)z * N + (y == 0 ? N - 1 : y - 1), yp = (int64_t)z * N + (y + 1 == N ? 0 : y + 1);
+    const int64_t zm = (int64_t)(z == 0 ? N - 1 : z - 1) * N + y, zp = (int64_t)(z + 1 == N ? 0 : z + 1) * N + y;
+    const float4 pym = *reinterpret_cast<const float4 *>(phi + ym * N + x0);
+    const float4 pyp = *reinterpret_cast<const float4 *>(phi + yp * N + x0);
+    const float4 pzm = *reinterpret_cast<const float4 *>(phi + zm * N + x0);
+    const float4 pzp = *reinterpret_cast<const float4 *>(phi + zp * N + x0);
+    float S[2][6];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      float dr[3], di[3];
+      dr[0] = t == 0 ? c01.z - xm.x : xp.x - c01.x;
+      di[0] = t == 0 ? c01.w - xm.y : xp.y - c01.y;
+      dr[1] = t == 0 ? pyp.x - pym.x : pyp.z - pym.z;
+      di[1] = t == 0 ? pyp.y - pym.y : pyp.w - pym.w;
+      dr[2] = t == 0 ? pzp.x - pzm.x : pzp.z - pzm.z;
+      di[2] = t == 0 ? pzp.y - pzm.y : pzp.w - pzm.w;
+      int c = 0;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j, ++c) S[t][c] = scale * (dr[i] * dr[j] + di[i] * di[j]);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) s[(c * kSrcRows + r) * LP + fpad(m)] = make_float2(S[0][c], S[1][c]);
+  }
+  __syncthreads();
+  {
+    const int ln = threadIdx.x / T, j = threadIdx.x % T;
+    float2 *line = s + ln * LP;
+    float2 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * T)];
+    __syncthreads();
+    f_stockham<M, 1, false>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
+  }
+  __syncthreads();
+  // X[k] = E[k] + W_N^k O[k], E = (Z[k] + conj Z[M-k]) / 2, O = (Z[k] - conj Z[M-k]) / 2i
+  for (int idx = threadIdx.x; idx < NL * NH; idx += blockDim.x) {
+    const int b = idx / NH, k = idx % NH;
+    const float2 zk = s[b * LP + fpad(k % M)], zc = f_conj(s[b * LP + fpad((M - k) % M)]);
+    const float2 e = f_add(zk, zc), d = f_sub(zk, zc);
+    const float2 E = make_float2(0.5f * e.x, 0.5f * e.y), O = make_float2(0.5f * d.y, -0.5f * d.x);
+    const float2 X = k == M ? f_sub(E, O) : f_add(E, k == 0 ? O : f_mul(tw[k], O));
+    const int c = b / kSrcRows, r = b % kSrcRows;
+    out[c * nhalf + (row0 + r) * NH + k] = X;
+  }
+}
+
+// Column pass in complex float: L-point FFTs along an axis of the half
+// spectrum for kLines adjacent kx, lines as in k_ff_cols; thread (j, c) of
+// column c loads its first-pass inputs from global memory and the last pass
+// stores to it.
+template <int L>
+__global__ void __launch_bounds__(kLines * L / 8) k_f_cols(float2 *__restrict__ data, int nh, int ninner, int64_t shi,
+                                                          int64_t slo, int64_t sj, const float4 *__restrict__ twff) {
+  constexpr int T = L / 8, LP = L + L / 8;
+  __shared__ float2 s[LP * kLines];
+  __shared__ float2 tw[L];  // W_L^k, k < L
+  for (int k = threadIdx.x; k < L / 2; k += blockDim.x) {
+    const float4 w = twff[k];
+    tw[k] = make_float2(w.x, w.z);
+    tw[k + L / 2] = make_float2(-w.x, -w.z);
+  }
+  const int nkb = (nh + kLines - 1) / kLines;
+  const int o = blockIdx.x / nkb, kx0 = (blockIdx.x % nkb) * kLines;
+  const int64_t base = (int64_t)(o / ninner) * shi + (int64_t)(o % ninner) * slo + kx0;
+  const int c = threadIdx.x % kLines, j = threadIdx.x / kLines;
+  const bool ok = kx0 + c < nh;
+  float2 v[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = ok ? data[base + (int64_t)(j + r * T) * sj + c] : make_float2(0.f, 0.f);
+  __syncthreads();  // twiddles
+  f_stockham<L, 1, false>(v, j, s + c, kLines, tw, 1, [&](int i, float2 x) {
+    if (ok) data[base + (int64_t)i * sj + c] = x;
+  });
+}
+
+template <int L>
+int gws_r2c_t(axg_ctx *ctx, const float2 *phi, float2 *out, float scale, const float4 *tw) {
+  constexpr int n = L, nh = L / 2 + 1, M = L / 2;
+  const int64_t rows = (int64_t)n * n;
+  AXG_LAUNCH(ctx, "gw_source_rows_fp32", k_gws_rows<M>, (unsigned)(rows / kSrcRows), 6 * kSrcRows * M / 8, 0, phi,
+             scale, out, tw);
+  const int nkb = (nh + kLines - 1) / kLines;
+  const int64_t plane = (int64_t)n * nh, vol = plane * n;
+  AXG_LAUNCH(ctx, "fft_f32_y", k_f_cols<L>, (unsigned)((int64_t)6 * n * nkb), kLines * L / 8, 0, out, nh, n, vol,
+             plane, (int64_t)nh, tw);
+  AXG_LAUNCH(ctx, "fft_f32_z", k_f_cols<L>, (unsigned)((int64_t)6 * n * nkb), kLines * L / 8, 0, out, nh, n, vol,
+             (int64_t)nh, plane, tw);
+  return AXG_OK;
+}
+
 }  // namespace
 
 // 16..512: the sizes the tests and the benchmark run; larger N keep cuFFT
@@ -329,5 +571,20 @@ int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch, b
     case 256: return d2z_t<256>(ctx, in, out, batch, tw, keep_ff);
     case 512: return d2z_t<512>(ctx, in, out, batch, tw, keep_ff);
     default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
+  }
+}
+
+int axg_gw_source_r2c_f32(axg_ctx *ctx, const float2 *phi, float2 *out, int n, float scale) {
+  if (!axg_ff_fft_supported(n)) return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "FP32 source transform size");
+  AXG_TRY(ensure_twiddles(ctx, n));
+  const float4 *tw = reinterpret_cast<const float4 *>(ctx->ff_tw);
+  switch (n) {
+    case 16: return gws_r2c_t<16>(ctx, phi, out, scale, tw);
+    case 32: return gws_r2c_t<32>(ctx, phi, out, scale, tw);
+    case 64: return gws_r2c_t<64>(ctx, phi, out, scale, tw);
+    case 128: return gws_r2c_t<128>(ctx, phi, out, scale, tw);
+    case 256: return gws_r2c_t<256>(ctx, phi, out, scale, tw);
+    case 512: return gws_r2c_t<512>(ctx, phi, out, scale, tw);
+    default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "FP32 source transform size");
   }
 }

@@ -783,8 +783,12 @@ int axg_gw_init(axg_ctx *ctx) {
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
   const size_t rs = fp32 ? 4 : 8;
+  // our own transforms for power-of-two N up to 512 (AXG_FFT_FF=0: cuFFT);
+  // FP32-mixed then never stores the real sources
+  ctx->gw_own_fft = axg_ff_use(n);
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->acc, (size_t)ctx->n3 * 64, "GW accumulators"));
-  AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)ctx->n3 * 6 * rs, "GW sources"));
+  if (!(fp32 && ctx->gw_own_fft))
+    AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)ctx->n3 * 6 * rs, "GW sources"));
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrcF, (size_t)nhalf * 6 * 2 * rs, "GW source spectra"));
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->n3 * 64, ctx->stream));
   if (fp32) {
@@ -810,12 +814,14 @@ int axg_gw_init(axg_ctx *ctx) {
   // float-float accumulators where the transforms are float-float too: the
   // whole Green accumulation then stays on the FP32 pipes but for the phase
   // reduction
-  ctx->acc_ff = fp32 || (ctx->gw_pol != nullptr && axg_ff_use(n));
-  int dims[3] = {n, n, n};
-  AXG_CUFFT_TRY(ctx, cufftPlanMany(&ctx->plan_gsrc, 3, dims, nullptr, 1, (int)ctx->n3, nullptr, 1,
-                                   (int)nhalf, fp32 ? CUFFT_R2C : CUFFT_D2Z, 6));
-  ctx->plan_gsrc_ok = true;
-  AXG_CUFFT_TRY(ctx, cufftSetStream(ctx->plan_gsrc, ctx->stream));
+  ctx->acc_ff = fp32 || (ctx->gw_pol != nullptr && ctx->gw_own_fft);
+  if (!ctx->gw_own_fft) {
+    int dims[3] = {n, n, n};
+    AXG_CUFFT_TRY(ctx, cufftPlanMany(&ctx->plan_gsrc, 3, dims, nullptr, 1, (int)ctx->n3, nullptr, 1,
+                                     (int)nhalf, fp32 ? CUFFT_R2C : CUFFT_D2Z, 6));
+    ctx->plan_gsrc_ok = true;
+    AXG_CUFFT_TRY(ctx, cufftSetStream(ctx->plan_gsrc, ctx->stream));
+  }
   return AXG_OK;
 }
 
@@ -830,10 +836,15 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   const int ref = ctx->p.compat == AXG_COMPAT_REF ? 1 : 0;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
-    float *src = (float *)ctx->gsrc;
-    AXG_LAUNCH(ctx, "gw_source_fp32", k_gw_source_f32, grid_for(ctx->n3), 256, 0,
-               (const float2 *)ctx->phi[ctx->cur], n, (float)(2.0 / (d * d)), src);
-    AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_gsrc, src, (cufftComplex *)ctx->gsrcF));
+    if (ctx->gw_own_fft) {
+      AXG_TRY(axg_gw_source_r2c_f32(ctx, (const float2 *)ctx->phi[ctx->cur], (float2 *)ctx->gsrcF, n,
+                                    (float)(2.0 / (d * d))));
+    } else {
+      float *src = (float *)ctx->gsrc;
+      AXG_LAUNCH(ctx, "gw_source_fp32", k_gw_source_f32, grid_for(ctx->n3), 256, 0,
+                 (const float2 *)ctx->phi[ctx->cur], n, (float)(2.0 / (d * d)), src);
+      AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_gsrc, src, (cufftComplex *)ctx->gsrcF));
+    }
     const float th = (float)tau, tl = (float)(tau - (double)th);
     AXG_LAUNCH(ctx, "gw_accumulate_fp32", k_gw_accumulate_f32, grid_for(nhalf), 256, 0,
                (const float2 *)ctx->gsrcF, ctx->gw_omega, n, th, tl, (float)dw, ref, (float4 *)ctx->acc);
@@ -846,7 +857,7 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   // the six source transforms: float-float for power-of-two N (FP64
   // accuracy on the FP32 pipes; kept as float-float pairs when the
   // float-float contraction reads them), else cuFFT
-  const bool ff = axg_ff_use(n), tab = ctx->gw_pol != nullptr;
+  const bool ff = ctx->gw_own_fft, tab = ctx->gw_pol != nullptr;
   if (ff)
     AXG_TRY(axg_ff_d2z(ctx, ctx->gsrc, ctx->gsrcF, n, 6, tab));
   else

@@ -96,6 +96,8 @@ struct axg_ctx {
                                // [n*n*(n/2+1)] double |k| dwav; or null
   bool acc_ff = false;         // Green accumulators are float-float float4 (FP32-mixed, and the FP64 paths
                                // on the float-float transforms), else double2
+  bool gw_own_fft = false;     // Green sources transformed by axg_fft_ff.cu (FP64: float-float D2Z; FP32:
+                               // the fused source + R2C), else by cuFFT; fixed when the context is made
   float *ff_tw = nullptr;      // float-float FFT twiddles W_n^k, k < n/2 (axg_fft_ff.cu)
   int ff_tw_n = 0;
   cufftHandle plan_gsrc = 0;
@@ -262,6 +264,9 @@ bool axg_ff_use(int n);
 // complex value in the same 16 bytes, for a consumer that reads it so
 int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch, bool keep_ff = false);
 int axg_ff_z2z(axg_ctx *ctx, double2 *data, int n, int inverse);  // in place, one n^3 volume
+// the six FP32-mixed Green sources of phi and their forward transforms, out
+// [6][n][n][n/2+1] complex float (cuFFT R2C layout); n as axg_ff_fft_supported
+int axg_gw_source_r2c_f32(axg_ctx *ctx, const float2 *phi, float2 *out, int n, float scale);
 int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem,
                        long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,
                        int *d_err, bool fp32, bool uij, double dspa, bool persistent);

@@ -89,6 +89,29 @@ def test_green_float_float_fft_matches_cufft(monkeypatch, n):
     assert rel(out["1"], out["0"]) < 1e-12
 
 
+@pytest.mark.parametrize("n", [16, 32, 64, 128])
+def test_green_fp32_fused_source_transform_matches_cufft(monkeypatch, n):
+    """FP32-mixed Green mode forms the six sources inside its own row
+    transform and runs the y and z passes in complex float for power-of-two
+    N; its accumulators agree with the cuFFT R2C path to FP32 rounding."""
+    phi, phid = init_state(n, 2)
+    p = params(n, ag.PREC_FP32_MIXED, ag.GW_GREEN, compat=ag.COMPAT_REF)
+    out = {}
+    for ff in ("1", "0"):
+        monkeypatch.setenv("AXG_FFT_FF", ff)
+        with ag.Lattice(p) as lat:
+            lat.upload(phi, phid)
+            lat.set_kernel_timing(True)
+            lat.symplectic_integration(2.0, 2.4, 0.4)
+            lat.synchronize()
+            names = set(k for k, _, _ in lat.kernel_timings())
+            out[ff] = lat.download_gw_green()
+        assert ("gw_source_rows_fp32" in names) == (ff == "1")
+    monkeypatch.delenv("AXG_FFT_FF")
+    assert np.any(out["1"] != 0)
+    assert rel(out["1"], out["0"]) < 2e-5
+
+
 @pytest.mark.parametrize("compat", [ag.COMPAT_REF, ag.COMPAT_INTENDED])
 def test_green_fp32_mixed_against_fp64_oracle(compat):
     """FP32 sources, R2C transforms and contractions with FP64 accumulators:
