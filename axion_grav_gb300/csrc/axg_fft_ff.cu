@@ -1,4 +1,5 @@
-// axg_fft_ff.cu -- 3-D FFTs at FP64 accuracy in float-float arithmetic.
+// axg_fft_ff.cu -- 3-D FFTs at FP64 accuracy in float-float arithmetic, and
+// the FP32 transform of the Green's-function sources.
 //
 // GB300 issues FP64 at 1/64 of its FP32 rate, and an FP64 FFT is bound by
 // it: cuFFT's 512^3 D2Z takes about 15.5 ms, while moving its bytes takes
@@ -18,11 +19,13 @@
 //   rows    : per x-row, the n reals as n/2 complex points z[m] = x[2m] +
 //             i x[2m+1], an n/2-point FFT, and the split of Z into the n/2+1
 //             outputs X[k] = E[k] + W_n^k O[k];
-//   y, z    : n-point FFTs along y and along z, 8 adjacent kx columns per
-//             CTA so every row of the tile is one 128-byte segment.
-// Each FFT is decimation in time in shared memory (bit-reversed load,
-// natural-order result), radix-2 stages fused in pairs in registers,
-// twiddles W_n^k from a float-float table made on the host in FP64.  Powers of two from 16 to 512.
+//   y, z    : n-point FFTs along y and along z, a few adjacent kx columns per
+//             CTA so every row of the tile is one 64-byte segment.
+// Each line is a Stockham radix-8 FFT in registers (f_stockham): a 512-point
+// line takes two shared-memory exchanges, the first pass reads its inputs
+// from global memory and the column passes' last pass writes there.
+// Twiddles W_n^k come from a float-float table made on the host in FP64.
+// Powers of two from 16 to 512.
 #include <cmath>
 #include <cstdlib>
 #include <vector>
@@ -36,301 +39,108 @@ namespace {
 __device__ __forceinline__ F2 re(float4 v) { return {v.x, v.y}; }
 __device__ __forceinline__ F2 im(float4 v) { return {v.z, v.w}; }
 __device__ __forceinline__ float4 cx(F2 r, F2 i) { return make_float4(r.h, r.l, i.h, i.l); }
+
+// Complex arithmetic of the two value types the transforms run in: complex
+// float (float2) and complex float-float (float4).
+__device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 c_half(float2 a) { return make_float2(0.5f * a.x, 0.5f * a.y); }
+__device__ __forceinline__ float2 c_div_2i(float2 d) { return make_float2(0.5f * d.y, -0.5f * d.x); }  // d / 2i
+
 __device__ __forceinline__ float4 c_add(float4 a, float4 b) { return cx(f2_add(re(a), re(b)), f2_add(im(a), im(b))); }
 __device__ __forceinline__ float4 c_sub(float4 a, float4 b) { return cx(f2_sub(re(a), re(b)), f2_sub(im(a), im(b))); }
-
 __device__ __forceinline__ float4 c_mul(float4 a, float4 b) {
   return cx(f2_dot2(re(a), re(b), im(a), im(b), -1.f), f2_dot2(re(a), im(b), im(a), re(b), 1.f));
 }
 __device__ __forceinline__ float4 c_conj(float4 a) { return make_float4(a.x, a.y, -a.z, -a.w); }
+__device__ __forceinline__ float4 c_neg(float4 a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
+__device__ __forceinline__ float4 c_half(float4 a) { return cx(f2_half(re(a)), f2_half(im(a))); }  // exact
+__device__ __forceinline__ float4 c_div_2i(float4 d) { return cx(f2_half(im(d)), f2_neg(f2_half(re(d)))); }
 
-__device__ __forceinline__ int brev(int j, int bits) { return (int)(__brev((unsigned)j) >> (32 - bits)); }
-
-constexpr int kLines = 8;   // lines per CTA
-constexpr int kThreads = 256;
-
-template <int L>
-__host__ __device__ constexpr int log2c() {
-  return L <= 1 ? 0 : 1 + log2c<L / 2>();
-}
-
-// In-place L-point FFTs of kLines interleaved lines in shared memory
-// (element i of line b at s[i * kLines + b]), input bit-reversed.  The
-// radix-2 stages are taken in pairs (h, 2h): a thread holds the four
-// elements m, m + h, m + 2h, m + 3h of a 4h-group in registers and applies
-//   stage h : (a, b), (c, d) with W = W_2h^m,
-//   stage 2h: (a, c) with V = W_4h^m, (b, d) with V W_4h^h = -i V (+i V
-//             for the inverse),
-// so a pair of stages is one shared-memory round trip and one barrier; the
-// first pair (h = 1) needs no twiddle at all.  An odd stage count ends with
-// a radix-2 stage.  Twiddle W_L^k = tw[k ts], tw being the W_(L ts)^k table;
-// INV conjugates them (exp(+2 pi i k / L)).
-__device__ __forceinline__ float4 c_mul_mi(float4 a, bool inv) {  // a (-i), or a (+i) for the inverse
-  return inv ? make_float4(-a.z, -a.w, a.x, a.y) : make_float4(a.z, a.w, -a.x, -a.y);
-}
-
-template <int L, bool INV = false>
-__device__ __forceinline__ void fft_lines(float4 *s, const float4 *tw, int ts) {
-  int h = 1;
-  for (; 4 * h <= L; h <<= 2) {
-    for (int idx = threadIdx.x; idx < kLines * (L / 4); idx += kThreads) {
-      const int b = idx % kLines, u = idx / kLines;
-      const int m = u & (h - 1), i0 = ((u - m) << 2) + m;
-      float4 x0 = s[i0 * kLines + b], x1 = s[(i0 + h) * kLines + b], x2 = s[(i0 + 2 * h) * kLines + b],
-             x3 = s[(i0 + 3 * h) * kLines + b];
-      if (h > 1) {
-        float4 w = tw[m * (L / (2 * h)) * ts];
-        if (INV) w = c_conj(w);
-        x1 = c_mul(w, x1);
-        x3 = c_mul(w, x3);
-      }
-      const float4 a1 = c_add(x0, x1), b1 = c_sub(x0, x1), c1 = c_add(x2, x3), d1 = c_sub(x2, x3);
-      float4 vc = c1, vd = d1;
-      if (h > 1) {
-        float4 v = tw[m * (L / (4 * h)) * ts];
-        if (INV) v = c_conj(v);
-        vc = c_mul(v, c1);
-        vd = c_mul(v, d1);
-      }
-      vd = c_mul_mi(vd, INV);
-      s[i0 * kLines + b] = c_add(a1, vc);
-      s[(i0 + 2 * h) * kLines + b] = c_sub(a1, vc);
-      s[(i0 + h) * kLines + b] = c_add(b1, vd);
-      s[(i0 + 3 * h) * kLines + b] = c_sub(b1, vd);
-    }
-    __syncthreads();
-  }
-  if (h < L) {  // one radix-2 stage left (h = L / 2)
-    const int step = (L / (2 * h)) * ts;
-    for (int idx = threadIdx.x; idx < kLines * (L / 2); idx += kThreads) {
-      const int b = idx % kLines, q = idx / kLines;
-      const int m = q & (h - 1), i0 = ((q - m) << 1) + m, i1 = i0 + h;
-      const float4 x0 = s[i0 * kLines + b], x1 = s[i1 * kLines + b];
-      float4 w = tw[m * step];
-      if (INV) w = c_conj(w);
-      const float4 t = h == 1 ? x1 : c_mul(w, x1);
-      s[i0 * kLines + b] = c_add(x0, t);
-      s[i1 * kLines + b] = c_sub(x0, t);
-    }
-    __syncthreads();
-  }
-}
-
-// Row pass: kLines rows of N = 2M reals -> M + 1 complex each (float-float).
-template <int M>
-__global__ void __launch_bounds__(kThreads) k_ff_rows(const double *__restrict__ in, float4 *__restrict__ out,
-                                                      int64_t rows, const float4 *__restrict__ tw) {
-  constexpr int N = 2 * M, NH = M + 1, LB = log2c<M>();
-  extern __shared__ float4 ff_sm[];
-  float4 *s = ff_sm, *tws = ff_sm + M * kLines;
-  for (int k = threadIdx.x; k < M; k += kThreads) tws[k] = tw[k];  // W_N^k, k < N / 2
-  const int64_t r0 = (int64_t)blockIdx.x * kLines;
-  for (int idx = threadIdx.x; idx < kLines * M; idx += kThreads) {
-    const int r = idx / M, m = idx % M;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (r0 + r < rows) {
-      const double2 x = reinterpret_cast<const double2 *>(in + (r0 + r) * N)[m];
-      v = cx(f2_from(x.x), f2_from(x.y));
-    }
-    s[brev(m, LB) * kLines + r] = v;
-  }
-  __syncthreads();
-  fft_lines<M>(s, tws, 2);  // W_M^j = W_N^(2j)
-  // X[k] = E[k] + W_N^k O[k], E = (Z[k] + conj Z[M-k]) / 2, O = (Z[k] - conj Z[M-k]) / 2i
-  for (int idx = threadIdx.x; idx < kLines * NH; idx += kThreads) {
-    const int r = idx / NH, k = idx % NH;
-    if (r0 + r >= rows) continue;
-    const float4 zk = s[(k % M) * kLines + r], zm = c_conj(s[((M - k) % M) * kLines + r]);
-    const float4 e = c_add(zk, zm), d = c_sub(zk, zm);
-    const float4 E = cx(f2_half(re(e)), f2_half(im(e)));
-    const float4 O = cx(f2_half(im(d)), f2_neg(f2_half(re(d))));
-    const float4 X = k == M ? c_sub(E, O) : c_add(E, k == 0 ? O : c_mul(tws[k], O));
-    out[(r0 + r) * NH + k] = X;
-  }
-}
-
-// Complex row pass: kLines contiguous rows of L complex doubles -> L
-// float-float points each, transformed in place of the input.
-template <int L, bool INV>
-__global__ void __launch_bounds__(kThreads) k_ff_rows_c2c(double2 *__restrict__ data, int64_t rows,
-                                                          const float4 *__restrict__ tw) {
-  constexpr int LB = log2c<L>();
-  extern __shared__ float4 ff_sm[];
-  float4 *s = ff_sm, *tws = ff_sm + L * kLines;
-  for (int k = threadIdx.x; k < L / 2; k += kThreads) tws[k] = tw[k];
-  const int64_t r0 = (int64_t)blockIdx.x * kLines;
-  for (int idx = threadIdx.x; idx < kLines * L; idx += kThreads) {
-    const int r = idx / L, j = idx % L;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (r0 + r < rows) {
-      const double2 x = data[(r0 + r) * L + j];
-      v = cx(f2_from(x.x), f2_from(x.y));
-    }
-    s[brev(j, LB) * kLines + r] = v;
-  }
-  __syncthreads();
-  fft_lines<L, INV>(s, tws, 1);
-  float4 *out = reinterpret_cast<float4 *>(data);
-  for (int idx = threadIdx.x; idx < kLines * L; idx += kThreads) {
-    const int r = idx / L, j = idx % L;
-    if (r0 + r < rows) out[(r0 + r) * L + j] = s[j * kLines + r];
-  }
-}
-
-// Column pass: L-point FFTs along an axis of the half spectrum for kLines
-// adjacent kx.  Line (o, kx): element j at (o / ninner) shi + (o % ninner)
-// slo + j sj + kx.  The last pass writes the double2 result in place.
-template <int L, bool INV = false>
-__global__ void __launch_bounds__(kThreads) k_ff_cols(float4 *__restrict__ data, int nh, int ninner, int64_t shi,
-                                                      int64_t slo, int64_t sj, const float4 *__restrict__ tw,
-                                                      int last) {
-  constexpr int LB = log2c<L>();
-  extern __shared__ float4 ff_sm[];
-  float4 *s = ff_sm, *tws = ff_sm + L * kLines;
-  for (int k = threadIdx.x; k < L / 2; k += kThreads) tws[k] = tw[k];  // W_L^k
-  const int nkb = (nh + kLines - 1) / kLines;
-  const int o = blockIdx.x / nkb, kx0 = (blockIdx.x % nkb) * kLines;
-  const int64_t base = (int64_t)(o / ninner) * shi + (int64_t)(o % ninner) * slo + kx0;
-  for (int idx = threadIdx.x; idx < kLines * L; idx += kThreads) {
-    const int c = idx % kLines, j = idx / kLines;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (kx0 + c < nh) v = data[base + j * sj + c];
-    s[brev(j, LB) * kLines + c] = v;
-  }
-  __syncthreads();
-  fft_lines<L, INV>(s, tws, 1);
-  for (int idx = threadIdx.x; idx < kLines * L; idx += kThreads) {
-    const int c = idx % kLines, j = idx / kLines;
-    if (kx0 + c >= nh) continue;
-    const float4 v = s[j * kLines + c];
-    if (last)
-      reinterpret_cast<double2 *>(data)[base + j * sj + c] = make_double2(f2_to(re(v)), f2_to(im(v)));
-    else
-      data[base + j * sj + c] = v;
-  }
-}
-
-template <int L>
-int set_smem(axg_ctx *ctx) {
-  AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ff_cols<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)((L * kLines + L / 2) * sizeof(float4))));
-  AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ff_rows<L / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)((L / 2 * kLines + L / 2) * sizeof(float4))));
-  return AXG_OK;
-}
-
-template <int L, bool INV>
-int z2z_t(axg_ctx *ctx, double2 *data, const float4 *tw) {
-  static bool attr = false;
-  const size_t sm = (L * kLines + L / 2) * sizeof(float4);
-  if (!attr) {
-    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ff_rows_c2c<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)sm));
-    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ff_cols<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    attr = true;
-  }
-  constexpr int n = L;
-  const int64_t rows = (int64_t)n * n, plane = (int64_t)n * n, vol = plane * n;
-  float4 *f = reinterpret_cast<float4 *>(data);
-  AXG_LAUNCH(ctx, "fft_ff_rows_c2c", (k_ff_rows_c2c<L, INV>), (unsigned)((rows + kLines - 1) / kLines), kThreads, sm,
-             data, rows, tw);
-  const int nkb = n / kLines;
-  AXG_LAUNCH(ctx, "fft_ff_y", (k_ff_cols<L, INV>), (unsigned)((int64_t)n * nkb), kThreads, sm, f, n, n, vol, plane,
-             (int64_t)n, tw, 0);
-  AXG_LAUNCH(ctx, "fft_ff_z", (k_ff_cols<L, INV>), (unsigned)((int64_t)n * nkb), kThreads, sm, f, n, n, vol,
-             (int64_t)n, plane, tw, 1);
-  return AXG_OK;
-}
-
-template <int L>
-int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 *tw, bool keep_ff) {
-  static bool attr = false;
-  if (!attr) {
-    AXG_TRY(set_smem<L>(ctx));
-    attr = true;
-  }
-  constexpr int n = L, nh = L / 2 + 1;
-  const int64_t rows = (int64_t)batch * n * n;
-  float4 *f = reinterpret_cast<float4 *>(out);
-  AXG_LAUNCH(ctx, "fft_ff_rows", k_ff_rows<L / 2>, (unsigned)((rows + kLines - 1) / kLines), kThreads,
-             (L / 2 * kLines + L / 2) * sizeof(float4), in, f, rows, tw);
-  const int nkb = (nh + kLines - 1) / kLines;
-  const size_t sm = (L * kLines + L / 2) * sizeof(float4);
-  const int64_t plane = (int64_t)n * nh, vol = plane * n;
-  // y: lines (field, z); z: lines (field, y)
-  AXG_LAUNCH(ctx, "fft_ff_y", k_ff_cols<L>, (unsigned)((int64_t)batch * n * nkb), kThreads, sm, f, nh, n, vol,
-             plane, (int64_t)nh, tw, 0);
-  AXG_LAUNCH(ctx, "fft_ff_z", k_ff_cols<L>, (unsigned)((int64_t)batch * n * nkb), kThreads, sm, f, nh, n, vol,
-             (int64_t)nh, plane, tw, keep_ff ? 0 : 1);
-  return AXG_OK;
-}
-
-// ---------------------------------------------------------------------------
-// FP32 transform of the six Green's-function sources, the source computation
-// fused into the row pass.  The FP32-mixed Green step needs the forward
-// transforms of S_ij = (2 / d^2) (dr_i dr_j + di_i di_j), d_i the raw
-// central differences of phi: the row kernel forms S_ij for its rows from
-// phi (the stencil rows come through L1 / L2) and runs the real-to-half x
-// transform of all six at once, so the real sources never reach HBM; the y
-// and z passes are the column passes above in complex float.  Output as
-// cuFFT's R2C: [6][n][n][n/2+1] complex float.  Twiddles are the high parts
-// of the float-float table, i.e. W_n^k rounded to float.
-
-__device__ __forceinline__ float2 f_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 f_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 f_mul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 f_conj(float2 a) { return make_float2(a.x, -a.y); }
-
-// In-register DFTs of 2, 4 and 8 points, natural order in and out; INV uses
-// exp(+2 pi i / R).  The 8-point one is two 4-point DFTs of the even and odd
-// inputs joined with W_8^k = exp(-+ 2 pi i k / 8).
+// a W_4 = a (-i), inverse a (+i): exact
 template <bool INV>
-__device__ __forceinline__ float2 f_mul_w4(float2 a) {  // a W_4 = a (-i), inverse a (+i)
+__device__ __forceinline__ float2 c_w4(float2 a) {
   return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
-constexpr float kRs2 = 0.70710678118654752440f;  // 1 / sqrt 2
 template <bool INV>
-__device__ __forceinline__ float2 f_mul_w8(float2 a) {  // a W_8: (1 -+ i) / sqrt 2
+__device__ __forceinline__ float4 c_w4(float4 a) {
+  return INV ? make_float4(-a.z, -a.w, a.x, a.y) : make_float4(a.z, a.w, -a.x, -a.y);
+}
+
+// a W_8 = a (1 -+ i) / sqrt 2 and a W_8^3 = a (-1 -+ i) / sqrt 2 (the upper
+// sign forward); 1 / sqrt 2 as a float and as a float-float pair
+constexpr float kRs2 = 0.70710678118654752440f;
+constexpr float kRs2Hi = 0.70710676908493041992f, kRs2Lo = 1.2101617485882343e-08f;
+template <bool INV>
+__device__ __forceinline__ float2 c_w8(float2 a) {
   return INV ? make_float2((a.x - a.y) * kRs2, (a.x + a.y) * kRs2) : make_float2((a.x + a.y) * kRs2, (a.y - a.x) * kRs2);
 }
 template <bool INV>
-__device__ __forceinline__ float2 f_mul_w8_3(float2 a) {  // a W_8^3: (-1 -+ i) / sqrt 2
+__device__ __forceinline__ float2 c_w8_3(float2 a) {
   return INV ? make_float2((-a.x - a.y) * kRs2, (a.x - a.y) * kRs2)
              : make_float2((a.y - a.x) * kRs2, (-a.x - a.y) * kRs2);
 }
 template <bool INV>
-__device__ __forceinline__ void f_dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3) {
-  const float2 a = f_add(x0, x2), b = f_sub(x0, x2), c = f_add(x1, x3), d = f_mul_w4<INV>(f_sub(x1, x3));
-  x0 = f_add(a, c);
-  x1 = f_add(b, d);
-  x2 = f_sub(a, c);
-  x3 = f_sub(b, d);
+__device__ __forceinline__ float4 c_w8(float4 a) {
+  const F2 r = re(a), i = im(a), s = {kRs2Hi, kRs2Lo};
+  return INV ? cx(f2_mul(f2_sub(r, i), s), f2_mul(f2_add(r, i), s)) : cx(f2_mul(f2_add(r, i), s), f2_mul(f2_sub(i, r), s));
 }
-template <int R, bool INV>
-__device__ __forceinline__ void f_dft(float2 *v) {
+template <bool INV>
+__device__ __forceinline__ float4 c_w8_3(float4 a) {
+  const F2 r = re(a), i = im(a), s = {kRs2Hi, kRs2Lo};
+  return INV ? cx(f2_neg(f2_mul(f2_add(r, i), s)), f2_mul(f2_sub(r, i), s))
+             : cx(f2_mul(f2_sub(i, r), s), f2_neg(f2_mul(f2_add(r, i), s)));
+}
+
+template <typename T>
+__device__ __forceinline__ T c_zero() {
+  T z;
+  if constexpr (sizeof(T) == 8) z = make_float2(0.f, 0.f);
+  else z = make_float4(0.f, 0.f, 0.f, 0.f);
+  return z;
+}
+
+// a complex float-float from two doubles (re, im)
+__device__ __forceinline__ float4 c_from(double2 x) { return cx(f2_from(x.x), f2_from(x.y)); }
+
+// In-register DFTs of 2, 4 and 8 points, natural order in and out; INV uses
+// exp(+2 pi i / R).  The 8-point one is two 4-point DFTs of the even and odd
+// inputs joined with W_8^k.
+template <bool INV, typename T>
+__device__ __forceinline__ void c_dft4(T &x0, T &x1, T &x2, T &x3) {
+  const T a = c_add(x0, x2), b = c_sub(x0, x2), c = c_add(x1, x3), d = c_w4<INV>(c_sub(x1, x3));
+  x0 = c_add(a, c);
+  x1 = c_add(b, d);
+  x2 = c_sub(a, c);
+  x3 = c_sub(b, d);
+}
+template <int R, bool INV, typename T>
+__device__ __forceinline__ void c_dft(T *v) {
   if constexpr (R == 2) {
-    const float2 t = v[0];
-    v[0] = f_add(t, v[1]);
-    v[1] = f_sub(t, v[1]);
+    const T t = v[0];
+    v[0] = c_add(t, v[1]);
+    v[1] = c_sub(t, v[1]);
   } else if constexpr (R == 4) {
-    f_dft4<INV>(v[0], v[1], v[2], v[3]);
+    c_dft4<INV>(v[0], v[1], v[2], v[3]);
   } else {
-    float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
-    f_dft4<INV>(e0, e1, e2, e3);
-    f_dft4<INV>(o0, o1, o2, o3);
-    o1 = f_mul_w8<INV>(o1);
-    o2 = f_mul_w4<INV>(o2);
-    o3 = f_mul_w8_3<INV>(o3);
-    v[0] = f_add(e0, o0);
-    v[4] = f_sub(e0, o0);
-    v[1] = f_add(e1, o1);
-    v[5] = f_sub(e1, o1);
-    v[2] = f_add(e2, o2);
-    v[6] = f_sub(e2, o2);
-    v[3] = f_add(e3, o3);
-    v[7] = f_sub(e3, o3);
+    T e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    c_dft4<INV>(e0, e1, e2, e3);
+    c_dft4<INV>(o0, o1, o2, o3);
+    o1 = c_w8<INV>(o1);
+    o2 = c_w4<INV>(o2);
+    o3 = c_w8_3<INV>(o3);
+    v[0] = c_add(e0, o0);
+    v[4] = c_sub(e0, o0);
+    v[1] = c_add(e1, o1);
+    v[5] = c_sub(e1, o1);
+    v[2] = c_add(e2, o2);
+    v[6] = c_sub(e2, o2);
+    v[3] = c_add(e3, o3);
+    v[7] = c_sub(e3, o3);
   }
 }
 
@@ -346,35 +156,34 @@ __device__ __forceinline__ void f_dft(float2 *v) {
 // pass hands its outputs to `store`.  tw[k] = W_(L ts)^k, k < L ts.
 __device__ __forceinline__ int fpad(int i) { return i + (i >> 3); }
 
-template <int L, int NS, bool INV, typename Store>
-__device__ __forceinline__ void f_stockham(float2 v[8], int j, float2 *line, int ls, const float2 *tw, int ts,
-                                           Store store) {
-  constexpr int REM = L / NS, R = REM >= 8 ? 8 : REM, NI = 8 / R, T = L / 8;
+template <int L, int NS, bool INV, typename T, typename Store>
+__device__ __forceinline__ void f_stockham(T v[8], int j, T *line, int ls, const T *tw, int ts, Store store) {
+  constexpr int REM = L / NS, R = REM >= 8 ? 8 : REM, NI = 8 / R, TH = L / 8;
 #pragma unroll
   for (int q = 0; q < NI; ++q) {
-    const int jj = j + q * T;
+    const int jj = j + q * TH;
     if constexpr (NS > 1) {
       const int k = jj & (NS - 1);
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        float2 w = tw[r * k * (L / (NS * R)) * ts];
-        if (INV) w = f_conj(w);
-        v[q * R + r] = f_mul(v[q * R + r], w);
+        T w = tw[r * k * (L / (NS * R)) * ts];
+        if (INV) w = c_conj(w);
+        v[q * R + r] = c_mul(v[q * R + r], w);
       }
     }
-    f_dft<R, INV>(&v[q * R]);
+    c_dft<R, INV>(&v[q * R]);
   }
   if constexpr (NS * R == L) {
 #pragma unroll
     for (int q = 0; q < NI; ++q) {
-      const int jj = j + q * T;
+      const int jj = j + q * TH;
 #pragma unroll
       for (int r = 0; r < R; ++r) store(jj + r * NS, v[q * R + r]);  // last pass: NS = L / R, jj < NS
     }
   } else {
 #pragma unroll
     for (int q = 0; q < NI; ++q) {
-      const int jj = j + q * T, d = (jj / NS) * NS * R + (jj & (NS - 1));
+      const int jj = j + q * TH, d = (jj / NS) * NS * R + (jj & (NS - 1));
 #pragma unroll
       for (int r = 0; r < R; ++r) line[fpad(d + r * NS) * ls] = v[q * R + r];
     }
@@ -383,30 +192,184 @@ __device__ __forceinline__ void f_stockham(float2 v[8], int j, float2 *line, int
 #pragma unroll
     for (int q = 0; q < 8 / R2; ++q)
 #pragma unroll
-      for (int r = 0; r < R2; ++r) v[q * R2 + r] = line[fpad(j + q * T + r * (L / R2)) * ls];
+      for (int r = 0; r < R2; ++r) v[q * R2 + r] = line[fpad(j + q * TH + r * (L / R2)) * ls];
     __syncthreads();
     f_stockham<L, NS2, INV>(v, j, line, ls, tw, ts, store);
   }
 }
+
+// the twiddle table W_L^k, k < L, in shared memory from the first L / 2
+// entries of the float-float table (W^(k + L/2) = -W^k)
+__device__ __forceinline__ void load_tw(float4 *tw, const float4 *__restrict__ twff, int half) {
+  for (int k = threadIdx.x; k < half; k += blockDim.x) {
+    const float4 w = twff[k];
+    tw[k] = w;
+    tw[k + half] = c_neg(w);
+  }
+}
+__device__ __forceinline__ void load_tw(float2 *tw, const float4 *__restrict__ twff, int half) {
+  for (int k = threadIdx.x; k < half; k += blockDim.x) {
+    const float4 w = twff[k];
+    tw[k] = make_float2(w.x, w.z);
+    tw[k + half] = make_float2(-w.x, -w.z);
+  }
+}
+
+// The split of an M-point FFT Z of packed reals into X[k], k <= M:
+// X[k] = E[k] + W_N^k O[k], E = (Z[k] + conj Z[M-k]) / 2,
+// O = (Z[k] - conj Z[M-k]) / 2i (W_N^M = -1).
+template <int M, typename T>
+__device__ __forceinline__ T real_split(const T *line, int k, const T *tw) {
+  const T zk = line[fpad(k % M)], zc = c_conj(line[fpad((M - k) % M)]);
+  const T E = c_half(c_add(zk, zc)), O = c_div_2i(c_sub(zk, zc));
+  return k == M ? c_sub(E, O) : c_add(E, k == 0 ? O : c_mul(tw[k], O));
+}
+
+constexpr int kFfRows = 8;   // rows per CTA of the float-float real row pass
+constexpr int kFfCRows = 4;  // rows per CTA of the float-float complex row pass
+constexpr int kFfCols = 4;   // kx columns per CTA of the float-float column passes (64 bytes)
+constexpr int kFCols = 8;    // kx columns per CTA of the float column passes (64 bytes)
+
+// Row pass: kFfRows rows of N = 2M reals -> M + 1 complex each (float-float).
+template <int M>
+__global__ void __launch_bounds__(kFfRows * M / 8) k_ff_rows(const double *__restrict__ in, float4 *__restrict__ out,
+                                                             int64_t rows, const float4 *__restrict__ twff) {
+  constexpr int N = 2 * M, NH = M + 1, TH = M / 8, LP = M + M / 8;
+  __shared__ float4 s[kFfRows * LP];
+  __shared__ float4 tw[N];  // W_N^k, k < N
+  load_tw(tw, twff, M);
+  const int64_t r0 = (int64_t)blockIdx.x * kFfRows;
+  const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
+  const bool ok = r0 + ln < rows;
+  const double2 *x = reinterpret_cast<const double2 *>(in + (r0 + ln) * N);
+  float4 v[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = ok ? c_from(x[j + r * TH]) : c_zero<float4>();
+  __syncthreads();  // twiddles
+  float4 *line = s + ln * LP;
+  f_stockham<M, 1, false>(v, j, line, 1, tw, 2, [&](int i, float4 z) { line[fpad(i)] = z; });  // W_M = W_N^2
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < kFfRows * NH; idx += blockDim.x) {
+    const int b = idx / NH, k = idx % NH;
+    if (r0 + b < rows) out[(r0 + b) * NH + k] = real_split<M>(s + b * LP, k, tw);
+  }
+}
+
+// Complex row pass: kFfCRows contiguous rows of L complex doubles -> L
+// float-float points each, transformed in place of the input (each CTA
+// reads all of its rows before it writes).
+template <int L, bool INV>
+__global__ void __launch_bounds__(kFfCRows * L / 8) k_ff_rows_c2c(double2 *__restrict__ data, int64_t rows,
+                                                                  const float4 *__restrict__ twff) {
+  constexpr int TH = L / 8, LP = L + L / 8;
+  __shared__ float4 s[kFfCRows * LP];
+  __shared__ float4 tw[L];
+  load_tw(tw, twff, L / 2);
+  const int64_t r0 = (int64_t)blockIdx.x * kFfCRows;
+  const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
+  const bool ok = r0 + ln < rows;
+  float4 v[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = ok ? c_from(data[(r0 + ln) * L + j + r * TH]) : c_zero<float4>();
+  __syncthreads();
+  float4 *out = reinterpret_cast<float4 *>(data) + (r0 + ln) * L;
+  f_stockham<L, 1, INV>(v, j, s + ln * LP, 1, tw, 1, [&](int i, float4 z) {
+    if (ok) out[i] = z;
+  });
+}
+
+// Column pass: L-point FFTs along an axis of the half spectrum for NC
+// adjacent kx.  Line (o, kx): element j at (o / ninner) shi + (o % ninner)
+// slo + j sj + kx.  Thread (j, c) of column c loads its first-pass inputs
+// from global memory and the last pass stores there; with `last` (float-
+// float only) the result goes out as double2 in place.
+template <typename T, int L, int NC, bool INV>
+__global__ void __launch_bounds__(NC * L / 8) k_cols(T *__restrict__ data, int nh, int ninner, int64_t shi,
+                                                     int64_t slo, int64_t sj, const float4 *__restrict__ twff,
+                                                     int last) {
+  constexpr int TH = L / 8, LP = L + L / 8;
+  __shared__ T s[LP * NC];
+  __shared__ T tw[L];  // W_L^k, k < L
+  load_tw(tw, twff, L / 2);
+  const int nkb = (nh + NC - 1) / NC;
+  const int o = blockIdx.x / nkb, kx0 = (blockIdx.x % nkb) * NC;
+  const int64_t base = (int64_t)(o / ninner) * shi + (int64_t)(o % ninner) * slo + kx0;
+  const int c = threadIdx.x % NC, j = threadIdx.x / NC;
+  const bool ok = kx0 + c < nh;
+  T v[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = ok ? data[base + (int64_t)(j + r * TH) * sj + c] : c_zero<T>();
+  __syncthreads();  // twiddles
+  f_stockham<L, 1, INV>(v, j, s + c, NC, tw, 1, [&](int i, T z) {
+    if (!ok) return;
+    const int64_t a = base + (int64_t)i * sj + c;
+    if constexpr (sizeof(T) == 16) {
+      if (last) {
+        reinterpret_cast<double2 *>(data)[a] = make_double2(f2_to(re(z)), f2_to(im(z)));
+        return;
+      }
+    }
+    data[a] = z;
+  });
+}
+
+template <int L, bool INV>
+int z2z_t(axg_ctx *ctx, double2 *data, const float4 *tw) {
+  constexpr int n = L;
+  const int64_t rows = (int64_t)n * n, plane = (int64_t)n * n, vol = plane * n;
+  float4 *f = reinterpret_cast<float4 *>(data);
+  AXG_LAUNCH(ctx, "fft_ff_rows_c2c", (k_ff_rows_c2c<L, INV>), (unsigned)((rows + kFfCRows - 1) / kFfCRows),
+             kFfCRows * L / 8, 0, data, rows, tw);
+  const int nkb = n / kFfCols;
+  AXG_LAUNCH(ctx, "fft_ff_y", (k_cols<float4, L, kFfCols, INV>), (unsigned)((int64_t)n * nkb), kFfCols * L / 8, 0, f,
+             n, n, vol, plane, (int64_t)n, tw, 0);
+  AXG_LAUNCH(ctx, "fft_ff_z", (k_cols<float4, L, kFfCols, INV>), (unsigned)((int64_t)n * nkb), kFfCols * L / 8, 0, f,
+             n, n, vol, (int64_t)n, plane, tw, 1);
+  return AXG_OK;
+}
+
+template <int L>
+int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 *tw, bool keep_ff) {
+  constexpr int n = L, nh = L / 2 + 1;
+  const int64_t rows = (int64_t)batch * n * n;
+  float4 *f = reinterpret_cast<float4 *>(out);
+  AXG_LAUNCH(ctx, "fft_ff_rows", k_ff_rows<L / 2>, (unsigned)((rows + kFfRows - 1) / kFfRows), kFfRows * L / 16, 0,
+             in, f, rows, tw);
+  const int nkb = (nh + kFfCols - 1) / kFfCols;
+  const int64_t plane = (int64_t)n * nh, vol = plane * n;
+  // y: lines (field, z); z: lines (field, y)
+  AXG_LAUNCH(ctx, "fft_ff_y", (k_cols<float4, L, kFfCols, false>), (unsigned)((int64_t)batch * n * nkb),
+             kFfCols * L / 8, 0, f, nh, n, vol, plane, (int64_t)nh, tw, 0);
+  AXG_LAUNCH(ctx, "fft_ff_z", (k_cols<float4, L, kFfCols, false>), (unsigned)((int64_t)batch * n * nkb),
+             kFfCols * L / 8, 0, f, nh, n, vol, (int64_t)nh, plane, tw, keep_ff ? 0 : 1);
+  return AXG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 transform of the six Green's-function sources, the source computation
+// fused into the row pass.  The FP32-mixed Green step needs the forward
+// transforms of S_ij = (2 / d^2) (dr_i dr_j + di_i di_j), d_i the raw
+// central differences of phi: the row kernel forms S_ij for its rows from
+// phi (the stencil rows come through L1 / L2) and runs the real-to-half x
+// transform of all six at once, so the real sources never reach HBM; the y
+// and z passes are the column passes in complex float.  Output as cuFFT's
+// R2C: [6][n][n][n/2+1] complex float.  Twiddles are the high parts of the
+// float-float table, i.e. W_n^k rounded to float.
 
 constexpr int kSrcRows = 2;  // x-rows per CTA of the source row pass (6 x 2 lines)
 
 // Row pass with the sources, for rows (y, z) = row0 .. row0 + kSrcRows - 1
 // of the N = 2M lattice.  Line c kSrcRows + r holds source c of row r
 // packed as M complex points z[m] = S(2m) + i S(2m + 1); an M-point FFT per
-// line (M / 8 threads each), then X[k] = E[k] + W_N^k O[k] for k <= M.
+// line (M / 8 threads each), then the split into X[k], k <= M.
 template <int M>
 __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 *__restrict__ phi, float scale,
                                                                    float2 *__restrict__ out,
                                                                    const float4 *__restrict__ twff) {
-  constexpr int N = 2 * M, NH = M + 1, NL = 6 * kSrcRows, T = M / 8, LP = M + M / 8;
+  constexpr int N = 2 * M, NH = M + 1, NL = 6 * kSrcRows, TH = M / 8, LP = M + M / 8;
   __shared__ float2 s[NL * LP];
   __shared__ float2 tw[N];  // W_N^k, k < N
-  for (int k = threadIdx.x; k < M; k += blockDim.x) {
-    const float4 w = twff[k];
-    tw[k] = make_float2(w.x, w.z);
-    tw[k + M] = make_float2(-w.x, -w.z);
-  }
+  load_tw(tw, twff, M);
   const int64_t row0 = (int64_t)blockIdx.x * kSrcRows, nhalf = (int64_t)N * N * NH;
   for (int idx = threadIdx.x; idx < kSrcRows * M; idx += blockDim.x) {
     const int r = idx / M, m = idx % M;
@@ -442,54 +405,20 @@ __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 
   }
   __syncthreads();
   {
-    const int ln = threadIdx.x / T, j = threadIdx.x % T;
+    const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
     float2 *line = s + ln * LP;
     float2 v[8];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * T)];
+    for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * TH)];
     __syncthreads();
     f_stockham<M, 1, false>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
   }
   __syncthreads();
-  // X[k] = E[k] + W_N^k O[k], E = (Z[k] + conj Z[M-k]) / 2, O = (Z[k] - conj Z[M-k]) / 2i
   for (int idx = threadIdx.x; idx < NL * NH; idx += blockDim.x) {
     const int b = idx / NH, k = idx % NH;
-    const float2 zk = s[b * LP + fpad(k % M)], zc = f_conj(s[b * LP + fpad((M - k) % M)]);
-    const float2 e = f_add(zk, zc), d = f_sub(zk, zc);
-    const float2 E = make_float2(0.5f * e.x, 0.5f * e.y), O = make_float2(0.5f * d.y, -0.5f * d.x);
-    const float2 X = k == M ? f_sub(E, O) : f_add(E, k == 0 ? O : f_mul(tw[k], O));
     const int c = b / kSrcRows, r = b % kSrcRows;
-    out[c * nhalf + (row0 + r) * NH + k] = X;
+    out[c * nhalf + (row0 + r) * NH + k] = real_split<M>(s + b * LP, k, tw);
   }
-}
-
-// Column pass in complex float: L-point FFTs along an axis of the half
-// spectrum for kLines adjacent kx, lines as in k_ff_cols; thread (j, c) of
-// column c loads its first-pass inputs from global memory and the last pass
-// stores to it.
-template <int L>
-__global__ void __launch_bounds__(kLines * L / 8) k_f_cols(float2 *__restrict__ data, int nh, int ninner, int64_t shi,
-                                                          int64_t slo, int64_t sj, const float4 *__restrict__ twff) {
-  constexpr int T = L / 8, LP = L + L / 8;
-  __shared__ float2 s[LP * kLines];
-  __shared__ float2 tw[L];  // W_L^k, k < L
-  for (int k = threadIdx.x; k < L / 2; k += blockDim.x) {
-    const float4 w = twff[k];
-    tw[k] = make_float2(w.x, w.z);
-    tw[k + L / 2] = make_float2(-w.x, -w.z);
-  }
-  const int nkb = (nh + kLines - 1) / kLines;
-  const int o = blockIdx.x / nkb, kx0 = (blockIdx.x % nkb) * kLines;
-  const int64_t base = (int64_t)(o / ninner) * shi + (int64_t)(o % ninner) * slo + kx0;
-  const int c = threadIdx.x % kLines, j = threadIdx.x / kLines;
-  const bool ok = kx0 + c < nh;
-  float2 v[8];
-#pragma unroll
-  for (int r = 0; r < 8; ++r) v[r] = ok ? data[base + (int64_t)(j + r * T) * sj + c] : make_float2(0.f, 0.f);
-  __syncthreads();  // twiddles
-  f_stockham<L, 1, false>(v, j, s + c, kLines, tw, 1, [&](int i, float2 x) {
-    if (ok) data[base + (int64_t)i * sj + c] = x;
-  });
 }
 
 template <int L>
@@ -498,12 +427,12 @@ int gws_r2c_t(axg_ctx *ctx, const float2 *phi, float2 *out, float scale, const f
   const int64_t rows = (int64_t)n * n;
   AXG_LAUNCH(ctx, "gw_source_rows_fp32", k_gws_rows<M>, (unsigned)(rows / kSrcRows), 6 * kSrcRows * M / 8, 0, phi,
              scale, out, tw);
-  const int nkb = (nh + kLines - 1) / kLines;
+  const int nkb = (nh + kFCols - 1) / kFCols;
   const int64_t plane = (int64_t)n * nh, vol = plane * n;
-  AXG_LAUNCH(ctx, "fft_f32_y", k_f_cols<L>, (unsigned)((int64_t)6 * n * nkb), kLines * L / 8, 0, out, nh, n, vol,
-             plane, (int64_t)nh, tw);
-  AXG_LAUNCH(ctx, "fft_f32_z", k_f_cols<L>, (unsigned)((int64_t)6 * n * nkb), kLines * L / 8, 0, out, nh, n, vol,
-             (int64_t)nh, plane, tw);
+  AXG_LAUNCH(ctx, "fft_f32_y", (k_cols<float2, L, kFCols, false>), (unsigned)((int64_t)6 * n * nkb), kFCols * L / 8, 0,
+             out, nh, n, vol, plane, (int64_t)nh, tw, 0);
+  AXG_LAUNCH(ctx, "fft_f32_z", (k_cols<float2, L, kFCols, false>), (unsigned)((int64_t)6 * n * nkb), kFCols * L / 8, 0,
+             out, nh, n, vol, (int64_t)nh, plane, tw, 0);
   return AXG_OK;
 }
 
