@@ -62,6 +62,24 @@ __device__ __forceinline__ F2 f2_from(double x) {
   return {h, __double2float_rn(x - (double)h)};
 }
 
+// x = h + l from the bit fields of x, no FP64 instruction (for kernels whose
+// FP64 pipe is busy with other work): h is x truncated to 24 significant
+// bits (sign, rebiased exponent and the top 23 mantissa bits moved into a
+// float), l the remaining 29 mantissa bits as an integer, converted to float
+// (rounded to 24 bits) and scaled by the power of two of their place.
+// |l| < ulp(h), about 48 significant bits in all.  Exponents outside
+// [2^-74, 2^128), zeros, subnormals and non-finite x take f2_from.
+__device__ __forceinline__ F2 f2_from_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e < 949u || e > 1150u) return f2_from(x);
+  const unsigned sign = hi & 0x80000000u;
+  const float h = __uint_as_float(sign | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+  const float l = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu), __uint_as_float((e - 948u) << 23));
+  return {h, __uint_as_float(__float_as_uint(l) | sign)};
+}
+
 __device__ __forceinline__ double f2_to(F2 a) { return (double)a.h + (double)a.l; }
 
 #endif  // AXG_FF_H

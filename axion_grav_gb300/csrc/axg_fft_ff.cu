@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "axg_ff.h"
+#include "axg_gw_source.h"
 #include "axg_internal.h"
 
 namespace {
@@ -328,13 +329,10 @@ int z2z_t(axg_ctx *ctx, double2 *data, const float4 *tw) {
   return AXG_OK;
 }
 
+// the y and z passes of a batched float-float D2Z whose row pass is done
 template <int L>
-int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 *tw, bool keep_ff) {
+int d2z_cols_t(axg_ctx *ctx, float4 *f, int batch, const float4 *tw, bool keep_ff) {
   constexpr int n = L, nh = L / 2 + 1;
-  const int64_t rows = (int64_t)batch * n * n;
-  float4 *f = reinterpret_cast<float4 *>(out);
-  AXG_LAUNCH(ctx, "fft_ff_rows", k_ff_rows<L / 2>, (unsigned)((rows + kFfRows - 1) / kFfRows), kFfRows * L / 16, 0,
-             in, f, rows, tw);
   const int nkb = (nh + kFfCols - 1) / kFfCols;
   const int64_t plane = (int64_t)n * nh, vol = plane * n;
   // y: lines (field, z); z: lines (field, y)
@@ -343,6 +341,80 @@ int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 
   AXG_LAUNCH(ctx, "fft_ff_z", (k_cols<float4, L, kFfCols, false>), (unsigned)((int64_t)batch * n * nkb),
              kFfCols * L / 8, 0, f, nh, n, vol, (int64_t)nh, plane, tw, keep_ff ? 0 : 1);
   return AXG_OK;
+}
+
+template <int L>
+int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 *tw, bool keep_ff) {
+  constexpr int n = L;
+  const int64_t rows = (int64_t)batch * n * n;
+  float4 *f = reinterpret_cast<float4 *>(out);
+  AXG_LAUNCH(ctx, "fft_ff_rows", k_ff_rows<L / 2>, (unsigned)((rows + kFfRows - 1) / kFfRows), kFfRows * L / 16, 0,
+             in, f, rows, tw);
+  return d2z_cols_t<L>(ctx, f, batch, tw, keep_ff);
+}
+
+// FP64-plain Green step: the six FP64 sources (gw_sources_fp64, the
+// reference's operations) formed inside the float-float row pass, so they
+// never reach HBM.  One CTA per x-row (y, z): six lines, one per source, of
+// M = N / 2 packed points z[m] = S(2m) + i S(2m + 1).  The FP64 pipe does
+// the sources' arithmetic only; their float-float split runs on the integer
+// pipes (f2_from_bits).  Output as k_ff_rows for batch 6.
+template <int M>
+__global__ void __launch_bounds__(6 * M / 8) k_ff_gws_rows(const double2 *__restrict__ phi, double d, double inv_d,
+                                                           int d_pow2, float4 *__restrict__ out,
+                                                           const float4 *__restrict__ twff) {
+  constexpr int N = 2 * M, NH = M + 1, TH = M / 8, LP = M + M / 8;
+  __shared__ float4 s[6 * LP];
+  __shared__ float4 tw[N];  // W_N^k, k < N
+  load_tw(tw, twff, M);
+  const int64_t row = blockIdx.x, nhalf = (int64_t)N * N * NH;
+  const int y = (int)(row % N), z = (int)(row / N);
+  const double2 *prow = phi + row * N;
+  const double2 *pym = phi + ((int64_t)z * N + (y == 0 ? N - 1 : y - 1)) * N;
+  const double2 *pyp = phi + ((int64_t)z * N + (y + 1 == N ? 0 : y + 1)) * N;
+  const double2 *pzm = phi + ((int64_t)(z == 0 ? N - 1 : z - 1) * N + y) * N;
+  const double2 *pzp = phi + ((int64_t)(z + 1 == N ? 0 : z + 1) * N + y) * N;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const int x0 = 2 * m;
+    const double2 p0 = prow[x0], p1 = prow[x0 + 1];
+    const double2 xm = prow[x0 == 0 ? N - 1 : x0 - 1], xp = prow[x0 + 2 == N ? 0 : x0 + 2];
+    double S0[6], S1[6];
+    {
+      const double2 pa[3] = {p1, pyp[x0], pzp[x0]}, pb[3] = {xm, pym[x0], pzm[x0]};
+      gw_sources_fp64(pa, pb, d, inv_d, d_pow2, S0);
+    }
+    {
+      const double2 pa[3] = {xp, pyp[x0 + 1], pzp[x0 + 1]}, pb[3] = {p0, pym[x0 + 1], pzm[x0 + 1]};
+      gw_sources_fp64(pa, pb, d, inv_d, d_pow2, S1);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) s[c * LP + fpad(m)] = cx(f2_from_bits(S0[c]), f2_from_bits(S1[c]));
+  }
+  __syncthreads();
+  {
+    const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
+    float4 *line = s + ln * LP;
+    float4 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * TH)];
+    __syncthreads();
+    f_stockham<M, 1, false>(v, j, line, 1, tw, 2, [&](int i, float4 x) { line[fpad(i)] = x; });  // W_M = W_N^2
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 6 * NH; idx += blockDim.x) {
+    const int b = idx / NH, k = idx % NH;
+    out[b * nhalf + row * NH + k] = real_split<M>(s + b * LP, k, tw);
+  }
+}
+
+template <int L>
+int ff_gws_d2z_t(axg_ctx *ctx, const double2 *phi, double d, double inv_d, int d_pow2, double2 *out,
+                 const float4 *tw, bool keep_ff) {
+  constexpr int n = L, M = L / 2;
+  float4 *f = reinterpret_cast<float4 *>(out);
+  AXG_LAUNCH(ctx, "gw_source_rows_fp64", k_ff_gws_rows<M>, (unsigned)((int64_t)n * n), 6 * M / 8, 0, phi, d, inv_d,
+             d_pow2, f, tw);
+  return d2z_cols_t<L>(ctx, f, 6, tw, keep_ff);
 }
 
 // ---------------------------------------------------------------------------
@@ -515,5 +587,21 @@ int axg_gw_source_r2c_f32(axg_ctx *ctx, const float2 *phi, float2 *out, int n, f
     case 256: return gws_r2c_t<256>(ctx, phi, out, scale, tw);
     case 512: return gws_r2c_t<512>(ctx, phi, out, scale, tw);
     default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "FP32 source transform size");
+  }
+}
+
+int axg_gw_source_d2z_ff(axg_ctx *ctx, const double2 *phi, double d, double inv_d, int d_pow2, double2 *out, int n,
+                         bool keep_ff) {
+  if (!axg_ff_fft_supported(n)) return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
+  AXG_TRY(ensure_twiddles(ctx, n));
+  const float4 *tw = reinterpret_cast<const float4 *>(ctx->ff_tw);
+  switch (n) {
+    case 16: return ff_gws_d2z_t<16>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
+    case 32: return ff_gws_d2z_t<32>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
+    case 64: return ff_gws_d2z_t<64>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
+    case 128: return ff_gws_d2z_t<128>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
+    case 256: return ff_gws_d2z_t<256>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
+    case 512: return ff_gws_d2z_t<512>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
+    default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
   }
 }

@@ -31,6 +31,7 @@
 #include "axg_binning.h"
 #include "axg_detmath.h"
 #include "axg_ff.h"
+#include "axg_gw_source.h"
 #include "axg_internal.h"
 
 namespace {
@@ -42,8 +43,7 @@ constexpr double kBigHInMstar = 2.1332e-42 / 2.435e18;
 
 __device__ __forceinline__ int kint(int j, int n) { return (j + n / 2) % n - n / 2; }
 
-// FP64 sources in the reference's operation order; division by d = 2 dx is
-// a multiplication by 1/d when d is a power of two (the same single rounding)
+// FP64 sources in the reference's operation order (gw_sources_fp64)
 __global__ void k_gw_source(const double2 *__restrict__ phi, int n, double d, double inv_d, int d_pow2,
                             double *__restrict__ src) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
@@ -56,23 +56,11 @@ __global__ void k_gw_source(const double2 *__restrict__ phi, int n, double d, do
     const int64_t sy1 = iz * n2 + (int64_t)(iy == 0 ? n - 1 : iy - 1) * n + ix;
     const int64_t sz2 = (int64_t)(iz + 1 == n ? 0 : iz + 1) * n2 + (int64_t)iy * n + ix;
     const int64_t sz1 = (int64_t)(iz == 0 ? n - 1 : iz - 1) * n2 + (int64_t)iy * n + ix;
-    const int64_t a[3] = {sx2, sy2, sz2}, b[3] = {sx1, sy1, sz1};
-    double dr[3], di[3];
+    const double2 pa[3] = {phi[sx2], phi[sy2], phi[sz2]}, pb[3] = {phi[sx1], phi[sy1], phi[sz1]};
+    double S[6];
+    gw_sources_fp64(pa, pb, d, inv_d, d_pow2, S);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const double2 pa = phi[a[k]], pb = phi[b[k]];
-      const double xr = AXD_SUB(pa.x, pb.x), xi = AXD_SUB(pa.y, pb.y);
-      dr[k] = d_pow2 ? axg_mul_pow2(xr, inv_d) : AXD_DIV(xr, d);
-      di[k] = d_pow2 ? axg_mul_pow2(xi, inv_d) : AXD_DIV(xi, d);
-    }
-    int c = 0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j <= i; ++j, ++c) {
-        const double r1 = AXD_ADD(AXD_MUL(dr[i], dr[j]), AXD_MUL(di[i], di[j]));
-        src[c * n3 + s] = axg_mul_pow2(r1, 2.0);  // == r1 + r1
-      }
+    for (int c = 0; c < 6; ++c) src[c * n3 + s] = S[c];
   }
 }
 
@@ -784,11 +772,11 @@ int axg_gw_init(axg_ctx *ctx) {
   const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
   const size_t rs = fp32 ? 4 : 8;
   // our own transforms for power-of-two N up to 512 (AXG_FFT_FF=0: cuFFT);
-  // FP32-mixed then never stores the real sources
+  // they form the sources inside their row pass, so the real sources are
+  // never stored
   ctx->gw_own_fft = axg_ff_use(n);
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->acc, (size_t)ctx->n3 * 64, "GW accumulators"));
-  if (!(fp32 && ctx->gw_own_fft))
-    AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)ctx->n3 * 6 * rs, "GW sources"));
+  if (!ctx->gw_own_fft) AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)ctx->n3 * 6 * rs, "GW sources"));
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrcF, (size_t)nhalf * 6 * 2 * rs, "GW source spectra"));
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->n3 * 64, ctx->stream));
   if (fp32) {
@@ -852,16 +840,18 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   }
   int ex;
   const int pow2 = std::frexp(d, &ex) == 0.5;
-  AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source, grid_for(ctx->n3), 256, 0, (const double2 *)ctx->phi[ctx->cur], n,
-             d, 1.0 / d, pow2, ctx->gsrc);
   // the six source transforms: float-float for power-of-two N (FP64
-  // accuracy on the FP32 pipes; kept as float-float pairs when the
-  // float-float contraction reads them), else cuFFT
+  // accuracy on the FP32 pipes, the sources formed in the row pass; kept as
+  // float-float pairs when the float-float contraction reads them), else
+  // the FP64 sources and cuFFT
   const bool ff = ctx->gw_own_fft, tab = ctx->gw_pol != nullptr;
-  if (ff)
-    AXG_TRY(axg_ff_d2z(ctx, ctx->gsrc, ctx->gsrcF, n, 6, tab));
-  else
+  if (ff) {
+    AXG_TRY(axg_gw_source_d2z_ff(ctx, (const double2 *)ctx->phi[ctx->cur], d, 1.0 / d, pow2, ctx->gsrcF, n, tab));
+  } else {
+    AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source, grid_for(ctx->n3), 256, 0, (const double2 *)ctx->phi[ctx->cur], n,
+               d, 1.0 / d, pow2, ctx->gsrc);
     AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
+  }
   const float dw_hi = (float)dw, dw_lo = (float)(dw - (double)dw_hi);
   const float2 *pol = reinterpret_cast<const float2 *>(ctx->gw_pol);
   const double *rates = ctx->gw_pol + 12 * nhalf;

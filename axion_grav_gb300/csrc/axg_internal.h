@@ -267,6 +267,10 @@ int axg_ff_z2z(axg_ctx *ctx, double2 *data, int n, int inverse);  // in place, o
 // the six FP32-mixed Green sources of phi and their forward transforms, out
 // [6][n][n][n/2+1] complex float (cuFFT R2C layout); n as axg_ff_fft_supported
 int axg_gw_source_r2c_f32(axg_ctx *ctx, const float2 *phi, float2 *out, int n, float scale);
+// the six FP64 Green sources of phi (d = 2 dx; inv_d, d_pow2 as
+// gw_sources_fp64) and their float-float D2Z, out as axg_ff_d2z for batch 6
+int axg_gw_source_d2z_ff(axg_ctx *ctx, const double2 *phi, double d, double inv_d, int d_pow2, double2 *out, int n,
+                         bool keep_ff);
 int axg_evo_batch_step(axg_ctx *any, cudaStream_t stream, const axg_ens_member_dev *d_mem, int nmem,
                        long long total_items, int cur, const axg_ens_coef *d_coef, int step, int cfg,
                        int *d_err, bool fp32, bool uij, double dspa, bool persistent);
