@@ -405,7 +405,7 @@ __device__ __forceinline__ int64_t gw_mirror_site(int hx, int hy, int hz, int n)
 // itself (kint(n/2) = -n/2) and is not -k: its polarisation is formed
 // directly.  |k|, and so the phase, is the same at both sites.
 template <typename SRC, bool ACCFF>
-__global__ void k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *__restrict__ pol,
+__global__ void __launch_bounds__(256, 3) k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *__restrict__ pol,
                                     const double *__restrict__ rates, int n, double dwav, double tau, double dw,
                                     float dw_hi, float dw_lo, int ref_compat, void *__restrict__ accp) {
   const int nh = n / 2 + 1;
