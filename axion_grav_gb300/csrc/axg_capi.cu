@@ -591,27 +591,56 @@ int axg_download_uij(axg_ctx *ctx, double *u, double *udot) {
   return AXG_OK;
 }
 
-// The FP32-mixed context keeps each accumulator component as a float-float
-// pair (hi, lo); the host side is always complex128 [4][N^3].
+// The device holds the accumulators of the stored half spectrum plus the
+// Nyquist-row mirrors (axg_gw_acc_entries); the site of -k in the other half
+// is the conjugate of its entry.  The host side is always the full
+// complex128 [4][N^3] array: download fills the other half by conjugation,
+// upload takes the stored half and the Nyquist-row mirrors (the reference's
+// accumulators are conjugate-symmetric, so nothing is lost).  FP32-mixed and
+// the float-float FP64 paths keep each component as a float-float pair.
+}  // extern "C"
+namespace {
+// for each device entry, the full-lattice site it holds
+template <typename F>
+void gw_acc_sites(int n, F f) {
+  const int nh = n / 2 + 1;
+  const int64_t nhalf = (int64_t)n * n * nh;
+  for (int hz = 0; hz < n; ++hz)
+    for (int hy = 0; hy < n; ++hy)
+      for (int hx = 0; hx < nh; ++hx) {
+        const int64_t h = ((int64_t)hz * n + hy) * nh + hx;
+        const int64_t s1 = ((int64_t)hz * n + hy) * n + hx;
+        const int64_t s2 = ((int64_t)(hz == 0 ? 0 : n - hz) * n + (hy == 0 ? 0 : n - hy)) * n + (n - hx);
+        const bool mirror = hx > 0 && hx < n / 2, nyq = mirror && (hy == n / 2 || hz == n / 2);
+        f(h, s1, mirror && !nyq ? s2 : -1);  // s2: the conjugate site
+        if (nyq) f(nhalf + gw_nyq_extra(hx, hy, hz, n), s2, -1);
+      }
+}
+}  // namespace
+extern "C" {
+
 int axg_upload_gw_green(axg_ctx *ctx, const double *acc) {
   if (!valid_ctx(ctx) || !acc) return AXG_ERR_ARG;
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
-  if (!ctx->acc_ff) {
-    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->acc, acc, (size_t)ctx->n3 * 64, cudaMemcpyHostToDevice, ctx->stream));
-    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    return AXG_OK;
-  }
-  const size_t total = (size_t)ctx->n3 * 4, chunk = (size_t)1 << 22;  // complex entries
-  std::vector<float4> buf(std::min(chunk, total));
-  float4 *dev = (float4 *)ctx->acc;
-  for (size_t o = 0; o < total; o += chunk) {
-    const size_t m = std::min(chunk, total - o);
-    for (size_t k = 0; k < m; ++k) {
-      const double re = acc[2 * (o + k)], im = acc[2 * (o + k) + 1];
-      const float rh = (float)re, ih = (float)im;
-      buf[k] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+  const int n = (int)ctx->n;
+  const int64_t n3 = ctx->n3, as = ctx->acc_stride;
+  for (int a = 0; a < 4; ++a) {
+    const double *src = acc + 2 * (size_t)a * n3;
+    if (ctx->acc_ff) {
+      std::vector<float4> buf((size_t)as);
+      gw_acc_sites(n, [&](int64_t e, int64_t s, int64_t) {
+        const double re = src[2 * s], im = src[2 * s + 1];
+        const float rh = (float)re, ih = (float)im;
+        buf[e] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+      });
+      AXG_CUDA_TRY(ctx, cudaMemcpy((float4 *)ctx->acc + a * as, buf.data(), (size_t)as * sizeof(float4),
+                                   cudaMemcpyHostToDevice));
+    } else {
+      std::vector<double2> buf((size_t)as);
+      gw_acc_sites(n, [&](int64_t e, int64_t s, int64_t) { buf[e] = make_double2(src[2 * s], src[2 * s + 1]); });
+      AXG_CUDA_TRY(ctx, cudaMemcpy((double2 *)ctx->acc + a * as, buf.data(), (size_t)as * sizeof(double2),
+                                   cudaMemcpyHostToDevice));
     }
-    AXG_CUDA_TRY(ctx, cudaMemcpy(dev + o, buf.data(), m * sizeof(float4), cudaMemcpyHostToDevice));
   }
   return AXG_OK;
 }
@@ -619,21 +648,31 @@ int axg_upload_gw_green(axg_ctx *ctx, const double *acc) {
 int axg_download_gw_green(axg_ctx *ctx, double *acc) {
   if (!valid_ctx(ctx) || !acc) return AXG_ERR_ARG;
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
-  if (!ctx->acc_ff) {
-    AXG_CUDA_TRY(ctx, cudaMemcpyAsync(acc, ctx->acc, (size_t)ctx->n3 * 64, cudaMemcpyDeviceToHost, ctx->stream));
-    AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    return AXG_OK;
-  }
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  const size_t total = (size_t)ctx->n3 * 4, chunk = (size_t)1 << 22;
-  std::vector<float4> buf(std::min(chunk, total));
-  const float4 *dev = (const float4 *)ctx->acc;
-  for (size_t o = 0; o < total; o += chunk) {
-    const size_t m = std::min(chunk, total - o);
-    AXG_CUDA_TRY(ctx, cudaMemcpy(buf.data(), dev + o, m * sizeof(float4), cudaMemcpyDeviceToHost));
-    for (size_t k = 0; k < m; ++k) {
-      acc[2 * (o + k)] = (double)buf[k].x + (double)buf[k].y;
-      acc[2 * (o + k) + 1] = (double)buf[k].z + (double)buf[k].w;
+  const int n = (int)ctx->n;
+  const int64_t n3 = ctx->n3, as = ctx->acc_stride;
+  for (int a = 0; a < 4; ++a) {
+    double *dst = acc + 2 * (size_t)a * n3;
+    auto put = [&](int64_t s, int64_t s2, double re, double im) {
+      dst[2 * s] = re;
+      dst[2 * s + 1] = im;
+      if (s2 >= 0) {
+        dst[2 * s2] = re;
+        dst[2 * s2 + 1] = -im;
+      }
+    };
+    if (ctx->acc_ff) {
+      std::vector<float4> buf((size_t)as);
+      AXG_CUDA_TRY(ctx, cudaMemcpy(buf.data(), (const float4 *)ctx->acc + a * as, (size_t)as * sizeof(float4),
+                                   cudaMemcpyDeviceToHost));
+      gw_acc_sites(n, [&](int64_t e, int64_t s, int64_t s2) {
+        put(s, s2, (double)buf[e].x + (double)buf[e].y, (double)buf[e].z + (double)buf[e].w);
+      });
+    } else {
+      std::vector<double2> buf((size_t)as);
+      AXG_CUDA_TRY(ctx, cudaMemcpy(buf.data(), (const double2 *)ctx->acc + a * as, (size_t)as * sizeof(double2),
+                                   cudaMemcpyDeviceToHost));
+      gw_acc_sites(n, [&](int64_t e, int64_t s, int64_t s2) { put(s, s2, buf[e].x, buf[e].y); });
     }
   }
   return AXG_OK;

@@ -90,33 +90,18 @@ __global__ void k_gw_source_f32(const float2 *__restrict__ phi, int n, float sca
   }
 }
 
-// |k| dwav per k-site as a float-float pair, the phase rate of the FP32 Green
-// accumulation
+// |k| dwav per stored half-spectrum entry as a float-float pair, the phase
+// rate of the FP32 Green accumulation
 __global__ void k_gw_omega(int n, double dwav, float2 *__restrict__ om) {
-  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int nh = n / 2 + 1;
+  const int64_t nhalf = (int64_t)n * n * nh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-    const double kx = (s % n + n / 2) % n - n / 2, ky = ((s / n) % n + n / 2) % n - n / 2,
-                 kz = (s / n2 + n / 2) % n - n / 2;
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
+    const double kx = kint((int)(h % nh), n), ky = kint((int)((h / nh) % n), n), kz = kint((int)(h / ((int64_t)nh * n)), n);
     const double w = sqrt(kx * kx + ky * ky + kz * kz) * dwav;
     const float hi = (float)w;
-    om[s] = make_float2(hi, (float)(w - (double)hi));
+    om[h] = make_float2(hi, (float)(w - (double)hi));
   }
-}
-
-// Half-spectrum index of k and whether the Green source is the conjugate of
-// the stored forward value (the backward transform of a real field is
-// conj(forward); the half spectrum holds kx <= n/2, the rest follows from
-// F(-k) = conj F(k)).
-__device__ __forceinline__ int64_t gw_half_index(int ix, int iy, int iz, int n, bool &conj_back) {
-  const int nh = n / 2 + 1;
-  if (ix < nh) {
-    conj_back = true;
-    return ((int64_t)iz * n + iy) * nh + ix;
-  }
-  conj_back = false;
-  const int jx = n - ix, jy = iy == 0 ? 0 : n - iy, jz = iz == 0 ? 0 : n - iz;
-  return ((int64_t)jz * n + jy) * nh + jx;
 }
 
 // get_comwav_grav (grav_waves.f90:157-191): p = (qz c - i s, qz s + i c, -r)
@@ -173,13 +158,14 @@ __device__ __forceinline__ void gw_contract(const V *__restrict__ srcF, int64_t 
   }
 }
 
+// Component a of entry s is acc[a astride + s].
 // a11 += w_c X+, a21 += w_s X+, a12 += w_c X-, a22 += w_s X- (INTENDED);
 // REF: per component a21 <- a12 + t21, a12 <- a21 + t12, i.e. after the six
 // components a12 = a12 + w_s X+ + w_c X-, a21 = a12(new) - w_c (last X-).
-__device__ __forceinline__ void gw_update(double2 *__restrict__ acc, int64_t n3, int64_t s, double wc, double ws,
+__device__ __forceinline__ void gw_update(double2 *__restrict__ acc, int64_t astride, int64_t s, double wc, double ws,
                                           const double xp[2], const double xm[2], const double lm[2],
                                           int ref_compat) {
-  double2 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
+  double2 a11 = acc[s], a21 = acc[astride + s], a12 = acc[2 * astride + s], a22 = acc[3 * astride + s];
   a11.x = fma(wc, xp[0], a11.x);
   a11.y = fma(wc, xp[1], a11.y);
   a22.x = fma(ws, xm[0], a22.x);
@@ -196,9 +182,9 @@ __device__ __forceinline__ void gw_update(double2 *__restrict__ acc, int64_t n3,
     a12.y = fma(wc, xm[1], a12.y);
   }
   acc[s] = a11;
-  acc[n3 + s] = a21;
-  acc[2 * n3 + s] = a12;
-  acc[3 * n3 + s] = a22;
+  acc[astride + s] = a21;
+  acc[2 * astride + s] = a12;
+  acc[3 * astride + s] = a22;
 }
 
 // The polarisation tensor and phase rate |k| dwav of every half-spectrum k:
@@ -233,29 +219,38 @@ __global__ void k_gw_pol_table(int n, double dwav, float2 *__restrict__ pol, dou
   }
 }
 
-// Green accumulation with the polarisation formed per k in FP64 (no table)
+// Green accumulation with the polarisation formed per k in FP64 (no table):
+// one thread per stored half-spectrum entry, as k_gw_accumulate_tab.  The
+// accumulators hold the stored half spectrum (plus the Nyquist-row mirrors);
+// the site of -k is the conjugate of its entry.
 __global__ void k_gw_accumulate(const double2 *__restrict__ srcF, int n, double dwav, double tau, double dw,
-                                int ref_compat, double2 *__restrict__ acc) {
-  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
-  const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+                                int ref_compat, int64_t astride, double2 *__restrict__ acc) {
+  const int nh = n / 2 + 1;
+  const int64_t nhalf = (int64_t)n * n * nh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-    const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / n2);
-    bool conj_back;
-    const int64_t hidx = gw_half_index(ix, iy, iz, n, conj_back);
-    const double kx = kint(ix, n), ky = kint(iy, n), kz = kint(iz, n);
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
+    const int hx = (int)(h % nh), hy = (int)((h / nh) % n), hz = (int)(h / ((int64_t)nh * n));
+    const double kx = kint(hx, n), ky = kint(hy, n), kz = kint(hz, n);
     const double qq = sqrt(kx * kx + ky * ky + kz * kz);
     double pr[6], pi[6];
     if (!gw_polarisation<double>(kx, ky, kz, qq, pr, pi)) {
       // k = 0: every e_ij is 0; the cross-wired REF updates still copy a12 into a21
-      if (ref_compat) acc[n3 + s] = acc[2 * n3 + s];
+      if (ref_compat) acc[astride + h] = acc[2 * astride + h];
       continue;
     }
     double sq, cq;
     sincos(qq * dwav * tau, &sq, &cq);
     double xp[2], xm[2], lm[2];
-    gw_contract<double, double2>(srcF, nhalf, hidx, conj_back, pr, pi, xp, xm, lm);
-    gw_update(acc, n3, s, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+    gw_contract<double, double2>(srcF, nhalf, h, true, pr, pi, xp, xm, lm);
+    gw_update(acc, astride, h, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+    if (hx > 0 && hx < n / 2 && (hy == n / 2 || hz == n / 2)) {
+      // the mirrored site on a Nyquist y / z row: its own polarisation; the
+      // same |k|, so the same phase
+      const double jkx = kint(n - hx, n), jky = kint(hy == 0 ? 0 : n - hy, n), jkz = kint(hz == 0 ? 0 : n - hz, n);
+      gw_polarisation<double>(jkx, jky, jkz, sqrt(jkx * jkx + jky * jky + jkz * jkz), pr, pi);
+      gw_contract<double, double2>(srcF, nhalf, h, false, pr, pi, xp, xm, lm);
+      gw_update(acc, astride, nhalf + gw_nyq_extra(hx, hy, hz, n), dw * cq, dw * sq, xp, xm, lm, ref_compat);
+    }
   }
 }
 
@@ -360,9 +355,9 @@ __device__ __forceinline__ void ff_contract(const SRC *__restrict__ srcF, int64_
 
 // float-float accumulators at site s: a11 += wc X+, a22 += ws X-, and a12,
 // a21 as in gw_update
-__device__ __forceinline__ void ff_update(float4 *__restrict__ acc, int64_t n3, int64_t s, F2 wc, F2 ws, F2 p0,
+__device__ __forceinline__ void ff_update(float4 *__restrict__ acc, int64_t astride, int64_t s, F2 wc, F2 ws, F2 p0,
                                           F2 p1, F2 m0, F2 m1, F2 l0, F2 l1, int ref_compat) {
-  float4 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
+  float4 a11 = acc[s], a21 = acc[astride + s], a12 = acc[2 * astride + s], a22 = acc[3 * astride + s];
   ff_axpy(a11, wc, p0, p1);
   ff_axpy(a22, ws, m0, m1);
   if (ref_compat) {
@@ -376,16 +371,11 @@ __device__ __forceinline__ void ff_update(float4 *__restrict__ acc, int64_t n3, 
     ff_axpy(a12, wc, m0, m1);
   }
   acc[s] = a11;
-  acc[n3 + s] = a21;
-  acc[2 * n3 + s] = a12;
-  acc[3 * n3 + s] = a22;
+  acc[astride + s] = a21;
+  acc[2 * astride + s] = a12;
+  acc[3 * astride + s] = a22;
 }
 
-// Full-array index of the site whose wave vector indices negate those of
-// half-spectrum entry (hx, hy, hz), 0 < hx < n/2.
-__device__ __forceinline__ int64_t gw_mirror_site(int hx, int hy, int hz, int n) {
-  return ((int64_t)(hz == 0 ? 0 : n - hz) * n + (hy == 0 ? 0 : n - hy)) * n + (n - hx);
-}
 
 // Green accumulation with the polarisation table: the contraction
 // X+- = sum e+- S runs in float-float on the FP32 pipes (four f2_dot2 per
@@ -395,38 +385,36 @@ __device__ __forceinline__ int64_t gw_mirror_site(int hx, int hy, int hz, int n)
 // the phase sin / cos are float-float (ff_sincos) and the updates run in
 // float-float, so a k-site issues about ten FP64 operations.
 //
-// One thread per stored half-spectrum entry h = (hx, hy, hz) updates the site
-// k itself and, for 0 < hx < n/2, the site of -k in the other half.  There
-// S(-k) = conj S(k) (real sources) and e+(-k) = conj e+(k), so X+-(-k) =
-// conj X+-(k): the negations are exact, so the mirrored site gets the bits a
-// contraction of its own would give, and the table entry, the six source
-// values and the phase are read and formed once for the pair.  When hy or hz
-// is the Nyquist index n/2 the mirrored site's wave vector index maps to
-// itself (kint(n/2) = -n/2) and is not -k: its polarisation is formed
-// directly.  |k|, and so the phase, is the same at both sites.
+// One thread per stored half-spectrum entry h = (hx, hy, hz).  The
+// accumulators hold that half spectrum only: for 0 < hx < n/2 the site of -k
+// in the other half has S(-k) = conj S(k) (real sources) and e+(-k) =
+// conj e+(k), so X+-(-k) = conj X+-(k) and its accumulators stay the exact
+// conjugates (the negations are exact, so they are the bits an update of
+// its own would give).  When hy or hz is the Nyquist index n/2 the mirrored
+// site's wave vector index maps to itself (kint(n/2) = -n/2) and is not -k:
+// its polarisation is formed directly and it has entries of its own
+// (gw_nyq_extra).  |k|, and so the phase, is the same at both sites.
 template <typename SRC, bool ACCFF>
 __global__ void __launch_bounds__(256, 3) k_gw_accumulate_tab(const SRC *__restrict__ srcF, const float2 *__restrict__ pol,
                                     const double *__restrict__ rates, int n, double dwav, double tau, double dw,
-                                    float dw_hi, float dw_lo, int ref_compat, void *__restrict__ accp) {
+                                    float dw_hi, float dw_lo, int ref_compat, int64_t astride,
+                                    void *__restrict__ accp) {
   const int nh = n / 2 + 1;
-  const int64_t n3 = (int64_t)n * n * n;
   const int64_t nhalf = (int64_t)n * n * nh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
     const int hx = (int)(h % nh), hy = (int)((h / nh) % n), hz = (int)(h / ((int64_t)nh * n));
-    const int64_t s1 = ((int64_t)hz * n + hy) * n + hx;
-    const bool mirror = hx > 0 && hx < n / 2;
     const double rate = rates[h];
     if (!(rate > 0)) {
-      // k = 0 (h = 0, no mirror): every e_ij is 0; the cross-wired REF
-      // updates still copy a12 into a21
+      // k = 0 (h = 0): every e_ij is 0; the cross-wired REF updates still
+      // copy a12 into a21
       if (ref_compat) {
         if constexpr (ACCFF) {
           float4 *acc = static_cast<float4 *>(accp);
-          acc[n3 + s1] = acc[2 * n3 + s1];
+          acc[astride + h] = acc[2 * astride + h];
         } else {
           double2 *acc = static_cast<double2 *>(accp);
-          acc[n3 + s1] = acc[2 * n3 + s1];
+          acc[astride + h] = acc[2 * astride + h];
         }
       }
       continue;
@@ -441,7 +429,7 @@ __global__ void __launch_bounds__(256, 3) k_gw_accumulate_tab(const SRC *__restr
     F2 p0, p1, m0, m1, l0, l1;
     ff_contract(srcF, nhalf, h, er, ei, true, p0, p1, m0, m1, l0, l1);
     // the mirrored site's own contraction on a Nyquist y or z row
-    const bool nyq = mirror && (hy == n / 2 || hz == n / 2);
+    const bool nyq = hx > 0 && hx < n / 2 && (hy == n / 2 || hz == n / 2);
     F2 q0, q1, r0, r1, v0, v1;
     if (nyq) {
       const int jx = n - hx, jy = hy == 0 ? 0 : n - hy, jz = hz == 0 ? 0 : n - hz;
@@ -455,29 +443,27 @@ __global__ void __launch_bounds__(256, 3) k_gw_accumulate_tab(const SRC *__restr
         ei[c] = f2_from(pi[c]);
       }
       ff_contract(srcF, nhalf, h, er, ei, false, q0, q1, r0, r1, v0, v1);
-    } else {
-      q0 = p0, q1 = f2_neg(p1), r0 = m0, r1 = f2_neg(m1), v0 = l0, v1 = f2_neg(l1);
     }
-    const int64_t s2 = mirror ? gw_mirror_site(hx, hy, hz, n) : -1;
+    const int64_t e2 = nyq ? nhalf + gw_nyq_extra(hx, hy, hz, n) : -1;
     if constexpr (ACCFF) {
       F2 sq, cq;
       ff_sincos(rate * tau, sq, cq);
       const F2 dwf = {dw_hi, dw_lo};
       const F2 wc = f2_add(f2_mul(dwf, cq), F2{0.f, 0.f}), ws = f2_add(f2_mul(dwf, sq), F2{0.f, 0.f});
       float4 *acc = static_cast<float4 *>(accp);
-      ff_update(acc, n3, s1, wc, ws, p0, p1, m0, m1, l0, l1, ref_compat);
-      if (mirror) ff_update(acc, n3, s2, wc, ws, q0, q1, r0, r1, v0, v1, ref_compat);
+      ff_update(acc, astride, h, wc, ws, p0, p1, m0, m1, l0, l1, ref_compat);
+      if (nyq) ff_update(acc, astride, e2, wc, ws, q0, q1, r0, r1, v0, v1, ref_compat);
     } else {
       double sq, cq;
       sincos(rate * tau, &sq, &cq);
       double2 *acc = static_cast<double2 *>(accp);
       {
         const double xp[2] = {f2_to(p0), f2_to(p1)}, xm[2] = {f2_to(m0), f2_to(m1)}, lm[2] = {f2_to(l0), f2_to(l1)};
-        gw_update(acc, n3, s1, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+        gw_update(acc, astride, h, dw * cq, dw * sq, xp, xm, lm, ref_compat);
       }
-      if (mirror) {
+      if (nyq) {
         const double xp[2] = {f2_to(q0), f2_to(q1)}, xm[2] = {f2_to(r0), f2_to(r1)}, lm[2] = {f2_to(v0), f2_to(v1)};
-        gw_update(acc, n3, s2, dw * cq, dw * sq, xp, xm, lm, ref_compat);
+        gw_update(acc, astride, e2, dw * cq, dw * sq, xp, xm, lm, ref_compat);
       }
     }
   }
@@ -514,9 +500,9 @@ __device__ __forceinline__ float gw_phase(float2 om, float th, float tl) {
 }
 
 // float-float accumulators at site s from FP32 X+, X- and the weights
-__device__ __forceinline__ void f32_update(float4 *__restrict__ acc, int64_t n3, int64_t s, float wc, float ws,
+__device__ __forceinline__ void f32_update(float4 *__restrict__ acc, int64_t astride, int64_t s, float wc, float ws,
                                            const float xp[2], const float xm[2], const float lm[2], int ref_compat) {
-  float4 a11 = acc[s], a21 = acc[n3 + s], a12 = acc[2 * n3 + s], a22 = acc[3 * n3 + s];
+  float4 a11 = acc[s], a21 = acc[astride + s], a12 = acc[2 * astride + s], a22 = acc[3 * astride + s];
   ff_add(a11.x, a11.y, wc * xp[0]);
   ff_add(a11.z, a11.w, wc * xp[1]);
   ff_add(a22.x, a22.y, ws * xm[0]);
@@ -534,53 +520,43 @@ __device__ __forceinline__ void f32_update(float4 *__restrict__ acc, int64_t n3,
     ff_add(a12.z, a12.w, wc * xm[1]);
   }
   acc[s] = a11;
-  acc[n3 + s] = a21;
-  acc[2 * n3 + s] = a12;
-  acc[3 * n3 + s] = a22;
+  acc[astride + s] = a21;
+  acc[2 * astride + s] = a12;
+  acc[3 * astride + s] = a22;
 }
 
 // FP32-mixed Green accumulation: FP32 sources, polarisation, phase and
 // contraction; the accumulators are float-float pairs (re hi, re lo, im hi,
 // im lo), so no FP64 instruction is issued per k-site.  One thread per stored
-// half-spectrum entry updates k and, for 0 < hx < n/2, -k (the conjugate
-// contraction; formed directly on Nyquist y / z rows), as in
-// k_gw_accumulate_tab.
+// half-spectrum entry; the accumulators hold that half spectrum and the
+// Nyquist-row mirrors, as in k_gw_accumulate_tab.
 __global__ void k_gw_accumulate_f32(const float2 *__restrict__ srcF, const float2 *__restrict__ om, int n, float th,
-                                    float tl, float dw, int ref_compat, float4 *__restrict__ acc) {
+                                    float tl, float dw, int ref_compat, int64_t astride, float4 *__restrict__ acc) {
   const int nh = n / 2 + 1;
-  const int64_t n3 = (int64_t)n * n * n;
   const int64_t nhalf = (int64_t)n * n * nh;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
     const int hx = (int)(h % nh), hy = (int)((h / nh) % n), hz = (int)(h / ((int64_t)nh * n));
-    const int64_t s1 = ((int64_t)hz * n + hy) * n + hx;
-    const bool mirror = hx > 0 && hx < n / 2;
     const float kx = (float)kint(hx, n), ky = (float)kint(hy, n), kz = (float)kint(hz, n);
     const float qq = sqrtf(kx * kx + ky * ky + kz * kz);
     float pr[6], pi[6];
     if (!gw_polarisation<float>(kx, ky, kz, qq, pr, pi)) {
-      if (ref_compat) acc[n3 + s1] = acc[2 * n3 + s1];  // k = 0 (h = 0, no mirror)
+      if (ref_compat) acc[astride + h] = acc[2 * astride + h];  // k = 0 (h = 0)
       continue;
     }
     float sq, cq;
-    sincosf(gw_phase(om[s1], th, tl), &sq, &cq);
+    sincosf(gw_phase(om[h], th, tl), &sq, &cq);
     const float wc = dw * cq, ws = dw * sq;
     float xp[2], xm[2], lm[2];
     gw_contract<float, float2>(srcF, nhalf, h, true, pr, pi, xp, xm, lm);
-    f32_update(acc, n3, s1, wc, ws, xp, xm, lm, ref_compat);
-    if (!mirror) continue;
-    const int64_t s2 = gw_mirror_site(hx, hy, hz, n);
-    if (hy == n / 2 || hz == n / 2) {
+    f32_update(acc, astride, h, wc, ws, xp, xm, lm, ref_compat);
+    if (hx > 0 && hx < n / 2 && (hy == n / 2 || hz == n / 2)) {
       const int jx = n - hx, jy = hy == 0 ? 0 : n - hy, jz = hz == 0 ? 0 : n - hz;
       const float jkx = (float)kint(jx, n), jky = (float)kint(jy, n), jkz = (float)kint(jz, n);
       gw_polarisation<float>(jkx, jky, jkz, sqrtf(jkx * jkx + jky * jky + jkz * jkz), pr, pi);
       gw_contract<float, float2>(srcF, nhalf, h, false, pr, pi, xp, xm, lm);
-    } else {
-      xp[1] = -xp[1];
-      xm[1] = -xm[1];
-      lm[1] = -lm[1];
+      f32_update(acc, astride, nhalf + gw_nyq_extra(hx, hy, hz, n), wc, ws, xp, xm, lm, ref_compat);
     }
-    f32_update(acc, n3, s2, wc, ws, xp, xm, lm, ref_compat);
   }
 }
 
@@ -594,25 +570,43 @@ __device__ __forceinline__ double acc_norm2(float4 z) {
   return re * re + im * im;
 }
 
-// Green accumulators -> numer / denom per bin (bin of |k|^2 from the table)
+// Green accumulators -> numer / denom per bin (bin of |k|^2 from the table).
+// A stored entry with 0 < hx < n/2 stands for k and -k (the same |k|): its
+// |A|^2 counts twice, or once plus the Nyquist-row mirror's own entry.
 template <typename A>
-__global__ void k_gw_bin_green(const A *__restrict__ acc, int n, const int16_t *__restrict__ tab, int nb,
-                               double *__restrict__ numer, double *__restrict__ denom) {
+__global__ void k_gw_bin_green(const A *__restrict__ acc, int n, int64_t astride, const int16_t *__restrict__ tab,
+                               int nb, double *__restrict__ numer, double *__restrict__ denom) {
   __shared__ double sn[kMaxBins], sd[kMaxBins];
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sn[b] = sd[b] = 0.0;
   __syncthreads();
-  const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
+  const int nh = n / 2 + 1;
+  const int64_t nhalf = (int64_t)n * n * nh;
   BinRun run;
-  for (int64_t s0 = run_start(); s0 < n3; s0 += run_stride()) {
-    for (int64_t s = s0; s < s0 + kRun && s < n3; ++s) {
-      const int kx = kint(s % n, n), ky = kint((s / n) % n, n), kz = kint(s / n2, n);
+  for (int64_t h0 = run_start(); h0 < nhalf; h0 += run_stride()) {
+    for (int64_t h = h0; h < h0 + kRun && h < nhalf; ++h) {
+      const int hx = (int)(h % nh), hy = (int)((h / nh) % n), hz = (int)(h / ((int64_t)nh * n));
+      const int kx = kint(hx, n), ky = kint(hy, n), kz = kint(hz, n);
       const int b = tab[kx * kx + ky * ky + kz * kz];
+      const bool mirror = hx > 0 && hx < n / 2;
       double v = 0.0;
       if (b >= 0) {
+        double v1 = 0.0;
 #pragma unroll
-        for (int a = 0; a < 4; ++a) v += acc_norm2(acc[a * n3 + s]);
+        for (int a = 0; a < 4; ++a) v1 += acc_norm2(acc[a * astride + h]);
+        v = v1;
+        if (mirror) {
+          if (hy == n / 2 || hz == n / 2) {
+            const int64_t e = nhalf + gw_nyq_extra(hx, hy, hz, n);
+            double v2 = 0.0;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) v2 += acc_norm2(acc[a * astride + e]);
+            v += v2;
+          } else {
+            v += v1;
+          }
+        }
       }
-      run.add(sn, sd, b, v, 1u);
+      run.add(sn, sd, b, v, mirror ? 2u : 1u);
     }
   }
   run.flush(sn, sd);
@@ -775,14 +769,14 @@ int axg_gw_init(axg_ctx *ctx) {
   // they form the sources inside their row pass, so the real sources are
   // never stored
   ctx->gw_own_fft = axg_ff_use(n);
-  AXG_TRY(axg_alloc(ctx, (void **)&ctx->acc, (size_t)ctx->n3 * 64, "GW accumulators"));
+  ctx->acc_stride = axg_gw_acc_entries(n);
+  AXG_TRY(axg_alloc(ctx, (void **)&ctx->acc, (size_t)ctx->acc_stride * 64, "GW accumulators"));
   if (!ctx->gw_own_fft) AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)ctx->n3 * 6 * rs, "GW sources"));
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrcF, (size_t)nhalf * 6 * 2 * rs, "GW source spectra"));
-  AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->n3 * 64, ctx->stream));
+  AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->acc_stride * 64, ctx->stream));
   if (fp32) {
-    AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_omega, (size_t)ctx->n3 * 8, "GW phase rates"));
-    AXG_LAUNCH(ctx, "gw_omega", k_gw_omega, grid_for(ctx->n3), 256, 0, n, kRefTwoPi / ctx->p.dspa / n,
-               ctx->gw_omega);
+    AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_omega, (size_t)nhalf * 8, "GW phase rates"));
+    AXG_LAUNCH(ctx, "gw_omega", k_gw_omega, grid_for(nhalf), 256, 0, n, kRefTwoPi / ctx->p.dspa / n, ctx->gw_omega);
   } else {
     // The FP64 polarisation table (13 doubles per half-spectrum k) when it
     // takes at most an eighth of the device memory (512^3: 7 GB); otherwise
@@ -835,7 +829,8 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
     }
     const float th = (float)tau, tl = (float)(tau - (double)th);
     AXG_LAUNCH(ctx, "gw_accumulate_fp32", k_gw_accumulate_f32, grid_for(nhalf), 256, 0,
-               (const float2 *)ctx->gsrcF, ctx->gw_omega, n, th, tl, (float)dw, ref, (float4 *)ctx->acc);
+               (const float2 *)ctx->gsrcF, ctx->gw_omega, n, th, tl, (float)dw, ref, ctx->acc_stride,
+               (float4 *)ctx->acc);
     return AXG_OK;
   }
   int ex;
@@ -858,20 +853,22 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   if (tab && ff && ctx->acc_ff)
     AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<float4, true>), grid_for(nhalf), 256, 0,
                reinterpret_cast<const float4 *>(ctx->gsrcF), pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref,
-               (void *)ctx->acc);
+               ctx->acc_stride, (void *)ctx->acc);
   else if (tab && ff)
     AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<float4, false>), grid_for(nhalf), 256, 0,
                reinterpret_cast<const float4 *>(ctx->gsrcF), pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref,
-               (void *)ctx->acc);
+               ctx->acc_stride, (void *)ctx->acc);
   else if (tab && ctx->acc_ff)
     AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<double2, true>), grid_for(nhalf), 256, 0,
-               (const double2 *)ctx->gsrcF, pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref, (void *)ctx->acc);
+               (const double2 *)ctx->gsrcF, pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref,
+               ctx->acc_stride, (void *)ctx->acc);
   else if (tab)
     AXG_LAUNCH(ctx, "gw_accumulate", (k_gw_accumulate_tab<double2, false>), grid_for(nhalf), 256, 0,
-               (const double2 *)ctx->gsrcF, pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref, (void *)ctx->acc);
+               (const double2 *)ctx->gsrcF, pol, rates, n, dwav, tau, dw, dw_hi, dw_lo, ref,
+               ctx->acc_stride, (void *)ctx->acc);
   else
-    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate, grid_for(ctx->n3), 256, 0, ctx->gsrcF, n, dwav, tau, dw, ref,
-               ctx->acc);
+    AXG_LAUNCH(ctx, "gw_accumulate", k_gw_accumulate, grid_for(nhalf), 256, 0, ctx->gsrcF, n, dwav, tau, dw, ref,
+               ctx->acc_stride, ctx->acc);
   return AXG_OK;
 }
 
@@ -900,10 +897,11 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
   AXG_TRY(axg_bin_table(ctx, AXG_BIN_GW, n, dwav, dq, nb, log_bins, edges.data(), &tab));
   if (ctx->p.gw_mode == AXG_GW_GREEN) {
     if (ctx->acc_ff)
-      AXG_LAUNCH(ctx, "gw_bin_green", k_gw_bin_green<float4>, 152 * 4, 256, 0, (const float4 *)ctx->acc, n, tab, nb,
-                 d_num, d_den);
+      AXG_LAUNCH(ctx, "gw_bin_green", k_gw_bin_green<float4>, 152 * 4, 256, 0, (const float4 *)ctx->acc, n,
+                 ctx->acc_stride, tab, nb, d_num, d_den);
     else
-      AXG_LAUNCH(ctx, "gw_bin_green", k_gw_bin_green<double2>, 152 * 4, 256, 0, ctx->acc, n, tab, nb, d_num, d_den);
+      AXG_LAUNCH(ctx, "gw_bin_green", k_gw_bin_green<double2>, 152 * 4, 256, 0, ctx->acc, n, ctx->acc_stride, tab, nb,
+                 d_num, d_den);
   } else if (ctx->p.gw_mode == AXG_GW_UIJ) {
     AXG_TRY(ensure_uij_fft(ctx));
     const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;

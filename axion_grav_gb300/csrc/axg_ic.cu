@@ -162,7 +162,7 @@ int zero_state(axg_ctx *ctx, bool keep_phid) {
   if (ctx->cphi) AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->cphi, 0, n3 * 2 * rs, ctx->stream));
   for (void *q : {ctx->u[0], ctx->u[1], ctx->ud, ctx->cu})
     if (q) AXG_CUDA_TRY(ctx, cudaMemsetAsync(q, 0, n3 * 6 * rs, ctx->stream));
-  if (ctx->acc) AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, n3 * 64, ctx->stream));
+  if (ctx->acc) AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->acc_stride * 64, ctx->stream));
   return AXG_OK;
 }
 

@@ -96,6 +96,7 @@ struct axg_ctx {
                                // [n*n*(n/2+1)] double |k| dwav; or null
   bool acc_ff = false;         // Green accumulators are float-float float4 (FP32-mixed, and the FP64 paths
                                // on the float-float transforms), else double2
+  int64_t acc_stride = 0;      // Green accumulator entries per component (axg_gw_acc_entries)
   bool gw_own_fft = false;     // Green sources transformed by axg_fft_ff.cu (FP64: float-float D2Z; FP32:
                                // the fused source + R2C), else by cuFFT; fixed when the context is made
   float *ff_tw = nullptr;      // float-float FFT twiddles W_n^k, k < n/2 (axg_fft_ff.cu)
@@ -264,6 +265,19 @@ bool axg_ff_use(int n);
 // complex value in the same 16 bytes, for a consumer that reads it so
 int axg_ff_d2z(axg_ctx *ctx, const double *in, double2 *out, int n, int batch, bool keep_ff = false);
 int axg_ff_z2z(axg_ctx *ctx, double2 *data, int n, int inverse);  // in place, one n^3 volume
+// The Green accumulators hold the stored half spectrum only: component a of
+// the entry h = (hz n + hy) (n/2 + 1) + hx is acc[a acc_stride + h], and the
+// site of -k is its conjugate (real sources, and e+(-k) = conj e+(k)).  On
+// the Nyquist y and z rows (hy or hz = n/2) the index of -k maps to itself,
+// not to -k, so for 0 < hx < n/2 those mirrored sites keep entries of their
+// own after the half spectrum: nhalf + gw_nyq_extra(hx, hy, hz, n).
+__host__ __device__ inline int64_t axg_gw_acc_entries(int n) {
+  return (int64_t)n * n * (n / 2 + 1) + (int64_t)(n / 2 - 1) * (2 * n - 1);
+}
+__host__ __device__ inline int64_t gw_nyq_extra(int hx, int hy, int hz, int n) {
+  return (int64_t)(hx - 1) * (2 * n - 1) + (hy == n / 2 ? hz : n + (hy < n / 2 ? hy : hy - 1));
+}
+
 // the six FP32-mixed Green sources of phi and their forward transforms, out
 // [6][n][n][n/2+1] complex float (cuFFT R2C layout); n as axg_ff_fft_supported
 int axg_gw_source_r2c_f32(axg_ctx *ctx, const float2 *phi, float2 *out, int n, float scale);

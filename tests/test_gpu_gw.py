@@ -133,6 +133,23 @@ def test_green_fp32_mixed_against_fp64_oracle(compat):
     np.testing.assert_allclose(gpw, pw, rtol=1e-3)
 
 
+@pytest.mark.parametrize("precision,n", [(ag.PREC_FP64_PLAIN, 16), (ag.PREC_FP64_PLAIN, 18),
+                                         (ag.PREC_FP32_MIXED, 16)])
+def test_green_accumulator_upload_download(precision, n):
+    """The device keeps the stored half spectrum and the Nyquist-row mirrors;
+    a conjugate-symmetric host array (the form the accumulation produces)
+    goes up and comes back unchanged, to the float-float precision."""
+    rng = np.random.default_rng(9)
+    acc = rng.standard_normal((4, n, n, n)) + 1j * rng.standard_normal((4, n, n, n))
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    other = (x > n // 2) & (y != n // 2) & (z != n // 2)  # sites whose entry is a conjugate
+    acc[:, other] = np.conj(acc[:, (n - z[other]) % n, (n - y[other]) % n, (n - x[other]) % n])
+    with ag.Lattice(params(n, precision, ag.GW_GREEN)) as lat:
+        lat.upload_gw_green(acc)
+        back = lat.download_gw_green()
+    assert rel(back, acc) < 1e-14
+
+
 def test_green_log_bins():
     n = 16
     phi, phid = init_state(n, 2)
