@@ -530,7 +530,7 @@ __device__ __forceinline__ void f32_update(float4 *__restrict__ acc, int64_t ast
 // im lo), so no FP64 instruction is issued per k-site.  One thread per stored
 // half-spectrum entry; the accumulators hold that half spectrum and the
 // Nyquist-row mirrors, as in k_gw_accumulate_tab.
-__global__ void k_gw_accumulate_f32(const float2 *__restrict__ srcF, const float2 *__restrict__ om, int n, float th,
+__global__ void __launch_bounds__(256, 4) k_gw_accumulate_f32(const float2 *__restrict__ srcF, const float2 *__restrict__ om, int n, float th,
                                     float tl, float dw, int ref_compat, int64_t astride, float4 *__restrict__ acc) {
   const int nh = n / 2 + 1;
   const int64_t nhalf = (int64_t)n * n * nh;
