@@ -113,10 +113,11 @@ def test_green_fp32_fused_source_transform_matches_cufft(monkeypatch, n):
 
 
 @pytest.mark.parametrize("compat", [ag.COMPAT_REF, ag.COMPAT_INTENDED])
-def test_green_fp32_mixed_against_fp64_oracle(compat):
-    """FP32 sources, R2C transforms and contractions with FP64 accumulators:
-    accumulators and the per-bin GW numerator against the FP64 oracle."""
-    n = 32
+@pytest.mark.parametrize("n", [18, 32])
+def test_green_fp32_mixed_against_fp64_oracle(compat, n):
+    """FP32 sources, transforms (own passes at N = 32, cuFFT R2C at N = 18)
+    and contractions with float-float accumulators: accumulators and the
+    per-bin GW numerator against the FP64 oracle."""
     phi, phid = init_state(n, 4)
     p64 = params(n, ag.PREC_FP64_PLAIN, ag.GW_GREEN, compat=compat)
     acc = np.zeros((4, n, n, n), np.complex128)
