@@ -359,12 +359,13 @@ int d2z_t(axg_ctx *ctx, const double *in, double2 *out, int batch, const float4 
 // M = N / 2 packed points z[m] = S(2m) + i S(2m + 1).  The FP64 pipe does
 // the sources' arithmetic only; their float-float split runs on the integer
 // pipes (f2_from_bits).  Output as k_ff_rows for batch 6.
+// One thread per packed point m in the source phase (M threads, one round).
 template <int M>
-__global__ void __launch_bounds__(6 * M / 8) k_ff_gws_rows(const double2 *__restrict__ phi, double d, double inv_d,
+__global__ void __launch_bounds__(M) k_ff_gws_rows(const double2 *__restrict__ phi, double d, double inv_d,
                                                            int d_pow2, float4 *__restrict__ out,
                                                            const float4 *__restrict__ twff) {
   constexpr int N = 2 * M, NH = M + 1, TH = M / 8, LP = M + M / 8;
-  __shared__ float4 s[6 * LP];
+  __shared__ float4 s[8 * LP];
   __shared__ float4 tw[N];  // W_N^k, k < N
   load_tw(tw, twff, M);
   const int64_t row = blockIdx.x, nhalf = (int64_t)N * N * NH;
@@ -389,9 +390,12 @@ __global__ void __launch_bounds__(6 * M / 8) k_ff_gws_rows(const double2 *__rest
     }
 #pragma unroll
     for (int c = 0; c < 6; ++c) s[c * LP + fpad(m)] = cx(f2_from_bits(S0[c]), f2_from_bits(S1[c]));
+    s[6 * LP + fpad(m)] = s[7 * LP + fpad(m)] = c_zero<float4>();
   }
   __syncthreads();
   {
+    // M threads = 8 lines of M / 8: lines 6 and 7 are scratch, transformed
+    // so that every thread reaches the same barriers, and never read
     const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
     float4 *line = s + ln * LP;
     float4 v[8];
@@ -412,8 +416,8 @@ int ff_gws_d2z_t(axg_ctx *ctx, const double2 *phi, double d, double inv_d, int d
                  const float4 *tw, bool keep_ff) {
   constexpr int n = L, M = L / 2;
   float4 *f = reinterpret_cast<float4 *>(out);
-  AXG_LAUNCH(ctx, "gw_source_rows_fp64", k_ff_gws_rows<M>, (unsigned)((int64_t)n * n), 6 * M / 8, 0, phi, d, inv_d,
-             d_pow2, f, tw);
+  AXG_LAUNCH(ctx, "gw_source_rows_fp64", k_ff_gws_rows<M>, (unsigned)((int64_t)n * n), M, 0, phi, d, inv_d, d_pow2,
+             f, tw);
   return d2z_cols_t<L>(ctx, f, 6, tw, keep_ff);
 }
 
