@@ -132,10 +132,18 @@ __global__ void k_spec_w2_hist(const double2 *__restrict__ W, int m, double *__r
 }
 
 // one block per bin pair ij (spectrum.f90:385-428 regrouped by |k|^2)
+// |k| = sqrt(iq2) dwav for every integer |k|^2 up to iq2max, formed once and
+// shared by all the (i, j) pairs of k_spec_mat instead of an FP64 square
+// root per pair and |k|^2 (FP64 runs at 1/64 of the FP32 rate on GB300)
+__global__ void k_spec_qtab(int64_t iq2max, double dwav, double *__restrict__ q) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= iq2max; i += (int64_t)gridDim.x * blockDim.x)
+    q[i] = sqrt((double)i) * dwav;
+}
+
 __global__ void k_spec_mat(const double *__restrict__ h, const double *__restrict__ cnt,
                            const double *__restrict__ mat_spec, const double *__restrict__ largeq0,
                            const double *__restrict__ dq_spec, const long long *__restrict__ range,
-                           double dwav, double *__restrict__ mat0, double *__restrict__ tat0) {
+                           const double *__restrict__ qtab, double *__restrict__ mat0, double *__restrict__ tat0) {
   const int ij = blockIdx.x;
   const long long lo = range[2 * ij], hi = range[2 * ij + 1];
   const double *tab = mat_spec + (int64_t)ij * (kNumLargeq + 1);
@@ -144,7 +152,7 @@ __global__ void k_spec_mat(const double *__restrict__ h, const double *__restric
   for (long long iq2 = lo + threadIdx.x; iq2 <= hi; iq2 += blockDim.x) {
     const double c = cnt[iq2];
     if (c == 0.0) continue;
-    const double q = sqrt((double)iq2) * dwav;
+    const double q = qtab[iq2];
     double d = (q - lq0) * idq;
     const double fl = floor(d);
     double u = 0.0;
@@ -401,13 +409,13 @@ int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, d
   // scratch: histogram + counts + mat0/tat0 + bin sums + pair ranges
   double *scratch = nullptr;
   long long *range = nullptr;
-  const size_t nscr = (size_t)(2 * (iq2max + 1) + 2 * num_cov + 2 * nb);
+  const size_t nscr = (size_t)(3 * (iq2max + 1) + 2 * num_cov + 2 * nb);
   AXG_TRY(axg_alloc(ctx, (void **)&scratch, nscr * 8, "spectrum scratch"));
   int rc = AXG_OK;
   do {
     if ((rc = axg_alloc(ctx, (void **)&range, (size_t)num_cov * 16, "pair ranges"))) break;
     double *h = scratch, *cnt = scratch + iq2max + 1, *mat0 = cnt + iq2max + 1, *tat0 = mat0 + num_cov,
-           *d_conv = tat0 + num_cov, *d_cnt = d_conv + nb;
+           *d_conv = tat0 + num_cov, *d_cnt = d_conv + nb, *qtab = d_cnt + nb;
     AXG_CUDA_TRY(ctx, cudaMemsetAsync(scratch, 0, nscr * 8, ctx->stream));
     // ---- compute_matrix_deconv (spectrum.f90:344-444) ----
     // the window is real: D2Z half spectrum (|W|^2 is the same for either sign)
@@ -430,8 +438,9 @@ int axg_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, d
       hr[2 * ij + 1] = std::min(imax2, (long long)iq2max);
     }
     AXG_CUDA_TRY(ctx, cudaMemcpyAsync(range, hr.data(), hr.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    AXG_LAUNCH(ctx, "spec_qtab", k_spec_qtab, grid_for(iq2max + 1), 256, 0, iq2max, dwav, qtab);
     AXG_LAUNCH(ctx, "spec_mat", k_spec_mat, num_cov, 256, 0, h, cnt, ctx->spec_mat, ctx->spec_largeq0,
-               ctx->spec_dq, range, dwav, mat0, tat0);
+               ctx->spec_dq, range, qtab, mat0, tat0);
     // ---- compute_conv_spec (spectrum.f90:466-567) ----
     if (fp32)
       AXG_LAUNCH(ctx, "spec_degrade", k_spec_degrade<float2>, grid_for(m3), 256, 0, (const float2 *)ctx->phid,
