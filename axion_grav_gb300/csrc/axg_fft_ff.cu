@@ -497,19 +497,136 @@ __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 
   }
 }
 
+// The u_ij spectrum's twelve real fields, tau u_c and u_c + tau u'_c (c =
+// 11, 21, 22, 31, 32, 33; FP32-mixed subtracts the Kahan compensation from
+// u first), formed inside the row pass as the Green sources are: one CTA per
+// x-row, twelve lines.  Output [12][n][n][n/2+1] complex float.
+template <int M>
+__global__ void __launch_bounds__(12 * M / 8) k_uij_rows(const float *__restrict__ u, const float *__restrict__ ud,
+                                                         const float *__restrict__ cu, int64_t n3, float tau,
+                                                         float2 *__restrict__ out, const float4 *__restrict__ twff) {
+  constexpr int N = 2 * M, NH = M + 1, TH = M / 8, LP = M + M / 8;
+  __shared__ float2 s[12 * LP];
+  __shared__ float2 tw[N];  // W_N^k, k < N
+  load_tw(tw, twff, M);
+  const int64_t row = blockIdx.x, nhalf = (int64_t)N * N * NH;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const int64_t x = row * N + 2 * m;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      float2 uv = *reinterpret_cast<const float2 *>(u + c * n3 + x);
+      if (cu) {
+        const float2 cv = *reinterpret_cast<const float2 *>(cu + c * n3 + x);
+        uv.x -= cv.x;
+        uv.y -= cv.y;
+      }
+      const float2 dv = *reinterpret_cast<const float2 *>(ud + c * n3 + x);
+      s[c * LP + fpad(m)] = make_float2(tau * uv.x, tau * uv.y);
+      s[(6 + c) * LP + fpad(m)] = make_float2(uv.x + tau * dv.x, uv.y + tau * dv.y);
+    }
+  }
+  __syncthreads();
+  {
+    const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
+    float2 *line = s + ln * LP;
+    float2 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * TH)];
+    __syncthreads();
+    f_stockham<M, 1, false>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 12 * NH; idx += blockDim.x) {
+    const int b = idx / NH, k = idx % NH;
+    out[b * nhalf + row * NH + k] = real_split<M>(s + b * LP, k, tw);
+  }
+}
+
+// The same twelve fields in FP64 (tau u_c and u_c + tau u'_c), split into
+// float-float on the integer pipes, in the float-float row pass.  Two CTAs
+// per x-row, six fields each; M threads, lines 6 and 7 scratch as in
+// k_ff_gws_rows.
+template <int M>
+__global__ void __launch_bounds__(M) k_ff_uij_rows(const double *__restrict__ u, const double *__restrict__ ud,
+                                                   int64_t n3, double tau, float4 *__restrict__ out,
+                                                   const float4 *__restrict__ twff) {
+  constexpr int N = 2 * M, NH = M + 1, TH = M / 8, LP = M + M / 8;
+  __shared__ float4 s[8 * LP];
+  __shared__ float4 tw[N];  // W_N^k, k < N
+  load_tw(tw, twff, M);
+  const int half = (int)(blockIdx.x & 1);
+  const int64_t row = blockIdx.x >> 1, nhalf = (int64_t)N * N * NH;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const int64_t x = row * N + 2 * m;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const double2 uv = *reinterpret_cast<const double2 *>(u + c * n3 + x);
+      double2 w;
+      if (half == 0) {
+        w = make_double2(tau * uv.x, tau * uv.y);
+      } else {
+        const double2 dv = *reinterpret_cast<const double2 *>(ud + c * n3 + x);
+        w = make_double2(uv.x + tau * dv.x, uv.y + tau * dv.y);
+      }
+      s[c * LP + fpad(m)] = cx(f2_from_bits(w.x), f2_from_bits(w.y));
+    }
+    s[6 * LP + fpad(m)] = s[7 * LP + fpad(m)] = c_zero<float4>();
+  }
+  __syncthreads();
+  {
+    const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
+    float4 *line = s + ln * LP;
+    float4 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * TH)];
+    __syncthreads();
+    f_stockham<M, 1, false>(v, j, line, 1, tw, 2, [&](int i, float4 x) { line[fpad(i)] = x; });  // W_M = W_N^2
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 6 * NH; idx += blockDim.x) {
+    const int b = idx / NH, k = idx % NH;
+    out[(half * 6 + b) * nhalf + row * NH + k] = real_split<M>(s + b * LP, k, tw);
+  }
+}
+
+// y and z passes in complex float of `batch` half spectra
+template <int L>
+int f_cols_t(axg_ctx *ctx, float2 *out, int batch, const float4 *tw) {
+  constexpr int n = L, nh = L / 2 + 1;
+  const int nkb = (nh + kFCols - 1) / kFCols;
+  const int64_t plane = (int64_t)n * nh, vol = plane * n;
+  AXG_LAUNCH(ctx, "fft_f32_y", (k_cols<float2, L, kFCols, false>), (unsigned)((int64_t)batch * n * nkb),
+             kFCols * L / 8, 0, out, nh, n, vol, plane, (int64_t)nh, tw, 0);
+  AXG_LAUNCH(ctx, "fft_f32_z", (k_cols<float2, L, kFCols, false>), (unsigned)((int64_t)batch * n * nkb),
+             kFCols * L / 8, 0, out, nh, n, vol, (int64_t)nh, plane, tw, 0);
+  return AXG_OK;
+}
+
+template <int L>
+int uij_r2c_t(axg_ctx *ctx, const float *u, const float *ud, const float *cu, float tau, float2 *out,
+              const float4 *tw) {
+  constexpr int n = L, M = L / 2;
+  AXG_LAUNCH(ctx, "uij_rows_fp32", k_uij_rows<M>, (unsigned)((int64_t)n * n), 12 * M / 8, 0, u, ud, cu,
+             (int64_t)n * n * n, tau, out, tw);
+  return f_cols_t<L>(ctx, out, 12, tw);
+}
+
+template <int L>
+int ff_uij_d2z_t(axg_ctx *ctx, const double *u, const double *ud, double tau, double2 *out, const float4 *tw) {
+  constexpr int n = L, M = L / 2;
+  float4 *f = reinterpret_cast<float4 *>(out);
+  AXG_LAUNCH(ctx, "uij_rows_fp64", k_ff_uij_rows<M>, (unsigned)(2 * (int64_t)n * n), M, 0, u, ud,
+             (int64_t)n * n * n, tau, f, tw);
+  return d2z_cols_t<L>(ctx, f, 12, tw, false);
+}
+
 template <int L>
 int gws_r2c_t(axg_ctx *ctx, const float2 *phi, float2 *out, float scale, const float4 *tw) {
-  constexpr int n = L, nh = L / 2 + 1, M = L / 2;
+  constexpr int n = L, M = L / 2;
   const int64_t rows = (int64_t)n * n;
   AXG_LAUNCH(ctx, "gw_source_rows_fp32", k_gws_rows<M>, (unsigned)(rows / kSrcRows), 6 * kSrcRows * M / 8, 0, phi,
              scale, out, tw);
-  const int nkb = (nh + kFCols - 1) / kFCols;
-  const int64_t plane = (int64_t)n * nh, vol = plane * n;
-  AXG_LAUNCH(ctx, "fft_f32_y", (k_cols<float2, L, kFCols, false>), (unsigned)((int64_t)6 * n * nkb), kFCols * L / 8, 0,
-             out, nh, n, vol, plane, (int64_t)nh, tw, 0);
-  AXG_LAUNCH(ctx, "fft_f32_z", (k_cols<float2, L, kFCols, false>), (unsigned)((int64_t)6 * n * nkb), kFCols * L / 8, 0,
-             out, nh, n, vol, (int64_t)nh, plane, tw, 0);
-  return AXG_OK;
+  return f_cols_t<L>(ctx, out, 6, tw);
 }
 
 }  // namespace
@@ -606,6 +723,36 @@ int axg_gw_source_d2z_ff(axg_ctx *ctx, const double2 *phi, double d, double inv_
     case 128: return ff_gws_d2z_t<128>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
     case 256: return ff_gws_d2z_t<256>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
     case 512: return ff_gws_d2z_t<512>(ctx, phi, d, inv_d, d_pow2, out, tw, keep_ff);
+    default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
+  }
+}
+
+int axg_uij_r2c_f32(axg_ctx *ctx, const float *u, const float *ud, const float *cu, float tau, float2 *out, int n) {
+  if (!axg_ff_fft_supported(n)) return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "FP32 u_ij transform size");
+  AXG_TRY(ensure_twiddles(ctx, n));
+  const float4 *tw = reinterpret_cast<const float4 *>(ctx->ff_tw);
+  switch (n) {
+    case 16: return uij_r2c_t<16>(ctx, u, ud, cu, tau, out, tw);
+    case 32: return uij_r2c_t<32>(ctx, u, ud, cu, tau, out, tw);
+    case 64: return uij_r2c_t<64>(ctx, u, ud, cu, tau, out, tw);
+    case 128: return uij_r2c_t<128>(ctx, u, ud, cu, tau, out, tw);
+    case 256: return uij_r2c_t<256>(ctx, u, ud, cu, tau, out, tw);
+    case 512: return uij_r2c_t<512>(ctx, u, ud, cu, tau, out, tw);
+    default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "FP32 u_ij transform size");
+  }
+}
+
+int axg_uij_d2z_ff(axg_ctx *ctx, const double *u, const double *ud, double tau, double2 *out, int n) {
+  if (!axg_ff_fft_supported(n)) return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
+  AXG_TRY(ensure_twiddles(ctx, n));
+  const float4 *tw = reinterpret_cast<const float4 *>(ctx->ff_tw);
+  switch (n) {
+    case 16: return ff_uij_d2z_t<16>(ctx, u, ud, tau, out, tw);
+    case 32: return ff_uij_d2z_t<32>(ctx, u, ud, tau, out, tw);
+    case 64: return ff_uij_d2z_t<64>(ctx, u, ud, tau, out, tw);
+    case 128: return ff_uij_d2z_t<128>(ctx, u, ud, tau, out, tw);
+    case 256: return ff_uij_d2z_t<256>(ctx, u, ud, tau, out, tw);
+    case 512: return ff_uij_d2z_t<512>(ctx, u, ud, tau, out, tw);
     default: return axg_set_error(ctx, AXG_ERR_UNSUPPORTED, "float-float FFT size");
   }
 }

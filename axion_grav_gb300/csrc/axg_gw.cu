@@ -743,11 +743,18 @@ int grid_for(int64_t count) {
 }
 
 int ensure_uij_fft(axg_ctx *ctx) {
-  if (ctx->plan_u_ok) return AXG_OK;
+  if (ctx->plan_u_ok || ctx->ubuf) return AXG_OK;
   const int n = (int)ctx->n;
   const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
   const size_t rs = fp32 ? 4 : 8;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
+  // our own transforms (power-of-two N up to 512; AXG_FFT_FF=0: cuFFT) form
+  // the twelve fields in their row pass: only the 12 x nhalf spectra
+  ctx->uij_own_fft = axg_ff_use(n);
+  if (ctx->uij_own_fft) {
+    AXG_TRY(axg_alloc(ctx, &ctx->ubuf, (size_t)12 * nhalf * 2 * rs, "u_ij spectra"));
+    return AXG_OK;
+  }
   // real input 12 x N^3 followed by complex output 12 x nhalf
   AXG_TRY(axg_alloc(ctx, &ctx->ubuf, (size_t)12 * ctx->n3 * rs + (size_t)12 * nhalf * 2 * rs, "u_ij FFT"));
   int dims[3] = {n, n, n};
@@ -909,22 +916,28 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
     const double dv = ctx->p.dspa * ctx->p.dspa * ctx->p.dspa;
     if (fp32) {
       float *w = (float *)ctx->ubuf;
-      float2 *F = (float2 *)(w + 12 * ctx->n3);
-      AXG_LAUNCH(ctx, "uij_prepare_fp32", (k_uij_prepare<float2, float>), grid_for(ctx->n3), 256, 0,
-                 (const float *)ctx->u[ctx->cur], (const float *)ctx->ud, (const float *)ctx->cu, ctx->n3,
-                 tau, w);
-      AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_u, w, (cufftComplex *)F));
+      float2 *F = ctx->uij_own_fft ? (float2 *)ctx->ubuf : (float2 *)(w + 12 * ctx->n3);
+      if (ctx->uij_own_fft) {
+        AXG_TRY(axg_uij_r2c_f32(ctx, (const float *)ctx->u[ctx->cur], (const float *)ctx->ud,
+                                (const float *)ctx->cu, (float)tau, F, n));
+      } else {
+        AXG_LAUNCH(ctx, "uij_prepare_fp32", (k_uij_prepare<float2, float>), grid_for(ctx->n3), 256, 0,
+                   (const float *)ctx->u[ctx->cur], (const float *)ctx->ud, (const float *)ctx->cu, ctx->n3,
+                   tau, w);
+        AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_u, w, (cufftComplex *)F));
+      }
       AXG_LAUNCH(ctx, "uij_bin_fp32", k_uij_bin<float2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
     } else {
       double *w = (double *)ctx->ubuf;
-      double2 *F = (double2 *)(w + 12 * ctx->n3);
-      AXG_LAUNCH(ctx, "uij_prepare_fp64", (k_uij_prepare<double2, double>), grid_for(ctx->n3), 256, 0,
-                 (const double *)ctx->u[ctx->cur], (const double *)ctx->ud, (const double *)nullptr, ctx->n3,
-                 tau, w);
-      if (axg_ff_use(n))
-        AXG_TRY(axg_ff_d2z(ctx, w, F, n, 12));
-      else
+      double2 *F = ctx->uij_own_fft ? (double2 *)ctx->ubuf : (double2 *)(w + 12 * ctx->n3);
+      if (ctx->uij_own_fft) {
+        AXG_TRY(axg_uij_d2z_ff(ctx, (const double *)ctx->u[ctx->cur], (const double *)ctx->ud, tau, F, n));
+      } else {
+        AXG_LAUNCH(ctx, "uij_prepare_fp64", (k_uij_prepare<double2, double>), grid_for(ctx->n3), 256, 0,
+                   (const double *)ctx->u[ctx->cur], (const double *)ctx->ud, (const double *)nullptr, ctx->n3,
+                   tau, w);
         AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_u, w, (cufftDoubleComplex *)F));
+      }
       AXG_LAUNCH(ctx, "uij_bin_fp64", k_uij_bin<double2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
     }
     (void)nhalf;

@@ -97,7 +97,8 @@ struct axg_ctx {
   bool acc_ff = false;         // Green accumulators are float-float float4 (FP32-mixed, and the FP64 paths
                                // on the float-float transforms), else double2
   int64_t acc_stride = 0;      // Green accumulator entries per component (axg_gw_acc_entries)
-  bool gw_own_fft = false;     // Green sources transformed by axg_fft_ff.cu (FP64: float-float D2Z; FP32:
+  bool gw_own_fft = false;
+  bool uij_own_fft = false;    // u_ij spectrum: fields formed in our own row transforms (no real buffer, no plan)     // Green sources transformed by axg_fft_ff.cu (FP64: float-float D2Z; FP32:
                                // the fused source + R2C), else by cuFFT; fixed when the context is made
   float *ff_tw = nullptr;      // float-float FFT twiddles W_n^k, k < n/2 (axg_fft_ff.cu)
   int ff_tw_n = 0;
@@ -281,6 +282,11 @@ __host__ __device__ inline int64_t gw_nyq_extra(int hx, int hy, int hz, int n) {
 // the six FP32-mixed Green sources of phi and their forward transforms, out
 // [6][n][n][n/2+1] complex float (cuFFT R2C layout); n as axg_ff_fft_supported
 int axg_gw_source_r2c_f32(axg_ctx *ctx, const float2 *phi, float2 *out, int n, float scale);
+// the u_ij spectrum's twelve real fields (tau u_c, u_c + tau u'_c) and their
+// forward transforms, out [12][n][n][n/2+1] complex (float, or double from
+// float-float); cu: the FP32 Kahan compensation of u, or null
+int axg_uij_r2c_f32(axg_ctx *ctx, const float *u, const float *ud, const float *cu, float tau, float2 *out, int n);
+int axg_uij_d2z_ff(axg_ctx *ctx, const double *u, const double *ud, double tau, double2 *out, int n);
 // the six FP64 Green sources of phi (d = 2 dx; inv_d, d_pow2 as
 // gw_sources_fp64) and their float-float D2Z, out as axg_ff_d2z for batch 6
 int axg_gw_source_d2z_ff(axg_ctx *ctx, const double2 *phi, double d, double inv_d, int d_pow2, double2 *out, int n,

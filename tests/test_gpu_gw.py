@@ -192,6 +192,33 @@ def test_uij_tt_spectrum(precision, tol):
     np.testing.assert_allclose(gpw, pw, rtol=tol)
 
 
+@pytest.mark.parametrize("precision,tol", [(ag.PREC_FP64_PLAIN, 1e-12), (ag.PREC_FP32_MIXED, 2e-5)])
+@pytest.mark.parametrize("n", [16, 64])
+def test_uij_spectrum_own_transforms_match_cufft(monkeypatch, precision, tol, n):
+    """For power-of-two N the u_ij spectrum forms its twelve fields inside its
+    own row transforms (complex float, or float-float for FP64); against the
+    prepare pass + cuFFT path (AXG_FFT_FF=0) the binned numerator agrees to
+    the transform precision."""
+    phi, phid = init_state(n, 5)
+    rng = np.random.default_rng(n)
+    u, ud = 0.1 * rng.standard_normal((6, n, n, n)), 0.1 * rng.standard_normal((6, n, n, n))
+    out = {}
+    for ff in ("1", "0"):
+        monkeypatch.setenv("AXG_FFT_FF", ff)
+        with ag.Lattice(params(n, precision, ag.GW_UIJ)) as lat:
+            lat.upload(phi, phid)
+            lat.upload_uij(u, ud)
+            lat.set_kernel_timing(True)
+            out[ff] = lat.grav_spec_estimation(2.6)
+            lat.synchronize()
+            names = set(k for k, _, _ in lat.kernel_timings())
+        own = any(k.startswith("uij_rows") for k in names)
+        assert own == (ff == "1")
+    monkeypatch.delenv("AXG_FFT_FF")
+    np.testing.assert_array_equal(out["1"][3], out["0"][3])
+    np.testing.assert_allclose(out["1"][2], out["0"][2], rtol=tol)
+
+
 def test_green_requires_mode():
     with ag.Lattice(params(16, ag.PREC_FP64_PLAIN, ag.GW_NONE)) as lat:
         with pytest.raises(ag.AxgError):
