@@ -66,11 +66,13 @@ __global__ void k_drift_fp64(double2 *__restrict__ phi, const double2 *__restric
 
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+// UIJ: also kick the six u_ij (a template parameter, so the phi-only kick
+// keeps the registers, and the resident warps, of its own work)
+template <bool UIJ>
 __global__ void __launch_bounds__(256) k_kick_fp64(const double2 *__restrict__ phi,
                                                    double2 *__restrict__ phid,
                                                    const double *__restrict__ u,
-                                                   double *__restrict__ ud, int n, KickCoeffs k,
-                                                   int uij) {
+                                                   double *__restrict__ ud, int n, KickCoeffs k) {
   const int ix = blockIdx.x * blockDim.x + threadIdx.x;
   const int iy = blockIdx.y * blockDim.y + threadIdx.y;
   const int iz = blockIdx.z;
@@ -114,7 +116,7 @@ __global__ void __launch_bounds__(256) k_kick_fp64(const double2 *__restrict__ p
   double pi_ = AXD_ADD(AXD_MUL(k.f1, pd.y), AXD_MUL(k.f2, li));
   pi_ = AXD_ADD(pi_, AXD_MUL(k.f3, vi));
   phid[c] = make_double2(pr, pi_);
-  if (uij) {
+  if constexpr (UIJ) {
     double dr[3], di[3];
     dr[0] = div_d(AXD_SUB(px2.x, px1.x), k.d, k.inv_d, k.d_pow2);
     di[0] = div_d(AXD_SUB(px2.y, px1.y), k.d, k.inv_d, k.d_pow2);
@@ -1002,9 +1004,12 @@ int axg_evo_kick_plain(axg_ctx *ctx, double t, double dt) {
   dim3 block(32, 8);
   dim3 grid((n + 31) / 32, (n + 7) / 8, n);
   const int b = ctx->cur;
-  AXG_LAUNCH(ctx, "kick_fp64_plain", k_kick_fp64, grid, block, 0, (const double2 *)ctx->phi[b],
-             (double2 *)ctx->phid, (const double *)ctx->u[b], (double *)ctx->ud, n, k,
-             ctx->p.gw_mode == AXG_GW_UIJ ? 1 : 0);
+  if (ctx->p.gw_mode == AXG_GW_UIJ)
+    AXG_LAUNCH(ctx, "kick_fp64_plain", k_kick_fp64<true>, grid, block, 0, (const double2 *)ctx->phi[b],
+               (double2 *)ctx->phid, (const double *)ctx->u[b], (double *)ctx->ud, n, k);
+  else
+    AXG_LAUNCH(ctx, "kick_fp64_plain", k_kick_fp64<false>, grid, block, 0, (const double2 *)ctx->phi[b],
+               (double2 *)ctx->phid, (const double *)nullptr, (double *)nullptr, n, k);
   return AXG_OK;
 }
 
