@@ -229,7 +229,7 @@ __device__ __forceinline__ T real_split(const T *line, int k, const T *tw) {
 constexpr int kFfRows = 8;   // rows per CTA of the float-float real row pass
 constexpr int kFfCRows = 4;  // rows per CTA of the float-float complex row pass
 constexpr int kFfCols = 4;   // kx columns per CTA of the float-float column passes (64 bytes)
-constexpr int kFCols = 8;    // kx columns per CTA of the float column passes (64 bytes)
+constexpr int kFCols = 8;    // kx columns per CTA of the float column passes (64 bytes; 16 measured slower)
 
 // Row pass: kFfRows rows of N = 2M reals -> M + 1 complex each (float-float).
 template <int M>
@@ -284,13 +284,19 @@ __global__ void __launch_bounds__(kFfCRows * L / 8) k_ff_rows_c2c(double2 *__res
 // slo + j sj + kx.  Thread (j, c) of column c loads its first-pass inputs
 // from global memory and the last pass stores there; with `last` (float-
 // float only) the result goes out as double2 in place.
+template <typename T, int L, int NC>
+constexpr size_t cols_smem() {
+  return ((size_t)(L + L / 8) * NC + L) * sizeof(T);
+}
+
 template <typename T, int L, int NC, bool INV>
 __global__ void __launch_bounds__(NC * L / 8) k_cols(T *__restrict__ data, int nh, int ninner, int64_t shi,
                                                      int64_t slo, int64_t sj, const float4 *__restrict__ twff,
                                                      int last) {
   constexpr int TH = L / 8, LP = L + L / 8;
-  __shared__ T s[LP * NC];
-  __shared__ T tw[L];  // W_L^k, k < L
+  extern __shared__ __align__(16) unsigned char cols_sm[];
+  T *s = reinterpret_cast<T *>(cols_sm);
+  T *tw = s + LP * NC;  // W_L^k, k < L
   load_tw(tw, twff, L / 2);
   const int nkb = (nh + NC - 1) / NC;
   const int o = blockIdx.x / nkb, kx0 = (blockIdx.x % nkb) * NC;
@@ -314,6 +320,21 @@ __global__ void __launch_bounds__(NC * L / 8) k_cols(T *__restrict__ data, int n
   });
 }
 
+// launch k_cols<T, L, NC, INV> (its shared memory may exceed the 48 KB default)
+template <typename T, int L, int NC, bool INV>
+int launch_cols(axg_ctx *ctx, const char *name, int64_t blocks, T *data, int nh, int ninner, int64_t shi, int64_t slo,
+                int64_t sj, const float4 *tw, int last) {
+  static bool attr = false;
+  constexpr size_t sm = cols_smem<T, L, NC>();
+  if (!attr && sm > 48 * 1024) {
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_cols<T, L, NC, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    attr = true;
+  }
+  AXG_LAUNCH(ctx, name, (k_cols<T, L, NC, INV>), (unsigned)blocks, NC * L / 8, sm, data, nh, ninner, shi, slo, sj, tw,
+             last);
+  return AXG_OK;
+}
+
 template <int L, bool INV>
 int z2z_t(axg_ctx *ctx, double2 *data, const float4 *tw) {
   constexpr int n = L;
@@ -322,10 +343,10 @@ int z2z_t(axg_ctx *ctx, double2 *data, const float4 *tw) {
   AXG_LAUNCH(ctx, "fft_ff_rows_c2c", (k_ff_rows_c2c<L, INV>), (unsigned)((rows + kFfCRows - 1) / kFfCRows),
              kFfCRows * L / 8, 0, data, rows, tw);
   const int nkb = n / kFfCols;
-  AXG_LAUNCH(ctx, "fft_ff_y", (k_cols<float4, L, kFfCols, INV>), (unsigned)((int64_t)n * nkb), kFfCols * L / 8, 0, f,
-             n, n, vol, plane, (int64_t)n, tw, 0);
-  AXG_LAUNCH(ctx, "fft_ff_z", (k_cols<float4, L, kFfCols, INV>), (unsigned)((int64_t)n * nkb), kFfCols * L / 8, 0, f,
-             n, n, vol, (int64_t)n, plane, tw, 1);
+  AXG_TRY((launch_cols<float4, L, kFfCols, INV>(ctx, "fft_ff_y", (int64_t)n * nkb, f, n, n, vol, plane, (int64_t)n,
+                                                 tw, 0)));
+  AXG_TRY((launch_cols<float4, L, kFfCols, INV>(ctx, "fft_ff_z", (int64_t)n * nkb, f, n, n, vol, (int64_t)n, plane,
+                                                 tw, 1)));
   return AXG_OK;
 }
 
@@ -336,10 +357,10 @@ int d2z_cols_t(axg_ctx *ctx, float4 *f, int batch, const float4 *tw, bool keep_f
   const int nkb = (nh + kFfCols - 1) / kFfCols;
   const int64_t plane = (int64_t)n * nh, vol = plane * n;
   // y: lines (field, z); z: lines (field, y)
-  AXG_LAUNCH(ctx, "fft_ff_y", (k_cols<float4, L, kFfCols, false>), (unsigned)((int64_t)batch * n * nkb),
-             kFfCols * L / 8, 0, f, nh, n, vol, plane, (int64_t)nh, tw, 0);
-  AXG_LAUNCH(ctx, "fft_ff_z", (k_cols<float4, L, kFfCols, false>), (unsigned)((int64_t)batch * n * nkb),
-             kFfCols * L / 8, 0, f, nh, n, vol, (int64_t)nh, plane, tw, keep_ff ? 0 : 1);
+  AXG_TRY((launch_cols<float4, L, kFfCols, false>(ctx, "fft_ff_y", (int64_t)batch * n * nkb, f, nh, n, vol, plane,
+                                                   (int64_t)nh, tw, 0)));
+  AXG_TRY((launch_cols<float4, L, kFfCols, false>(ctx, "fft_ff_z", (int64_t)batch * n * nkb, f, nh, n, vol,
+                                                   (int64_t)nh, plane, tw, keep_ff ? 0 : 1)));
   return AXG_OK;
 }
 
@@ -595,10 +616,10 @@ int f_cols_t(axg_ctx *ctx, float2 *out, int batch, const float4 *tw) {
   constexpr int n = L, nh = L / 2 + 1;
   const int nkb = (nh + kFCols - 1) / kFCols;
   const int64_t plane = (int64_t)n * nh, vol = plane * n;
-  AXG_LAUNCH(ctx, "fft_f32_y", (k_cols<float2, L, kFCols, false>), (unsigned)((int64_t)batch * n * nkb),
-             kFCols * L / 8, 0, out, nh, n, vol, plane, (int64_t)nh, tw, 0);
-  AXG_LAUNCH(ctx, "fft_f32_z", (k_cols<float2, L, kFCols, false>), (unsigned)((int64_t)batch * n * nkb),
-             kFCols * L / 8, 0, out, nh, n, vol, (int64_t)nh, plane, tw, 0);
+  AXG_TRY((launch_cols<float2, L, kFCols, false>(ctx, "fft_f32_y", (int64_t)batch * n * nkb, out, nh, n, vol, plane,
+                                                  (int64_t)nh, tw, 0)));
+  AXG_TRY((launch_cols<float2, L, kFCols, false>(ctx, "fft_f32_z", (int64_t)batch * n * nkb, out, nh, n, vol,
+                                                  (int64_t)nh, plane, tw, 0)));
   return AXG_OK;
 }
 
