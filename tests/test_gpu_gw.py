@@ -219,6 +219,28 @@ def test_uij_spectrum_own_transforms_match_cufft(monkeypatch, precision, tol, n)
     np.testing.assert_allclose(out["1"][2], out["0"][2], rtol=tol)
 
 
+@pytest.mark.parametrize("precision,rs", [(ag.PREC_FP64_PLAIN, 8), (ag.PREC_FP32_MIXED, 4)])
+def test_own_transforms_store_no_real_fields(monkeypatch, precision, rs):
+    """With the library's own transforms the Green sources and the u_ij
+    spectrum's twelve fields are formed inside the row passes: against the
+    cuFFT path the context holds their real buffers less (6 and 12 fields
+    of N^3 reals), and only a twiddle table more."""
+    n = 64
+    mem = {}
+    for ff in ("1", "0"):
+        monkeypatch.setenv("AXG_FFT_FF", ff)
+        with ag.Lattice(params(n, precision, ag.GW_GREEN)) as lat:
+            mem[("green", ff)] = lat.memory_bytes()
+        with ag.Lattice(params(n, precision, ag.GW_UIJ)) as lat:
+            lat.ic_gaussian_flat(1.0)
+            lat.grav_spec_estimation(2.0)
+            mem[("uij", ff)] = lat.memory_bytes()
+    monkeypatch.delenv("AXG_FFT_FF")
+    tw = n // 2 * 16  # the own transforms' float-float twiddle table
+    assert mem[("green", "0")] - mem[("green", "1")] >= 6 * n ** 3 * rs - tw
+    assert mem[("uij", "0")] - mem[("uij", "1")] >= 12 * n ** 3 * rs - tw
+
+
 def test_green_requires_mode():
     with ag.Lattice(params(16, ag.PREC_FP64_PLAIN, ag.GW_NONE)) as lat:
         with pytest.raises(ag.AxgError):
