@@ -102,6 +102,7 @@ EXPORTED_SYMBOLS = (
     "axg_ensemble_size", "axg_ensemble_member", "axg_ensemble_leapfrog", "axg_ensemble_autotune",
     "axg_ensemble_launch_count", "axg_adjoint_gw_band", "axg_spectrum_covariance", "axg_compute_crho_cov",
     "axg_epsilon", "axg_ensemble_set_tile", "axg_ensemble_set_launch_mode", "axg_ensemble_launch_mode",
+    "axg_selftest_wait_timeout",
 )
 
 _lib = None
@@ -169,6 +170,7 @@ def load_library():
         "axg_kernel_timing": ([c_ctx, ctypes.c_int, ctypes.c_char_p, ctypes.c_int64, i64p, dp],
                               ctypes.c_int),
         "axg_launch_count": ([c_ctx, i64p], ctypes.c_int),
+        "axg_selftest_wait_timeout": ([c_ctx, ctypes.c_int64], ctypes.c_int),
         "axg_tile_count": ([], ctypes.c_int),
         "axg_tile_info": ([ctypes.c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32),
                            P(ctypes.c_int32)], ctypes.c_int),
@@ -334,12 +336,18 @@ class Lattice:
         self._check(self.lib.axg_download_uij(self._ctx, _dptr(u), _dptr(ud)))
         return u, ud
 
+    @property
+    def gw_n(self) -> int:
+        """Side of the Green's-function GW grid: ngrid / 2**degrade_spec
+        (init_grav, grav_waves.f90:37-45)."""
+        return self.n >> int(self.params.degrade_spec)
+
     def upload_gw_green(self, acc: np.ndarray):
-        assert acc.dtype == np.complex128 and acc.size == 4 * self.n ** 3
+        assert acc.dtype == np.complex128 and acc.size == 4 * self.gw_n ** 3
         self._check(self.lib.axg_upload_gw_green(self._ctx, _dptr(acc.view(np.float64))))
 
     def download_gw_green(self) -> np.ndarray:
-        n = self.n
+        n = self.gw_n
         acc = np.empty((4, n, n, n), np.complex128)
         self._check(self.lib.axg_download_gw_green(self._ctx, _dptr(acc.view(np.float64))))
         return acc
@@ -515,6 +523,11 @@ class Lattice:
         v = ctypes.c_int64()
         self._check(self.lib.axg_launch_count(self._ctx, ctypes.byref(v)))
         return v.value
+
+    def selftest_wait_timeout(self, wait_cycles: int = 2_000_000):
+        """Run the give-up path of the bounded stage wait (axg_selftest_wait_timeout);
+        raises AxgError(ERR_TIMEOUT) when the path works."""
+        self._check(self.lib.axg_selftest_wait_timeout(self._ctx, int(wait_cycles)))
 
 
 class Ensemble:

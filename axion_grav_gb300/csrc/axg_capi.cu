@@ -451,6 +451,11 @@ int axg_create(const axg_params *pin, axg_ctx **out) {
   if (!(p.dspa > 0) || !(p.sigma_cr > 0)) return axg_set_error(nullptr, AXG_ERR_ARG, "dspa/sigma_cr");
   if (p.degrade_spec < 0 || (p.ngrid >> p.degrade_spec) < 2 || ((p.ngrid >> p.degrade_spec) << p.degrade_spec) != p.ngrid)
     return axg_set_error(nullptr, AXG_ERR_ARG, "degrade_spec");
+  // Green's mode runs on the GW grid ngrid / 2^degrade_spec (grav_waves.f90:37-45);
+  // its half-spectrum accumulators need that side even and >= 4
+  if (p.gw_mode == AXG_GW_GREEN && (((p.ngrid >> p.degrade_spec) & 1) || (p.ngrid >> p.degrade_spec) < 4))
+    return axg_set_error(nullptr, AXG_ERR_UNSUPPORTED,
+                         "gw_mode GREEN needs ngrid / 2^degrade_spec even and >= 4 (the GW grid of init_grav)");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
     cudaGetLastError();
@@ -622,8 +627,8 @@ extern "C" {
 int axg_upload_gw_green(axg_ctx *ctx, const double *acc) {
   if (!valid_ctx(ctx) || !acc) return AXG_ERR_ARG;
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
-  const int n = (int)ctx->n;
-  const int64_t n3 = ctx->n3, as = ctx->acc_stride;
+  const int n = ctx->gw_n;  // the GW grid (ngrid / 2^degrade_spec)
+  const int64_t n3 = (int64_t)n * n * n, as = ctx->acc_stride;
   for (int a = 0; a < 4; ++a) {
     const double *src = acc + 2 * (size_t)a * n3;
     if (ctx->acc_ff) {
@@ -649,8 +654,8 @@ int axg_download_gw_green(axg_ctx *ctx, double *acc) {
   if (!valid_ctx(ctx) || !acc) return AXG_ERR_ARG;
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  const int n = (int)ctx->n;
-  const int64_t n3 = ctx->n3, as = ctx->acc_stride;
+  const int n = ctx->gw_n;  // the GW grid (ngrid / 2^degrade_spec)
+  const int64_t n3 = (int64_t)n * n * n, as = ctx->acc_stride;
   for (int a = 0; a < 4; ++a) {
     double *dst = acc + 2 * (size_t)a * n3;
     auto put = [&](int64_t s, int64_t s2, double re, double im) {
@@ -821,7 +826,10 @@ namespace {
 // compensation, phi'; u, its compensation and u' when present) so that a
 // resumed FP32 run continues bit for bit; the complex128 file alone fixes
 // only the compensated value phi - c.  Layout: "AXGFP32" NUL, int64 N, int64
-// uij, the arrays, CRC-32 of everything before it.
+// uij, int64 CRC-32 of the complex128 checkpoint it belongs to, the arrays,
+// CRC-32 of everything before it.  A sidecar whose recorded checkpoint CRC
+// differs from the checkpoint being read belongs to another checkpoint
+// (one rewritten since, by this library or another writer) and is ignored.
 struct RawField {
   void *dev;
   size_t bytes;
@@ -838,10 +846,10 @@ std::vector<RawField> fp32_fields(axg_ctx *ctx) {
 }
 const char kFp32Magic[8] = {'A', 'X', 'G', 'F', 'P', '3', '2', 0};
 
-int write_fp32_sidecar(axg_ctx *ctx, const std::string &path) {
+int write_fp32_sidecar(axg_ctx *ctx, const std::string &path, uint32_t chk_crc) {
   FILE *f = std::fopen(path.c_str(), "wb");
   if (!f) return axg_set_error(ctx, AXG_ERR_IO, "cannot open " + path);
-  const int64_t hdr[2] = {ctx->n, ctx->p.gw_mode == AXG_GW_UIJ ? 1 : 0};
+  const int64_t hdr[3] = {ctx->n, ctx->p.gw_mode == AXG_GW_UIJ ? 1 : 0, (int64_t)chk_crc};
   uint32_t crc = crc32_update(0, (const unsigned char *)kFp32Magic, 8);
   crc = crc32_update(crc, (const unsigned char *)hdr, sizeof(hdr));
   int rc = AXG_OK;
@@ -863,12 +871,13 @@ int write_fp32_sidecar(axg_ctx *ctx, const std::string &path) {
   return rc;
 }
 
-// 1: restored, 0: no sidecar, < 0: error (a sidecar that exists must verify)
-int read_fp32_sidecar(axg_ctx *ctx, const std::string &path) {
+// 1: restored, 0: no sidecar of this checkpoint, < 0: error (a sidecar of
+// this checkpoint must verify)
+int read_fp32_sidecar(axg_ctx *ctx, const std::string &path, uint32_t chk_crc) {
   FILE *f = std::fopen(path.c_str(), "rb");
   if (!f) return 0;
   char magic[8];
-  int64_t hdr[2];
+  int64_t hdr[3];
   int rc = AXG_OK;
   if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kFp32Magic, 8) != 0 ||
       std::fread(hdr, 1, sizeof(hdr), f) != sizeof(hdr)) {
@@ -878,6 +887,10 @@ int read_fp32_sidecar(axg_ctx *ctx, const std::string &path) {
   if (hdr[0] != ctx->n || hdr[1] != (ctx->p.gw_mode == AXG_GW_UIJ ? 1 : 0)) {
     std::fclose(f);
     return axg_set_error(ctx, AXG_ERR_IO, "FP32 sidecar: lattice or u_ij mismatch");
+  }
+  if (hdr[2] != (int64_t)chk_crc) {  // written beside an older checkpoint of this path
+    std::fclose(f);
+    return 0;
   }
   uint32_t crc = crc32_update(0, (const unsigned char *)magic, 8);
   crc = crc32_update(crc, (const unsigned char *)hdr, sizeof(hdr));
@@ -937,8 +950,10 @@ int axg_write_chk(axg_ctx *ctx, const char *path) {
   std::fclose(c);
   if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    return write_fp32_sidecar(ctx, std::string(path) + ".fp32");
+    return write_fp32_sidecar(ctx, std::string(path) + ".fp32", crc);
   }
+  // an FP32 sidecar left by an earlier checkpoint of this path is stale
+  std::remove((std::string(path) + ".fp32").c_str());
   return AXG_OK;
 }
 
@@ -988,7 +1003,7 @@ int axg_read_chk(axg_ctx *ctx, const char *path) {
   if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
     // the raw FP32 state, when its sidecar is there, replaces the converted one
     AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    const int r = read_fp32_sidecar(ctx, std::string(path) + ".fp32");
+    const int r = read_fp32_sidecar(ctx, std::string(path) + ".fp32", crc);
     if (r < 0) return r;
   }
   return AXG_OK;

@@ -205,13 +205,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: gives up after kWaitCycles and reports failure.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+// Bounded wait: gives up after `limit` SM cycles (kWaitCycles in the
+// kernels) and reports failure.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long limit = kWaitCycles) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
 __device__ __forceinline__ void fence_barrier_init() {
@@ -1097,6 +1098,33 @@ int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd) {
   }
   ctx->cur = o;
   return AXG_OK;
+}
+
+namespace {
+// The give-up path of the bounded stage wait, run on its own: one CTA
+// initialises a stage barrier that expects one arrival, issues no copy and
+// never arrives, so every thread's bounded wait runs out after `limit`
+// cycles; the CTA then raises the timeout flag exactly as the fused kernel
+// does (__syncthreads_or, one atomicCAS) and returns.  Nothing is in flight
+// when it gives up.
+__global__ void k_wait_timeout_selftest(long long limit, int *err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bar), 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(smem_u32(&bar), 0, limit);
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) atomicCAS(err, 0, AXG_KERR_MBAR_TIMEOUT);
+  }
+}
+}  // namespace
+
+extern "C" int axg_selftest_wait_timeout(axg_ctx *ctx, int64_t wait_cycles) {
+  if (!ctx || wait_cycles < 1000 || wait_cycles > kWaitCycles) return AXG_ERR_ARG;
+  AXG_LAUNCH(ctx, "wait_timeout_selftest", k_wait_timeout_selftest, 1, 128, 0, (long long)wait_cycles, ctx->d_err);
+  return axg_evo_check_error(ctx);
 }
 
 int axg_evo_check_error(axg_ctx *ctx) {

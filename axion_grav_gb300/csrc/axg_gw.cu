@@ -90,6 +90,80 @@ __global__ void k_gw_source_f32(const float2 *__restrict__ phi, int n, float sca
   }
 }
 
+// data1_to_arr_dphi_degrade (grav_waves.f90:358-415) fused with the six
+// sources, for degrade_spec > 0: one thread per cell of the GW grid
+// (m = n / deg a side).  The central differences of the deg^3 fine sites a
+// cell covers are summed in the reference's order (z, then y, then x; each
+// step (sum + phi(x + e)) - phi(x - e)), divided by d = deg^3 dx 2 and
+// multiplied as in gw_sources_fp64.  src: [6][m^3].
+__global__ void k_gw_source_degrade(const double2 *__restrict__ phi, int n, int deg, double d, double inv_d,
+                                    int d_pow2, double *__restrict__ src) {
+  const int m = n / deg;
+  const int64_t n2 = (int64_t)n * n, m3 = (int64_t)m * m * m;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < m3; c += stride) {
+    const int cx = (int)(c % m), cy = (int)((c / m) % m), cz = (int)(c / ((int64_t)m * m));
+    double xr[3] = {0.0, 0.0, 0.0}, xi[3] = {0.0, 0.0, 0.0};
+    for (int iz = cz * deg; iz < (cz + 1) * deg; ++iz) {
+      const int64_t z0 = iz * n2, zp = (iz + 1 == n ? 0 : iz + 1) * n2, zm = (iz == 0 ? n - 1 : iz - 1) * n2;
+      for (int iy = cy * deg; iy < (cy + 1) * deg; ++iy) {
+        const int64_t y0 = (int64_t)iy * n, yp = (int64_t)(iy + 1 == n ? 0 : iy + 1) * n,
+                      ym = (int64_t)(iy == 0 ? n - 1 : iy - 1) * n;
+        for (int ix = cx * deg; ix < (cx + 1) * deg; ++ix) {
+          const int xp = ix + 1 == n ? 0 : ix + 1, xm = ix == 0 ? n - 1 : ix - 1;
+          const double2 a[3] = {phi[z0 + y0 + xp], phi[z0 + yp + ix], phi[zp + y0 + ix]};
+          const double2 b[3] = {phi[z0 + y0 + xm], phi[z0 + ym + ix], phi[zm + y0 + ix]};
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            xr[k] = AXD_SUB(AXD_ADD(xr[k], a[k].x), b[k].x);
+            xi[k] = AXD_SUB(AXD_ADD(xi[k], a[k].y), b[k].y);
+          }
+        }
+      }
+    }
+    double S[6];
+    gw_sources_from_diff(xr, xi, d, inv_d, d_pow2, S);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) src[k * m3 + c] = S[k];
+  }
+}
+
+// The FP32-mixed form: the differences of the FP32 field are summed as
+// differences (sum + (phi(x + e) - phi(x - e))), which keeps the FP32 sum
+// accurate for smooth fields, and the products are scaled by 2 / d^2 once.
+__global__ void k_gw_source_degrade_f32(const float2 *__restrict__ phi, int n, int deg, float scale,
+                                        float *__restrict__ src) {
+  const int m = n / deg;
+  const int64_t n2 = (int64_t)n * n, m3 = (int64_t)m * m * m;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < m3; c += stride) {
+    const int cx = (int)(c % m), cy = (int)((c / m) % m), cz = (int)(c / ((int64_t)m * m));
+    float xr[3] = {0.f, 0.f, 0.f}, xi[3] = {0.f, 0.f, 0.f};
+    for (int iz = cz * deg; iz < (cz + 1) * deg; ++iz) {
+      const int64_t z0 = iz * n2, zp = (iz + 1 == n ? 0 : iz + 1) * n2, zm = (iz == 0 ? n - 1 : iz - 1) * n2;
+      for (int iy = cy * deg; iy < (cy + 1) * deg; ++iy) {
+        const int64_t y0 = (int64_t)iy * n, yp = (int64_t)(iy + 1 == n ? 0 : iy + 1) * n,
+                      ym = (int64_t)(iy == 0 ? n - 1 : iy - 1) * n;
+        for (int ix = cx * deg; ix < (cx + 1) * deg; ++ix) {
+          const int xp = ix + 1 == n ? 0 : ix + 1, xm = ix == 0 ? n - 1 : ix - 1;
+          const float2 a[3] = {phi[z0 + y0 + xp], phi[z0 + yp + ix], phi[zp + y0 + ix]};
+          const float2 b[3] = {phi[z0 + y0 + xm], phi[z0 + ym + ix], phi[zm + y0 + ix]};
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            xr[k] += a[k].x - b[k].x;
+            xi[k] += a[k].y - b[k].y;
+          }
+        }
+      }
+    }
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j <= i; ++j, ++k) src[k * m3 + c] = scale * (xr[i] * xr[j] + xi[i] * xi[j]);
+  }
+}
+
 // |k| dwav per stored half-spectrum entry as a float-float pair, the phase
 // rate of the FP32 Green accumulation
 __global__ void k_gw_omega(int n, double dwav, float2 *__restrict__ om) {
@@ -733,9 +807,10 @@ __global__ void k_uij_bin(const CV *__restrict__ F, int n, double dwav, double d
   }
 }
 
-double gw_fact(const axg_params &p) {
-  // grav_waves.f90:265-267
-  const double dwav = kRefTwoPi / p.dspa / p.ngrid;
+// grav_waves.f90:265-267 on an n^3 grid of spacing dspa (the GW grid of
+// init_grav for Green's mode, the lattice for u_ij)
+double gw_fact(const axg_params &p, int n, double dspa) {
+  const double dwav = kRefTwoPi / dspa / n;
   const double dv_wav = std::pow(dwav / kRefTwoPi, 3);
   const double tc = p.tau_cr;
   const double tc6 = tc * tc * tc * tc * tc * tc;
@@ -775,22 +850,31 @@ int ensure_uij_fft(axg_ctx *ctx) {
 }  // namespace
 
 int axg_gw_init(axg_ctx *ctx) {
-  const int n = (int)ctx->n;
+  // init_grav (grav_waves.f90:37-45): everything of Green's mode lives on the
+  // GW grid, the lattice coarse-grained by deg = 2^degrade_spec
+  const int deg = 1 << ctx->p.degrade_spec;
+  const int n = (int)ctx->n / deg;
+  ctx->gw_n = n;
+  ctx->gw_dspa = ctx->p.dspa * deg;
+  const int64_t n3 = (int64_t)n * n * n;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   const bool fp32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
   const size_t rs = fp32 ? 4 : 8;
   // our own transforms for power-of-two N up to 512 (AXG_FFT_FF=0: cuFFT);
-  // they form the sources inside their row pass, so the real sources are
-  // never stored
-  ctx->gw_own_fft = axg_ff_use(n);
+  // on the full lattice they form the sources inside their row pass, so the
+  // real sources are never stored.  Degraded sources are stored (n^3 is
+  // 1/8 of the lattice or less) and transformed by the float-float D2Z
+  // (FP64 paths) or cuFFT (FP32-mixed).
+  ctx->gw_own_fft = deg == 1 && axg_ff_use(n);
+  ctx->gw_ff_real = deg > 1 && !fp32 && axg_ff_use(n);
   ctx->acc_stride = axg_gw_acc_entries(n);
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->acc, (size_t)ctx->acc_stride * 64, "GW accumulators"));
-  if (!ctx->gw_own_fft) AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)ctx->n3 * 6 * rs, "GW sources"));
+  if (!ctx->gw_own_fft) AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)n3 * 6 * rs, "GW sources"));
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrcF, (size_t)nhalf * 6 * 2 * rs, "GW source spectra"));
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->acc_stride * 64, ctx->stream));
   if (fp32) {
     AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_omega, (size_t)nhalf * 8, "GW phase rates"));
-    AXG_LAUNCH(ctx, "gw_omega", k_gw_omega, grid_for(nhalf), 256, 0, n, kRefTwoPi / ctx->p.dspa / n, ctx->gw_omega);
+    AXG_LAUNCH(ctx, "gw_omega", k_gw_omega, grid_for(nhalf), 256, 0, n, kRefTwoPi / ctx->gw_dspa / n, ctx->gw_omega);
   } else {
     // The FP64 polarisation table (13 doubles per half-spectrum k) when it
     // takes at most an eighth of the device memory (512^3: 7 GB); otherwise
@@ -803,17 +887,17 @@ int axg_gw_init(axg_ctx *ctx) {
     const bool want = !(env && env[0] == '0');
     if (want && tb <= total / 8) {
       AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_pol, tb, "GW polarisation table"));
-      AXG_LAUNCH(ctx, "gw_pol_table", k_gw_pol_table, grid_for(nhalf), 256, 0, n, kRefTwoPi / ctx->p.dspa / n,
+      AXG_LAUNCH(ctx, "gw_pol_table", k_gw_pol_table, grid_for(nhalf), 256, 0, n, kRefTwoPi / ctx->gw_dspa / n,
                  reinterpret_cast<float2 *>(ctx->gw_pol), ctx->gw_pol + 12 * nhalf);
     }
   }
   // float-float accumulators where the transforms are float-float too: the
   // whole Green accumulation then stays on the FP32 pipes but for the phase
   // reduction
-  ctx->acc_ff = fp32 || (ctx->gw_pol != nullptr && ctx->gw_own_fft);
-  if (!ctx->gw_own_fft) {
+  ctx->acc_ff = fp32 || (ctx->gw_pol != nullptr && (ctx->gw_own_fft || ctx->gw_ff_real));
+  if (!ctx->gw_own_fft && !ctx->gw_ff_real) {
     int dims[3] = {n, n, n};
-    AXG_CUFFT_TRY(ctx, cufftPlanMany(&ctx->plan_gsrc, 3, dims, nullptr, 1, (int)ctx->n3, nullptr, 1,
+    AXG_CUFFT_TRY(ctx, cufftPlanMany(&ctx->plan_gsrc, 3, dims, nullptr, 1, (int)n3, nullptr, 1,
                                      (int)nhalf, fp32 ? CUFFT_R2C : CUFFT_D2Z, 6));
     ctx->plan_gsrc_ok = true;
     AXG_CUFFT_TRY(ctx, cufftSetStream(ctx->plan_gsrc, ctx->stream));
@@ -824,20 +908,28 @@ int axg_gw_init(axg_ctx *ctx) {
 // grav_wave_integration (grav_waves.f90:193-255) on the current phi
 int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   if (!ctx->acc) return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is not GREEN");
-  const int n = (int)ctx->n;
-  const double d = ctx->p.dspa * 2;
-  const double dv = ctx->p.dspa * ctx->p.dspa * ctx->p.dspa;
+  // the GW grid (n = ngrid / deg, spacing dspa deg): grav_waves.f90:37-45
+  const int n = ctx->gw_n, nl = (int)ctx->n, deg = nl / n;
+  const int64_t n3 = (int64_t)n * n * n;
+  // data1_to_arr_dphi: d = 2 dx (grav_waves.f90:337); degraded: deg^3 dx 2 (:383)
+  const double d = deg == 1 ? ctx->p.dspa * 2 : (double)(deg * deg * deg) * ctx->p.dspa * 2;
+  const double dv = ctx->gw_dspa * ctx->gw_dspa * ctx->gw_dspa;  // dv_spa_grav
   const double dw = tau * dtau * dv * (ctx->p.sigma_cr * ctx->p.sigma_cr);
-  const double dwav = kRefTwoPi / ctx->p.dspa / n;
+  const double dwav = kRefTwoPi / ctx->gw_dspa / n;  // dwav_grav
   const int ref = ctx->p.compat == AXG_COMPAT_REF ? 1 : 0;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   if (ctx->p.precision == AXG_PREC_FP32_MIXED) {
-    if (ctx->gw_own_fft) {
+    if (deg > 1) {
+      float *src = (float *)ctx->gsrc;
+      AXG_LAUNCH(ctx, "gw_source_degrade_fp32", k_gw_source_degrade_f32, grid_for(n3), 256, 0,
+                 (const float2 *)ctx->phi[ctx->cur], nl, deg, (float)(2.0 / (d * d)), src);
+      AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_gsrc, src, (cufftComplex *)ctx->gsrcF));
+    } else if (ctx->gw_own_fft) {
       AXG_TRY(axg_gw_source_r2c_f32(ctx, (const float2 *)ctx->phi[ctx->cur], (float2 *)ctx->gsrcF, n,
                                     (float)(2.0 / (d * d))));
     } else {
       float *src = (float *)ctx->gsrc;
-      AXG_LAUNCH(ctx, "gw_source_fp32", k_gw_source_f32, grid_for(ctx->n3), 256, 0,
+      AXG_LAUNCH(ctx, "gw_source_fp32", k_gw_source_f32, grid_for(n3), 256, 0,
                  (const float2 *)ctx->phi[ctx->cur], n, (float)(2.0 / (d * d)), src);
       AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_gsrc, src, (cufftComplex *)ctx->gsrcF));
     }
@@ -853,11 +945,18 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
   // accuracy on the FP32 pipes, the sources formed in the row pass; kept as
   // float-float pairs when the float-float contraction reads them), else
   // the FP64 sources and cuFFT
-  const bool ff = ctx->gw_own_fft, tab = ctx->gw_pol != nullptr;
-  if (ff) {
+  const bool ff = ctx->gw_own_fft || ctx->gw_ff_real, tab = ctx->gw_pol != nullptr;
+  if (deg > 1) {
+    AXG_LAUNCH(ctx, "gw_source_degrade_fp64", k_gw_source_degrade, grid_for(n3), 256, 0,
+               (const double2 *)ctx->phi[ctx->cur], nl, deg, d, 1.0 / d, pow2, ctx->gsrc);
+    if (ctx->gw_ff_real)
+      AXG_TRY(axg_ff_d2z(ctx, ctx->gsrc, ctx->gsrcF, n, 6, tab));
+    else
+      AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
+  } else if (ctx->gw_own_fft) {
     AXG_TRY(axg_gw_source_d2z_ff(ctx, (const double2 *)ctx->phi[ctx->cur], d, 1.0 / d, pow2, ctx->gsrcF, n, tab));
   } else {
-    AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source, grid_for(ctx->n3), 256, 0, (const double2 *)ctx->phi[ctx->cur], n,
+    AXG_LAUNCH(ctx, "gw_source_fp64", k_gw_source, grid_for(n3), 256, 0, (const double2 *)ctx->phi[ctx->cur], n,
                d, 1.0 / d, pow2, ctx->gsrc);
     AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_gsrc, ctx->gsrc, (cufftDoubleComplex *)ctx->gsrcF));
   }
@@ -888,16 +987,20 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
 
 int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *power, double *numer,
                 double *denom) {
-  const int n = (int)ctx->n;
+  // Green's mode bins on its GW grid (grav_waves.f90:37-45, coarse when
+  // degrade_spec > 0); u_ij on the lattice
+  const bool green = ctx->p.gw_mode == AXG_GW_GREEN;
+  const int n = green ? ctx->gw_n : (int)ctx->n;
+  const double dspa = green ? ctx->gw_dspa : ctx->p.dspa;
   const int nb = log_bins ? ctx->p.gw_log_bins : ctx->p.num_bin_grav;
   if (nb < 1 || nb > kMaxBins) return axg_set_error(ctx, AXG_ERR_ARG, "GW bin count out of range (1..256)");
-  const double dwav = kRefTwoPi / ctx->p.dspa / n;
+  const double dwav = kRefTwoPi / dspa / n;
   // bins: linear (grav_waves.f90:62-71) or log on [2 pi/(N dx), pi/dx]
   std::vector<double> edges(nb + 1);
-  const double qmax = kRefPi / ctx->p.dspa;
+  const double qmax = kRefPi / dspa;
   const double dq = qmax / nb;
   if (log_bins) {
-    const double kmin = kRefTwoPi / ctx->p.dspa / n;
+    const double kmin = kRefTwoPi / dspa / n;
     for (int k = 0; k <= nb; ++k) edges[k] = kmin * std::pow(qmax / kmin, (double)k / nb);
   } else {
     edges[0] = 0.0;
@@ -955,7 +1058,7 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
   AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), ctx->d_red, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost,
                                     ctx->stream));
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  const double fact = gw_fact(ctx->p);
+  const double fact = gw_fact(ctx->p, n, dspa);
   for (int k = 0; k < nb; ++k) {
     const double qc = log_bins ? std::sqrt(edges[k] * edges[k + 1]) : (edges[k + 1] + edges[k]) / 2;
     numer[k] = h[k];

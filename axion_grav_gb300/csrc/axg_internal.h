@@ -88,6 +88,11 @@ struct axg_ctx {
   size_t elem = 8;  // bytes of one real of the field storage
 
   // Green's-function GW state (grav_waves.f90)
+  // the GW grid of init_grav (grav_waves.f90:37-45): gw_n = ngrid / 2^degrade_spec
+  // sites a side, spacing gw_dspa = dspa 2^degrade_spec
+  int gw_n = 0;
+  double gw_dspa = 0;
+  bool gw_ff_real = false;  // degraded FP64 sources stored, then the float-float D2Z (axg_ff_d2z)
   double2 *acc = nullptr;  // Green accumulators [4][n3]; FP32-mixed: float4 (re hi, re lo, im hi, im lo)  // [4][n3]
   double *gsrc = nullptr;  // [6][n3] real sources S_ij (float for FP32-mixed)
   double2 *gsrcF = nullptr;  // [6][n*n*(n/2+1)] (float2 for FP32-mixed)

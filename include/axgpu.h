@@ -127,8 +127,9 @@ int axg_download(axg_ctx *ctx, double *phi, double *phidot, int64_t plane_stride
  * (1,1),(2,1),(2,2),(3,1),(3,2),(3,3) (grav_waves.f90:210-211 loop order). */
 int axg_upload_uij(axg_ctx *ctx, const double *u, const double *udot);
 int axg_download_uij(axg_ctx *ctx, double *u, double *udot);
-/* Four Green's-function accumulators arr_grav(2,2,N^3) as complex128
- * [4][N^3] in the order (1,1),(2,1),(1,2),(2,2) (grav_waves.f90:74). */
+/* Four Green's-function accumulators arr_grav(2,2,M^3) as complex128
+ * [4][M^3] in the order (1,1),(2,1),(1,2),(2,2) (grav_waves.f90:74), on the
+ * GW grid of init_grav: M = ngrid / 2^degrade_spec (grav_waves.f90:37-45). */
 int axg_upload_gw_green(axg_ctx *ctx, const double *acc);
 int axg_download_gw_green(axg_ctx *ctx, double *acc);
 
@@ -174,7 +175,12 @@ int axg_autotune(axg_ctx *ctx, int steps, int *best_cfg, double *best_ms_per_ste
 /* ------------------------------------------------------------------ */
 /* grav_spec_estimation (grav_waves.f90:257-321) for the current state.
  * Outputs are nbins = num_bin_grav long: bin centres (wave), power_grav,
- * numer and denom.  With AXG_GW_UIJ the TT-projected spectrum of u_ij. */
+ * numer and denom.  Green's mode bins on its GW grid: with degrade_spec > 0
+ * the sources are the deg^3-box-summed differences of
+ * data1_to_arr_dphi_degrade (grav_waves.f90:358-415), the grid has
+ * ngrid / deg sites of spacing dspa deg and the bins run to pi / (dspa deg)
+ * (grav_waves.f90:37-45, 62-71).  With AXG_GW_UIJ the TT-projected spectrum
+ * of u_ij on the full lattice. */
 int axg_grav_spec_estimation(axg_ctx *ctx, double tau, double *wave, double *power, double *numer,
                              double *denom);
 /* Same quantity binned in params.gw_log_bins logarithmic bins on
@@ -255,9 +261,12 @@ int axg_field_moments(axg_ctx *ctx, double tau, double out[4]);
 /* io_chk: raw complex128 phi block then phidot block, x fastest, global order
  * (evolve.f90:498-503); plus u_ij blocks when present and a CRC32 sidecar
  * file path+".crc".  FP32-mixed contexts also write path+".fp32", the raw
- * FP32 state with its Kahan compensations and a CRC32, and read it back when
- * present, so that a resumed run continues bit for bit (a damaged sidecar is
- * an error).  write_chk's param.chk is written by axg_write_param_chk. */
+ * FP32 state with its Kahan compensations, the CRC32 of the checkpoint it
+ * belongs to and a CRC32 of its own, and read it back when it belongs to the
+ * checkpoint being read, so that a resumed run continues bit for bit (a
+ * damaged sidecar is an error; one left by an earlier checkpoint of the path
+ * is ignored, and FP64 contexts remove it when they write).  write_chk's
+ * param.chk is written by axg_write_param_chk. */
 int axg_write_chk(axg_ctx *ctx, const char *path);
 int axg_read_chk(axg_ctx *ctx, const char *path);
 /* param.chk "idx tau flag" (evolve.f90:407-421, 445-448). */
@@ -280,6 +289,14 @@ int axg_kernel_timing(axg_ctx *ctx, int i, char *name, int64_t name_len, int64_t
                       double *total_ms);
 /* Number of kernels launched on this context since creation. */
 int axg_launch_count(const axg_ctx *ctx, int64_t *launches);
+/* Self-test of the failure path of the fused kernels' bounded TMA stage
+ * waits (no counterpart in the reference, whose errors end in MpiStop,
+ * utils.f90:44-73): one CTA waits on a stage barrier that nothing arrives
+ * on and issues no copy, gives up after wait_cycles SM cycles (1e3 .. 4e9)
+ * and raises the same device flag as a timed-out stage wait.  Returns
+ * AXG_ERR_TIMEOUT with the fused kernel's message; the flag is cleared and
+ * the context stays usable. */
+int axg_selftest_wait_timeout(axg_ctx *ctx, int64_t wait_cycles);
 
 /* ------------------------------------------------------------------ */
 /* adjoint (no counterpart in the reference)                            */
@@ -354,7 +371,9 @@ int axg_ensemble_launch_count(const axg_ensemble *e, int64_t *launches);
  * rejected with AXG_ERR_ARG), held by every GPU that loads the library until
  * the process exits.  The first call on a device looks up that array's device
  * address (once per device, with the device current); make that first call
- * before any stream capture.  All calls share the array, so calls that
+ * before any stream capture.  A cudaDeviceReset of a device ends the life of
+ * everything this library set up on it, that address included: after one,
+ * the process makes no further call into the library on that device.  All calls share the array, so calls that
  * overlap on the GPU race; serialise them (one stream, or synchronise).
  * Errors are reported through axg_last_error(NULL). */
 int axg_field_moments_noalloc(const axg_params *p, const double *d_phi, const double *d_phidot,

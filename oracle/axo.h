@@ -58,8 +58,13 @@ int64_t axo_symplectic_integration(const axg_params *p, double *phi, double *phi
 void axo_fft3d(int64_t n, double *data, int sign);
 /* 3-D real->half-complex not needed: full complex transforms only. */
 
+/* grav_waves.f90:37-45: the GW grid, ngrid / 2^degrade_spec sites a side of
+ * spacing dspa 2^degrade_spec (Green's-function accumulators are [4][ng^3][2]) */
+void axo_gw_grid(const axg_params *p, int64_t *ng, double *dspa_g);
 /* grav_waves.f90:323-356: dphi[3][N^3][2] */
 void axo_data1_to_arr_dphi(const axg_params *p, const double *phi, double *dphi);
+/* grav_waves.f90:358-415 (one rank): dphi[3][ng^3][2] */
+void axo_data1_to_arr_dphi_degrade(const axg_params *p, const double *phi, double *dphi);
 /* grav_waves.f90:157-191 (pol for component (i, j), 1-based) */
 void axo_get_comwav_grav(const axg_params *p, const int64_t ixyz[3], double *q, double pol[2],
                          int i, int j);

@@ -43,6 +43,7 @@ def lib():
                                             ctypes.c_double], ctypes.c_int64),
             "axo_fft3d": ([ctypes.c_int64, dp, ctypes.c_int], None),
             "axo_data1_to_arr_dphi": ([P, dp, dp], None),
+            "axo_data1_to_arr_dphi_degrade": ([P, dp, dp], None),
             "axo_grav_wave_integration": ([P, dp, dp, ctypes.c_double, ctypes.c_double], None),
             "axo_grav_spec_estimation": ([P, dp, dp, dp, dp, dp], None),
             "axo_uij_grav_spec": ([P, dp, dp, ctypes.c_double, dp, dp, dp, dp], None),
@@ -147,6 +148,38 @@ def fft3d(a: np.ndarray, sign: int):
     b = np.ascontiguousarray(a, dtype=np.complex128).copy()
     lib().axo_fft3d(b.shape[0], dptr(b), sign)
     return b
+
+
+def default_params(**kw):
+    """The defaults of axg_params_default (settings.f90 values), filled in
+    Python so that a process that only runs the oracle maps no GPU library."""
+    p = Params()
+    p.ngrid, p.precision, p.gw_mode = 64, 0, 0
+    p.num_bin, p.num_bin_grav, p.degrade_spec = 50, 25, 0
+    p.flags, p.compat, p.potential, p.n_dw, p.gw_log_bins = 1 | 2 | 4, 1, 0, 1, 64
+    p.dspa = p.sigma_cr = p.kappa = p.tau_cr = p.a_now = 1.0
+    p.width_cr, p.thickness_cr = 1.0 / np.sqrt(2.0), 1.0
+    p.lambda_, p.vev, p.ma2_power, p.seed = 1.0, 1.0, 2.0, 1
+    return p.update(**kw)
+
+
+def gw_grid(p):
+    """(ngrid_grav, dspa_grav) of init_grav (grav_waves.f90:37-45)."""
+    deg = 1 << p.degrade_spec
+    return p.ngrid // deg, p.dspa * deg
+
+
+def green_acc_zeros(p):
+    """Zeroed Green's-function accumulators arr_grav: [4][ng][ng][ng] complex128."""
+    ng = gw_grid(p)[0]
+    return np.zeros((4, ng, ng, ng), dtype=np.complex128)
+
+
+def data1_to_arr_dphi_degrade(p, phi):
+    ng = gw_grid(p)[0]
+    out = np.zeros((3, ng, ng, ng), dtype=np.complex128)
+    lib().axo_data1_to_arr_dphi_degrade(ctypes.byref(p), dptr(phi), dptr(out))
+    return out
 
 
 def grav_wave_integration(p, phi, acc, tau, dtau):

@@ -20,6 +20,15 @@
 static inline int64_t wrap(int64_t i, int64_t n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 static inline int64_t kint(int64_t j, int64_t n) { return (j + n / 2) % n - n / 2; }
 
+/* init_grav (grav_waves.f90:37-45): the Green's-function grid is the lattice
+ * coarse-grained by deg = 2^degrade_spec: ngrid_grav = ngrid / deg,
+ * dspa_grav = dspa * deg. */
+void axo_gw_grid(const axg_params *p, int64_t *ng, double *dspa_g) {
+  const int64_t deg = (int64_t)1 << p->degrade_spec;
+  *ng = p->ngrid / deg;
+  *dspa_g = p->dspa * (double)deg;
+}
+
 /* grav_waves.f90:323-356 (no degradation) */
 void axo_data1_to_arr_dphi(const axg_params *p, const double *phi, double *dphi) {
   const int64_t n = p->ngrid, n2 = n * n, n3 = n2 * n;
@@ -40,10 +49,44 @@ void axo_data1_to_arr_dphi(const axg_params *p, const double *phi, double *dphi)
       }
 }
 
+/* grav_waves.f90:358-415 data1_to_arr_dphi_degrade on one rank: per coarse
+ * cell the central differences of the deg^3 fine sites it covers are summed
+ * (z outer, then y, then x, each step (sum + phi(x+e)) - phi(x-e)), then
+ * divided by d = deg^3 dspa 2.  dphi[3][ng^3][2]. */
+void axo_data1_to_arr_dphi_degrade(const axg_params *p, const double *phi, double *dphi) {
+  const int64_t n = p->ngrid, n2 = n * n, deg = (int64_t)1 << p->degrade_spec, m = n / deg, m3 = m * m * m;
+  const double d = (double)(deg * deg * deg) * p->dspa * 2;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int64_t cz = 0; cz < m; ++cz)
+    for (int64_t cy = 0; cy < m; ++cy)
+      for (int64_t cx = 0; cx < m; ++cx) {
+        double sr[3] = {0.0, 0.0, 0.0}, si[3] = {0.0, 0.0, 0.0};
+        for (int64_t iz = cz * deg; iz < (cz + 1) * deg; ++iz)
+          for (int64_t iy = cy * deg; iy < (cy + 1) * deg; ++iy)
+            for (int64_t ix = cx * deg; ix < (cx + 1) * deg; ++ix) {
+              const int64_t a[3] = {iz * n2 + iy * n + wrap(ix + 1, n), iz * n2 + wrap(iy + 1, n) * n + ix,
+                                    wrap(iz + 1, n) * n2 + iy * n + ix};
+              const int64_t b[3] = {iz * n2 + iy * n + wrap(ix - 1, n), iz * n2 + wrap(iy - 1, n) * n + ix,
+                                    wrap(iz - 1, n) * n2 + iy * n + ix};
+              for (int k = 0; k < 3; ++k) {
+                sr[k] = (sr[k] + phi[2 * a[k]]) - phi[2 * b[k]];
+                si[k] = (si[k] + phi[2 * a[k] + 1]) - phi[2 * b[k] + 1];
+              }
+            }
+        const int64_t c = (cz * m + cy) * m + cx;
+        for (int k = 0; k < 3; ++k) {
+          dphi[2 * (k * m3 + c)] = sr[k] / d;
+          dphi[2 * (k * m3 + c) + 1] = si[k] / d;
+        }
+      }
+}
+
 /* grav_waves.f90:157-191, 0-based FFT indices in ixyz */
 void axo_get_comwav_grav(const axg_params *p, const int64_t ixyz[3], double *q, double pol[2],
                          int i, int j) {
-  const int64_t n = p->ngrid;
+  int64_t n;
+  double dspa_g;
+  axo_gw_grid(p, &n, &dspa_g);
   double qh[3];
   for (int k = 0; k < 3; ++k) qh[k] = (double)kint(ixyz[k], n);
   double qq = qh[0] * qh[0] + qh[1] * qh[1];
@@ -75,18 +118,25 @@ void axo_get_comwav_grav(const axg_params *p, const int64_t ixyz[3], double *q, 
       pol[1] = 0.0;
     }
   }
-  const double dwav = REF_TWOPI / p->dspa / n;
+  const double dwav = REF_TWOPI / dspa_g / n; /* dwav_grav, grav_waves.f90:43 */
   *q = qq * dwav;
 }
 
 /* grav_waves.f90:193-255 */
 void axo_grav_wave_integration(const axg_params *p, const double *phi, double *acc, double tau,
                                double dtau) {
-  const int64_t n = p->ngrid, n2 = n * n, n3 = n2 * n;
+  int64_t n;
+  double dspa_g;
+  axo_gw_grid(p, &n, &dspa_g);
+  const int64_t n2 = n * n, n3 = n2 * n;
   double *dphi = (double *)malloc(sizeof(double) * 2 * 3 * n3);
   double *buf = (double *)malloc(sizeof(double) * 2 * n3);
-  axo_data1_to_arr_dphi(p, phi, dphi);
-  const double dv = p->dspa * p->dspa * p->dspa;
+  /* grav_waves.f90:203-207: the degraded differences unless degrade_spec = 0 */
+  if (p->degrade_spec > 0)
+    axo_data1_to_arr_dphi_degrade(p, phi, dphi);
+  else
+    axo_data1_to_arr_dphi(p, phi, dphi);
+  const double dv = dspa_g * dspa_g * dspa_g; /* dv_spa_grav, grav_waves.f90:44 */
   const double dw = tau * dtau * dv * (p->sigma_cr * p->sigma_cr);
   const int ref = p->compat == AXG_COMPAT_REF;
   double *a11 = acc, *a21 = acc + 2 * n3, *a12 = acc + 4 * n3, *a22 = acc + 6 * n3;
@@ -152,10 +202,9 @@ void axo_grav_wave_integration(const axg_params *p, const double *phi, double *a
   free(buf);
 }
 
-/* grav_waves.f90:265-267 normalisation */
-static double gw_fact(const axg_params *p) {
-  const int64_t n = p->ngrid;
-  double dwav = REF_TWOPI / p->dspa / n;
+/* grav_waves.f90:265-267 normalisation on an n^3 grid of spacing dspa */
+static double gw_fact(const axg_params *p, int64_t n, double dspa) {
+  double dwav = REF_TWOPI / dspa / n;
   double dv_wav = pow(dwav / REF_TWOPI, 3);
   double tc = p->tau_cr;
   double tc6 = tc * tc * tc * tc * tc * tc;
@@ -163,12 +212,10 @@ static double gw_fact(const axg_params *p) {
   return 1 / tc6 / (BIGH_IN_MSTAR * BIGH_IN_MSTAR) / a4 / 3 / (REF_TWOPI * REF_TWOPI) * dv_wav;
 }
 
-static void lin_edges(const axg_params *p, int nb, double *wave, double *dq_out) {
-  double qmax = REF_PI / p->dspa;
+/* grav_waves.f90:62-71 bins on (0, pi / dspa] */
+static void lin_edges(double dspa, int nb, double *wave, double *dq_out) {
+  double qmax = REF_PI / dspa;
   double dq = qmax / nb;
-  double w = 0.0;
-  for (int k = 1; k <= nb; ++k) w = w + dq;
-  (void)w;
   double prev = 0.0;
   for (int k = 1; k <= nb; ++k) {
     double cur = prev + dq;
@@ -181,11 +228,14 @@ static void lin_edges(const axg_params *p, int nb, double *wave, double *dq_out)
 /* grav_waves.f90:257-321 */
 void axo_grav_spec_estimation(const axg_params *p, const double *acc, double *wave,
                               double *power, double *numer, double *denom) {
-  const int64_t n = p->ngrid, n2 = n * n, n3 = n2 * n;
+  int64_t n;
+  double dspa_g;
+  axo_gw_grid(p, &n, &dspa_g);
+  const int64_t n2 = n * n, n3 = n2 * n;
   const int nb = p->num_bin_grav;
   double dq;
-  lin_edges(p, nb, wave, &dq);
-  double fact = gw_fact(p);
+  lin_edges(dspa_g, nb, wave, &dq);
+  double fact = gw_fact(p, n, dspa_g);
   for (int k = 0; k < nb; ++k) numer[k] = denom[k] = 0.0;
   for (int64_t s = 0; s < n3; ++s) {
     int64_t ixyz[3] = {s % n, (s / n) % n, s / n2};
@@ -209,9 +259,8 @@ void axo_grav_spec_estimation(const axg_params *p, const double *acc, double *wa
   }
 }
 
-static void log_edges(const axg_params *p, int nlog, double *edges) {
-  const int64_t n = p->ngrid;
-  double kmin = REF_TWOPI / p->dspa / n, kmax = REF_PI / p->dspa;
+static void log_edges(int64_t n, double dspa, int nlog, double *edges) {
+  double kmin = REF_TWOPI / dspa / n, kmax = REF_PI / dspa;
   for (int k = 0; k <= nlog; ++k) edges[k] = kmin * pow(kmax / kmin, (double)k / nlog);
 }
 
@@ -230,10 +279,13 @@ static int log_bin(double q, const double *edges, int nlog) {
 
 void axo_grav_spec_log_green(const axg_params *p, const double *acc, double *edges,
                              double *power, double *numer, double *denom) {
-  const int64_t n = p->ngrid, n2 = n * n, n3 = n2 * n;
+  int64_t n;
+  double dspa_g;
+  axo_gw_grid(p, &n, &dspa_g);
+  const int64_t n2 = n * n, n3 = n2 * n;
   const int nl = p->gw_log_bins;
-  log_edges(p, nl, edges);
-  double fact = gw_fact(p);
+  log_edges(n, dspa_g, nl, edges);
+  double fact = gw_fact(p, n, dspa_g);
   for (int k = 0; k < nl; ++k) numer[k] = denom[k] = 0.0;
   for (int64_t s = 0; s < n3; ++s) {
     int64_t ixyz[3] = {s % n, (s / n) % n, s / n2};
@@ -357,8 +409,8 @@ void axo_uij_grav_spec(const axg_params *p, const double *u, const double *udot,
   double *qa = (double *)malloc(sizeof(double) * n3), *va = (double *)malloc(sizeof(double) * n3);
   uij_numer(p, u, udot, tau, qa, va);
   double dq;
-  lin_edges(p, nb, wave, &dq);
-  double fact = gw_fact(p);
+  lin_edges(p->dspa, nb, wave, &dq);
+  double fact = gw_fact(p, p->ngrid, p->dspa);
   for (int k = 0; k < nb; ++k) numer[k] = denom[k] = 0.0;
   for (int64_t s = 0; s < n3; ++s) {
     double q = qa[s];
@@ -382,8 +434,8 @@ void axo_uij_grav_spec_log(const axg_params *p, const double *u, const double *u
   const int nl = p->gw_log_bins;
   double *qa = (double *)malloc(sizeof(double) * n3), *va = (double *)malloc(sizeof(double) * n3);
   uij_numer(p, u, udot, tau, qa, va);
-  log_edges(p, nl, edges);
-  double fact = gw_fact(p);
+  log_edges(p->ngrid, p->dspa, nl, edges);
+  double fact = gw_fact(p, p->ngrid, p->dspa);
   for (int k = 0; k < nl; ++k) numer[k] = denom[k] = 0.0;
   for (int64_t s = 0; s < n3; ++s) {
     double q = qa[s];

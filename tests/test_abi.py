@@ -76,3 +76,29 @@ def test_create_without_gpu_fails_loudly(built):
         pytest.skip("GPU present")
     with pytest.raises(ag.AxgError):
         ag.Lattice(ag.default_params(ngrid=16))
+
+
+def test_oracle_default_params_match_library(built):
+    # the oracle fills the same defaults without loading the GPU library
+    from oracle import axo
+    a, b = ag.default_params(), axo.default_params()
+    for name, _ in ag.Params._fields_:
+        assert getattr(a, name) == getattr(b, name), name
+
+
+def test_green_on_odd_or_tiny_gw_grid_is_rejected(built):
+    # Green's mode runs on ngrid / 2^degrade_spec (grav_waves.f90:37-45); a
+    # GW grid that is odd or below 4 sites is refused before any device work
+    lib = ag.load_library()
+    out = ctypes.c_void_p()
+    for n, deg in ((24, 3), (16, 3), (8, 2)):
+        p = ag.default_params(ngrid=n, degrade_spec=deg, gw_mode=ag.GW_GREEN)
+        assert lib.axg_create(ctypes.byref(p), ctypes.byref(out)) == -7, (n, deg)
+        assert b"GW grid" in lib.axg_last_error(None)
+    # the same degrade_spec is fine without Green's mode (the field spectrum
+    # coarse-grains on its own)
+    p = ag.default_params(ngrid=24, degrade_spec=3, gw_mode=ag.GW_NONE)
+    rc = lib.axg_create(ctypes.byref(p), ctypes.byref(out))
+    assert rc != -7
+    if rc == 0:
+        lib.axg_destroy(out)

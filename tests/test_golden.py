@@ -51,5 +51,7 @@ def test_golden_inputs_are_nontrivial():
     assert d["counts"][0] > 0 and d["counts"][1] > 0 and len(d["strings"]) == d["counts"][0]
     g = load("green_ref_8")
     assert np.any(g["acc"] != 0) and g["nt"] > 0
+    g = load("green_degrade1_ref_16")
+    assert g["acc"].shape == (4, 8, 8, 8) and g["phi0"].shape == (16, 16, 16) and np.any(g["acc"] != 0)
     lf = load("leapfrog_uij_ref_6")
     assert not np.array_equal(lf["phi"], lf["phi0"])

@@ -350,6 +350,62 @@ def test_fp32_checkpoint_resume_is_bit_exact(tmp_path):
             lat.read_chk(path)
 
 
+def test_fp32_sidecar_of_an_older_checkpoint_is_not_used(tmp_path):
+    """The .fp32 sidecar records the CRC of the checkpoint it was written
+    with.  An FP64 context that rewrites the checkpoint removes the old
+    sidecar, and a sidecar put back beside a different checkpoint is
+    ignored: the FP32 resume then takes the complex128 checkpoint's state."""
+    import shutil
+    n = 32
+    st_a, st_b = random_state(n, 21, 0.2), random_state(n, 22, 0.2)
+    path = str(tmp_path / "run.chk")
+    p32 = make_params(n, ag.PREC_FP32_MIXED, ag.GW_UIJ)
+    p64 = make_params(n, ag.PREC_FP64_PLAIN, ag.GW_UIJ)
+    with ag.Lattice(p32) as lat:
+        lat.upload(st_a[0], st_a[1])
+        lat.upload_uij(st_a[2], st_a[3])
+        lat.leapfrog(1.5, 0.02, 3, True, False)
+        lat.write_chk(path)
+    shutil.copy(path + ".fp32", str(tmp_path / "old.fp32"))
+    with ag.Lattice(p64) as lat:
+        lat.upload(st_b[0], st_b[1])
+        lat.upload_uij(st_b[2], st_b[3])
+        lat.write_chk(path)
+    import os
+    assert not os.path.exists(path + ".fp32")
+    shutil.copy(str(tmp_path / "old.fp32"), path + ".fp32")
+    with ag.Lattice(p32) as lat:
+        lat.read_chk(path)
+        g = lat.download()
+    # state B as FP32 storage, not the state the old sidecar holds
+    assert np.max(np.abs(g[0] - st_b[0])) < 1e-6 and np.max(np.abs(g[1] - st_b[1])) < 1e-6
+
+
+def test_wait_timeout_status_and_recovery():
+    """The give-up path of the bounded TMA stage wait: a barrier that nothing
+    arrives on (no copy issued) runs out after a short limit, the call
+    returns ERR_TIMEOUT with the stage-wait message, and the context keeps
+    working: a fused FP64 step afterwards is bit-exact against the oracle."""
+    n = 32
+    p = make_params(n, ag.PREC_FP64_FUSED, ag.GW_UIJ)
+    st = random_state(n, 31, 0.1)
+    with ag.Lattice(p) as lat:
+        lat.upload(st[0], st[1])
+        lat.upload_uij(st[2], st[3])
+        for _ in range(2):
+            with pytest.raises(ag.AxgError, match="ERR_TIMEOUT.*timed out"):
+                lat.selftest_wait_timeout(2_000_000)
+        lat.leapfrog(1.5, 0.02, 4, True, True)
+        g = lat.download()
+        gu = lat.download_uij()
+        with pytest.raises(ag.AxgError, match="ERR_ARG"):
+            lat.selftest_wait_timeout(10)
+    phi, phid, u, ud = (a.copy() for a in st)
+    axo.leapfrog(p, phi, phid, u, ud, None, 1.5, 0.02, 4, True, True)
+    assert np.array_equal(g[0], phi) and np.array_equal(g[1], phid)
+    assert np.array_equal(gu[0], u) and np.array_equal(gu[1], ud)
+
+
 def test_kernel_timing_and_launch_count():
     n = 64
     p = make_params(n, ag.PREC_FP32_MIXED, ag.GW_UIJ)

@@ -64,13 +64,13 @@ def test_defects_against_golden():
         np.testing.assert_allclose(a, d[k], rtol=1e-12)
 
 
-@pytest.mark.parametrize("case", ["green_ref_8", "green_intended_8"])
+@pytest.mark.parametrize("case", ["green_ref_8", "green_intended_8", "green_degrade1_ref_16"])
 def test_green_against_golden(case):
     d = load(case)
     n = d["phi0"].shape[0]
     p = ag.default_params(ngrid=n, precision=ag.PREC_FP64_PLAIN, gw_mode=ag.GW_GREEN, dspa=0.75, sigma_cr=1.0,
                           kappa=0.1, tau_cr=1.0, a_now=1.0, num_bin_grav=25, gw_log_bins=12, seed=3,
-                          potential=ag.POT_QUARTIC, compat=int(d["compat"]))
+                          potential=ag.POT_QUARTIC, compat=int(d["compat"]), degrade_spec=int(d["degrade_spec"]))
     with ag.Lattice(p) as lat:
         lat.upload(d["phi0"], d["phid0"])
         assert lat.symplectic_integration(GREEN["t1"], GREEN["t2"], GREEN["eps"]) == int(d["nt"])

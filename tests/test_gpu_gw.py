@@ -134,6 +134,52 @@ def test_green_fp32_mixed_against_fp64_oracle(compat, n):
     np.testing.assert_allclose(gpw, pw, rtol=1e-3)
 
 
+@pytest.mark.parametrize("compat", [ag.COMPAT_REF, ag.COMPAT_INTENDED])
+@pytest.mark.parametrize("precision,n,deg", [
+    (ag.PREC_FP64_PLAIN, 32, 1),   # GW grid 16^3: float-float D2Z of the stored sources
+    (ag.PREC_FP64_PLAIN, 32, 2),   # 8^3: cuFFT D2Z
+    (ag.PREC_FP64_FUSED, 64, 1),   # 32^3
+    (ag.PREC_FP64_PLAIN, 24, 1),   # 12^3: cuFFT, N not a power of two
+    (ag.PREC_FP32_MIXED, 32, 1),
+    (ag.PREC_FP32_MIXED, 64, 2),
+])
+def test_green_degraded_against_oracle(compat, precision, n, deg):
+    """degrade_spec > 0: the sources are the deg^3-box-summed central
+    differences of data1_to_arr_dphi_degrade (grav_waves.f90:358-415) and
+    the accumulation, polarisation, bins and normalisation run on the GW
+    grid ngrid / deg of spacing dx deg (grav_waves.f90:37-45, 62-71).
+    FP64 paths: accumulators within 1e-10 of the oracle, counts exact;
+    FP32-mixed: accumulators within 1e-4, numerator and power 1e-3 per bin."""
+    phi, phid = init_state(n, 5)
+    p64 = params(n, ag.PREC_FP64_PLAIN, ag.GW_GREEN, compat=compat, degrade_spec=deg)
+    acc = axo.green_acc_zeros(p64)
+    assert acc.shape == (4, n >> deg, n >> deg, n >> deg)
+    a_phi = phi.copy()
+    nt = axo.symplectic_integration(p64, a_phi, phid.copy(), None, None, acc, 2.0, 2.8, 0.4)
+    w, pw, nu, de = axo.grav_spec_estimation(p64, acc)
+    e, lpw, lnu, lde = axo.grav_spec_log_green(p64, acc)
+    with ag.Lattice(params(n, precision, ag.GW_GREEN, compat=compat, degrade_spec=deg)) as lat:
+        lat.upload(phi, phid)
+        assert lat.symplectic_integration(2.0, 2.8, 0.4) == nt
+        g_phi, _ = lat.download()
+        g_acc = lat.download_gw_green()
+        gw_, gpw, gnu, gde = lat.grav_spec_estimation(2.8)
+        ge, glpw, glnu, glde = lat.grav_spec_log(2.8)
+    assert np.any(acc != 0)
+    fp64 = precision != ag.PREC_FP32_MIXED
+    if fp64:
+        assert np.array_equal(g_phi, a_phi)
+    assert rel(g_acc, acc) < (1e-10 if fp64 else 1e-4)
+    np.testing.assert_array_equal(gde, de)
+    np.testing.assert_array_equal(glde, lde)
+    np.testing.assert_allclose(gw_, w, rtol=1e-15)
+    np.testing.assert_allclose(ge, e, rtol=1e-14)
+    tol = 1e-9 if fp64 else 1e-3
+    np.testing.assert_allclose(gnu, nu, rtol=tol)
+    np.testing.assert_allclose(gpw, pw, rtol=tol)
+    np.testing.assert_allclose(glnu, lnu, rtol=tol)
+
+
 @pytest.mark.parametrize("precision,n", [(ag.PREC_FP64_PLAIN, 16), (ag.PREC_FP64_PLAIN, 18),
                                          (ag.PREC_FP32_MIXED, 16)])
 def test_green_accumulator_upload_download(precision, n):

@@ -1,4 +1,5 @@
 """CPU checks of the oracle (test infrastructure) against known answers."""
+import ctypes
 import math
 
 import numpy as np
@@ -219,3 +220,105 @@ def test_oracle_leapfrog_time_reversible():
     axo.leapfrog(p, a[0], a[1], a[2], a[3], None, 12.4, -0.2, 12, True, True)
     for got, want in zip(a, (phi, phid, u, ud)):
         assert np.max(np.abs(got - want)) < 1e-12 * max(1.0, np.max(np.abs(want)))
+
+
+REF_PI = 3.14159265359  # potential.f90:8
+
+
+def np_dphi(p, phi):
+    """grav_waves.f90:323-415 restated with numpy: central differences, summed
+    over the deg^3 fine sites of each GW-grid cell and divided by deg^3 2 dx."""
+    n, deg = p.ngrid, 1 << p.degrade_spec
+    m = n // deg
+    out = []
+    for axis in (2, 1, 0):  # x, y, z; arrays are [z][y][x]
+        diff = np.roll(phi, -1, axis) - np.roll(phi, 1, axis)
+        if deg > 1:
+            diff = diff.reshape(m, deg, m, deg, m, deg).sum(axis=(1, 3, 5))
+        out.append(diff / (deg ** 3 * p.dspa * 2))
+    return out
+
+
+def np_green_kick(p, phi, acc, tau, dtau):
+    """grav_waves.f90:193-255 restated with numpy on the GW grid of
+    init_grav (grav_waves.f90:37-45), including the cross-wired updates of
+    compat = REF (grav_waves.f90:239-242)."""
+    deg = 1 << p.degrade_spec
+    m, dspa_g = p.ngrid // deg, p.dspa * deg
+    dphi = np_dphi(p, phi)
+    dw = tau * dtau * dspa_g ** 3 * p.sigma_cr ** 2
+    k1 = ((np.arange(m) + m // 2) % m - m // 2).astype(float)
+    kz, ky, kx = np.meshgrid(k1, k1, k1, indexing="ij")
+    q = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    qs = np.where(q > 0, q, 1.0)
+    hx, hy, hz = kx / qs, ky / qs, kz / qs
+    r = np.sqrt(hx ** 2 + hy ** 2)
+    rs = np.where(r > 0, r, 1.0)
+    c, s = np.where(r > 0, hx / rs, 1.0), np.where(r > 0, hy / rs, 0.0)
+    pv = [hz * c - 1j * s, hz * s + 1j * c, -r + 0j]
+    ph = q * (2 * REF_PI / dspa_g / m) * tau
+    cq, sq = np.cos(ph), np.sin(ph)
+    a11, a21, a12, a22 = (acc[i] for i in range(4))
+    for i in range(3):
+        for j in range(i + 1):
+            src = dphi[i] * np.conj(dphi[j]) + np.conj(dphi[i]) * dphi[j]
+            F = np.fft.ifftn(src) * m ** 3  # FFTW_BACKWARD, unnormalised
+            pol = pv[i] * pv[j] / (2 if i == j else 1)
+            polp = np.where(q > 0, pol, 0) * dw
+            poln = np.conj(polp)
+            a11 += cq * polp * F
+            if p.compat == 1:
+                new21 = a12 + sq * polp * F
+                a12[...] = new21 + cq * poln * F
+                a21[...] = new21
+            else:
+                a21 += sq * polp * F
+                a12 += cq * poln * F
+            a22 += sq * poln * F
+
+
+@pytest.mark.parametrize("n,deg", [(8, 1), (16, 2), (12, 1), (8, 0)])
+def test_degraded_differences_match_numpy(n, deg):
+    p = axo.default_params(ngrid=n, degrade_spec=deg, dspa=0.7, gw_mode=1)
+    rng = np.random.default_rng(n + deg)
+    phi = rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))
+    want = np_dphi(p, phi)
+    if deg == 0:
+        got = np.zeros((3, n, n, n), np.complex128)
+        axo.lib().axo_data1_to_arr_dphi(ctypes.byref(p), axo.dptr(phi), axo.dptr(got))
+    else:
+        got = axo.data1_to_arr_dphi_degrade(p, phi)
+    for k in range(3):
+        np.testing.assert_allclose(got[k], want[k], rtol=0, atol=1e-13 * np.max(np.abs(want[k])))
+
+
+@pytest.mark.parametrize("compat", [0, 1])
+@pytest.mark.parametrize("n,deg", [(16, 1), (16, 2), (12, 1), (8, 0)])
+def test_green_kick_and_spectrum_match_numpy(compat, n, deg):
+    """The oracle's Green's-function kick on the GW grid (degraded or not)
+    against the numpy restatement, and its spectrum bins against the
+    coarse-grid edges pi / (dx deg) / 25 (grav_waves.f90:62-71)."""
+    p = axo.default_params(ngrid=n, degrade_spec=deg, dspa=0.6, sigma_cr=1.3, gw_mode=1, compat=compat)
+    rng = np.random.default_rng(7 * n + deg)
+    phi = rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))
+    acc = axo.green_acc_zeros(p)
+    want = np.zeros_like(acc)
+    for tau, dtau in ((2.0, 0.1), (2.1, 0.1)):
+        axo.grav_wave_integration(p, phi, acc, tau, dtau)
+        np_green_kick(p, phi, want, tau, dtau)
+        phi = phi * np.exp(0.3j)
+    np.testing.assert_allclose(acc, want, rtol=0, atol=1e-12 * np.max(np.abs(want)))
+    w, pw, nu, de = axo.grav_spec_estimation(p, acc)
+    dspa_g = p.dspa * (1 << deg)
+    dq = REF_PI / dspa_g / p.num_bin_grav
+    np.testing.assert_allclose(w, (np.arange(p.num_bin_grav) + 0.5) * dq, rtol=1e-14)
+    m = n >> deg
+    k1 = ((np.arange(m) + m // 2) % m - m // 2).astype(float)
+    kz, ky, kx = np.meshgrid(k1, k1, k1, indexing="ij")
+    q = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2) * (2 * REF_PI / dspa_g / m)
+    iq = np.floor(q / dq + 0.5 + 0.5)  # nint(q / dq + 0.5)
+    power = np.sum(np.abs(acc) ** 2, axis=0)
+    for b in range(p.num_bin_grav):
+        sel = (q > 0) & (iq == b + 1)
+        assert de[b] == np.count_nonzero(sel)
+        np.testing.assert_allclose(nu[b], power[sel].sum(), rtol=1e-12)

@@ -38,6 +38,23 @@ def test_noalloc_moments_match_context_entry_point():
         np.testing.assert_array_equal(again, got)
 
 
+@pytest.mark.parametrize("n", [32, 24])
+def test_noalloc_moments_match_oracle(n):
+    """Directly against the FP64 oracle (axo.field_moments), also for a
+    lattice side that is not a power of two, on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    from oracle import axo
+    p = ag.default_params(ngrid=n, precision=ag.PREC_FP64_PLAIN, dspa=0.5, sigma_cr=1.0, kappa=0.1)
+    for seed, tau in ((3, 1.1), (4, 2.3)):
+        phi, phid = state(n, seed)
+        want = axo.field_moments(p, phi, phid, tau)
+        d_phi = torch.from_numpy(phi.view(np.float64).copy()).cuda()
+        d_phid = torch.from_numpy(phid.view(np.float64).copy()).cuda()
+        torch.cuda.synchronize()
+        got = ag.field_moments_noalloc(p, d_phi.data_ptr(), d_phid.data_ptr(), tau)
+        np.testing.assert_allclose(got, want, rtol=1e-12)
+
+
 def test_noalloc_rejects_lattices_beyond_its_scratch():
     p = ag.default_params(ngrid=2050)
     with pytest.raises(ag.AxgError, match="scratch limit"):
