@@ -4,7 +4,7 @@
 // of the run,
 //   J = sum_{kmin <= |k| <= kmax} 1/2 sum_ij (|W'_TT(k)|^2 + k^2 |W_TT(k)|^2),
 //   W = dx^3 FFT(tau u), W' = dx^3 FFT(u + tau u'),
-// i.e. the band sum of the numerator of axg_grav_spec_estimation (GW_UIJ).
+// i.e. half the band sum of the numerator of axg_grav_spec_estimation (GW_UIJ).
 // Outputs: J, dJ/dlambda (quartic model: A = lambda/2, B = -lambda v^2/2) and
 // the gradients with respect to the initial phi and phi' (complex, d/dRe +
 // i d/dIm), from which the gradients with respect to Fourier-mode amplitudes

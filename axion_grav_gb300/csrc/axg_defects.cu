@@ -44,11 +44,20 @@ constexpr double kRemovalPhdiff = 7 * kRefPi / 4;
 constexpr int kMaxIter = 1000;
 constexpr int kNumSimp = 4;
 
+// The FP64 value of site s.  comp: the Kahan compensation of an FP32-mixed
+// phi (else null); the value is then (double)v - (double)c, the snapshot
+// axg_download returns, so the FP64 decisions are those of the host's
+// classification of the downloaded field.
 template <typename V>
-__device__ __forceinline__ void load_c(const V *a, int64_t s, double &re, double &im) {
+__device__ __forceinline__ void load_c(const V *a, const V *comp, int64_t s, double &re, double &im) {
   const V v = a[s];
   re = (double)v.x;
   im = (double)v.y;
+  if (comp) {
+    const V c = comp[s];
+    re = re - (double)c.x;
+    im = im - (double)c.y;
+  }
 }
 
 // FP32 phase of each site.  For an FP64 field a component outside the FP32
@@ -139,7 +148,11 @@ struct BlockCount3 {
   }
 };
 
-constexpr float kMargin = 2e-5f;  // >> 4 (2 x 1e-6 phase error + FP32 rounding of a gap)
+// >> 4 (2 x 1e-6 phase error + FP32 rounding of a gap).  The phase error
+// budget of 1e-6 covers atan2f (3 ulp) and, for an FP32-mixed field, the
+// Kahan compensation the FP32 phase leaves out (|c| <= ulp(phi) / 2, so
+// <= 1.2e-7 rad).
+constexpr float kMargin = 2e-5f;
 
 __device__ __forceinline__ void cswapf(float &a, float &b) {
   const float lo = fminf(a, b), hi = fmaxf(a, b);
@@ -183,14 +196,15 @@ __device__ __forceinline__ bool classify_sorted_f(const float p[8], int which, i
 }
 
 template <typename V>
-__device__ __forceinline__ double phase64(const V *phi, int64_t s) {
+__device__ __forceinline__ double phase64(const V *phi, const V *comp, int64_t s) {
   double re, im;
-  load_c(phi, s, re, im);
+  load_c(phi, comp, s, re, im);
   return axd_atan2(im, re);
 }
 
 template <typename V>
-__global__ void k_classify(const float *__restrict__ ph, const V *__restrict__ phi, int n, int which,
+__global__ void k_classify(const float *__restrict__ ph, const V *__restrict__ phi, const V *__restrict__ cphi, int n,
+                           int which,
                            int8_t *__restrict__ flags, unsigned long long *__restrict__ counts) {
   const int64_t n3 = (int64_t)n * n * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -214,7 +228,7 @@ __global__ void k_classify(const float *__restrict__ ph, const V *__restrict__ p
       }
       if (!known) {  // the FP64 classification of the host
         double d[8];
-        for (int c = 0; c < 8; ++c) d[c] = phase64(phi, corner(n, ix, iy, iz, c));
+        for (int c = 0; c < 8; ++c) d[c] = phase64(phi, cphi, corner(n, ix, iy, iz, c));
         sort8(d);
         f = classify_sorted(d, which);
       }
@@ -257,7 +271,7 @@ __device__ __forceinline__ bool pierced_f(float a, float b, float c, float d, bo
 }
 
 template <typename V>
-__global__ void k_winding(const float *__restrict__ ph, const V *__restrict__ phi, int n,
+__global__ void k_winding(const float *__restrict__ ph, const V *__restrict__ phi, const V *__restrict__ cphi, int n,
                           unsigned long long *__restrict__ counts) {
   const int64_t n2 = (int64_t)n * n, n3 = n2 * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -277,8 +291,8 @@ __global__ void k_winding(const float *__restrict__ ph, const V *__restrict__ ph
 #pragma unroll
       for (int o = 0; o < 3; ++o) {
         if (!pierced_f(ph[q[o][0]], ph[q[o][1]], ph[q[o][2]], ph[q[o][3]], hit[o]))
-          hit[o] = pierced(phase64(phi, q[o][0]), phase64(phi, q[o][1]), phase64(phi, q[o][2]),
-                           phase64(phi, q[o][3]));
+          hit[o] = pierced(phase64(phi, cphi, q[o][0]), phase64(phi, cphi, q[o][1]), phase64(phi, cphi, q[o][2]),
+                           phase64(phi, cphi, q[o][3]));
       }
     }
     tally.add(hit[0], hit[1], hit[2]);
@@ -922,7 +936,7 @@ __device__ void pp_inverse4(double *ap) {
 
 // defects_3d.f90:605-692 (VEL=0)
 template <typename V>
-__device__ void velocity_string(const V *phi, const V *phid, int n, double dspa, int ix, int iy,
+__device__ void velocity_string(const V *phi, const V *cphi, const V *phid, int n, double dspa, int ix, int iy,
                                 int iz, const double pos[3], double vel[3]) {
   double wr[4] = {0, 0, 0, 0}, wi[4] = {0, 0, 0, 0}, dr[4] = {0, 0, 0, 0}, di[4] = {0, 0, 0, 0};
   double mat[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, mat0[10];
@@ -939,8 +953,8 @@ __device__ void velocity_string(const V *phi, const V *phid, int n, double dspa,
         d[1] = i - pos[0] - 0.5;
         const int64_t s = ((int64_t)zz * n + yy) * n + xx;
         double pr, pi_, qr, qi;
-        load_c(phi, s, pr, pi_);
-        load_c(phid, s, qr, qi);
+        load_c(phi, cphi, s, pr, pi_);
+        load_c(phid, (const V *)nullptr, s, qr, qi);
         for (int l = 0; l < 4; ++l) {
           wr[l] = wr[l] + d[l] * pr;
           wi[l] = wi[l] + d[l] * pi_;
@@ -1122,7 +1136,8 @@ __device__ void position_wall(const double ph[8], double pos[3], double dir[3], 
 // launch) and advances its search one chi2 evaluation per pass (see
 // search_prepare); the grid is sized to the resident CTAs.
 template <typename V>
-__global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, const V *__restrict__ phid, int n,
+__global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, const V *__restrict__ cphi,
+                                                    const V *__restrict__ phid, int n,
                                                     double dspa, uint64_t seed, const int64_t *__restrict__ cells,
                                                     int64_t ncell, double *__restrict__ out,
                                                     unsigned long long *__restrict__ next) {
@@ -1142,7 +1157,7 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
     s = cells[k];
     const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
     for (int c = 0; c < 8; ++c) {
-      pc[c] = phase64(phi, corner(n, ix, iy, iz, c));
+      pc[c] = phase64(phi, cphi, corner(n, ix, iy, iz, c));
       phf[c] = (float)pc[c];
     }
     search_init(S);
@@ -1153,7 +1168,7 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
       const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
       double pos[3], dir[3], vel[3], gof, l;
       string_result(S, pos, dir, &gof, &l);
-      velocity_string(phi, phid, n, dspa, ix, iy, iz, pos, vel);
+      velocity_string(phi, cphi, phid, n, dspa, ix, iy, iz, pos, vel);
       double *r = out + 13 * k;
       r[0] = pos[0] + ix + 0.5;
       r[1] = pos[1] + iy + 0.5;
@@ -1179,14 +1194,15 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
 }
 
 template <typename V>
-__global__ void __launch_bounds__(128) k_wall_fit(const V *__restrict__ phi, int n, const int64_t *__restrict__ cells,
+__global__ void __launch_bounds__(128) k_wall_fit(const V *__restrict__ phi, const V *__restrict__ cphi, int n,
+                                                  const int64_t *__restrict__ cells,
                                                   int64_t ncell, double *__restrict__ out) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ncell) return;
   const int64_t s = cells[k];
   const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
   double pc[8];
-  for (int c = 0; c < 8; ++c) pc[c] = phase64(phi, corner(n, ix, iy, iz, c));
+  for (int c = 0; c < 8; ++c) pc[c] = phase64(phi, cphi, corner(n, ix, iy, iz, c));
   double pos[3], dir[3], gof, a;
   position_wall(pc, pos, dir, &gof, &a);
   double *r = out + 10 * k;
@@ -1464,10 +1480,12 @@ int axg_def_classify(axg_ctx *ctx, int which, int64_t counts[3]) {
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_cnt, 0, 3 * sizeof(unsigned long long), ctx->stream));
   if (ctx->p.precision == AXG_PREC_FP32_MIXED)
     AXG_LAUNCH(ctx, "defect_classify", k_classify<float2>, grid_for(ctx->n3), 256, 0, ctx->phase,
-               (const float2 *)ctx->phi[ctx->cur], (int)ctx->n, which, ctx->flags, ctx->d_cnt);
+               (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, (int)ctx->n, which, ctx->flags,
+               ctx->d_cnt);
   else
     AXG_LAUNCH(ctx, "defect_classify", k_classify<double2>, grid_for(ctx->n3), 256, 0, ctx->phase,
-               (const double2 *)ctx->phi[ctx->cur], (int)ctx->n, which, ctx->flags, ctx->d_cnt);
+               (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, (int)ctx->n, which, ctx->flags,
+               ctx->d_cnt);
   unsigned long long h[3];
   AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_cnt, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1484,10 +1502,10 @@ int axg_def_winding(axg_ctx *ctx, int64_t counts[3]) {
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_cnt + 3, 0, 3 * sizeof(unsigned long long), ctx->stream));
   if (ctx->p.precision == AXG_PREC_FP32_MIXED)
     AXG_LAUNCH(ctx, "string_winding", k_winding<float2>, grid_for(ctx->n3), 256, 0, ctx->phase,
-               (const float2 *)ctx->phi[ctx->cur], (int)ctx->n, ctx->d_cnt + 3);
+               (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, (int)ctx->n, ctx->d_cnt + 3);
   else
     AXG_LAUNCH(ctx, "string_winding", k_winding<double2>, grid_for(ctx->n3), 256, 0, ctx->phase,
-               (const double2 *)ctx->phi[ctx->cur], (int)ctx->n, ctx->d_cnt + 3);
+               (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, (int)ctx->n, ctx->d_cnt + 3);
   unsigned long long h[3];
   AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_cnt + 3, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1536,20 +1554,22 @@ int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], dou
       AXG_CUDA_TRY(ctx, cudaMemsetAsync(next, 0, sizeof(unsigned long long), ctx->stream));
       if (f32)
         AXG_LAUNCH(ctx, "string_fit_fp32", k_string_fit<float2>, (unsigned)grid, 128, 0,
-                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->phid, n, ctx->p.dspa,
+                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, (const float2 *)ctx->phid, n,
+                   ctx->p.dspa,
                    (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
       else
         AXG_LAUNCH(ctx, "string_fit_fp64", k_string_fit<double2>, (unsigned)grid, 128, 0,
-                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)ctx->phid, n, ctx->p.dspa,
+                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, (const double2 *)ctx->phid, n,
+                   ctx->p.dspa,
                    (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
     }
     if (nw > 0) {
       if (ctx->p.precision == AXG_PREC_FP32_MIXED)
         AXG_LAUNCH(ctx, "wall_fit", k_wall_fit<float2>, (unsigned)((nw + 127) / 128), 128, 0,
-                   (const float2 *)ctx->phi[ctx->cur], n, cells + ns, nw, ctx->d_walls);
+                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, n, cells + ns, nw, ctx->d_walls);
       else
         AXG_LAUNCH(ctx, "wall_fit", k_wall_fit<double2>, (unsigned)((nw + 127) / 128), 128, 0,
-                   (const double2 *)ctx->phi[ctx->cur], n, cells + ns, nw, ctx->d_walls);
+                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, n, cells + ns, nw, ctx->d_walls);
     }
     AXG_LAUNCH(ctx, "defect_sums", k_defect_sums, 1, 256, 0, ctx->d_strings, ns, ctx->d_walls, nw,
                ctx->d_red);

@@ -22,8 +22,8 @@
 // Spectra: shell histograms in FP64 (grav_waves.f90:257-321), 25 linear bins
 // or log bins; the u_ij path (AXG_GW_UIJ) FFTs w = tau u and w' = u + tau u'
 // (R2C, FP32 for the FP32-mixed path), TT-projects per k and accumulates
-// 1/2 sum_ij (|W'_TT|^2 + k^2 |W_TT|^2), the continuum-equivalent of the
-// Green's-function numerator.
+// sum_ij (|W'_TT|^2 + k^2 |W_TT|^2), which over a k-shell tends to the
+// Green's-function numerator as dx -> 0 (second order in k dx).
 #include <cmath>
 #include <cstdlib>
 #include <vector>
@@ -788,10 +788,10 @@ __global__ void k_uij_bin(const CV *__restrict__ F, int n, double dwav, double d
           // FP32 spectra: the entry's energy in FP32, one conversion to the
           // FP64 shell sums (a handful of FP64 operations fewer per entry)
           const float e = tt_power<R>(Dr, Di, kh) + (float)k2 * (float)dwav2 * tt_power<R>(Ur, Ui, kh);
-          v = (double)e * (wgt * 0.5 * dv2);
+          v = (double)e * (wgt * dv2);
         } else {
           const double e0 = (double)tt_power<R>(Dr, Di, kh) * dv2, e1 = (double)tt_power<R>(Ur, Ui, kh) * dv2;
-          v = wgt * 0.5 * (e0 + (double)k2 * dwav2 * e1);
+          v = wgt * (e0 + (double)k2 * dwav2 * e1);
         }
       }
       run.add(sn, sd, b, v, wgt);

@@ -303,8 +303,8 @@ int axg_selftest_wait_timeout(axg_ctx *ctx, int64_t wait_cycles);
 /* ------------------------------------------------------------------ */
 /* Gradient of the band-integrated GW energy
  *   J = sum_{kmin <= |k| <= kmax} 1/2 sum_ij (|W'_TT|^2 + k^2 |W_TT|^2)
- * (the numerator of axg_grav_spec_estimation with gw_mode UIJ, summed over
- * the band, at the end of the run) after the leapfrog of axg_leapfrog(t1, dt,
+ * (half the numerator of axg_grav_spec_estimation with gw_mode UIJ, summed
+ * over the band, at the end of the run) after the leapfrog of axg_leapfrog(t1, dt,
  * nsteps, first_half, last_half) from the current state.  Forward run with a
  * checkpoint every `stride` steps; reverse sweep steps the state back by
  * time-reversibility (re-anchored on each checkpoint) and applies the

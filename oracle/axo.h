@@ -94,6 +94,9 @@ void axo_id_defects(const axg_params *p, const double *phi, const double *phidot
                     double sl[3], double wa[3], double svel[3], int64_t counts[3],
                     double *strings, int64_t max_strings, double *walls, int64_t max_walls,
                     int8_t *flags_out);
+/* the fits of id_defects for given string / wall cells (rows as axo_id_defects) */
+void axo_fit_cells(const axg_params *p, const double *phi, const double *phidot, const int64_t *scells,
+                   int64_t ns, double *sres, const int64_t *wcells, int64_t nw, double *wres);
 /* single-cell pieces for unit tests */
 void axo_position_string(const double ph[8], uint64_t seed, uint64_t cell, double pos[3],
                          double dir[3], double *gof, double *sl);

@@ -63,6 +63,7 @@ def lib():
             "axo_string_winding": ([P, dp, i64p], None),
             "axo_id_defects": ([P, dp, dp, ctypes.c_double, dp, dp, dp, i64p, dp, ctypes.c_int64, dp,
                                 ctypes.c_int64, ctypes.POINTER(ctypes.c_int8)], None),
+            "axo_fit_cells": ([P, dp, dp, i64p, ctypes.c_int64, dp, i64p, ctypes.c_int64, dp], None),
             "axo_position_string": ([dp, ctypes.c_uint64, ctypes.c_uint64, dp, dp, dp, dp], None),
             "axo_position_wall": ([dp, dp, dp, dp, dp], None),
             "axo_string_length": ([dp, dp], ctypes.c_double),
@@ -285,6 +286,19 @@ def id_defects(p, phi, phid, tau, max_strings=None, max_walls=None):
                          dptr(s), ms, dptr(w), mw, flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)))
     cnt = np.array(c[:], np.int64)
     return sl, wa, sv, cnt, s[:cnt[0]], w[:cnt[1]], flags
+
+
+def fit_cells(p, phi, phid, scells, wcells):
+    """Rows of the id_defects fits (as id_defects returns them) for the given
+    string and wall cell indices only."""
+    sc = np.ascontiguousarray(scells, np.int64)
+    wc = np.ascontiguousarray(wcells, np.int64)
+    s = np.zeros((max(len(sc), 1), 13))
+    w = np.zeros((max(len(wc), 1), 10))
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    lib().axo_fit_cells(ctypes.byref(p), dptr(phi), dptr(phid), sc.ctypes.data_as(i64p), len(sc), dptr(s),
+                        wc.ctypes.data_as(i64p), len(wc), dptr(w))
+    return s[:len(sc)], w[:len(wc)]
 
 
 def position_string(ph, seed, cell):

@@ -650,6 +650,60 @@ static void group_sums(const double *rows, int width, int vcol, int gcol, int64_
   free(tot);
 }
 
+/* The second pass of id_defects (defects_3d.f90:152-219) for one string
+ * cell s: position_string (435-603) on the 8 corner phases, velocity_string
+ * (605-692), the row pos(3) dir(3) vel(3) gof sl cell group. */
+static void fit_string_cell(const axg_params *p, const double *phi, const double *phidot, int64_t s,
+                            double *r) {
+  const int64_t n = p->ngrid, n2 = n * n, ix = s % n, iy = (s / n) % n, iz = s / n2;
+  int64_t cs[8];
+  double ph[8];
+  corner_sites(n, ix, iy, iz, cs);
+  for (int c = 0; c < 8; ++c) ph[c] = axd_atan2(phi[2 * cs[c] + 1], phi[2 * cs[c]]);
+  double pos[3], dir[3], vel[3], gof, l;
+  axo_position_string(ph, p->seed, (uint64_t)s, pos, dir, &gof, &l);
+  velocity_string(p, phi, phidot, ix, iy, iz, pos, vel);
+  r[0] = pos[0] + ix + 0.5;
+  r[1] = pos[1] + iy + 0.5;
+  r[2] = pos[2] + iz + 0.5;
+  r[3] = dir[0]; r[4] = dir[1]; r[5] = dir[2];
+  r[6] = vel[0]; r[7] = vel[1]; r[8] = vel[2];
+  r[9] = gof;
+  r[10] = l;
+  r[11] = (double)s;
+  r[12] = -1.0;
+}
+
+/* The same for one wall cell: position_wall (1058-1233), the row pos(3)
+ * dir(3) gof wa cell group. */
+static void fit_wall_cell(const axg_params *p, const double *phi, int64_t s, double *r) {
+  const int64_t n = p->ngrid, n2 = n * n, ix = s % n, iy = (s / n) % n, iz = s / n2;
+  int64_t cs[8];
+  double ph[8];
+  corner_sites(n, ix, iy, iz, cs);
+  for (int c = 0; c < 8; ++c) ph[c] = axd_atan2(phi[2 * cs[c] + 1], phi[2 * cs[c]]);
+  double pos[3], dir[3], gof, a;
+  position_wall_m(ph, pos, dir, &gof, &a);
+  r[0] = pos[0] + ix + 0.5;
+  r[1] = pos[1] + iy + 0.5;
+  r[2] = pos[2] + iz + 0.5;
+  r[3] = dir[0]; r[4] = dir[1]; r[5] = dir[2];
+  r[6] = gof;
+  r[7] = a;
+  r[8] = (double)s;
+  r[9] = -1.0;
+}
+
+/* The per-cell fits of id_defects for given cells only (a sample of a large
+ * lattice's flagged cells): rows as axo_id_defects writes them. */
+void axo_fit_cells(const axg_params *p, const double *phi, const double *phidot, const int64_t *scells,
+                   int64_t ns, double *sres, const int64_t *wcells, int64_t nw, double *wres) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < ns; ++k) fit_string_cell(p, phi, phidot, scells[k], sres + 13 * k);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < nw; ++k) fit_wall_cell(p, phi, wcells[k], wres + 10 * k);
+}
+
 /* defects_3d.f90:31-307 without grouping (group_strings = group_walls = .false.)
  * and the sums of add_string_length (1654-1733) / add_wall_area (2145-2204). */
 void axo_id_defects(const axg_params *p, const double *phi, const double *phidot, double tau,
@@ -671,45 +725,9 @@ void axo_id_defects(const axg_params *p, const double *phi, const double *phidot
   double *sres = (double *)calloc((size_t)(ns + 1) * 13, sizeof(double));
   double *wres = (double *)calloc((size_t)(nw + 1) * 10, sizeof(double));
 #pragma omp parallel for schedule(dynamic, 4)
-  for (int64_t k = 0; k < ns; ++k) {
-    int64_t s = scell[k], ix = s % n, iy = (s / n) % n, iz = s / n2;
-    int64_t cs[8];
-    double ph[8];
-    corner_sites(n, ix, iy, iz, cs);
-    for (int c = 0; c < 8; ++c) ph[c] = axd_atan2(phi[2 * cs[c] + 1], phi[2 * cs[c]]);
-    double pos[3], dir[3], vel[3], gof, l;
-    axo_position_string(ph, p->seed, (uint64_t)s, pos, dir, &gof, &l);
-    velocity_string(p, phi, phidot, ix, iy, iz, pos, vel);
-    double *r = sres + 13 * k;
-    r[0] = pos[0] + ix + 0.5;
-    r[1] = pos[1] + iy + 0.5;
-    r[2] = pos[2] + iz + 0.5;
-    r[3] = dir[0]; r[4] = dir[1]; r[5] = dir[2];
-    r[6] = vel[0]; r[7] = vel[1]; r[8] = vel[2];
-    r[9] = gof;
-    r[10] = l;
-    r[11] = (double)s;
-    r[12] = -1.0;
-  }
+  for (int64_t k = 0; k < ns; ++k) fit_string_cell(p, phi, phidot, scell[k], sres + 13 * k);
 #pragma omp parallel for schedule(dynamic, 4)
-  for (int64_t k = 0; k < nw; ++k) {
-    int64_t s = wcell[k], ix = s % n, iy = (s / n) % n, iz = s / n2;
-    int64_t cs[8];
-    double ph[8];
-    corner_sites(n, ix, iy, iz, cs);
-    for (int c = 0; c < 8; ++c) ph[c] = axd_atan2(phi[2 * cs[c] + 1], phi[2 * cs[c]]);
-    double pos[3], dir[3], gof, a;
-    position_wall_m(ph, pos, dir, &gof, &a);
-    double *r = wres + 10 * k;
-    r[0] = pos[0] + ix + 0.5;
-    r[1] = pos[1] + iy + 0.5;
-    r[2] = pos[2] + iz + 0.5;
-    r[3] = dir[0]; r[4] = dir[1]; r[5] = dir[2];
-    r[6] = gof;
-    r[7] = a;
-    r[8] = (double)s;
-    r[9] = -1.0;
-  }
+  for (int64_t k = 0; k < nw; ++k) fit_wall_cell(p, phi, wcell[k], wres + 10 * k);
   const double hor = tau / p->dspa;
   /* add_string_length (defects_3d.f90:1654-1733) */
   if ((p->flags & AXG_F_GROUP_STRINGS) && ns > 0) {

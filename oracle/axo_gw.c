@@ -311,10 +311,16 @@ void axo_grav_spec_log_green(const axg_params *p, const double *acc, double *edg
 /*
  * u_ij spectrum.  w = tau u, w' = u + tau u' (w = a u with a ~ tau obeys
  * w'' - lap w = tau sigma_cr^2 S_ij).  With W = dx^3 FFT(w):
- *   numer(k) = 1/2 sum_ij ( |W'^TT_ij|^2 + k^2 |W^TT_ij|^2 ),
- * which equals sum_pol (|A_c|^2 + |A_s|^2) of grav_waves.f90:283-284 summed
- * over a k-shell in the continuum limit.  TT: Lambda = P u P - P tr(P u)/2,
- * P = 1 - khat khat, khat from the integer wave vector.
+ *   numer(k) = sum_ij ( |W'^TT_ij|^2 + k^2 |W^TT_ij|^2 ).
+ * Summed over a k-shell it is the Green's-function numerator
+ * sum_pol (|A_c|^2 + |A_s|^2) of grav_waves.f90:283-284 in the continuum
+ * limit: with the polarisation p = e1 + i e2 of get_comwav_grav (157-191),
+ * |X+|^2 + |X-|^2 = sum_ij |(Lambda S)_ij|^2, and over a shell holding k and
+ * -k both reduce to sum_k |int e^{i k tau} tau sigma_cr^2 (Lambda S)(k) dtau|^2
+ * (dw carries the dx^3 of W).  The lattice wave equation of u_ij differs
+ * from the Green's function e^{i k tau} at O((k dx)^2).  TT:
+ * Lambda = P u P - P tr(P u)/2, P = 1 - khat khat, khat from the integer
+ * wave vector.
  */
 static void tt_accumulate(const double *Ur, const double *Ui, const double kh[3], double *out) {
   /* U symmetric 3x3 complex from 6 comps (11,21,22,31,32,33) */
@@ -397,7 +403,7 @@ static void uij_numer(const axg_params *p, const double *u, const double *udot, 
     tt_accumulate(Dr, Di, kh, &e0);
     tt_accumulate(Ur, Ui, kh, &e1);
     double k = qarr[s];
-    varr[s] = 0.5 * (e0 + k * k * e1);
+    varr[s] = e0 + k * k * e1;
   }
   free(W);
 }

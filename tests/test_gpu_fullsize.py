@@ -231,3 +231,110 @@ def test_green_fp64_512_float_float_transforms_match_cufft(monkeypatch):
     a, b = out["1"], out["0"]
     scale = _max_abs(b)
     assert scale > 0 and _max_abs_diff(a, b) / scale < 1e-12
+
+
+REF_PI = 3.14159265359  # potential.f90:8, the classification thresholds
+
+
+def _near_margin_cells(phi_slab, margin=2e-5):
+    """Cells of a z-slab (all but its last plane) whose classification
+    decisions (largest gap against the wrap gap, and against pi and 7 pi / 4,
+    defects_3d.f90:309-349) lie within `margin` rad of a threshold: the cells
+    the FP32 filter hands to the FP64 recomputation."""
+    ph = np.angle(phi_slab)
+    nz = ph.shape[0] - 1
+    corners = []
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                corners.append(np.roll(np.roll(ph[dz:dz + nz], -dy, 1), -dx, 2))
+    srt = np.sort(np.stack(corners), axis=0)
+    wrap = srt[0] - srt[-1] + 2 * np.pi
+    gmax = np.max(np.diff(srt, axis=0), axis=0)
+    big = np.maximum(wrap, gmax)
+    near = ((np.abs(gmax - wrap) < margin) | (np.abs(big - REF_PI) < margin) |
+            (np.abs(big - 7 * REF_PI / 4) < margin))
+    return int(np.count_nonzero(near))
+
+
+def _defect_parity(p_gpu, p64, evolve):
+    """Classification flags and counts and the plaquette windings of the
+    GPU's own evolved state against the oracle on the same snapshot."""
+    with ag.Lattice(p_gpu) as lat:
+        evolve(lat)
+        counts = lat.classify_cells(7)
+        flags = lat.defect_flags()
+        wind = lat.string_winding()
+        phi, _ = lat.download(phidot=False)
+    rf, rc = axo.classify_cells(p64, phi, 7, 0)
+    assert np.array_equal(counts, rc), (counts, rc)
+    assert np.array_equal(flags, rf)
+    assert np.array_equal(wind, axo.string_winding(p64, phi))
+    return counts, phi
+
+
+@pytest.mark.parametrize("precision", [ag.PREC_FP64_PLAIN, ag.PREC_FP32_MIXED])
+def test_defect_counts_bit_exact_on_the_512_snapshot(precision):
+    """The benchmark lattice (512^3, reference potential, Gaussian-flat IC)
+    after 40 steps: flags, string / wall / mask counts and windings of the
+    GPU classification (FP32 filter with FP64 recomputation inside the
+    margin) equal the oracle's FP64 classification of the same snapshot
+    (defects_3d.f90:31-103, 309-349), for the FP64 and the FP32-mixed state."""
+    if _host_gib() < 16:
+        pytest.skip("needs ~16 GiB of host memory")
+    n = 512
+    p = workload(n, precision, ag.GW_NONE)
+
+    def evolve(lat):
+        lat.ic_gaussian_flat(kcut=2.0 * np.pi / (8 * p.dspa))
+        lat.leapfrog(2.0, 0.25 * p.dspa, 40, True, True)
+
+    counts, phi = _defect_parity(p, workload(n, ag.PREC_FP64_PLAIN, ag.GW_NONE), evolve)
+    assert counts[0] > 10 ** 6 and counts[1] > 10 ** 6
+    # the FP64 recomputation was exercised: a 16-plane slab alone holds near-margin cells
+    assert _near_margin_cells(phi[:17]) > 0
+
+
+@pytest.mark.parametrize("precision", [ag.PREC_FP64_FUSED, ag.PREC_FP32_MIXED])
+def test_defect_counts_bit_exact_256_quartic_ndw2(precision):
+    """256^3 quartic model with the N_DW = 2 axion term switched on mid-run
+    (tau_on = 11, run from 10 to 18): counts, flags and windings bit-exact
+    against the oracle on the same snapshot."""
+    if _host_gib() < 8:
+        pytest.skip("needs ~8 GiB of host memory")
+    n = 256
+    p = quartic(n, precision, ag.GW_NONE)
+
+    def evolve(lat):
+        lat.ic_gaussian_flat(kcut=1.0)
+        lat.leapfrog(10.0, 0.2, 40, True, True)
+
+    counts, _ = _defect_parity(p, quartic(n, ag.PREC_FP64_PLAIN, ag.GW_NONE), evolve)
+    assert counts[0] > 0 and counts[1] > 0
+
+
+def test_id_defects_fits_bit_exact_on_a_128_sample():
+    """128^3 benchmark physics evolved to tau ~ 2.6 (about 10^5 string and
+    3 10^5 wall cells): a random sample of 256 string and 256 wall cells of
+    the GPU's id_defects lists, refitted by the oracle from the same
+    snapshot, agrees bit for bit (gof, an exp, to 1e-14); the global sums
+    are checked against the oracle's full call at smaller sizes."""
+    n = 128
+    p = workload(n, ag.PREC_FP64_PLAIN, ag.GW_NONE)
+    with ag.Lattice(p) as lat:
+        lat.ic_gaussian_flat(kcut=2.0 * np.pi / (8 * p.dspa))
+        lat.leapfrog(2.0, 0.25 * p.dspa, 10, True, True)
+        tau = 2.0 + 10 * 0.25 * p.dspa
+        sl, wa, sv, cnt = lat.id_defects(1, tau)
+        S, W = lat.defect_lists(int(cnt[0]), int(cnt[1]))
+        phi, phid = lat.download()
+    assert cnt[0] > 10 ** 4 and cnt[1] > 10 ** 4
+    rng = np.random.default_rng(5)
+    si = np.sort(rng.choice(int(cnt[0]), 256, replace=False))
+    wi = np.sort(rng.choice(int(cnt[1]), 256, replace=False))
+    fs, fw = axo.fit_cells(p, phi, phid, S[si, 11].astype(np.int64), W[wi, 8].astype(np.int64))
+    cols = [0, 1, 2, 3, 4, 5, 6, 7, 8, 10, 11]
+    assert np.array_equal(S[si][:, cols], fs[:, cols])
+    np.testing.assert_allclose(S[si, 9], fs[:, 9], rtol=1e-14)
+    wcols = [0, 1, 2, 3, 4, 5, 7, 8]
+    assert np.array_equal(W[wi][:, wcols], fw[:, wcols])

@@ -291,3 +291,37 @@ def test_green_requires_mode():
     with ag.Lattice(params(16, ag.PREC_FP64_PLAIN, ag.GW_NONE)) as lat:
         with pytest.raises(ag.AxgError):
             lat.grav_spec_estimation(1.0)
+
+
+def _modes_on_gpu(n, precision, phi0, L=32.0):
+    dt, steps = 0.1 * 32 / n, 100 * n // 32  # dt in proportion to dx
+    kw = dict(ngrid=n, precision=precision, potential=ag.POT_QUARTIC, dspa=L / n, sigma_cr=0.05, kappa=0.1,
+              compat=ag.COMPAT_INTENDED, num_bin_grav=25 * n // 32, **{"lambda": 1.0})
+    out = []
+    for gw in (ag.GW_GREEN, ag.GW_UIJ):
+        with ag.Lattice(ag.default_params(gw_mode=gw, **kw)) as lat:
+            lat.upload(phi0, np.zeros_like(phi0))
+            if gw == ag.GW_UIJ:
+                z = np.zeros((6, n, n, n))
+                lat.upload_uij(z, z)
+            lat.leapfrog(1.0, dt, steps, True, True)
+            out.append(lat.grav_spec_estimation(1.0 + steps * dt)[2])
+    return tuple(out)
+
+
+def test_mode_u_converges_to_mode_g_on_the_gpu():
+    """Mode U (u_ij leapfrog + TT spectrum) against Mode G (the reference's
+    Green's-function method, grav_waves.f90:193-321) through the C-ABI, the
+    same band-limited field in one box at dx = 1, 1/2, 1/4 (dt = dx / 10):
+    the band-integrated difference of their numerators falls at second order
+    (a factor 4 expected per halving) and is below 3 % at dx = 1.  The
+    FP32-mixed paths show the same difference at dx = 1/2 to 2e-3."""
+    import gw_crosscheck
+    ns = (32, 64, 128)
+    fields = gw_crosscheck.band_limited_fields(list(ns))
+    spectra = [_modes_on_gpu(n, ag.PREC_FP64_PLAIN, f) for n, f in zip(ns, fields)]
+    e = gw_crosscheck.mode_u_vs_g(spectra)
+    assert e[0] < 0.03
+    assert e[1] < e[0] / 3 and e[2] < e[1] / 3, e
+    e32 = gw_crosscheck.mode_u_vs_g([_modes_on_gpu(64, ag.PREC_FP32_MIXED, fields[1])])[0]
+    assert abs(e32 - e[1]) < 2e-3, (e32, e[1])

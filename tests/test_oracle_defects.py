@@ -163,3 +163,18 @@ def test_grouping_four_straight_strings():
     assert len(set(S[:, 12].astype(int))) == 4
     # each string is one group of length ~N; 2*hor = 4 < N so all count as long strings
     assert sl[1] == pytest.approx(sl[0]) and sl[0] / (4 * n) == pytest.approx(1.0, abs=0.05)
+
+
+def test_fit_cells_reproduces_id_defects_rows():
+    # the per-cell fits for a chosen subset equal the rows of the full call
+    n = 12
+    rng = np.random.default_rng(17)
+    phi = (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n))).astype(np.complex128)
+    phid = (0.1 * (rng.standard_normal((n, n, n)) + 1j * rng.standard_normal((n, n, n)))).astype(np.complex128)
+    p = params(n)
+    sl, wa, sv, cnt, S, W, _ = axo.id_defects(p, phi, phid, 3.0)
+    assert cnt[0] > 10 and cnt[1] > 10
+    si = rng.choice(int(cnt[0]), 7, replace=False)
+    wi = rng.choice(int(cnt[1]), 5, replace=False)
+    fs, fw = axo.fit_cells(p, phi, phid, S[si, 11].astype(np.int64), W[wi, 8].astype(np.int64))
+    assert np.array_equal(fs, S[si]) and np.array_equal(fw, W[wi])
