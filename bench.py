@@ -150,11 +150,21 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+WORKLOAD_KW = dict(potential=0, sigma_cr=1.0, kappa=0.1, seed=1)  # potential 0: potential.f90
+
+
 def workload_params(ag, n, precision, gw, device=0):
     # 512^3 periodic lattice, reference potential (potential.f90), sigma_cr = 1,
     # dx = boxsize * tau_fin / N with boxsize 1, tau_fin 32; kappa 0.1.
-    return ag.default_params(ngrid=n, precision=precision, gw_mode=gw, potential=ag.POT_REFERENCE,
-                             dspa=32.0 / n, sigma_cr=1.0, kappa=0.1, seed=1, device=device)
+    return ag.default_params(ngrid=n, precision=precision, gw_mode=gw, dspa=32.0 / n, device=device, **WORKLOAD_KW)
+
+
+def workload_name(n):
+    """config.workload of both arms: the work one step does, independent of
+    the implementation that does it."""
+    return (f"{n}^3 periodic lattice, one leapfrog step (kick+drift) of phi and six u_ij per site "
+            f"(one site-update = one kick+drift of all 7 fields at one site); reference potential "
+            f"(potential.f90), Gaussian-flat seeded IC (Philox key 1, |k| <= 2 pi / (8 dx))")
 
 
 def bench_ours(ag, n, precision, gw, steps, warmup, dist, device, t0=2.0, eps=0.25, clocks=False,
@@ -470,15 +480,11 @@ def accuracy_fp32(ag, n, steps, device):
 def cpu_oracle_rate(n, steps, threads=None, warmup=1):
     """FP64 CPU restatement of evolve.f90 (phi + six u_ij), all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    from oracle import axo
-    import axion_grav_gb300 as ag
+    from oracle import axo  # the oracle's own parameter defaults: no GPU library is loaded
 
-    p = workload_params(ag, n, ag.PREC_FP64_PLAIN, ag.GW_UIJ)
-    rng = np.random.default_rng(0)
-    phi = np.empty((n, n, n), np.complex128)
-    phid = np.zeros((n, n, n), np.complex128)
-    for z in range(n):  # chunked fill keeps peak memory low
-        phi[z] = np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
+    p = axo.default_params(ngrid=n, precision=0, gw_mode=2, dspa=32.0 / n, **WORKLOAD_KW)
+    # the GPU arm's initial state: the same seeded Gaussian-flat field
+    phi, phid = axo.ic_gaussian_flat(p, kcut=2.0 * np.pi / (8 * p.dspa))
     u = np.zeros((6, n, n, n))
     ud = np.zeros((6, n, n, n))
     dt, _ = axo.get_dtau(p, 2.0, 32.0, 0.25)
@@ -510,8 +516,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{n}^3 lattice leapfrog of phi + 6 u_ij (one site-update = one kick+drift of all "
-                               f"7 fields at one site)", "n": n, "gw_mode": "uij",
+        "config": {"workload": workload_name(n), "n": n, "gw_mode": "uij", "precision": "fp64",
+                   "parallelism": f"OpenMP x{cores} (rank 0 only)",
                    "implementation": "CPU restatement of evolve.f90 (oracle/, C + OpenMP, FP64); the Fortran "
                                      "reference needs ifort/MPI/MKL/FFTW, none present"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
@@ -687,15 +693,16 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{n}^3 periodic lattice, one leapfrog step (kick+drift) of phi and six u_ij "
-                                   f"per site, FP32-mixed fused TMA kernel with Kahan drift; reference potential "
-                                   f"(potential.f90), Gaussian-flat seeded IC",
+            "config": {"workload": workload_name(n),
                        "n": n, "gw_mode": "uij", "precision": "fp32_mixed", "parallelism": f"replicas x{world}",
+                       "implementation": "FP32-mixed fused TMA kernel with Kahan-compensated drifts (libaxgpu.so)",
                        "l2": "no flush: state %.1f GiB >> 126 MB L2" % (sites * 96 / 2 ** 30),
                        "tile": r32["tile_shape"]},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r32["launches"],
-            "clocks": r32["clocks"], "fp64_plain": fp64, "ensemble": ensemble, "accuracy": accuracy,
-            "adjoint": adjoint, "phi_only": phi_only, "green": green, "output_calls": output_calls,
+            "clocks": r32["clocks"], "adjoint": adjoint, "phi_only": phi_only, "green": green,
+            "output_calls": output_calls,
+            # last, so that a reader keeping only the tail of the line sees them
+            "ensemble": ensemble, "accuracy": accuracy, "fp64_plain": fp64,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -26,7 +26,7 @@ def build(force: bool = False) -> str:
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in srcs + hdrs):
             return LIB
-    cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
+    cmd = ["gcc", "-O3", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
            "-fno-fast-math", "-I" + HERE, "-I" + os.path.join(ROOT, "include"),
            "-I" + os.path.join(ROOT, "axion_grav_gb300", "csrc"), *srcs, "-o", LIB + ".tmp", "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
