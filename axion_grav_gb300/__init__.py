@@ -102,7 +102,7 @@ EXPORTED_SYMBOLS = (
     "axg_ensemble_size", "axg_ensemble_member", "axg_ensemble_leapfrog", "axg_ensemble_autotune",
     "axg_ensemble_launch_count", "axg_adjoint_gw_band", "axg_spectrum_covariance", "axg_compute_crho_cov",
     "axg_epsilon", "axg_ensemble_set_tile", "axg_ensemble_set_launch_mode", "axg_ensemble_launch_mode",
-    "axg_selftest_wait_timeout",
+    "axg_selftest_wait_timeout", "axg_ensemble_grav_spec_mean", "axg_ensemble_defect_mean",
 )
 
 _lib = None
@@ -190,6 +190,9 @@ def load_library():
                                    ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "axg_ensemble_autotune": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_int), dp], ctypes.c_int),
         "axg_ensemble_launch_count": ([ctypes.c_void_p, P(ctypes.c_int64)], ctypes.c_int),
+        "axg_ensemble_grav_spec_mean": ([ctypes.c_void_p, ctypes.c_double, dp, dp, dp, dp], ctypes.c_int),
+        "axg_ensemble_defect_mean": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, dp, dp, dp, dp],
+                                     ctypes.c_int),
         "axg_spectrum_covariance": ([c_ctx, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, P(ctypes.c_int)],
                                     ctypes.c_int),
         "axg_compute_crho_cov": ([c_ctx, dp, dp], ctypes.c_int),
@@ -584,6 +587,21 @@ class Ensemble:
         v = ctypes.c_int64()
         self._check(self.lib.axg_ensemble_launch_count(self._e, ctypes.byref(v)))
         return v.value
+
+    def grav_spec_mean(self, tau: float):
+        """axg_ensemble_grav_spec_mean: (wave, power mean, power standard
+        error, modes) over the members' GW spectra."""
+        nb = int(self._params[0].num_bin_grav)
+        w, m, s, d = (np.zeros(nb) for _ in range(4))
+        self._check(self.lib.axg_ensemble_grav_spec_mean(self._e, tau, _dptr(w), _dptr(m), _dptr(s), _dptr(d)))
+        return w, m, s, d
+
+    def defect_mean(self, idx: int, tau: float):
+        """axg_ensemble_defect_mean: (xi mean, xi standard error, A mean, A
+        standard error), three components each."""
+        xm, xs, am, as_ = (np.zeros(3) for _ in range(4))
+        self._check(self.lib.axg_ensemble_defect_mean(self._e, idx, tau, _dptr(xm), _dptr(xs), _dptr(am), _dptr(as_)))
+        return xm, xs, am, as_
 
     def close(self):
         if self._e:

@@ -405,3 +405,80 @@ int axg_ensemble_autotune(axg_ensemble *e, int steps, int *best_cfg, double *bes
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Ensemble outputs: per-realisation results of the members' own calls,
+// averaged bin by bin / component by component on the host.
+// ---------------------------------------------------------------------------
+namespace {
+// mean and standard error of the mean of v[0..n), n >= 1
+void mean_sem(const std::vector<double> &v, double *mean, double *sem) {
+  double s = 0.0;
+  for (double x : v) s += x;
+  const double m = s / (double)v.size();
+  double q = 0.0;
+  for (double x : v) q += (x - m) * (x - m);
+  *mean = m;
+  *sem = v.size() > 1 ? std::sqrt(q / (double)(v.size() - 1) / (double)v.size()) : 0.0;
+}
+}  // namespace
+
+extern "C" {
+
+int axg_ensemble_grav_spec_mean(axg_ensemble *e, double tau, double *wave, double *power_mean, double *power_sem,
+                                double *denom) {
+  if (!e || !power_mean) return AXG_ERR_ARG;
+  if (!e->uij) return ens_error(e, AXG_ERR_STATE, "ensemble GW spectrum: members run gw_mode NONE");
+  const int nb = e->m[0]->p.num_bin_grav;
+  for (auto *c : e->m)
+    if (c->p.num_bin_grav != nb) return ens_error(e, AXG_ERR_ARG, "members differ in num_bin_grav");
+  std::vector<std::vector<double>> per(nb);
+  std::vector<double> w(nb), pw(nb), nu(nb), de(nb), dsum(nb, 0.0);
+  for (auto *c : e->m) {
+    const int rc = axg_grav_spec_estimation(c, tau, w.data(), pw.data(), nu.data(), de.data());
+    if (rc != AXG_OK) return ens_error(e, rc, std::string("member spectrum: ") + c->err);
+    for (int k = 0; k < nb; ++k) {
+      dsum[k] += de[k];
+      if (de[k] > 0) per[k].push_back(pw[k]);
+    }
+  }
+  for (int k = 0; k < nb; ++k) {
+    double m = 0.0, s = 0.0;
+    if (!per[k].empty()) mean_sem(per[k], &m, &s);
+    power_mean[k] = m;
+    if (power_sem) power_sem[k] = s;
+    if (denom) denom[k] = dsum[k];
+    if (wave) wave[k] = w[k];  // the members share dspa, so the linear bins coincide
+  }
+  return AXG_OK;
+}
+
+int axg_ensemble_defect_mean(axg_ensemble *e, int64_t idx, double tau, double xi_mean[3], double xi_sem[3],
+                             double area_mean[3], double area_sem[3]) {
+  if (!e || !xi_mean || !(tau > 0)) return AXG_ERR_ARG;
+  std::vector<std::vector<double>> xi(3), ar(3);
+  for (auto *c : e->m) {
+    double sl[3], wa[3], sv[3];
+    int64_t counts[3];
+    const int rc = axg_id_defects(c, idx, tau, sl, wa, sv, counts);
+    if (rc != AXG_OK) return ens_error(e, rc, std::string("member id_defects: ") + c->err);
+    // defects_and_spectrum (evolve.f90:191-192): xi = (tau/dx)^2 sl / N^3 / 4, A = (tau/dx) wa / N^3 / 2
+    const double h = tau / c->p.dspa, n3 = (double)c->n3;
+    for (int k = 0; k < 3; ++k) {
+      xi[k].push_back(h * h * sl[k] / n3 / 4);
+      ar[k].push_back(h * wa[k] / n3 / 2);
+    }
+  }
+  for (int k = 0; k < 3; ++k) {
+    double m, s;
+    mean_sem(xi[k], &m, &s);
+    xi_mean[k] = m;
+    if (xi_sem) xi_sem[k] = s;
+    mean_sem(ar[k], &m, &s);
+    if (area_mean) area_mean[k] = m;
+    if (area_sem) area_sem[k] = s;
+  }
+  return AXG_OK;
+}
+
+}  // extern "C"

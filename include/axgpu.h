@@ -355,6 +355,24 @@ int axg_ensemble_set_tile(axg_ensemble *e, int cfg);
 int axg_ensemble_set_launch_mode(axg_ensemble *e, int persistent);
 int axg_ensemble_launch_mode(const axg_ensemble *e, int *persistent);
 int axg_ensemble_launch_count(const axg_ensemble *e, int64_t *launches);
+/* Ensemble means of the per-realisation outputs at conformal time tau, from
+ * each member's own call (so every realisation's result is the one its own
+ * lattice gives):
+ *  - the GW spectrum of grav_spec_estimation (grav_waves.f90:257-321; gw_mode
+ *    UIJ): the members share dspa, so their num_bin_grav linear bins on
+ *    (0, pi/dx] coincide; power_mean / power_sem = mean and standard error
+ *    of power_grav over the members with modes in the bin, denom = modes
+ *    summed over the members, wave = bin centres (any output may be NULL
+ *    but power_mean);
+ *  - the string parameter xi = (tau/dx)^2 sl / N^3 / 4 and the wall
+ *    parameter A = (tau/dx) wa / N^3 / 2 of defects_and_spectrum
+ *    (evolve.f90:191-192) from each member's id_defects (defects_3d.f90:31-307,
+ *    the member's flags select strings / walls / grouping): mean and
+ *    standard error per component. */
+int axg_ensemble_grav_spec_mean(axg_ensemble *e, double tau, double *wave, double *power_mean, double *power_sem,
+                                double *denom);
+int axg_ensemble_defect_mean(axg_ensemble *e, int64_t idx, double tau, double xi_mean[3], double xi_sem[3],
+                             double area_mean[3], double area_sem[3]);
 
 /* ------------------------------------------------------------------ */
 /* allocation-free diagnostics                                          */

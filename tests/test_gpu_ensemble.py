@@ -126,3 +126,43 @@ def test_ensemble_autotune_restores_state_and_spectra_per_member():
 def test_ensemble_rejects_mixed_physics():
     with pytest.raises(ag.AxgError):
         ag.Ensemble([member_params(32, 1), member_params(32, 2).update(dspa=0.25)])
+
+
+def test_ensemble_means_equal_the_mean_of_single_runs():
+    """The ensemble outputs of the batched workload (config of 96
+    realisations, here 5 uneven members): the mean GW spectrum and the mean
+    string and wall parameters equal the mean over each realisation's own
+    single-lattice results (the members are bit-identical to single runs),
+    with the standard error of that mean."""
+    ps = [member_params(n, 300 + i) for i, n in enumerate(SIZES)]
+    dt, t0, nsteps = 0.02, 1.6, 10
+    tau = t0 + dt * nsteps
+    with ag.Ensemble(ps) as ens:
+        for i, m in enumerate(ens.members):
+            m.ic_gaussian_flat(1.5, 300 + i)
+        ens.leapfrog(t0, dt, nsteps, True, True, use_graph=True)
+        w, pm, ps_, de = ens.grav_spec_mean(tau)
+        xm, xs, am, as_ = ens.defect_mean(1, tau)
+    singles = []
+    for i, p in enumerate(ps):
+        with ag.Lattice(p) as lat:
+            lat.ic_gaussian_flat(1.5, 300 + i)
+            lat.leapfrog(t0, dt, nsteps, True, True)
+            sw, spw, snu, sde = lat.grav_spec_estimation(tau)
+            sl, wa, sv, cnt = lat.id_defects(1, tau)
+        h = tau / p.dspa
+        singles.append((sw, spw, sde, h * h * sl / p.ngrid ** 3 / 4, h * wa / p.ngrid ** 3 / 2))
+    np.testing.assert_array_equal(w, singles[0][0])
+    np.testing.assert_array_equal(de, np.sum([s[2] for s in singles], axis=0))
+    for k in range(len(w)):
+        vals = [s[1][k] for s in singles if s[2][k] > 0]
+        want = np.mean(vals) if vals else 0.0
+        assert pm[k] == pytest.approx(want, rel=1e-13, abs=0.0)
+        if len(vals) > 1:
+            assert ps_[k] == pytest.approx(np.std(vals, ddof=1) / np.sqrt(len(vals)), rel=1e-9)
+    xi = np.array([s[3] for s in singles])
+    ar = np.array([s[4] for s in singles])
+    np.testing.assert_allclose(xm, xi.mean(axis=0), rtol=1e-13)
+    np.testing.assert_allclose(xs, xi.std(axis=0, ddof=1) / np.sqrt(len(ps)), rtol=1e-9)
+    np.testing.assert_allclose(am, ar.mean(axis=0), rtol=1e-13)
+    assert xm[0] > 0 and np.all(pm[1:] >= 0) and pm.max() > 0
