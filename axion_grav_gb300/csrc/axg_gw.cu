@@ -693,22 +693,22 @@ __global__ void k_gw_bin_green(const A *__restrict__ acc, int n, int64_t astride
   }
 }
 
-// u_ij: 12 real fields (tau u_c, u_c + tau u'_c), scaled by dx^3 at use
-template <typename V, typename R>
+// u_ij: one of the 12 real fields (f < 6: tau u_f; else u_c + tau u'_c,
+// c = f - 6), scaled by dx^3 at use; the cuFFT path transforms them one at
+// a time through one real buffer of n^3
+template <typename R>
 __global__ void k_uij_prepare(const R *__restrict__ u, const R *__restrict__ ud, const R *__restrict__ cu,
-                              int64_t n3, double tau, R *__restrict__ w) {
+                              int64_t n3, double tau, int f, R *__restrict__ w) {
+  const int c = f < 6 ? f : f - 6;
+  const R *uc = u + c * n3, *udc = ud + c * n3, *cuc = cu ? cu + c * n3 : nullptr;
+  const R t = (R)tau;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride) {
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      // in the precision of the spectrum: FP32 for FP32-mixed (the Kahan
-      // compensation is below FP32 resolution of u; it is applied all the same)
-      R uv = u[c * n3 + s];
-      if (cu) uv -= cu[c * n3 + s];
-      const R t = (R)tau;
-      w[c * n3 + s] = t * uv;
-      w[(6 + c) * n3 + s] = uv + t * ud[c * n3 + s];
-    }
+    // in the precision of the spectrum: FP32 for FP32-mixed (the Kahan
+    // compensation is below FP32 resolution of u; it is applied all the same)
+    R uv = uc[s];
+    if (cuc) uv -= cuc[s];
+    w[s] = f < 6 ? t * uv : uv + t * udc[s];
   }
 }
 
@@ -837,11 +837,11 @@ int ensure_uij_fft(axg_ctx *ctx) {
     AXG_TRY(axg_alloc(ctx, &ctx->ubuf, (size_t)12 * nhalf * 2 * rs, "u_ij spectra"));
     return AXG_OK;
   }
-  // real input 12 x N^3 followed by complex output 12 x nhalf
-  AXG_TRY(axg_alloc(ctx, &ctx->ubuf, (size_t)12 * ctx->n3 * rs + (size_t)12 * nhalf * 2 * rs, "u_ij FFT"));
-  int dims[3] = {n, n, n};
-  AXG_CUFFT_TRY(ctx, cufftPlanMany(&ctx->plan_u, 3, dims, nullptr, 1, (int)ctx->n3, nullptr, 1,
-                                   (int)nhalf, fp32 ? CUFFT_R2C : CUFFT_D2Z, 12));
+  // one real field of N^3 followed by the complex output 12 x nhalf; the
+  // twelve fields go through the real buffer one at a time (at 1024^3 a
+  // batch of twelve would need 48 GiB of real input and cuFFT rejects it)
+  AXG_TRY(axg_alloc(ctx, &ctx->ubuf, (size_t)ctx->n3 * rs + (size_t)12 * nhalf * 2 * rs, "u_ij FFT"));
+  AXG_CUFFT_TRY(ctx, cufftPlan3d(&ctx->plan_u, n, n, n, fp32 ? CUFFT_R2C : CUFFT_D2Z));
   AXG_CUFFT_TRY(ctx, cufftSetStream(ctx->plan_u, ctx->stream));
   ctx->plan_u_ok = true;
   return AXG_OK;
@@ -1026,31 +1026,34 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
     const double dv = ctx->p.dspa * ctx->p.dspa * ctx->p.dspa;
     if (fp32) {
       float *w = (float *)ctx->ubuf;
-      float2 *F = ctx->uij_own_fft ? (float2 *)ctx->ubuf : (float2 *)(w + 12 * ctx->n3);
+      float2 *F = ctx->uij_own_fft ? (float2 *)ctx->ubuf : (float2 *)(w + ctx->n3);
       if (ctx->uij_own_fft) {
         AXG_TRY(axg_uij_r2c_f32(ctx, (const float *)ctx->u[ctx->cur], (const float *)ctx->ud,
                                 (const float *)ctx->cu, (float)tau, F, n));
       } else {
-        AXG_LAUNCH(ctx, "uij_prepare_fp32", (k_uij_prepare<float2, float>), grid_for(ctx->n3), 256, 0,
-                   (const float *)ctx->u[ctx->cur], (const float *)ctx->ud, (const float *)ctx->cu, ctx->n3,
-                   tau, w);
-        AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_u, w, (cufftComplex *)F));
+        for (int f = 0; f < 12; ++f) {
+          AXG_LAUNCH(ctx, "uij_prepare_fp32", k_uij_prepare<float>, grid_for(ctx->n3), 256, 0,
+                     (const float *)ctx->u[ctx->cur], (const float *)ctx->ud, (const float *)ctx->cu, ctx->n3, tau,
+                     f, w);
+          AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_u, w, (cufftComplex *)F + f * nhalf));
+        }
       }
       AXG_LAUNCH(ctx, "uij_bin_fp32", k_uij_bin<float2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
     } else {
       double *w = (double *)ctx->ubuf;
-      double2 *F = ctx->uij_own_fft ? (double2 *)ctx->ubuf : (double2 *)(w + 12 * ctx->n3);
+      double2 *F = ctx->uij_own_fft ? (double2 *)ctx->ubuf : (double2 *)(w + ctx->n3);
       if (ctx->uij_own_fft) {
         AXG_TRY(axg_uij_d2z_ff(ctx, (const double *)ctx->u[ctx->cur], (const double *)ctx->ud, tau, F, n));
       } else {
-        AXG_LAUNCH(ctx, "uij_prepare_fp64", (k_uij_prepare<double2, double>), grid_for(ctx->n3), 256, 0,
-                   (const double *)ctx->u[ctx->cur], (const double *)ctx->ud, (const double *)nullptr, ctx->n3,
-                   tau, w);
-        AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_u, w, (cufftDoubleComplex *)F));
+        for (int f = 0; f < 12; ++f) {
+          AXG_LAUNCH(ctx, "uij_prepare_fp64", k_uij_prepare<double>, grid_for(ctx->n3), 256, 0,
+                     (const double *)ctx->u[ctx->cur], (const double *)ctx->ud, (const double *)nullptr, ctx->n3,
+                     tau, f, w);
+          AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_u, w, (cufftDoubleComplex *)F + f * nhalf));
+        }
       }
       AXG_LAUNCH(ctx, "uij_bin_fp64", k_uij_bin<double2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
     }
-    (void)nhalf;
   } else {
     return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is NONE");
   }

@@ -457,6 +457,66 @@ def bench_output_calls(ag, n, device, steps=200, max_fit_cells=2_000_000):
     return out
 
 
+def bench_config2(ag, device, n=1024, steps=200, every=10, gw_outputs=8):
+    """The 1024^3 FP32-mixed workload: phi and six u_ij, quartic potential
+    (lambda = v = 1, dx = 1, sigma_cr = 0.005), the axion term
+    m_a^2 (tau / tau_on)^2 (1 - cos N_DW theta) / N_DW^2 switched on half-way
+    through the run, N_DW = 1 and 2; string and wall classification and the
+    plaquette winding every `every` steps, the GW spectrum (linear and log
+    bins) at `gw_outputs` output times.  Steps are timed with CUDA events on
+    the library's stream, output calls with the host clock (each ends with a
+    synchronising download of its result)."""
+    try:
+        import torch
+
+        free = torch.cuda.mem_get_info(device)[0]
+    except Exception:
+        free = None
+    if free is not None and free < 200 * 2 ** 30:
+        return {"skipped": f"needs ~200 GiB of free device memory, {free / 2 ** 30:.0f} GiB free"}
+    t0, dt = 10.0, 0.2
+    nout = steps // every
+    gw_at = {int(round(nout * (k + 1) / gw_outputs)) for k in range(gw_outputs)}
+    res = {"n": n, "steps": steps, "defects_every": every, "gw_outputs": sorted(gw_at), "tau_start": t0, "dt": dt}
+    for ndw in (1, 2):
+        tau_on = t0 + dt * steps / 2
+        p = ag.default_params(ngrid=n, precision=ag.PREC_FP32_MIXED, gw_mode=ag.GW_UIJ, potential=ag.POT_QUARTIC,
+                              dspa=1.0, sigma_cr=0.005, vev=1.0, n_dw=ndw, ma2_0=1e-3, tau_axion_on=tau_on,
+                              ma2_power=2.0, seed=1, gw_log_bins=64, flags=7, device=device, **{"lambda": 1.0})
+        w0 = time.perf_counter()
+        with ag.Lattice(p) as lat:
+            lat.ic_gaussian_flat(kcut=1.0)
+            step_ms, cls_s, wind_s, gw_s, counts, winds = 0.0, [], [], [], [], []
+            t = t0
+            for k in range(1, nout + 1):
+                lat.event_record(0)
+                lat.leapfrog(t, dt, every, True, True)
+                lat.event_record(1)
+                step_ms += lat.event_elapsed(0, 1)
+                t += dt * every
+                c0 = time.perf_counter()
+                c = lat.classify_cells(7)
+                cls_s.append(time.perf_counter() - c0)
+                c0 = time.perf_counter()
+                wnd = lat.string_winding()
+                wind_s.append(time.perf_counter() - c0)
+                counts.append([int(x) for x in c])
+                winds.append(int(wnd.sum()))
+                if k in gw_at:
+                    c0 = time.perf_counter()
+                    lat.grav_spec_estimation(t)
+                    lat.grav_spec_log(t)
+                    gw_s.append(time.perf_counter() - c0)
+        res[f"n_dw_{ndw}"] = {
+            "tau_axion_on": tau_on, "tau_end": t, "wall_s": time.perf_counter() - w0,
+            "step_ms": step_ms / steps, "classify_ms": 1e3 * float(np.median(cls_s)),
+            "winding_ms": 1e3 * float(np.median(wind_s)), "gw_spectra_ms": 1e3 * float(np.median(gw_s)),
+            "string_wall_mask_counts_first_last": [counts[0], counts[-1]],
+            "pierced_plaquettes_first_last": [winds[0], winds[-1]],
+            "site_updates_per_s": float(n) ** 3 / (step_ms / steps * 1e-3)}
+    return res
+
+
 def accuracy_fp32(ag, n, steps, device):
     """GW (u_ij TT) spectrum and field moments of the FP32-mixed path against
     the FP64-plain path (bit-identical to the FP64 CPU restatement) after the
@@ -564,6 +624,9 @@ def main():
     ap.add_argument("--tile", type=int, default=None,
                     help="fused-kernel tile index (axg_tile_info) instead of autotuning the headline arm")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
+    ap.add_argument("--no-config2", action="store_true", help="skip the 1024^3 axion-term workload block")
+    ap.add_argument("--config2-steps", type=int, default=200,
+                    help="leapfrog steps of the 1024^3 workload (2560 reach tau ~ L / 2)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -691,6 +754,13 @@ def main():
         except Exception as exc:
             adjoint = {"error": str(exc)}
 
+    config2 = None
+    if rank == 0 and not args.no_config2:
+        try:
+            config2 = bench_config2(ag, local, steps=args.config2_steps)
+        except Exception as exc:
+            config2 = {"error": str(exc)}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -714,7 +784,7 @@ def main():
                        "tile": r32["tile_shape"]},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r32["launches"],
             "clocks": r32["clocks"], "adjoint": adjoint, "phi_only": phi_only, "green": green,
-            "output_calls": output_calls,
+            "output_calls": output_calls, "axion_1024": config2,
             # last, so that a reader keeping only the tail of the line sees them
             "ensemble": ensemble, "accuracy": accuracy, "fp64_plain": fp64,
         }

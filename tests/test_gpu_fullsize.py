@@ -186,6 +186,18 @@ def test_adjoint_256_lambda_against_finite_differences():
     assert dl == pytest.approx((Jp - Jm) / (2 * eps), rel=1e-5)
 
 
+def test_adjoint_256_lambda_fd_over_the_full_2000_steps():
+    """The gradient workload at its full length: 256^3, 2000 leapfrog steps
+    (tau 1 -> 401), checkpoints every 64 steps, dJ/dlambda against the
+    central difference (eps = 1e-4) of J from three FP64 runs."""
+    eps = 1e-4
+    J, dl, *_ = _adjoint_256(1.0, 2000, 64)
+    Jp = _adjoint_256(1.0 + eps, 2000, 64)[0]
+    Jm = _adjoint_256(1.0 - eps, 2000, 64)[0]
+    assert J > 0
+    assert dl == pytest.approx((Jp - Jm) / (2 * eps), rel=1e-4)
+
+
 def test_adjoint_256_dot_product_against_tangent_linear():
     """<dJ/dphi0, dphi> + <dJ/dphi'0, dphi'> + dJ/dlambda dlambda equals the
     FP64 tangent-linear oracle's directional derivative at 256^3."""
