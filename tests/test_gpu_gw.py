@@ -269,8 +269,10 @@ def test_uij_spectrum_own_transforms_match_cufft(monkeypatch, precision, tol, n)
 def test_own_transforms_store_no_real_fields(monkeypatch, precision, rs):
     """With the library's own transforms the Green sources and the u_ij
     spectrum's twelve fields are formed inside the row passes: against the
-    cuFFT path the context holds their real buffers less (6 and 12 fields
-    of N^3 reals), and only a twiddle table more."""
+    cuFFT path the context holds their real buffers less (6 fields of N^3
+    reals for the Green sources; one field for the u_ij spectrum, whose
+    cuFFT path transforms the twelve through one real buffer), and only a
+    twiddle table more."""
     n = 64
     mem = {}
     for ff in ("1", "0"):
@@ -284,7 +286,7 @@ def test_own_transforms_store_no_real_fields(monkeypatch, precision, rs):
     monkeypatch.delenv("AXG_FFT_FF")
     tw = n // 2 * 16  # the own transforms' float-float twiddle table
     assert mem[("green", "0")] - mem[("green", "1")] >= 6 * n ** 3 * rs - tw
-    assert mem[("uij", "0")] - mem[("uij", "1")] >= 12 * n ** 3 * rs - tw
+    assert mem[("uij", "0")] - mem[("uij", "1")] >= n ** 3 * rs - tw
 
 
 def test_green_requires_mode():
