@@ -445,20 +445,10 @@ __device__ __forceinline__ double atan2_sel(double y, double x, const AtanTab &t
   // by the last select)
   const bool swap = __double_as_longlong(ay) > __double_as_longlong(ax);
   const double num = swap ? ax : ay, den = swap ? ay : ax;
-  const double t = AXD_DIV(num, den);
-  int k = (int)AXD_ADD(AXD_MUL(t, 8.0), 0.5);
-  k = k < 0 ? 0 : (k > 8 ? 8 : k);  // only NaN t (both zero or both infinite) can leave 0..8
+  const int k = axd_atan_bucket(num, den);  // 0..8 (integer and FP32 pipes)
   const double c = tab.c[k];
-  const double r = AXD_DIV(AXD_SUB(t, c), AXD_FMA(t, c, 1.0));
-  const double r2 = AXD_MUL(r, r);
-  double p = -0.06666666666666667;
-  p = AXD_FMA(p, r2, 0.07692307692307693);
-  p = AXD_FMA(p, r2, -0.09090909090909091);
-  p = AXD_FMA(p, r2, 0.1111111111111111);
-  p = AXD_FMA(p, r2, -0.14285714285714285);
-  p = AXD_FMA(p, r2, 0.2);
-  p = AXD_FMA(p, r2, -0.3333333333333333);
-  const double atr = AXD_FMA(AXD_MUL(r, r2), p, r);
+  const double r = AXD_DIV(AXD_FMA(-c, den, num), AXD_FMA(c, num, den));
+  const double atr = axd_atan_series(r);
   const double hi = tab.hi[k], lo = AXD_ADD(tab.lo[k], atr);
   const bool sgnx = axd_signbit(x);
   // swap: pi/2 - (hi + lo), and pi minus that for x < 0; no swap and x < 0:
@@ -728,7 +718,8 @@ __device__ __forceinline__ void search_second(StringSearch &S, double chi2s) {
 
 // Advance S to its next chi2 evaluation; true with the point in P, false
 // when the lane has none this pass (screening budget spent, or finished).
-__device__ bool search_prepare(StringSearch &S, const float phf[8], uint64_t seed, uint64_t cell, double P[4]) {
+__device__ bool search_prepare(StringSearch &S, const float phf[8], uint64_t seed, uint64_t cell, double P[4],
+                               int screen) {
   const double chi2max = 8 * kRefPi * kRefPi, tol = 0.05;
   for (;;) {
     if (S.stage == kSearch) {
@@ -745,7 +736,7 @@ __device__ bool search_prepare(StringSearch &S, const float phf[8], uint64_t see
       for (int k = 1; k <= kNumSimp; ++k) thr = S.chi2_s[k] > thr ? S.chi2_s[k] : thr;
       for (int k = 0; k <= kNumSimp; ++k)
         if (S.chi2_s[k] != S.chi2_s[k]) thr = INFINITY;
-      for (int cnt = 0; cnt < 32 && S.i <= kMaxIter; ++cnt) {
+      for (int cnt = 0; cnt < screen && S.i <= kMaxIter; ++cnt) {
         string_start(seed, cell, S.i, S.t_s);
         if (!((double)chi2_string_lower(phf, S.t_s) > thr)) {
           for (int k = 0; k < 4; ++k) P[k] = S.t_s[k];
@@ -1132,6 +1123,12 @@ __device__ void position_wall(const double ph[8], double pos[3], double dir[3], 
   *wa = area;
 }
 
+// FP32 screens per start-phase pass of a lane (search_prepare): a pass
+// screens at most this many random starts, so lanes in the start phase hold
+// the warp's Nelder-Mead lanes back for a few FP32 bounds only (8 measured
+// fastest of 2..32 at 128^3).
+constexpr int kScreenPerPass = 8;
+
 // String fits, lane-scheduled: each lane takes cells from *next (zero at
 // launch) and advances its search one chi2 evaluation per pass (see
 // search_prepare); the grid is sized to the resident CTAs.
@@ -1187,7 +1184,7 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
     }
     if (__all_sync(0xffffffffu, k < 0)) break;
     double P[4];
-    const bool need = k >= 0 && search_prepare(S, phf, seed, (uint64_t)s, P);
+    const bool need = k >= 0 && search_prepare(S, phf, seed, (uint64_t)s, P, kScreenPerPass);
     __syncwarp();
     if (need) search_consume(S, calc_chi2_string(pc, P, tab));
   }
@@ -1555,13 +1552,11 @@ int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], dou
       if (f32)
         AXG_LAUNCH(ctx, "string_fit_fp32", k_string_fit<float2>, (unsigned)grid, 128, 0,
                    (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, (const float2 *)ctx->phid, n,
-                   ctx->p.dspa,
-                   (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
+                   ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
       else
         AXG_LAUNCH(ctx, "string_fit_fp64", k_string_fit<double2>, (unsigned)grid, 128, 0,
                    (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, (const double2 *)ctx->phid, n,
-                   ctx->p.dspa,
-                   (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
+                   ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
     }
     if (nw > 0) {
       if (ctx->p.precision == AXG_PREC_FP32_MIXED)

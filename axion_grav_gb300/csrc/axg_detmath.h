@@ -14,14 +14,19 @@
  * The reference obtains cell-corner phases as aimag(log(phi))
  * (defects_3d.f90:92), i.e. the principal argument atan2(Im, Re).  axd_atan2
  * below is a project-written atan2:
- *   t = min(|x|,|y|)/max(|x|,|y|) in [0,1];  k = round(8 t), c = k/8;
- *   atan t = atan(c) + atan(r),  r = (t - c)/(1 + t c),  |r| <= 1/16;
+ *   n = min(|x|,|y|), d = max(|x|,|y|), t = n / d in [0,1];
+ *   k = round(8 t) from an FP32 ratio of n and d (bit fields only), c = k/8;
+ *   atan t = atan(c) + atan(r),  r = (n - c d)/(d + c n) (one division, the
+ *   numerator and denominator each one fused multiply-add), |r| <= 1/16 +
+ *   2^-20;
  *   atan(r) = r - r^3/3 + r^5/5 - ... - r^15/15 (Taylor series of atan, the
  *   first omitted term is below 1e-18 relative);
  *   atan(k/8) is tabulated as a double-double (hi + lo) computed to 300 bits.
  * The quadrant is restored with pi/2 and pi carried as double-doubles.  This
  * is the classical table-driven argument reduction (e.g. J.-M. Muller,
- * "Elementary Functions", ch. 6); accuracy is about 1 ulp.
+ * "Elementary Functions", ch. 6); accuracy is 1 ulp.  Forming r from n and d
+ * instead of from the rounded ratio t saves a division and the rounding of
+ * t (the earlier form, r = (t - c)/(1 + t c), reached 2 ulp).
  *
  * axd_sincos reduces by pi/2 with a three-part Cody-Waite constant and uses
  * the Taylor series of sin / cos to degree 17 / 18 on |r| <= pi/4.
@@ -50,6 +55,9 @@
 #define AXD_DIV(a, b) __ddiv_rn((a), (b))
 #define AXD_FMA(a, b, c) __fma_rn((a), (b), (c))
 #define AXD_SQRT(a) __dsqrt_rn((a))
+#define AXF_MUL(a, b) __fmul_rn((a), (b))
+#define AXF_ADD(a, b) __fadd_rn((a), (b))
+#define AXF_DIV(a, b) __fdiv_rn((a), (b))
 #else
 #define AXD_ADD(a, b) ((a) + (b))
 #define AXD_SUB(a, b) ((a) - (b))
@@ -57,6 +65,9 @@
 #define AXD_DIV(a, b) ((a) / (b))
 #define AXD_FMA(a, b, c) fma((a), (b), (c))
 #define AXD_SQRT(a) sqrt((a))
+#define AXF_MUL(a, b) ((a) * (b))
+#define AXF_ADD(a, b) ((a) + (b))
+#define AXF_DIV(a, b) ((a) / (b))
 #endif
 
 /* pi, pi/2 as double-doubles (hi + lo). */
@@ -119,13 +130,36 @@ AXD_FN double axd_copysign(double mag, double sgn) {
   return m.d;
 }
 
-/* atan of t in [0,1], returned as hi + lo pieces summed into one double. */
-AXD_FN double axd_atan01_parts(double t, double *hi_out) {
-  int k = (int)AXD_ADD(AXD_MUL(t, 8.0), 0.5); /* t*8 is exact */
-  double c = (double)k * 0.125;                 /* exact */
-  double r = AXD_DIV(AXD_SUB(t, c), AXD_FMA(t, c, 1.0));
+AXD_FN uint64_t axd_bits(double v) {
+  union { double d; uint64_t u; } b;
+  b.d = v;
+  return b.u;
+}
+
+AXD_FN float axd_f_from_bits(uint32_t v) {
+  union { float f; uint32_t u; } b;
+  b.u = v;
+  return b.f;
+}
+
+/* k = round(8 n / d) for magnitudes 0 <= n <= d (d > 0): the FP32 ratio of
+ * n and d, both scaled by d's exponent and cut to 24 significant bits from
+ * their bit fields (no FP64 instruction; a subnormal or out-of-range n
+ * counts as 0).  The bucket can be the neighbouring one only where 8 t lies
+ * within 2^-20 of a half-integer, so |r| <= 1/16 + 2^-20 in axd_atan2. */
+AXD_FN int axd_atan_bucket(double n, double d) {
+  const uint64_t bn = axd_bits(n), bd = axd_bits(d);
+  const int en = (int)(bn >> 52), ed = (int)(bd >> 52);
+  const int e = en - ed + 127;
+  const float nf = (e >= 1 && en > 0) ? axd_f_from_bits(((uint32_t)e << 23) | (uint32_t)((bn >> 29) & 0x7fffffu)) : 0.0f;
+  const float df = axd_f_from_bits((127u << 23) | (uint32_t)((bd >> 29) & 0x7fffffu));
+  const int k = (int)AXF_ADD(AXF_MUL(AXF_DIV(nf, df), 8.0f), 0.5f);
+  return k > 8 ? 8 : k;
+}
+
+/* atan(r) = r + r r2 P(r2), P = -1/3 + r2/5 - r2^2/7 + ... - r2^6/15 */
+AXD_FN double axd_atan_series(double r) {
   double r2 = AXD_MUL(r, r);
-  /* atan(r) = r + r*r2*P(r2), P = -1/3 + r2/5 - r2^2/7 + ... - r2^6/15 */
   double p = -0.06666666666666667;
   p = AXD_FMA(p, r2, 0.07692307692307693);
   p = AXD_FMA(p, r2, -0.09090909090909091);
@@ -133,9 +167,17 @@ AXD_FN double axd_atan01_parts(double t, double *hi_out) {
   p = AXD_FMA(p, r2, -0.14285714285714285);
   p = AXD_FMA(p, r2, 0.2);
   p = AXD_FMA(p, r2, -0.3333333333333333);
-  double atr = AXD_FMA(AXD_MUL(r, r2), p, r);
+  return AXD_FMA(AXD_MUL(r, r2), p, r);
+}
+
+/* atan(n / d) for 0 <= n <= d as hi + lo pieces; the low-order part is
+ * returned, the table value in *hi_out. */
+AXD_FN double axd_atan_ratio_parts(double n, double d, double *hi_out) {
+  const int k = axd_atan_bucket(n, d);
+  const double c = (double)k * 0.125; /* exact */
+  const double r = AXD_DIV(AXD_FMA(-c, d, n), AXD_FMA(c, n, d));
   *hi_out = axd_atan_tab_hi(k);
-  return AXD_ADD(axd_atan_tab_lo(k), atr); /* low-order part */
+  return AXD_ADD(axd_atan_tab_lo(k), axd_atan_series(r)); /* low-order part */
 }
 
 /* Principal argument of x + i y in [-pi, pi]; C99 atan2 semantics for zeros. */
@@ -150,9 +192,8 @@ AXD_FN double axd_atan2(double y, double x) {
   int swap = ay > ax;
   double num = swap ? ax : ay;
   double den = swap ? ay : ax;
-  double t = AXD_DIV(num, den);
   double hi;
-  double lo = axd_atan01_parts(t, &hi);
+  double lo = axd_atan_ratio_parts(num, den, &hi);
   double a;
   if (swap) {
     /* pi/2 - (hi + lo) */
