@@ -26,13 +26,15 @@
 //   4. compaction: string and wall cells listed in cell order
 //   5. fits      : string cells lane-scheduled from a counter -- the search
 //                  of position_string (1001 random starts, screened in FP32,
-//                  + Nelder-Mead, defects_3d.f90:435-603), string_length
+//                  + Nelder-Mead, defects_3d.f90:435-603; the chi2 in
+//                  float-float on the FP32 pipes, axg_ffchi2.h), string_length
 //                  (1027-1056), velocity_string (605-692), position_wall
 //                  (1058-1233)
 //   6. sums      : add_string_length / add_wall_area without grouping
 #include <cmath>
 
 #include "axg_detmath.h"
+#include "axg_ffchi2.h"
 #include "axg_internal.h"
 
 namespace {
@@ -405,119 +407,6 @@ __global__ void k_compact(const int8_t *__restrict__ flags, int64_t n3, const in
 }
 
 // ---------------- per-cell fits ----------------
-// atan(k/8) as hi + lo (axd_atan_tab_hi / axd_atan_tab_lo), k = 0..8, in
-// shared memory: the string-fit kernel indexes it per lane
-struct AtanTab {
-  double hi[9], lo[9], c[9];  // c[k] = k / 8
-};
-
-__device__ __forceinline__ void atan_tab_fill(AtanTab &t) {
-  for (int k = threadIdx.x; k < 9; k += blockDim.x) {
-    t.hi[k] = axd_atan_tab_hi(k);
-    t.lo[k] = axd_atan_tab_lo(k);
-    t.c[k] = (double)k * 0.125;
-  }
-}
-
-// FP64 comparisons issue on the FP64 pipe, at 1/64 of the FP32 rate on
-// GB300; these give the same answers from the bit patterns on the integer
-// pipe.  dkey orders non-NaN doubles as signed integers (-0 below +0, which
-// no comparison below can meet: it compares with nonzero constants or
-// between magnitudes).
-__device__ __forceinline__ long long dkey(double x) {
-  const long long b = __double_as_longlong(x);
-  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-}
-__device__ __forceinline__ bool is_nan_bits(double x) {
-  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
-}
-__device__ __forceinline__ bool is_zero_bits(double x) {
-  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) == 0;
-}
-
-// axd_atan2 with the branches turned into selects: the same IEEE operations
-// on the same operands, so the same bits, but no control flow, which lets
-// the compiler overlap the eight corner evaluations of a chi2 (their
-// divisions and polynomial chains are independent).
-__device__ __forceinline__ double atan2_sel(double y, double x, const AtanTab &tab) {
-  const double ax = axd_fabs(x), ay = axd_fabs(y);
-  // magnitudes: their bit patterns order as integers (a NaN case is replaced
-  // by the last select)
-  const bool swap = __double_as_longlong(ay) > __double_as_longlong(ax);
-  const double num = swap ? ax : ay, den = swap ? ay : ax;
-  const int k = axd_atan_bucket(num, den);  // 0..8 (integer and FP32 pipes)
-  const double c = tab.c[k];
-  const double r = AXD_DIV(AXD_FMA(-c, den, num), AXD_FMA(c, num, den));
-  const double atr = axd_atan_series(r);
-  const double hi = tab.hi[k], lo = AXD_ADD(tab.lo[k], atr);
-  const bool sgnx = axd_signbit(x);
-  // swap: pi/2 - (hi + lo), and pi minus that for x < 0; no swap and x < 0:
-  // pi - (hi + lo); otherwise hi + lo
-  const double A = AXD_ADD(AXD_SUB(swap ? AXD_PIO2_HI : AXD_PI_HI, hi), AXD_SUB(swap ? AXD_PIO2_LO : AXD_PI_LO, lo));
-  const double B = AXD_ADD(hi, lo);
-  const double C = AXD_ADD(AXD_SUB(AXD_PI_HI, A), AXD_PI_LO);
-  double a = swap ? (sgnx ? C : A) : (sgnx ? A : B);
-  a = axd_copysign(a, y);
-  const double on_x = sgnx ? axd_copysign(AXD_ADD(AXD_PI_HI, AXD_PI_LO), y) : y;  // ay == 0
-  const double on_y = axd_copysign(AXD_ADD(AXD_PIO2_HI, AXD_PIO2_LO), y);         // ax == 0
-  a = is_zero_bits(ax) ? on_y : a;
-  a = is_zero_bits(ay) ? on_x : a;
-  return (is_nan_bits(x) || is_nan_bits(y)) ? AXD_ADD(x, y) : a;
-}
-
-// defects_3d.f90:385-433.  The corner offsets are +-1/2, so x cos(phi) and
-// the like are exact halvings of one product; they are formed once, and the
-// sums that do not depend on every corner coordinate are shared.  Every
-// value, and the order of every rounding, is that of the plain
-// per-corner loop
-//   du = -u0 + cm (x cp + y sp) - z sm,  dv = -v0 - x sp + y cp,
-//   d = ph - atan2(dv, du) wrapped into [-pi, pi),
-// so the result is bit-identical to it.
-__device__ double calc_chi2_string(const double ph[8], const double pr[4], const AtanTab &tab) {
-  const double mu = pr[0], phi = pr[1];
-  double s4, c4, sp, cp;
-  axd_sincos(pr[3], &s4, &c4);
-  const double u0 = pr[2] * c4;
-  const double v0 = pr[2] * s4;
-  const double cm = mu;
-  const double sm = sqrt(1.0 - mu * mu);
-  axd_sincos(phi, &sp, &cp);
-  const double hcp = 0.5 * cp, hsp = 0.5 * sp, hsm = 0.5 * sm;  // x cp etc. for x = +1/2
-  double T[4], Wv[2];
-  for (int iy = 0; iy <= 1; ++iy)
-    for (int ix = 0; ix <= 1; ++ix) {
-      const double xcp = ix ? hcp : -hcp, ysp = iy ? hsp : -hsp;
-      T[iy * 2 + ix] = -u0 + cm * (xcp + ysp);
-    }
-  for (int ix = 0; ix <= 1; ++ix) Wv[ix] = -v0 - (ix ? hsp : -hsp);
-  double d[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int ix = i & 1, iy = (i >> 1) & 1, iz = i >> 2;
-    const double du = T[iy * 2 + ix] - (iz ? hsm : -hsm);
-    const double dv = Wv[ix] + (iy ? hcp : -hcp);
-    d[i] = ph[i] - atan2_sel(dv, du, tab);
-  }
-  // d >= pi and d < -pi from the integer keys; a NaN d takes one of the
-  // branches and stays the same NaN, as in the FP64 comparisons
-  const long long kp = dkey(kRefPi), km = dkey(-kRefPi);
-  double a = 0.0, b = 0.0;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    double e = d[i];
-    const long long ke = dkey(e);
-    if (ke >= kp)
-      e = e - kRefTwoPi;
-    else if (ke < km)
-      e = e + kRefTwoPi;
-    a = a + e * e;
-    b = b + e;
-  }
-  a = a * 0.125;  // exact: the same value as a / 8
-  b = b * 0.125;
-  return a - b * b;
-}
-
 // defects_3d.f90:1027-1056
 __device__ double string_length(const double pos[3], const double dir[3]) {
   const double atmax = 0.867, atmax0 = 0.86602540378378444;
@@ -638,10 +527,13 @@ __device__ float chi2_string_lower(const float phf[8], const double t[4]) {
 // the list), but never above the largest value kept at any earlier time.
 // The starts are therefore screened with FP32 lower bounds
 // (chi2_string_lower) against the largest kept value; only the starts that
-// pass are evaluated exactly, in draw order.  A screened-out start has an
-// exact chi2 above any threshold the sequential search could have compared
-// it with.  Every chi2 that enters a decision or the kept state is the FP64
-// value, so the fit is bit-identical to the sequential search.
+// pass are evaluated, in draw order.  A screened-out start has a chi2 above
+// any threshold the sequential search could have compared it with (the
+// bound's 1e-4 margin covers the 1e-14 between the FP64 chi2 it was
+// derived for and the float-float chi2 the search uses).  Every chi2 that
+// enters a decision or the kept state is the float-float value of
+// axd_chi2_string_ff (axg_ffchi2.h), which the CPU restatement evaluates
+// too, so the fit is bit-identical to its sequential search.
 struct StringSearch {
   double p_s[5][4], chi2_s[5], c_s[4], t_s[4], s_s[4], chi2;
   int n0, i, it, stage;
@@ -1138,11 +1030,8 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
                                                     double dspa, uint64_t seed, const int64_t *__restrict__ cells,
                                                     int64_t ncell, double *__restrict__ out,
                                                     unsigned long long *__restrict__ next) {
-  __shared__ AtanTab tab;
-  atan_tab_fill(tab);
-  __syncthreads();
   StringSearch S;
-  double pc[8];
+  axd_ff pcf[8];  // corner phases as float-float pairs (the chi2 runs in float-float)
   float phf[8];
   int64_t k = -1, s = 0;
   auto fetch = [&]() {
@@ -1154,8 +1043,9 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
     s = cells[k];
     const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
     for (int c = 0; c < 8; ++c) {
-      pc[c] = phase64(phi, cphi, corner(n, ix, iy, iz, c));
-      phf[c] = (float)pc[c];
+      const double pc = phase64(phi, cphi, corner(n, ix, iy, iz, c));
+      pcf[c] = axd_ff_from(pc);
+      phf[c] = (float)pc;
     }
     search_init(S);
   };
@@ -1186,7 +1076,7 @@ __global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, c
     double P[4];
     const bool need = k >= 0 && search_prepare(S, phf, seed, (uint64_t)s, P, kScreenPerPass);
     __syncwarp();
-    if (need) search_consume(S, calc_chi2_string(pc, P, tab));
+    if (need) search_consume(S, axd_chi2_string_ff(pcf, P));
   }
 }
 

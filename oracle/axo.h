@@ -97,6 +97,10 @@ void axo_id_defects(const axg_params *p, const double *phi, const double *phidot
 /* the fits of id_defects for given string / wall cells (rows as axo_id_defects) */
 void axo_fit_cells(const axg_params *p, const double *phi, const double *phidot, const int64_t *scells,
                    int64_t ns, double *sres, const int64_t *wcells, int64_t nw, double *wres);
+/* the string-fit chi2 (defects_3d.f90:385-433): the float-float form the
+ * fits use, and FP64 as its yardstick */
+double axo_chi2_string_ff(const double ph[8], const double pr[4]);
+double axo_chi2_string_fp64(const double ph[8], const double pr[4]);
 /* single-cell pieces for unit tests */
 void axo_position_string(const double ph[8], uint64_t seed, uint64_t cell, double pos[3],
                          double dir[3], double *gof, double *sl);

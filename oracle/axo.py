@@ -63,6 +63,8 @@ def lib():
             "axo_string_winding": ([P, dp, i64p], None),
             "axo_id_defects": ([P, dp, dp, ctypes.c_double, dp, dp, dp, i64p, dp, ctypes.c_int64, dp,
                                 ctypes.c_int64, ctypes.POINTER(ctypes.c_int8)], None),
+            "axo_chi2_string_ff": ([dp, dp], ctypes.c_double),
+            "axo_chi2_string_fp64": ([dp, dp], ctypes.c_double),
             "axo_fit_cells": ([P, dp, dp, i64p, ctypes.c_int64, dp, i64p, ctypes.c_int64, dp], None),
             "axo_position_string": ([dp, ctypes.c_uint64, ctypes.c_uint64, dp, dp, dp, dp], None),
             "axo_position_wall": ([dp, dp, dp, dp, dp], None),

@@ -15,6 +15,7 @@
 
 #include "axo.h"
 #include "axg_detmath.h"
+#include "axg_ffchi2.h"
 
 #define REF_PI 3.14159265359
 #define REF_TWOPI (2 * REF_PI)
@@ -136,8 +137,9 @@ void axo_string_winding(const axg_params *p, const double *phi, int64_t counts[3
   free(ph);
 }
 
-/* defects_3d.f90:385-433 */
-static double calc_chi2_string(const double ph[8], const double pr[4]) {
+/* defects_3d.f90:385-433 in FP64, kept as the yardstick of the float-float
+ * chi2 the fits use (a CPU test compares the two) */
+double axo_chi2_string_fp64(const double ph[8], const double pr[4]) {
   double mu = pr[0], phi = pr[1];
   double s4, c4, sp, cp;
   axd_sincos(pr[3], &s4, &c4);
@@ -170,6 +172,15 @@ static double calc_chi2_string(const double ph[8], const double pr[4]) {
   b = b / 8;
   return a - b * b;
 }
+
+/* defects_3d.f90:385-433 as the fits evaluate it: float-float arithmetic
+ * (axg_ffchi2.h), the corner phases split into float-float pairs */
+double axo_chi2_string_ff(const double ph[8], const double pr[4]) {
+  axd_ff f[8];
+  for (int i = 0; i < 8; ++i) f[i] = axd_ff_from(ph[i]);
+  return axd_chi2_string_ff(f, pr);
+}
+#define calc_chi2_string axo_chi2_string_ff
 
 /* defects_3d.f90:1027-1056 */
 double axo_string_length(const double pos[3], const double dir[3]) {

@@ -21,7 +21,8 @@ def build(force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     srcs = sorted(os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith(".c"))
     hdrs = [os.path.join(HERE, "axo.h"), os.path.join(ROOT, "include", "axgpu.h"),
-            os.path.join(ROOT, "axion_grav_gb300", "csrc", "axg_detmath.h"), os.path.abspath(__file__)]
+            os.path.join(ROOT, "axion_grav_gb300", "csrc", "axg_detmath.h"),
+            os.path.join(ROOT, "axion_grav_gb300", "csrc", "axg_ffchi2.h"), os.path.abspath(__file__)]
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in srcs + hdrs):
