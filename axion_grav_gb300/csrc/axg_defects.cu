@@ -1023,9 +1023,12 @@ constexpr int kScreenPerPass = 8;
 
 // String fits, lane-scheduled: each lane takes cells from *next (zero at
 // launch) and advances its search one chi2 evaluation per pass (see
-// search_prepare); the grid is sized to the resident CTAs.
+// search_prepare); the grid is sized to the resident CTAs.  The float-float
+// chi2 is a long chain of dependent FP32 operations, so the kernel is bound
+// by latency: capped at 96 registers (a few spills) it holds 5 CTAs per SM
+// instead of 3 (128^3: 237 -> 158 ms; 4, 6 and 8 CTAs measured slower).
 template <typename V>
-__global__ void __launch_bounds__(128) k_string_fit(const V *__restrict__ phi, const V *__restrict__ cphi,
+__global__ void __launch_bounds__(128, 5) k_string_fit(const V *__restrict__ phi, const V *__restrict__ cphi,
                                                     const V *__restrict__ phid, int n,
                                                     double dspa, uint64_t seed, const int64_t *__restrict__ cells,
                                                     int64_t ncell, double *__restrict__ out,
