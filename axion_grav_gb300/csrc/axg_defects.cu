@@ -885,7 +885,31 @@ __device__ void velocity_string(const V *phi, const V *cphi, const V *phid, int 
 }
 
 // defects_3d.f90:1058-1233
-__device__ void position_wall(const double ph[8], double pos[3], double dir[3], double *gof,
+// The 20 x 20 grid of wall directions of position_wall (defects_3d.f90:
+// 1135-1160): d0 = (sqrt(1 - mu^2) cos phi, sqrt(1 - mu^2) sin phi, mu) for
+// mu = ((2 imu - 20) - 1) / 20, phi = pi ((2 iphi - 1) - 20) / 20, in the
+// reference's operations; the same for every cell, so k_wall_fit forms it
+// once per CTA in shared memory.
+struct WallGrid {
+  double d0[400][4];  // d0 and phi
+};
+
+__device__ void wall_grid_fill(WallGrid &g) {
+  for (int idx = threadIdx.x; idx < 400; idx += blockDim.x) {
+    const int imu = idx / 20 + 1, iphi = idx % 20 + 1;
+    const double mu = ((double)(-20 + 2 * imu) - 1.0) / 20;
+    const double phi = kRefPi * ((2 * iphi - 1.0) - 20) / 20;
+    double sp, cp;
+    axd_sincos(phi, &sp, &cp);
+    const double sq = sqrt(1 - mu * mu);
+    g.d0[idx][0] = sq * cp;
+    g.d0[idx][1] = sq * sp;
+    g.d0[idx][2] = mu;
+    g.d0[idx][3] = phi;
+  }
+}
+
+__device__ void position_wall(const double ph[8], const WallGrid &grid, double pos[3], double dir[3], double *gof,
                               double *wa) {
   double pp[12][3], th[12], uv[12][2], sn[8], cs[8];
   for (int i = 0; i < 8; ++i) axd_sincos(ph[i], &sn[i], &cs[i]);
@@ -928,13 +952,9 @@ __device__ void position_wall(const double ph[8], double pos[3], double dir[3], 
   }
   double chi2min = 6.0, mut = 0.0, phit = 0.0, wt = 0.0;
   for (int imu = 1; imu <= 20; ++imu) {
-    const double mu = ((double)(-20 + 2 * imu) - 1.0) / 20;
     for (int iphi = 1; iphi <= 20; ++iphi) {
-      const double phi = kRefPi * ((2 * iphi - 1.0) - 20) / 20;
-      double sp, cp;
-      axd_sincos(phi, &sp, &cp);
-      const double sq = sqrt(1 - mu * mu);
-      const double d0[3] = {sq * cp, sq * sp, mu};
+      const double *d0 = grid.d0[(imu - 1) * 20 + (iphi - 1)];
+      const double mu = d0[2], phi = d0[3];
       double w = 0.0, chi2 = 0.0;
       for (int i = 0; i < m; ++i) {
         double d = pp[i][0] * d0[0] + pp[i][1] * d0[1];
@@ -1087,6 +1107,9 @@ template <typename V>
 __global__ void __launch_bounds__(128) k_wall_fit(const V *__restrict__ phi, const V *__restrict__ cphi, int n,
                                                   const int64_t *__restrict__ cells,
                                                   int64_t ncell, double *__restrict__ out) {
+  __shared__ WallGrid grid;
+  wall_grid_fill(grid);
+  __syncthreads();
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ncell) return;
   const int64_t s = cells[k];
@@ -1094,7 +1117,7 @@ __global__ void __launch_bounds__(128) k_wall_fit(const V *__restrict__ phi, con
   double pc[8];
   for (int c = 0; c < 8; ++c) pc[c] = phase64(phi, cphi, corner(n, ix, iy, iz, c));
   double pos[3], dir[3], gof, a;
-  position_wall(pc, pos, dir, &gof, &a);
+  position_wall(pc, grid, pos, dir, &gof, &a);
   double *r = out + 10 * k;
   r[0] = pos[0] + ix + 0.5;
   r[1] = pos[1] + iy + 0.5;
