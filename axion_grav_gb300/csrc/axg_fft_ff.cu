@@ -157,7 +157,7 @@ __device__ __forceinline__ void c_dft(T *v) {
 // pass hands its outputs to `store`.  tw[k] = W_(L ts)^k, k < L ts.
 __device__ __forceinline__ int fpad(int i) { return i + (i >> 3); }
 
-template <int L, int NS, bool INV, typename T, typename Store>
+template <int L, int NS, bool INV, bool REC = false, typename T, typename Store>
 __device__ __forceinline__ void f_stockham(T v[8], int j, T *line, int ls, const T *tw, int ts, Store store) {
   constexpr int REM = L / NS, R = REM >= 8 ? 8 : REM, NI = 8 / R, TH = L / 8;
 #pragma unroll
@@ -165,11 +165,25 @@ __device__ __forceinline__ void f_stockham(T v[8], int j, T *line, int ls, const
     const int jj = j + q * TH;
     if constexpr (NS > 1) {
       const int k = jj & (NS - 1);
+      if constexpr (REC) {
+        // one table read; the powers by complex multiplication (REC is for
+        // the FP32 transforms: the rows' tables were read with strides that
+        // put most lanes of a warp on a few banks)
+        T w1 = tw[k * (L / (NS * R)) * ts];
+        if (INV) w1 = c_conj(w1);
+        T w = w1;
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        T w = tw[r * k * (L / (NS * R)) * ts];
-        if (INV) w = c_conj(w);
-        v[q * R + r] = c_mul(v[q * R + r], w);
+        for (int r = 1; r < R; ++r) {
+          v[q * R + r] = c_mul(v[q * R + r], w);
+          w = c_mul(w, w1);
+        }
+      } else {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          T w = tw[r * k * (L / (NS * R)) * ts];
+          if (INV) w = c_conj(w);
+          v[q * R + r] = c_mul(v[q * R + r], w);
+        }
       }
     }
     c_dft<R, INV>(&v[q * R]);
@@ -195,7 +209,7 @@ __device__ __forceinline__ void f_stockham(T v[8], int j, T *line, int ls, const
 #pragma unroll
       for (int r = 0; r < R2; ++r) v[q * R2 + r] = line[fpad(j + q * TH + r * (L / R2)) * ls];
     __syncthreads();
-    f_stockham<L, NS2, INV>(v, j, line, ls, tw, ts, store);
+    f_stockham<L, NS2, INV, REC>(v, j, line, ls, tw, ts, store);
   }
 }
 
@@ -508,7 +522,7 @@ __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 
 #pragma unroll
     for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * TH)];
     __syncthreads();
-    f_stockham<M, 1, false>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
+    f_stockham<M, 1, false, true>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < NL * NH; idx += blockDim.x) {
@@ -554,7 +568,7 @@ __global__ void __launch_bounds__(12 * M / 8) k_uij_rows(const float *__restrict
 #pragma unroll
     for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * TH)];
     __syncthreads();
-    f_stockham<M, 1, false>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
+    f_stockham<M, 1, false, true>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < 12 * NH; idx += blockDim.x) {

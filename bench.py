@@ -396,7 +396,7 @@ def bench_adjoint(ag, device, n=256, steps=2000, stride=64, fp64_steps=256):
     return out
 
 
-def bench_output_calls(ag, n, device, steps=200, max_fit_cells=2_000_000):
+def bench_output_calls(ag, n, device, steps=200, max_fit_cells=40_000_000):
     """Per-call cost of the output-time routines on the evolved FP32-mixed
     lattice (host wall clock around each call; every call synchronises):
     plaquette winding, cell classification, defect fits and sums, field
@@ -411,8 +411,9 @@ def bench_output_calls(ag, n, device, steps=200, max_fit_cells=2_000_000):
         tau = 2.0 + dt * steps
         out["tau"] = tau
 
-        def timed(name, fn, reps=3):
-            fn()  # first call allocates plans / tables
+        def timed(name, fn, reps=3, warm=True):
+            if warm:
+                fn()  # first call allocates plans / tables
             lat.set_kernel_timing(True)
             t0 = time.perf_counter()
             for _ in range(reps):
@@ -429,7 +430,7 @@ def bench_output_calls(ag, n, device, steps=200, max_fit_cells=2_000_000):
         out["classify_cells"]["counts"] = [int(c) for c in counts]
         cells = int(counts[0] + counts[1])
         if cells <= max_fit_cells:
-            r = timed("id_defects", lambda: lat.id_defects(1, tau), reps=1)
+            r = timed("id_defects", lambda: lat.id_defects(1, tau), reps=1, warm=False)
             out["id_defects"]["fitted_cells"] = cells
             out["id_defects"]["cells_per_s"] = cells / (out["id_defects"]["ms"] * 1e-3)
         else:
