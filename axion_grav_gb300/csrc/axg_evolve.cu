@@ -21,12 +21,12 @@
 
 #include "axg_detmath.h"
 #include "axg_internal.h"
+#include "axg_tma.h"
 
 namespace {
 
 constexpr int kStages = 4;            // TMA ring depth (z-1, z, z+1, prefetch)
 constexpr int kPwStages = 2;          // pointwise ring depth (z, prefetch of z+1)
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz: mbarrier wait limit
 
 // ------------------------------------------------------------------------
 // FP64-plain kernels (evolve.f90:259-281 and 283-339)
@@ -181,62 +181,8 @@ __global__ void k_drift_fp32(float2 *__restrict__ phi, const float2 *__restrict_
   }
 }
 
-// ------------------------------------------------------------------------
-// TMA / mbarrier primitives (inline PTX)
-// ------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: gives up after `limit` SM cycles (kWaitCycles in the
-// kernels) and reports failure.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long limit = kWaitCycles) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (clock64() - t0 > limit) return false;
-  }
-}
-__device__ __forceinline__ void fence_barrier_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1,
-                                            int c2, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1,
-                                            int c2, int c3, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-      : "memory");
-}
+// TMA / mbarrier primitives (inline PTX): axg_tma.h
+using namespace axg_tma;
 
 // ------------------------------------------------------------------------
 // fused kernel: one stage of shared memory holds one z-plane of the stencil
@@ -1122,9 +1068,14 @@ __global__ void k_wait_timeout_selftest(long long limit, int *err) {
 }  // namespace
 
 extern "C" int axg_selftest_wait_timeout(axg_ctx *ctx, int64_t wait_cycles) {
-  if (!ctx || wait_cycles < 1000 || wait_cycles > kWaitCycles) return AXG_ERR_ARG;
+  if (!ctx || wait_cycles < 1000 || wait_cycles > axg_tma::kWaitCycles) return AXG_ERR_ARG;
   AXG_LAUNCH(ctx, "wait_timeout_selftest", k_wait_timeout_selftest, 1, 128, 0, (long long)wait_cycles, ctx->d_err);
   return axg_evo_check_error(ctx);
+}
+
+int axg_encode_tmap(axg_ctx *ctx, CUtensorMap *m, CUtensorMapDataType dt, int rank, void *base,
+                    const cuuint64_t *dims, const cuuint64_t *strides, const cuuint32_t *box) {
+  return encode(ctx, m, dt, rank, base, dims, strides, box);
 }
 
 int axg_evo_check_error(axg_ctx *ctx) {
@@ -1134,7 +1085,7 @@ int axg_evo_check_error(axg_ctx *ctx) {
   if (h == AXG_KERR_MBAR_TIMEOUT) {
     int z = 0;
     cudaMemcpy(ctx->d_err, &z, sizeof(int), cudaMemcpyHostToDevice);
-    return axg_set_error(ctx, AXG_ERR_TIMEOUT, "fused kernel: TMA stage wait timed out");
+    return axg_set_error(ctx, AXG_ERR_TIMEOUT, "TMA stage wait timed out (fused kernel or FFT column pass)");
   }
   if (h != 0) {
     int z = 0;

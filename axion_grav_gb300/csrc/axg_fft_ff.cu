@@ -21,11 +21,16 @@
 //             outputs X[k] = E[k] + W_n^k O[k];
 //   y, z    : n-point FFTs along y and along z, a few adjacent kx columns per
 //             CTA so every row of the tile is one 64-byte segment.
+// The complex-float transforms (FP32-mixed Green sources and u_ij fields)
+// store their half spectra with kx rows padded to a multiple of 4 complex
+// values (axg_f32_spec_pitch): their y pass reads 32-byte rows on sector
+// boundaries, and their z pass moves its tiles by TMA (k_cols_z_tma).
 // Each line is a Stockham radix-8 FFT in registers (f_stockham): a 512-point
 // line takes two shared-memory exchanges, the first pass reads its inputs
 // from global memory and the column passes' last pass writes there.
 // Twiddles W_n^k come from a float-float table made on the host in FP64.
 // Powers of two from 16 to 512.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <vector>
@@ -33,6 +38,7 @@
 #include "axg_ff.h"
 #include "axg_gw_source.h"
 #include "axg_internal.h"
+#include "axg_tma.h"
 
 namespace {
 
@@ -157,7 +163,21 @@ __device__ __forceinline__ void c_dft(T *v) {
 // pass hands its outputs to `store`.  tw[k] = W_(L ts)^k, k < L ts.
 __device__ __forceinline__ int fpad(int i) { return i + (i >> 3); }
 
-template <int L, int NS, bool INV, bool REC = false, typename T, typename Store>
+// Unpadded lines of 8-byte (complex float) elements, element i at fswz(i):
+// the low four bits, the element's bank pair within 128 bytes, XORed with
+// bits 3..6.  Aligned runs of 16 elements (a half warp's 8-byte request) keep
+// 16 distinct bank pairs, and so do the passes' stride-8 and stride-64
+// writes.  With 8-byte elements the i + i / 8 padding made every consecutive
+// read and write two-way conflicted; with 16-byte elements (float-float,
+// 8 lanes per request) it is conflict-free and stays.
+__device__ __forceinline__ int fswz(int i) { return i ^ ((i >> 3) & 15); }
+template <bool SW>
+__device__ __forceinline__ int fidx(int i) {
+  if constexpr (SW) return fswz(i);
+  else return fpad(i);
+}
+
+template <int L, int NS, bool INV, bool REC = false, bool SW = false, typename T, typename Store>
 __device__ __forceinline__ void f_stockham(T v[8], int j, T *line, int ls, const T *tw, int ts, Store store) {
   constexpr int REM = L / NS, R = REM >= 8 ? 8 : REM, NI = 8 / R, TH = L / 8;
 #pragma unroll
@@ -167,9 +187,9 @@ __device__ __forceinline__ void f_stockham(T v[8], int j, T *line, int ls, const
       const int k = jj & (NS - 1);
       if constexpr (REC) {
         // one table read; the powers by complex multiplication (REC is for
-        // the FP32 transforms: the rows' tables were read with strides that
-        // put most lanes of a warp on a few banks)
-        T w1 = tw[k * (L / (NS * R)) * ts];
+        // the FP32 transforms).  SW: tw is the per-pass table of
+        // load_twc, tw[NS + k] = W_(NS R)^k, read at consecutive k.
+        T w1 = SW ? tw[NS + k] : tw[k * (L / (NS * R)) * ts];
         if (INV) w1 = c_conj(w1);
         T w = w1;
 #pragma unroll
@@ -200,16 +220,16 @@ __device__ __forceinline__ void f_stockham(T v[8], int j, T *line, int ls, const
     for (int q = 0; q < NI; ++q) {
       const int jj = j + q * TH, d = (jj / NS) * NS * R + (jj & (NS - 1));
 #pragma unroll
-      for (int r = 0; r < R; ++r) line[fpad(d + r * NS) * ls] = v[q * R + r];
+      for (int r = 0; r < R; ++r) line[fidx<SW>(d + r * NS) * ls] = v[q * R + r];
     }
     __syncthreads();
     constexpr int NS2 = NS * R, R2 = L / NS2 >= 8 ? 8 : L / NS2;
 #pragma unroll
     for (int q = 0; q < 8 / R2; ++q)
 #pragma unroll
-      for (int r = 0; r < R2; ++r) v[q * R2 + r] = line[fpad(j + q * TH + r * (L / R2)) * ls];
+      for (int r = 0; r < R2; ++r) v[q * R2 + r] = line[fidx<SW>(j + q * TH + r * (L / R2)) * ls];
     __syncthreads();
-    f_stockham<L, NS2, INV, REC>(v, j, line, ls, tw, ts, store);
+    f_stockham<L, NS2, INV, REC, SW>(v, j, line, ls, tw, ts, store);
   }
 }
 
@@ -240,10 +260,57 @@ __device__ __forceinline__ T real_split(const T *line, int k, const T *tw) {
   return k == M ? c_sub(E, O) : c_add(E, k == 0 ? O : c_mul(tw[k], O));
 }
 
+// The twiddles of the FP32 row transforms in shared memory, from the
+// float-float W_N^k table (N = 2M, high parts): tws[k] = W_N^k for k <= M / 2
+// (the split) and twc[NS + k] = W_(NS R)^k, k < NS, for each pass NS > 1 of
+// the M-point transform (NS a power of 8, R = min(8, M / NS); the ranges
+// [NS, 2 NS) are disjoint).
+template <int M>
+__device__ __forceinline__ void load_tw_rows(float2 *tws, float2 *twc, const float4 *__restrict__ twff) {
+  for (int e = threadIdx.x; e < M + M / 2 + 1; e += blockDim.x) {
+    if (e <= M / 2) {
+      const float4 w = twff[e];
+      tws[e] = make_float2(w.x, w.z);
+      continue;
+    }
+    const int c = e - (M / 2 + 1);
+    int ns = 1;
+    while (ns * 8 <= c) ns *= 8;
+    const int k = c - ns;
+    if (ns == 1 || k >= ns) continue;  // unused entries
+    const int R = M / ns >= 8 ? 8 : M / ns;
+    const float4 w = twff[k * (2 * M / (ns * R))];
+    twc[c] = make_float2(w.x, w.z);
+  }
+}
+
+// The split of the FP32 row transforms, two outputs per read pair: with
+// E = (Z[k] + conj Z[M-k]) / 2, O = (Z[k] - conj Z[M-k]) / 2i and
+// P = W_N^k O, X[k] = E + P and X[M - k] = conj(E - P) (E and O of M - k are
+// the conjugates of those of k, W_N^(M-k) = -conj W_N^k); k = 0 gives X[0]
+// and X[M], and its thread adds X[M/2].  Lines of M elements at fswz(i);
+// task t of line b for t < M / 2, consecutive t on consecutive threads.
+template <int M, typename Out>
+__device__ __forceinline__ void split_pairs(const float2 *s, int nl, const float2 *tws, Out out) {
+  constexpr int H = M / 2;
+  for (int task = threadIdx.x; task < nl * H; task += blockDim.x) {
+    const int b = task / H, t = task % H;
+    const float2 *line = s + b * M;
+    const float2 zk = line[fswz(t)], zm = c_conj(line[fswz((M - t) & (M - 1))]);
+    const float2 E = c_half(c_add(zk, zm)), O = c_div_2i(c_sub(zk, zm));
+    const float2 P = c_mul(tws[t], O);
+    out(b, t, c_add(E, P));
+    out(b, M - t, c_conj(c_sub(E, P)));
+    if (t == 0) {
+      const float2 zh = line[fswz(H)], zhc = c_conj(zh);
+      out(b, H, c_add(c_half(c_add(zh, zhc)), c_mul(tws[H], c_div_2i(c_sub(zh, zhc)))));
+    }
+  }
+}
+
 constexpr int kFfRows = 8;   // rows per CTA of the float-float real row pass
 constexpr int kFfCRows = 4;  // rows per CTA of the float-float complex row pass
 constexpr int kFfCols = 4;   // kx columns per CTA of the float-float column passes (64 bytes)
-constexpr int kFCols = 8;    // kx columns per CTA of the float column passes (64 bytes; 16 measured slower)
 
 // Row pass: kFfRows rows of N = 2M reals -> M + 1 complex each (float-float).
 template <int M>
@@ -475,13 +542,13 @@ constexpr int kSrcRows = 2;  // x-rows per CTA of the source row pass (6 x 2 lin
 // line (M / 8 threads each), then the split into X[k], k <= M.
 template <int M>
 __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 *__restrict__ phi, float scale,
-                                                                   float2 *__restrict__ out,
+                                                                   float2 *__restrict__ out, int sp,
                                                                    const float4 *__restrict__ twff) {
-  constexpr int N = 2 * M, NH = M + 1, NL = 6 * kSrcRows, TH = M / 8, LP = M + M / 8;
-  __shared__ float2 s[NL * LP];
-  __shared__ float2 tw[N];  // W_N^k, k < N
-  load_tw(tw, twff, M);
-  const int64_t row0 = (int64_t)blockIdx.x * kSrcRows, nhalf = (int64_t)N * N * NH;
+  constexpr int N = 2 * M, NL = 6 * kSrcRows, TH = M / 8;
+  __shared__ float2 s[NL * M];
+  __shared__ float2 tws[M / 2 + 1], twc[M];
+  load_tw_rows<M>(tws, twc, twff);
+  const int64_t row0 = (int64_t)blockIdx.x * kSrcRows, nspec = (int64_t)N * N * sp;
   for (int idx = threadIdx.x; idx < kSrcRows * M; idx += blockDim.x) {
     const int r = idx / M, m = idx % M;
     const int64_t row = row0 + r;
@@ -512,24 +579,22 @@ __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 
         for (int j = 0; j <= i; ++j, ++c) S[t][c] = scale * (dr[i] * dr[j] + di[i] * di[j]);
     }
 #pragma unroll
-    for (int c = 0; c < 6; ++c) s[(c * kSrcRows + r) * LP + fpad(m)] = make_float2(S[0][c], S[1][c]);
+    for (int c = 0; c < 6; ++c) s[(c * kSrcRows + r) * M + fswz(m)] = make_float2(S[0][c], S[1][c]);
   }
   __syncthreads();
   {
     const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
-    float2 *line = s + ln * LP;
+    float2 *line = s + ln * M;
     float2 v[8];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * TH)];
+    for (int r = 0; r < 8; ++r) v[r] = line[fswz(j + r * TH)];
     __syncthreads();
-    f_stockham<M, 1, false, true>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
+    f_stockham<M, 1, false, true, true>(v, j, line, 1, twc, 1, [&](int i, float2 x) { line[fswz(i)] = x; });
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < NL * NH; idx += blockDim.x) {
-    const int b = idx / NH, k = idx % NH;
-    const int c = b / kSrcRows, r = b % kSrcRows;
-    out[c * nhalf + (row0 + r) * NH + k] = real_split<M>(s + b * LP, k, tw);
-  }
+  split_pairs<M>(s, NL, tws, [&](int b, int k, float2 x) {
+    out[(b / kSrcRows) * nspec + (row0 + b % kSrcRows) * sp + k] = x;
+  });
 }
 
 // The u_ij spectrum's twelve real fields, tau u_c and u_c + tau u'_c (c =
@@ -539,42 +604,38 @@ __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 
 template <int M>
 __global__ void __launch_bounds__(12 * M / 8) k_uij_rows(const float *__restrict__ u, const float *__restrict__ ud,
                                                          const float *__restrict__ cu, int64_t n3, float tau,
-                                                         float2 *__restrict__ out, const float4 *__restrict__ twff) {
-  constexpr int N = 2 * M, NH = M + 1, TH = M / 8, LP = M + M / 8;
-  __shared__ float2 s[12 * LP];
-  __shared__ float2 tw[N];  // W_N^k, k < N
-  load_tw(tw, twff, M);
-  const int64_t row = blockIdx.x, nhalf = (int64_t)N * N * NH;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) {
-    const int64_t x = row * N + 2 * m;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      float2 uv = *reinterpret_cast<const float2 *>(u + c * n3 + x);
-      if (cu) {
-        const float2 cv = *reinterpret_cast<const float2 *>(cu + c * n3 + x);
-        uv.x -= cv.x;
-        uv.y -= cv.y;
-      }
-      const float2 dv = *reinterpret_cast<const float2 *>(ud + c * n3 + x);
-      s[c * LP + fpad(m)] = make_float2(tau * uv.x, tau * uv.y);
-      s[(6 + c) * LP + fpad(m)] = make_float2(uv.x + tau * dv.x, uv.y + tau * dv.y);
+                                                         float2 *__restrict__ out, int sp,
+                                                         const float4 *__restrict__ twff) {
+  constexpr int N = 2 * M, TH = M / 8;
+  __shared__ float2 s[12 * M];
+  __shared__ float2 tws[M / 2 + 1], twc[M];
+  load_tw_rows<M>(tws, twc, twff);
+  const int64_t row = blockIdx.x, nspec = (int64_t)N * N * sp;
+  for (int idx = threadIdx.x; idx < 6 * M; idx += blockDim.x) {
+    const int c = idx / M, m = idx % M;
+    const int64_t x = c * n3 + row * N + 2 * m;
+    float2 uv = *reinterpret_cast<const float2 *>(u + x);
+    if (cu) {
+      const float2 cv = *reinterpret_cast<const float2 *>(cu + x);
+      uv.x -= cv.x;
+      uv.y -= cv.y;
     }
+    const float2 dv = *reinterpret_cast<const float2 *>(ud + x);
+    s[c * M + fswz(m)] = make_float2(tau * uv.x, tau * uv.y);
+    s[(6 + c) * M + fswz(m)] = make_float2(uv.x + tau * dv.x, uv.y + tau * dv.y);
   }
   __syncthreads();
   {
     const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
-    float2 *line = s + ln * LP;
+    float2 *line = s + ln * M;
     float2 v[8];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = line[fpad(j + r * TH)];
+    for (int r = 0; r < 8; ++r) v[r] = line[fswz(j + r * TH)];
     __syncthreads();
-    f_stockham<M, 1, false, true>(v, j, line, 1, tw, 2, [&](int i, float2 x) { line[fpad(i)] = x; });  // W_M = W_N^2
+    f_stockham<M, 1, false, true, true>(v, j, line, 1, twc, 1, [&](int i, float2 x) { line[fswz(i)] = x; });
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < 12 * NH; idx += blockDim.x) {
-    const int b = idx / NH, k = idx % NH;
-    out[b * nhalf + row * NH + k] = real_split<M>(s + b * LP, k, tw);
-  }
+  split_pairs<M>(s, 12, tws, [&](int b, int k, float2 x) { out[b * nspec + row * sp + k] = x; });
 }
 
 // The same twelve fields in FP64 (tau u_c and u_c + tau u'_c), split into
@@ -624,16 +685,128 @@ __global__ void __launch_bounds__(M) k_ff_uij_rows(const double *__restrict__ u,
   }
 }
 
-// y and z passes in complex float of `batch` half spectra
+// z pass of the complex-float half spectra through TMA.  Persistent CTAs
+// walk tiles of kFzCols kx columns x L z-points (one ky row of one field);
+// a tile arrives by cp.async.bulk.tensor in one of kFzStages shared-memory
+// stages while the CTA transforms the one before, and leaves by a bulk
+// tensor store from its own stage.  The spectra's rows are padded
+// (axg_f32_spec_pitch) so that their byte stride suits TMA; the last kx
+// block reaches past the pitch, where TMA loads zeros and drops the stores.
+// Each z-line is 64 bytes wide in 512 planes a megabyte apart: the plain
+// column kernel reached 0.53 of the DRAM peak on it, limited by the loads in
+// flight.  A stage wait that runs out raises AXG_KERR_MBAR_TIMEOUT.
+constexpr int kFzCols = 8;    // kx columns per tile: 64-byte boxes
+constexpr int kFzStages = 2;  // 3 and 4 stages at one CTA per SM measured slower
+constexpr int kFyCols = 4;    // kx columns per CTA of the y pass (32-byte rows, sector aligned at the padded pitch)
+
 template <int L>
-int f_cols_t(axg_ctx *ctx, float2 *out, int batch, const float4 *tw) {
+constexpr size_t zt_smem() {
+  return (size_t)(kFzStages * L * kFzCols + (L + L / 8) * kFzCols + L) * sizeof(float2) + 8 * kFzStages + 16 + 128;
+}
+
+template <int L>
+__global__ void __launch_bounds__(kFzCols * L / 8, (1024 / (kFzCols * L / 8)) < 32 ? 1024 / (kFzCols * L / 8) : 32)
+    k_cols_z_tma(const __grid_constant__ CUtensorMap tm, int nkb, int ny, int ntiles,
+                 const float4 *__restrict__ twff, int *err) {
+  using namespace axg_tma;
+  constexpr int TH = L / 8, LP = L + L / 8, TILE = L * kFzCols, BOX = L < 256 ? L : 256, S = kFzStages;
+  constexpr uint32_t BYTES = TILE * sizeof(float2);
+  extern __shared__ unsigned char zt_raw[];
+  unsigned char *sm =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(zt_raw) + 127) & ~uintptr_t(127));
+  float2 *tile = reinterpret_cast<float2 *>(sm);  // [S][L][kFzCols], dense as the TMA box
+  float2 *xb = tile + S * TILE;                    // exchange lines, element i of column c at fpad(i) kFzCols + c
+  float2 *tw = xb + LP * kFzCols;                  // W_L^k, k < L
+  uint64_t *bars = reinterpret_cast<uint64_t *>(tw + L);
+  int &fail = *reinterpret_cast<int *>(bars + S);
+  load_tw(tw, twff, L / 2);
+  const uint32_t bar0 = smem_u32(bars);
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < S; ++q) mbar_init(bar0 + 8 * q, 1);
+    fence_barrier_init();
+    fail = 0;
+  }
+  __syncthreads();
+  auto issue = [&](int t, int st) {  // tile t: (field, ky) = o, kx block kb
+    const int o = t / nkb, kb = t % nkb;
+    const uint32_t dst = smem_u32(tile + st * TILE), bar = bar0 + 8 * st;
+    mbar_expect_tx(bar, BYTES);
+#pragma unroll
+    for (int h = 0; h < L / BOX; ++h)
+      tma_load_4d(dst + h * BOX * kFzCols * (int)sizeof(float2), &tm, kb * kFzCols, o % ny, h * BOX, o / ny, bar);
+  };
+  if (threadIdx.x == 0)
+    for (int q = 0; q < S - 1; ++q)
+      if (blockIdx.x + q * (int)gridDim.x < ntiles) issue(blockIdx.x + q * gridDim.x, q);
+  const int c = threadIdx.x % kFzCols, j = threadIdx.x / kFzCols;
+  int i = 0;
+  for (int t = blockIdx.x; t < ntiles; ++i, t += gridDim.x) {
+    const int st = i % S;
+    const int tn = t + (S - 1) * (int)gridDim.x;
+    if (threadIdx.x == 0 && tn < ntiles) {
+      bulk_wait_read0();  // the store of the previous tile, from the stage about to be refilled, has read it
+      issue(tn, (i + S - 1) % S);
+    }
+    if (!mbar_wait_bounded(bar0 + 8 * st, (i / S) & 1)) fail = 1;
+    __syncthreads();
+    if (fail) break;
+    float2 *tl = tile + st * TILE;
+    float2 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = tl[(j + r * TH) * kFzCols + c];
+    f_stockham<L, 1, false>(v, j, xb + c, kFzCols, tw, 1, [&](int ii, float2 z) { tl[ii * kFzCols + c] = z; });
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int o = t / nkb, kb = t % nkb;
+      const uint32_t src = smem_u32(tl);
+#pragma unroll
+      for (int h = 0; h < L / BOX; ++h)
+        tma_store_4d(&tm, src + h * BOX * kFzCols * (int)sizeof(float2), kb * kFzCols, o % ny, h * BOX, o / ny);
+      bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (fail) {
+      atomicCAS(err, 0, AXG_KERR_MBAR_TIMEOUT);
+      for (int q = 1; q < S; ++q) mbar_wait_bounded(bar0 + 8 * ((i + q) % S), ((i + q) / S) & 1, 100000000LL);
+    }
+    bulk_wait0();
+  }
+}
+
+// y and z passes in complex float of `batch` half spectra, rows of pitch sp
+// (axg_f32_spec_pitch): the y pass by k_cols (kFyCols columns, 32-byte
+// rows on sector boundaries), the z pass by k_cols_z_tma
+template <int L>
+int f_cols_t(axg_ctx *ctx, float2 *out, int batch, int sp, const float4 *tw) {
   constexpr int n = L, nh = L / 2 + 1;
-  const int nkb = (nh + kFCols - 1) / kFCols;
-  const int64_t plane = (int64_t)n * nh, vol = plane * n;
-  AXG_TRY((launch_cols<float2, L, kFCols, false>(ctx, "fft_f32_y", (int64_t)batch * n * nkb, out, nh, n, vol, plane,
-                                                  (int64_t)nh, tw, 0)));
-  AXG_TRY((launch_cols<float2, L, kFCols, false>(ctx, "fft_f32_z", (int64_t)batch * n * nkb, out, nh, n, vol,
-                                                  (int64_t)nh, plane, tw, 0)));
+  const int64_t plane = (int64_t)n * sp, vol = plane * n;
+  const int nky = (nh + kFyCols - 1) / kFyCols;
+  AXG_TRY((launch_cols<float2, L, kFyCols, false>(ctx, "fft_f32_y", (int64_t)batch * n * nky, out, nh, n, vol, plane,
+                                                   (int64_t)sp, tw, 0)));
+  CUtensorMap m;
+  constexpr int BOX = L < 256 ? L : 256;
+  const cuuint64_t dims[4] = {(cuuint64_t)sp, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)batch};
+  const cuuint64_t str[3] = {(cuuint64_t)sp * 8, (cuuint64_t)plane * 8, (cuuint64_t)vol * 8};
+  const cuuint32_t box[4] = {kFzCols, 1, BOX, 1};
+  AXG_TRY(axg_encode_tmap(ctx, &m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, out, dims, str, box));  // (re, im) float pairs
+  constexpr size_t smem = zt_smem<L>();
+  constexpr int threads = kFzCols * L / 8;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_cols_z_tma<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_cols_z_tma<L>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per = 0;
+    AXG_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cols_z_tma<L>, threads, smem));
+    if (per < 1) return axg_set_error(ctx, AXG_ERR_CUDA, "z-pass kernel does not fit on an SM");
+    per_sm = per;
+  }
+  int sms = 0;
+  AXG_CUDA_TRY(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int nkb = (nh + kFzCols - 1) / kFzCols, ntiles = batch * n * nkb;
+  const int grid = std::min(ntiles, sms * per_sm);
+  AXG_LAUNCH(ctx, "fft_f32_z", k_cols_z_tma<L>, (unsigned)grid, threads, smem, m, nkb, n, ntiles, tw, ctx->d_err);
   return AXG_OK;
 }
 
@@ -641,9 +814,10 @@ template <int L>
 int uij_r2c_t(axg_ctx *ctx, const float *u, const float *ud, const float *cu, float tau, float2 *out,
               const float4 *tw) {
   constexpr int n = L, M = L / 2;
+  const int sp = axg_f32_spec_pitch(n);
   AXG_LAUNCH(ctx, "uij_rows_fp32", k_uij_rows<M>, (unsigned)((int64_t)n * n), 12 * M / 8, 0, u, ud, cu,
-             (int64_t)n * n * n, tau, out, tw);
-  return f_cols_t<L>(ctx, out, 12, tw);
+             (int64_t)n * n * n, tau, out, sp, tw);
+  return f_cols_t<L>(ctx, out, 12, sp, tw);
 }
 
 template <int L>
@@ -659,9 +833,10 @@ template <int L>
 int gws_r2c_t(axg_ctx *ctx, const float2 *phi, float2 *out, float scale, const float4 *tw) {
   constexpr int n = L, M = L / 2;
   const int64_t rows = (int64_t)n * n;
+  const int sp = axg_f32_spec_pitch(n);
   AXG_LAUNCH(ctx, "gw_source_rows_fp32", k_gws_rows<M>, (unsigned)(rows / kSrcRows), 6 * kSrcRows * M / 8, 0, phi,
-             scale, out, tw);
-  return f_cols_t<L>(ctx, out, 6, tw);
+             scale, out, sp, tw);
+  return f_cols_t<L>(ctx, out, 6, sp, tw);
 }
 
 }  // namespace

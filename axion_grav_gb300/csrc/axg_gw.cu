@@ -603,14 +603,19 @@ __device__ __forceinline__ void f32_update(float4 *__restrict__ acc, int64_t ast
 // contraction; the accumulators are float-float pairs (re hi, re lo, im hi,
 // im lo), so no FP64 instruction is issued per k-site.  One thread per stored
 // half-spectrum entry; the accumulators hold that half spectrum and the
-// Nyquist-row mirrors, as in k_gw_accumulate_tab.
-__global__ void __launch_bounds__(256, 4) k_gw_accumulate_f32(const float2 *__restrict__ srcF, const float2 *__restrict__ om, int n, float th,
-                                    float tl, float dw, int ref_compat, int64_t astride, float4 *__restrict__ acc) {
+// Nyquist-row mirrors, as in k_gw_accumulate_tab.  The source spectra have
+// kx rows of sp entries (the own transforms pad them), the accumulators and
+// phase rates rows of n/2 + 1.
+__global__ void __launch_bounds__(256, 4) k_gw_accumulate_f32(const float2 *__restrict__ srcF, int sp,
+                                                              const float2 *__restrict__ om, int n, float th,
+                                                              float tl, float dw, int ref_compat, int64_t astride,
+                                                              float4 *__restrict__ acc) {
   const int nh = n / 2 + 1;
-  const int64_t nhalf = (int64_t)n * n * nh;
+  const int64_t nhalf = (int64_t)n * n * nh, nspec = (int64_t)n * n * sp;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nhalf; h += stride) {
     const int hx = (int)(h % nh), hy = (int)((h / nh) % n), hz = (int)(h / ((int64_t)nh * n));
+    const int64_t hs = (h / nh) * sp + hx;  // the entry in the source spectra
     const float kx = (float)kint(hx, n), ky = (float)kint(hy, n), kz = (float)kint(hz, n);
     const float qq = sqrtf(kx * kx + ky * ky + kz * kz);
     float pr[6], pi[6];
@@ -622,13 +627,13 @@ __global__ void __launch_bounds__(256, 4) k_gw_accumulate_f32(const float2 *__re
     sincosf(gw_phase(om[h], th, tl), &sq, &cq);
     const float wc = dw * cq, ws = dw * sq;
     float xp[2], xm[2], lm[2];
-    gw_contract<float, float2>(srcF, nhalf, h, true, pr, pi, xp, xm, lm);
+    gw_contract<float, float2>(srcF, nspec, hs, true, pr, pi, xp, xm, lm);
     f32_update(acc, astride, h, wc, ws, xp, xm, lm, ref_compat);
     if (hx > 0 && hx < n / 2 && (hy == n / 2 || hz == n / 2)) {
       const int jx = n - hx, jy = hy == 0 ? 0 : n - hy, jz = hz == 0 ? 0 : n - hz;
       const float jkx = (float)kint(jx, n), jky = (float)kint(jy, n), jkz = (float)kint(jz, n);
       gw_polarisation<float>(jkx, jky, jkz, sqrtf(jkx * jkx + jky * jky + jkz * jkz), pr, pi);
-      gw_contract<float, float2>(srcF, nhalf, h, false, pr, pi, xp, xm, lm);
+      gw_contract<float, float2>(srcF, nspec, hs, false, pr, pi, xp, xm, lm);
       f32_update(acc, astride, nhalf + gw_nyq_extra(hx, hy, hz, n), wc, ws, xp, xm, lm, ref_compat);
     }
   }
@@ -751,14 +756,16 @@ __device__ R tt_power(const R Ur[6], const R Ui[6], const R kh[3]) {
   return s;
 }
 
+// F: the twelve half spectra, kx rows of sp entries
 template <typename CV>
-__global__ void k_uij_bin(const CV *__restrict__ F, int n, double dwav, double dv, const int16_t *__restrict__ tab,
-                          int nb, double *__restrict__ numer, double *__restrict__ denom) {
+__global__ void k_uij_bin(const CV *__restrict__ F, int sp, int n, double dwav, double dv,
+                          const int16_t *__restrict__ tab, int nb, double *__restrict__ numer,
+                          double *__restrict__ denom) {
   __shared__ double sn[kMaxBins], sd[kMaxBins];
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sn[b] = sd[b] = 0.0;
   __syncthreads();
   const int nh = n / 2 + 1;
-  const int64_t nhalf = (int64_t)n * n * nh;
+  const int64_t nhalf = (int64_t)n * n * nh, nspec = (int64_t)n * n * sp;
   const double dv2 = dv * dv, dwav2 = dwav * dwav;
   BinRun run;
   for (int64_t h0 = run_start(); h0 < nhalf; h0 += run_stride()) {
@@ -777,7 +784,8 @@ __global__ void k_uij_bin(const CV *__restrict__ F, int n, double dwav, double d
         R Ur[6], Ui[6], Dr[6], Di[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-          const CV a = F[c * nhalf + h], d = F[(6 + c) * nhalf + h];
+          const int64_t hs = (h / nh) * sp + ix;
+          const CV a = F[c * nspec + hs], d = F[(6 + c) * nspec + hs];
           Ur[c] = a.x;
           Ui[c] = a.y;
           Dr[c] = d.x;
@@ -833,8 +841,12 @@ int ensure_uij_fft(axg_ctx *ctx) {
   // our own transforms (power-of-two N up to 512; AXG_FFT_FF=0: cuFFT) form
   // the twelve fields in their row pass: only the 12 x nhalf spectra
   ctx->uij_own_fft = axg_ff_use(n);
+  ctx->u_pitch = n / 2 + 1;
   if (ctx->uij_own_fft) {
-    AXG_TRY(axg_alloc(ctx, &ctx->ubuf, (size_t)12 * nhalf * 2 * rs, "u_ij spectra"));
+    if (fp32) ctx->u_pitch = axg_f32_spec_pitch(n);
+    const size_t bytes = (size_t)12 * n * n * ctx->u_pitch * 2 * rs;
+    AXG_TRY(axg_alloc(ctx, &ctx->ubuf, bytes, "u_ij spectra"));
+    AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->ubuf, 0, bytes, ctx->stream));  // the padding columns
     return AXG_OK;
   }
   // one real field of N^3 followed by the complex output 12 x nhalf; the
@@ -870,7 +882,12 @@ int axg_gw_init(axg_ctx *ctx) {
   ctx->acc_stride = axg_gw_acc_entries(n);
   AXG_TRY(axg_alloc(ctx, (void **)&ctx->acc, (size_t)ctx->acc_stride * 64, "GW accumulators"));
   if (!ctx->gw_own_fft) AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrc, (size_t)n3 * 6 * rs, "GW sources"));
-  AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrcF, (size_t)nhalf * 6 * 2 * rs, "GW source spectra"));
+  ctx->gsrc_pitch = fp32 && ctx->gw_own_fft ? axg_f32_spec_pitch(n) : n / 2 + 1;
+  {
+    const size_t bytes = (size_t)n * n * ctx->gsrc_pitch * 6 * 2 * rs;
+    AXG_TRY(axg_alloc(ctx, (void **)&ctx->gsrcF, bytes, "GW source spectra"));
+    AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->gsrcF, 0, bytes, ctx->stream));  // the padding columns
+  }
   AXG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->acc_stride * 64, ctx->stream));
   if (fp32) {
     AXG_TRY(axg_alloc(ctx, (void **)&ctx->gw_omega, (size_t)nhalf * 8, "GW phase rates"));
@@ -935,8 +952,8 @@ int axg_gw_integration(axg_ctx *ctx, double tau, double dtau) {
     }
     const float th = (float)tau, tl = (float)(tau - (double)th);
     AXG_LAUNCH(ctx, "gw_accumulate_fp32", k_gw_accumulate_f32, grid_for(nhalf), 256, 0,
-               (const float2 *)ctx->gsrcF, ctx->gw_omega, n, th, tl, (float)dw, ref, ctx->acc_stride,
-               (float4 *)ctx->acc);
+               (const float2 *)ctx->gsrcF, ctx->gsrc_pitch, ctx->gw_omega, n, th, tl, (float)dw, ref,
+               ctx->acc_stride, (float4 *)ctx->acc);
     return AXG_OK;
   }
   int ex;
@@ -1038,7 +1055,8 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
           AXG_CUFFT_TRY(ctx, cufftExecR2C(ctx->plan_u, w, (cufftComplex *)F + f * nhalf));
         }
       }
-      AXG_LAUNCH(ctx, "uij_bin_fp32", k_uij_bin<float2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
+      AXG_LAUNCH(ctx, "uij_bin_fp32", k_uij_bin<float2>, 152 * 4, 256, 0, F, ctx->u_pitch, n, dwav, dv, tab, nb,
+                 d_num, d_den);
     } else {
       double *w = (double *)ctx->ubuf;
       double2 *F = ctx->uij_own_fft ? (double2 *)ctx->ubuf : (double2 *)(w + ctx->n3);
@@ -1052,7 +1070,8 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
           AXG_CUFFT_TRY(ctx, cufftExecD2Z(ctx->plan_u, w, (cufftDoubleComplex *)F + f * nhalf));
         }
       }
-      AXG_LAUNCH(ctx, "uij_bin_fp64", k_uij_bin<double2>, 152 * 4, 256, 0, F, n, dwav, dv, tab, nb, d_num, d_den);
+      AXG_LAUNCH(ctx, "uij_bin_fp64", k_uij_bin<double2>, 152 * 4, 256, 0, F, ctx->u_pitch, n, dwav, dv, tab, nb,
+                 d_num, d_den);
     }
   } else {
     return axg_set_error(ctx, AXG_ERR_STATE, "gw_mode is NONE");
@@ -1061,6 +1080,7 @@ int axg_gw_spec(axg_ctx *ctx, double tau, int log_bins, double *wave, double *po
   AXG_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), ctx->d_red, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost,
                                     ctx->stream));
   AXG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  AXG_TRY(axg_evo_check_error(ctx));  // a TMA wait of the z pass that ran out
   const double fact = gw_fact(ctx->p, n, dspa);
   for (int k = 0; k < nb; ++k) {
     const double qc = log_bins ? std::sqrt(edges[k] * edges[k + 1]) : (edges[k + 1] + edges[k]) / 2;

@@ -102,9 +102,11 @@ struct axg_ctx {
   bool acc_ff = false;         // Green accumulators are float-float float4 (FP32-mixed, and the FP64 paths
                                // on the float-float transforms), else double2
   int64_t acc_stride = 0;      // Green accumulator entries per component (axg_gw_acc_entries)
-  bool gw_own_fft = false;
-  bool uij_own_fft = false;    // u_ij spectrum: fields formed in our own row transforms (no real buffer, no plan)     // Green sources transformed by axg_fft_ff.cu (FP64: float-float D2Z; FP32:
+  bool gw_own_fft = false;     // Green sources transformed by axg_fft_ff.cu (FP64: float-float D2Z; FP32:
                                // the fused source + R2C), else by cuFFT; fixed when the context is made
+  bool uij_own_fft = false;    // u_ij spectrum: fields formed in our own row transforms (no real buffer, no plan)
+  int gsrc_pitch = 0;          // kx row pitch of gsrcF (axg_f32_spec_pitch for the FP32 own transforms, else n/2+1)
+  int u_pitch = 0;             // kx row pitch of the u_ij spectra in ubuf (likewise)
   float *ff_tw = nullptr;      // float-float FFT twiddles W_n^k, k < n/2 (axg_fft_ff.cu)
   int ff_tw_n = 0;
   cufftHandle plan_gsrc = 0;
@@ -253,6 +255,9 @@ int axg_evo_drift(axg_ctx *ctx, double h);                  // drift of current 
 int axg_evo_kick_plain(axg_ctx *ctx, double t, double dt);  // FP64-plain kick (phi, u)
 int axg_evo_kick_drift(axg_ctx *ctx, double t, double dt, double dtd);  // fused step
 int axg_evo_check_error(axg_ctx *ctx);
+// cuTensorMapEncodeTiled (interleave and swizzle none, L2 promotion 256 B)
+int axg_encode_tmap(axg_ctx *ctx, CUtensorMap *m, CUtensorMapDataType dt, int rank, void *base,
+                    const cuuint64_t *dims, const cuuint64_t *strides, const cuuint32_t *box);
 int axg_evo_tile_count();
 axg_tile_cfg axg_evo_tile(int i);
 int axg_evo_tile_supported(const axg_ctx *ctx, int i);
@@ -284,12 +289,18 @@ __host__ __device__ inline int64_t gw_nyq_extra(int hx, int hy, int hz, int n) {
   return (int64_t)(hx - 1) * (2 * n - 1) + (hy == n / 2 ? hz : n + (hy < n / 2 ? hy : hy - 1));
 }
 
+// Row pitch (complex values) of the complex-float half spectra of the own
+// transforms: n/2 + 1 rounded up to a multiple of 4, so that every kx row
+// starts on a 32-byte sector and the rows' byte stride suits TMA (a multiple
+// of 16).  Columns n/2 + 1 .. pitch - 1 are padding that no consumer reads.
+inline int axg_f32_spec_pitch(int n) { return (n / 2 + 1 + 3) & ~3; }
 // the six FP32-mixed Green sources of phi and their forward transforms, out
-// [6][n][n][n/2+1] complex float (cuFFT R2C layout); n as axg_ff_fft_supported
+// [6][n][n][pitch] complex float (cuFFT's R2C values, rows of
+// axg_f32_spec_pitch(n)); n as axg_ff_fft_supported
 int axg_gw_source_r2c_f32(axg_ctx *ctx, const float2 *phi, float2 *out, int n, float scale);
 // the u_ij spectrum's twelve real fields (tau u_c, u_c + tau u'_c) and their
-// forward transforms, out [12][n][n][n/2+1] complex (float, or double from
-// float-float); cu: the FP32 Kahan compensation of u, or null
+// forward transforms, out [12][n][n][pitch] complex float (rows of
+// axg_f32_spec_pitch(n)); cu: the FP32 Kahan compensation of u, or null
 int axg_uij_r2c_f32(axg_ctx *ctx, const float *u, const float *ud, const float *cu, float tau, float2 *out, int n);
 int axg_uij_d2z_ff(axg_ctx *ctx, const double *u, const double *ud, double tau, double2 *out, int n);
 // the six FP64 Green sources of phi (d = 2 dx; inv_d, d_pow2 as

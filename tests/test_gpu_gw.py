@@ -89,7 +89,7 @@ def test_green_float_float_fft_matches_cufft(monkeypatch, n):
     assert rel(out["1"], out["0"]) < 1e-12
 
 
-@pytest.mark.parametrize("n", [16, 32, 64, 128])
+@pytest.mark.parametrize("n", [16, 32, 64, 128, 256])
 def test_green_fp32_fused_source_transform_matches_cufft(monkeypatch, n):
     """FP32-mixed Green mode forms the six sources inside its own row
     transform and runs the y and z passes in complex float for power-of-two
@@ -239,7 +239,7 @@ def test_uij_tt_spectrum(precision, tol):
 
 
 @pytest.mark.parametrize("precision,tol", [(ag.PREC_FP64_PLAIN, 1e-12), (ag.PREC_FP32_MIXED, 2e-5)])
-@pytest.mark.parametrize("n", [16, 64])
+@pytest.mark.parametrize("n", [16, 64, 256])
 def test_uij_spectrum_own_transforms_match_cufft(monkeypatch, precision, tol, n):
     """For power-of-two N the u_ij spectrum forms its twelve fields inside its
     own row transforms (complex float, or float-float for FP64); against the
@@ -272,7 +272,8 @@ def test_own_transforms_store_no_real_fields(monkeypatch, precision, rs):
     cuFFT path the context holds their real buffers less (6 fields of N^3
     reals for the Green sources; one field for the u_ij spectrum, whose
     cuFFT path transforms the twelve through one real buffer), and only a
-    twiddle table more."""
+    twiddle table more.  The complex-float half spectra of the own
+    transforms have kx rows padded to a multiple of 4 entries."""
     n = 64
     mem = {}
     for ff in ("1", "0"):
@@ -285,8 +286,10 @@ def test_own_transforms_store_no_real_fields(monkeypatch, precision, rs):
             mem[("uij", ff)] = lat.memory_bytes()
     monkeypatch.delenv("AXG_FFT_FF")
     tw = n // 2 * 16  # the own transforms' float-float twiddle table
-    assert mem[("green", "0")] - mem[("green", "1")] >= 6 * n ** 3 * rs - tw
-    assert mem[("uij", "0")] - mem[("uij", "1")] >= n ** 3 * rs - tw
+    nh = n // 2 + 1
+    pad = 0 if rs == 8 else n * n * (((nh + 3) & ~3) - nh) * 2 * rs  # per field
+    assert mem[("green", "0")] - mem[("green", "1")] >= 6 * n ** 3 * rs - tw - 6 * pad
+    assert mem[("uij", "0")] - mem[("uij", "1")] >= n ** 3 * rs - tw - 12 * pad
 
 
 def test_green_requires_mode():

@@ -196,3 +196,60 @@ def test_float_float_chi2_matches_fp64():
         b = axo.lib().axo_chi2_string_fp64(axo.dptr(ph), axo.dptr(pr))
         worst = max(worst, abs(a - b) / max(abs(b), 1.0))
     assert worst < 1e-13, worst
+
+
+def _chi2_string_numpy(ph, pr):
+    """defects_3d.f90:385-433 restated in numpy FP64 with the platform's
+    libm sin, cos and atan2: shares no code with the oracle or the kernels.
+    ph: (S, 8) corner phases, pr: (S, 4) = (mu, phi, r, theta)."""
+    ref_pi = 3.14159265359  # potential.f90:8
+    mu, phi, r, th = pr[:, 0], pr[:, 1], pr[:, 2], pr[:, 3]
+    u0, v0 = r * np.cos(th), r * np.sin(th)
+    sm, sp, cp = np.sqrt(1.0 - mu * mu), np.sin(phi), np.cos(phi)
+    a = np.zeros(len(pr))
+    b = np.zeros(len(pr))
+    near = np.zeros(len(pr), bool)
+    for iz in range(2):
+        for iy in range(2):
+            for ix in range(2):
+                x, y, z = ix - 0.5, iy - 0.5, iz - 0.5
+                du = -u0 + mu * (x * cp + y * sp) - z * sm
+                dv = -v0 - x * sp + y * cp
+                d = ph[:, (iz * 2 + iy) * 2 + ix] - np.arctan2(dv, du)
+                near |= np.abs(np.abs(d) - ref_pi) < 1e-9
+                d = np.where(d >= ref_pi, d - 2 * ref_pi, np.where(d < -ref_pi, d + 2 * ref_pi, d))
+                a += d * d
+                b += d
+    a, b = a / 8, b / 8
+    return a - b * b, near
+
+
+def test_float_float_chi2_matches_independent_libm_restatement():
+    """The chi2 the oracle and the kernels share (float-float, project atan2
+    and sin/cos) against an independent numpy restatement on libm: equal to
+    1e-12 of max(chi2, 1) over the fit's parameter box, corner phases drawn
+    uniformly and from near-string configurations (small chi2)."""
+    rng = np.random.default_rng(12)
+    lo = np.array([-1.0, -np.pi, 0.0, -np.pi])
+    hi = np.array([1.0, np.pi, np.sqrt(3.0) / 2, np.pi])
+    S = 3000
+    pr = lo + (hi - lo) * rng.random((S, 4))
+    ph = rng.uniform(-np.pi, np.pi, (S, 8))
+    # half the cells: phases of the model at a nearby parameter point plus noise
+    pr2 = np.clip(pr + 0.05 * rng.standard_normal((S, 4)), lo, hi)
+    mu, phi, r, th = pr2[:, 0], pr2[:, 1], pr2[:, 2], pr2[:, 3]
+    u0, v0 = r * np.cos(th), r * np.sin(th)
+    sm, sp, cp = np.sqrt(1.0 - mu * mu), np.sin(phi), np.cos(phi)
+    for i, (ix, iy, iz) in enumerate((ix, iy, iz) for iz in range(2) for iy in range(2) for ix in range(2)):
+        x, y, z = ix - 0.5, iy - 0.5, iz - 0.5
+        du = -u0 + mu * (x * cp + y * sp) - z * sm
+        dv = -v0 - x * sp + y * cp
+        ph[S // 2:, i] = (np.arctan2(dv, du) + 0.01 * rng.standard_normal(S))[S // 2:]
+    ph = np.mod(ph + np.pi, 2 * np.pi) - np.pi
+    ref, near = _chi2_string_numpy(ph, pr)
+    worst = 0.0
+    for s in np.flatnonzero(~near):
+        a = axo.lib().axo_chi2_string_ff(axo.dptr(np.ascontiguousarray(ph[s])), axo.dptr(np.ascontiguousarray(pr[s])))
+        worst = max(worst, abs(a - ref[s]) / max(abs(ref[s]), 1.0))
+    assert (~near).sum() > 0.99 * S
+    assert worst < 1e-12, worst
