@@ -464,7 +464,12 @@ __device__ __forceinline__ void string_start(uint64_t seed, uint64_t cell, int i
 //   chi2  : a = <d^2> moves by at most (2 pi + E) E, b^2 = <d>^2 by at most
 //           (2 pi + E + 2e-6)(E + 2e-6), FP32 summation by below 2e-5;
 // and the total is doubled, plus 1e-4.
-__device__ float chi2_string_lower(const float phf[8], const double t[4]) {
+//
+// Kept out of line: inlined into the search step (with its eight atan2f and
+// two sincosf) it made the string-fit loop's code outgrow the instruction
+// cache (ncu at 128^3: 9.1 "no instruction" stalls per issue); one copy took
+// the 128^3 fits from 152 to 106 ms.
+__device__ __noinline__ float chi2_string_lower(const float phf[8], const double t[4]) {
   constexpr float kDuv = 4e-6f, kAng = 2e-6f, kPh = 2e-6f;
   constexpr float kPiF = (float)kRefPi, kTwoPiF = (float)kRefTwoPi;
   const float mu = (float)t[0], ph = (float)t[1], rad = (float)t[2], ang = (float)t[3];
@@ -892,6 +897,7 @@ __device__ void velocity_string(const V *phi, const V *cphi, const V *phid, int 
 // once per CTA in shared memory.
 struct WallGrid {
   double d0[400][4];  // d0 and phi
+  float f[400][3];    // d0 rounded to FP32, for the screen of position_wall
 };
 
 __device__ void wall_grid_fill(WallGrid &g) {
@@ -906,8 +912,24 @@ __device__ void wall_grid_fill(WallGrid &g) {
     g.d0[idx][1] = sq * sp;
     g.d0[idx][2] = mu;
     g.d0[idx][3] = phi;
+    for (int k = 0; k < 3; ++k) g.f[idx][k] = (float)g.d0[idx][k];
   }
 }
+
+// The direction search of position_wall screened in FP32.  Per direction
+// the reference forms d_i = pp_i . d0, W = sum d_i, S = sum d_i^2 and
+// chi2 = S - m w^2 with w = max(W, 0) / m, i.e. chi2 = S - max(W, 0)^2 / m.
+// With |pp| < 0.87 (each component in (-0.5, 0.5)), |d0| = 1 and m <= 12,
+// the FP32 value differs from the FP64 one by less than kWallScreenErr:
+// inputs rounded to FP32 and three products and two sums move d by < 5e-7,
+// so W by < 1.3e-5 and S by < 2e-5; max(W, 0)^2 / m is Lipschitz in W
+// (either branch of the reference's w < 0 test), < 9e-5 for |W| <= 10.4;
+// the remaining roundings are below 1e-5.  The FP32 error is thus below
+// 1.3e-4; the screen allows 1e-3.  A direction whose FP32 value exceeds the
+// smallest FP32 value by more than twice that cannot hold the FP64 minimum,
+// so evaluating only the others in FP64, in the reference's loop order and
+// with its strict-less update, selects the same direction and w.
+constexpr float kWallScreenErr = 1e-3f;
 
 __device__ void position_wall(const double ph[8], const WallGrid &grid, double pos[3], double dir[3], double *gof,
                               double *wa) {
@@ -950,9 +972,27 @@ __device__ void position_wall(const double ph[8], const WallGrid &grid, double p
     *wa = 0.0;
     return;
   }
+  float ppf[12][3];
+  for (int i = 0; i < m; ++i)
+    for (int k = 0; k < 3; ++k) ppf[i][k] = (float)pp[i][k];
+  auto screen = [&](int idx) {
+    const float *g = grid.f[idx];
+    float W = 0.0f, S = 0.0f;
+    for (int i = 0; i < m; ++i) {
+      const float d = ppf[i][0] * g[0] + ppf[i][1] * g[1] + ppf[i][2] * g[2];
+      W += d;
+      S += d * d;
+    }
+    const float wp = fmaxf(W, 0.0f);
+    return S - wp * wp / (float)m;
+  };
+  float fmin = INFINITY;
+  for (int idx = 0; idx < 400; ++idx) fmin = fminf(fmin, screen(idx));
+  const float fcut = fmin + 2 * kWallScreenErr;
   double chi2min = 6.0, mut = 0.0, phit = 0.0, wt = 0.0;
   for (int imu = 1; imu <= 20; ++imu) {
     for (int iphi = 1; iphi <= 20; ++iphi) {
+      if (!(screen((imu - 1) * 20 + (iphi - 1)) <= fcut)) continue;
       const double *d0 = grid.d0[(imu - 1) * 20 + (iphi - 1)];
       const double mu = d0[2], phi = d0[3];
       double w = 0.0, chi2 = 0.0;

@@ -352,3 +352,25 @@ def test_id_defects_fits_bit_exact_on_a_128_sample():
     np.testing.assert_allclose(S[si, 9], fs[:, 9], rtol=1e-14)
     wcols = [0, 1, 2, 3, 4, 5, 7, 8]
     assert np.array_equal(W[wi][:, wcols], fw[:, wcols])
+
+
+@pytest.mark.parametrize("precision", [ag.PREC_FP64_PLAIN, ag.PREC_FP32_MIXED])
+def test_wall_fits_bit_exact_on_every_128_cell(precision):
+    """Every wall cell of the evolved 128^3 benchmark lattice (about 3 10^5),
+    refitted by the oracle from the same snapshot, agrees bit for bit: the
+    GPU screens the 400 wall directions in FP32 and evaluates only those
+    near the minimum in FP64, which must select the reference's direction."""
+    n = 128
+    p = workload(n, precision, ag.GW_NONE)
+    with ag.Lattice(p) as lat:
+        lat.ic_gaussian_flat(kcut=2.0 * np.pi / (8 * p.dspa))
+        lat.leapfrog(2.0, 0.25 * p.dspa, 10, True, True)
+        tau = 2.0 + 10 * 0.25 * p.dspa
+        sl, wa, sv, cnt = lat.id_defects(1, tau)
+        S, W = lat.defect_lists(int(cnt[0]), int(cnt[1]))
+        phi, phid = lat.download()
+    assert cnt[1] > 10 ** 5
+    _, fw = axo.fit_cells(p, phi, phid, np.zeros(0, np.int64), W[:, 8].astype(np.int64))
+    wcols = [0, 1, 2, 3, 4, 5, 7, 8]
+    assert np.array_equal(W[:, wcols], fw[:, wcols])
+    np.testing.assert_allclose(W[:, 6], fw[:, 6], rtol=1e-14)
