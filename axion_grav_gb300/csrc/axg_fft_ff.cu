@@ -288,14 +288,23 @@ __device__ __forceinline__ void load_tw_rows(float2 *tws, float2 *twc, const flo
 // E = (Z[k] + conj Z[M-k]) / 2, O = (Z[k] - conj Z[M-k]) / 2i and
 // P = W_N^k O, X[k] = E + P and X[M - k] = conj(E - P) (E and O of M - k are
 // the conjugates of those of k, W_N^(M-k) = -conj W_N^k); k = 0 gives X[0]
-// and X[M], and its thread adds X[M/2].  Lines of M elements at fswz(i);
-// task t of line b for t < M / 2, consecutive t on consecutive threads.
+// and X[M], and its thread adds X[M/2].  Line b at s + b rowline_pitch<M>(),
+// element i at fswz(i); task t of line b for t < M / 2, consecutive t on
+// consecutive threads.
+//
+// Line pitch: M elements where a half warp's 16 threads lie in one line
+// (M >= 128); shorter lines are M + M / 8 apart, so that the two or more
+// lines of a half warp start on different banks.
+template <int M>
+constexpr int rowline_pitch() {
+  return M >= 128 ? M : M + M / 8;
+}
 template <int M, typename Out>
 __device__ __forceinline__ void split_pairs(const float2 *s, int nl, const float2 *tws, Out out) {
   constexpr int H = M / 2;
   for (int task = threadIdx.x; task < nl * H; task += blockDim.x) {
     const int b = task / H, t = task % H;
-    const float2 *line = s + b * M;
+    const float2 *line = s + b * rowline_pitch<M>();
     const float2 zk = line[fswz(t)], zm = c_conj(line[fswz((M - t) & (M - 1))]);
     const float2 E = c_half(c_add(zk, zm)), O = c_div_2i(c_sub(zk, zm));
     const float2 P = c_mul(tws[t], O);
@@ -536,6 +545,23 @@ int ff_gws_d2z_t(axg_ctx *ctx, const double2 *phi, double d, double inv_d, int d
 
 constexpr int kSrcRows = 2;  // x-rows per CTA of the source row pass (6 x 2 lines)
 
+// Opts a kernel into `smem` bytes of dynamic shared memory above the 48 KB
+// default on the current device (a host-side call, repeated per launch so
+// that every device a context runs on gets it)
+template <typename K>
+int allow_smem(axg_ctx *ctx, K kern, size_t smem) {
+  if (smem > 48 * 1024)
+    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  return AXG_OK;
+}
+
+// Dynamic shared memory of the FP32 row kernels: nl lines, then the split
+// and per-pass twiddles
+template <int M>
+constexpr size_t rows_f32_smem(int nl) {
+  return ((size_t)nl * rowline_pitch<M>() + (M / 2 + 1) + M) * sizeof(float2);
+}
+
 // Row pass with the sources, for rows (y, z) = row0 .. row0 + kSrcRows - 1
 // of the N = 2M lattice.  Line c kSrcRows + r holds source c of row r
 // packed as M complex points z[m] = S(2m) + i S(2m + 1); an M-point FFT per
@@ -544,9 +570,10 @@ template <int M>
 __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 *__restrict__ phi, float scale,
                                                                    float2 *__restrict__ out, int sp,
                                                                    const float4 *__restrict__ twff) {
-  constexpr int N = 2 * M, NL = 6 * kSrcRows, TH = M / 8;
-  __shared__ float2 s[NL * M];
-  __shared__ float2 tws[M / 2 + 1], twc[M];
+  constexpr int N = 2 * M, NL = 6 * kSrcRows, TH = M / 8, LP = rowline_pitch<M>();
+  extern __shared__ __align__(16) unsigned char rows_sm[];
+  float2 *s = reinterpret_cast<float2 *>(rows_sm);
+  float2 *tws = s + NL * LP, *twc = tws + (M / 2 + 1);
   load_tw_rows<M>(tws, twc, twff);
   const int64_t row0 = (int64_t)blockIdx.x * kSrcRows, nspec = (int64_t)N * N * sp;
   for (int idx = threadIdx.x; idx < kSrcRows * M; idx += blockDim.x) {
@@ -579,12 +606,12 @@ __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 
         for (int j = 0; j <= i; ++j, ++c) S[t][c] = scale * (dr[i] * dr[j] + di[i] * di[j]);
     }
 #pragma unroll
-    for (int c = 0; c < 6; ++c) s[(c * kSrcRows + r) * M + fswz(m)] = make_float2(S[0][c], S[1][c]);
+    for (int c = 0; c < 6; ++c) s[(c * kSrcRows + r) * LP + fswz(m)] = make_float2(S[0][c], S[1][c]);
   }
   __syncthreads();
   {
     const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
-    float2 *line = s + ln * M;
+    float2 *line = s + ln * LP;
     float2 v[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) v[r] = line[fswz(j + r * TH)];
@@ -606,9 +633,10 @@ __global__ void __launch_bounds__(12 * M / 8) k_uij_rows(const float *__restrict
                                                          const float *__restrict__ cu, int64_t n3, float tau,
                                                          float2 *__restrict__ out, int sp,
                                                          const float4 *__restrict__ twff) {
-  constexpr int N = 2 * M, TH = M / 8;
-  __shared__ float2 s[12 * M];
-  __shared__ float2 tws[M / 2 + 1], twc[M];
+  constexpr int N = 2 * M, TH = M / 8, LP = rowline_pitch<M>();
+  extern __shared__ __align__(16) unsigned char rows_sm[];
+  float2 *s = reinterpret_cast<float2 *>(rows_sm);
+  float2 *tws = s + 12 * LP, *twc = tws + (M / 2 + 1);
   load_tw_rows<M>(tws, twc, twff);
   const int64_t row = blockIdx.x, nspec = (int64_t)N * N * sp;
   for (int idx = threadIdx.x; idx < 6 * M; idx += blockDim.x) {
@@ -621,13 +649,13 @@ __global__ void __launch_bounds__(12 * M / 8) k_uij_rows(const float *__restrict
       uv.y -= cv.y;
     }
     const float2 dv = *reinterpret_cast<const float2 *>(ud + x);
-    s[c * M + fswz(m)] = make_float2(tau * uv.x, tau * uv.y);
-    s[(6 + c) * M + fswz(m)] = make_float2(uv.x + tau * dv.x, uv.y + tau * dv.y);
+    s[c * LP + fswz(m)] = make_float2(tau * uv.x, tau * uv.y);
+    s[(6 + c) * LP + fswz(m)] = make_float2(uv.x + tau * dv.x, uv.y + tau * dv.y);
   }
   __syncthreads();
   {
     const int ln = threadIdx.x / TH, j = threadIdx.x % TH;
-    float2 *line = s + ln * M;
+    float2 *line = s + ln * LP;
     float2 v[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) v[r] = line[fswz(j + r * TH)];
@@ -793,16 +821,11 @@ int f_cols_t(axg_ctx *ctx, float2 *out, int batch, int sp, const float4 *tw) {
   AXG_TRY(axg_encode_tmap(ctx, &m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, out, dims, str, box));  // (re, im) float pairs
   constexpr size_t smem = zt_smem<L>();
   constexpr int threads = kFzCols * L / 8;
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_cols_z_tma<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_cols_z_tma<L>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    int per = 0;
-    AXG_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cols_z_tma<L>, threads, smem));
-    if (per < 1) return axg_set_error(ctx, AXG_ERR_CUDA, "z-pass kernel does not fit on an SM");
-    per_sm = per;
-  }
-  int sms = 0;
+  AXG_TRY(allow_smem(ctx, k_cols_z_tma<L>, smem));
+  AXG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_cols_z_tma<L>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  int per_sm = 0, sms = 0;
+  AXG_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cols_z_tma<L>, threads, smem));
+  if (per_sm < 1) return axg_set_error(ctx, AXG_ERR_CUDA, "z-pass kernel does not fit on an SM");
   AXG_CUDA_TRY(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   const int nkb = (nh + kFzCols - 1) / kFzCols, ntiles = batch * n * nkb;
   const int grid = std::min(ntiles, sms * per_sm);
@@ -815,7 +838,9 @@ int uij_r2c_t(axg_ctx *ctx, const float *u, const float *ud, const float *cu, fl
               const float4 *tw) {
   constexpr int n = L, M = L / 2;
   const int sp = axg_f32_spec_pitch(n);
-  AXG_LAUNCH(ctx, "uij_rows_fp32", k_uij_rows<M>, (unsigned)((int64_t)n * n), 12 * M / 8, 0, u, ud, cu,
+  constexpr size_t smem = rows_f32_smem<M>(12);
+  AXG_TRY(allow_smem(ctx, k_uij_rows<M>, smem));
+  AXG_LAUNCH(ctx, "uij_rows_fp32", k_uij_rows<M>, (unsigned)((int64_t)n * n), 12 * M / 8, smem, u, ud, cu,
              (int64_t)n * n * n, tau, out, sp, tw);
   return f_cols_t<L>(ctx, out, 12, sp, tw);
 }
@@ -834,8 +859,10 @@ int gws_r2c_t(axg_ctx *ctx, const float2 *phi, float2 *out, float scale, const f
   constexpr int n = L, M = L / 2;
   const int64_t rows = (int64_t)n * n;
   const int sp = axg_f32_spec_pitch(n);
-  AXG_LAUNCH(ctx, "gw_source_rows_fp32", k_gws_rows<M>, (unsigned)(rows / kSrcRows), 6 * kSrcRows * M / 8, 0, phi,
-             scale, out, sp, tw);
+  constexpr size_t smem = rows_f32_smem<M>(6 * kSrcRows);
+  AXG_TRY(allow_smem(ctx, k_gws_rows<M>, smem));
+  AXG_LAUNCH(ctx, "gw_source_rows_fp32", k_gws_rows<M>, (unsigned)(rows / kSrcRows), 6 * kSrcRows * M / 8, smem,
+             phi, scale, out, sp, tw);
   return f_cols_t<L>(ctx, out, 6, sp, tw);
 }
 

@@ -839,7 +839,7 @@ int ensure_uij_fft(axg_ctx *ctx) {
   const size_t rs = fp32 ? 4 : 8;
   const int64_t nhalf = (int64_t)n * n * (n / 2 + 1);
   // our own transforms (power-of-two N up to 512; AXG_FFT_FF=0: cuFFT) form
-  // the twelve fields in their row pass: only the 12 x nhalf spectra
+  // the twelve fields in their row pass: only the 12 half spectra are stored
   ctx->uij_own_fft = axg_ff_use(n);
   ctx->u_pitch = n / 2 + 1;
   if (ctx->uij_own_fft) {

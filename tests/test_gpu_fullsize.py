@@ -374,3 +374,4 @@ def test_wall_fits_bit_exact_on_every_128_cell(precision):
     wcols = [0, 1, 2, 3, 4, 5, 7, 8]
     assert np.array_equal(W[:, wcols], fw[:, wcols])
     np.testing.assert_allclose(W[:, 6], fw[:, 6], rtol=1e-14)
+
