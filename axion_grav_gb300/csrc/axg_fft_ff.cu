@@ -299,15 +299,24 @@ template <int M>
 constexpr int rowline_pitch() {
   return M >= 128 ? M : M + M / 8;
 }
-template <int M, typename Out>
-__device__ __forceinline__ void split_pairs(const float2 *s, int nl, const float2 *tws, Out out) {
-  constexpr int H = M / 2;
-  for (int task = threadIdx.x; task < nl * H; task += blockDim.x) {
-    const int b = task / H, t = task % H;
-    const float2 *line = s + b * rowline_pitch<M>();
-    const float2 zk = line[fswz(t)], zm = c_conj(line[fswz((M - t) & (M - 1))]);
+//
+// The row kernels run 12 lines of M / 8 threads, i.e. 3 M / 2 threads:
+// thread x takes t = x mod (M / 2) in lines x / (M / 2) + 3 i, so its two
+// read addresses within a line and its twiddle serve all of its lines.
+template <int M, int NL, typename Out>
+__device__ __forceinline__ void split_pairs(const float2 *s, const float2 *tws, Out out) {
+  constexpr int H = M / 2, LP = rowline_pitch<M>(), BS = 3;  // blockDim.x = BS H
+  static_assert(NL % BS == 0, "split_pairs: lines in groups of three");
+  const int t = threadIdx.x % H, b0 = threadIdx.x / H;
+  const int ik = fswz(t), im = fswz((M - t) & (M - 1));
+  const float2 w = tws[t];
+#pragma unroll
+  for (int i = 0; i < NL / BS; ++i) {
+    const int b = b0 + BS * i;
+    const float2 *line = s + b * LP;
+    const float2 zk = line[ik], zm = c_conj(line[im]);
     const float2 E = c_half(c_add(zk, zm)), O = c_div_2i(c_sub(zk, zm));
-    const float2 P = c_mul(tws[t], O);
+    const float2 P = c_mul(w, O);
     out(b, t, c_add(E, P));
     out(b, M - t, c_conj(c_sub(E, P)));
     if (t == 0) {
@@ -576,37 +585,49 @@ __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 
   float2 *tws = s + NL * LP, *twc = tws + (M / 2 + 1);
   load_tw_rows<M>(tws, twc, twff);
   const int64_t row0 = (int64_t)blockIdx.x * kSrcRows, nspec = (int64_t)N * N * sp;
-  for (int idx = threadIdx.x; idx < kSrcRows * M; idx += blockDim.x) {
-    const int r = idx / M, m = idx % M;
-    const int64_t row = row0 + r;
-    const int y = (int)(row % N), z = (int)(row / N), x0 = 2 * m;
-    const float2 *prow = phi + row * N;
-    const float4 c01 = *reinterpret_cast<const float4 *>(prow + x0);  // phi(x0), phi(x0 + 1)
-    const float2 xm = prow[x0 == 0 ? N - 1 : x0 - 1], xp = prow[x0 + 2 == N ? 0 : x0 + 2];
-    const int64_t ym = (int64_t)z * N + (y == 0 ? N - 1 : y - 1), yp = (int64_t)z * N + (y + 1 == N ? 0 : y + 1);
-    const int64_t zm = (int64_t)(z == 0 ? N - 1 : z - 1) * N + y, zp = (int64_t)(z + 1 == N ? 0 : z + 1) * N + y;
-    const float4 pym = *reinterpret_cast<const float4 *>(phi + ym * N + x0);
-    const float4 pyp = *reinterpret_cast<const float4 *>(phi + yp * N + x0);
-    const float4 pzm = *reinterpret_cast<const float4 *>(phi + zm * N + x0);
-    const float4 pzp = *reinterpret_cast<const float4 *>(phi + zp * N + x0);
-    float S[2][6];
+  // Sources: thread m < M forms both rows' six sources at x = 2m, 2m + 1.
+  // The rows are y0 and y0 + 1 of one z plane (y0 even), so their
+  // y-neighbours are the rows y0 - 1 .. y0 + 2, two of them the rows
+  // themselves: 12 loads for the pair instead of 14.
+  static_assert(kSrcRows == 2, "the source phase pairs rows y0 and y0 + 1");
+  const int y0 = (int)(row0 % N), z = (int)(row0 / N);
+  const int64_t zr = (int64_t)z * N, zmr = (int64_t)(z == 0 ? N - 1 : z - 1) * N,
+                zpr = (int64_t)(z + 1 == N ? 0 : z + 1) * N;
+  const float2 *r0 = phi + (zr + y0) * N, *r1 = r0 + N;
+  const float2 *rym = phi + (zr + (y0 == 0 ? N - 1 : y0 - 1)) * N;
+  const float2 *ryp = phi + (zr + (y0 + 2 == N ? 0 : y0 + 2)) * N;
+  const float2 *rzm0 = phi + (zmr + y0) * N, *rzm1 = rzm0 + N;
+  const float2 *rzp0 = phi + (zpr + y0) * N, *rzp1 = rzp0 + N;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const int x0 = 2 * m, xl = x0 == 0 ? N - 1 : x0 - 1, xr = x0 + 2 == N ? 0 : x0 + 2;
+    auto ld4 = [&](const float2 *row) { return *reinterpret_cast<const float4 *>(row + x0); };
+    const float4 a_m = ld4(rym), a_0 = ld4(r0), a_1 = ld4(r1), a_p = ld4(ryp);
+    const float4 zm0 = ld4(rzm0), zm1 = ld4(rzm1), zp0 = ld4(rzp0), zp1 = ld4(rzp1);
+    const float2 xm0 = r0[xl], xp0 = r0[xr], xm1 = r1[xl], xp1 = r1[xr];
 #pragma unroll
-    for (int t = 0; t < 2; ++t) {
-      float dr[3], di[3];
-      dr[0] = t == 0 ? c01.z - xm.x : xp.x - c01.x;
-      di[0] = t == 0 ? c01.w - xm.y : xp.y - c01.y;
-      dr[1] = t == 0 ? pyp.x - pym.x : pyp.z - pym.z;
-      di[1] = t == 0 ? pyp.y - pym.y : pyp.w - pym.w;
-      dr[2] = t == 0 ? pzp.x - pzm.x : pzp.z - pzm.z;
-      di[2] = t == 0 ? pzp.y - pzm.y : pzp.w - pzm.w;
-      int c = 0;
+    for (int r = 0; r < 2; ++r) {
+      const float4 c01 = r ? a_1 : a_0, pym = r ? a_0 : a_m, pyp = r ? a_p : a_1;  // phi(x0), phi(x0 + 1)
+      const float4 pzm = r ? zm1 : zm0, pzp = r ? zp1 : zp0;
+      const float2 xm = r ? xm1 : xm0, xp = r ? xp1 : xp0;
+      float S[2][6];
 #pragma unroll
-      for (int i = 0; i < 3; ++i)
+      for (int t = 0; t < 2; ++t) {
+        float dr[3], di[3];
+        dr[0] = t == 0 ? c01.z - xm.x : xp.x - c01.x;
+        di[0] = t == 0 ? c01.w - xm.y : xp.y - c01.y;
+        dr[1] = t == 0 ? pyp.x - pym.x : pyp.z - pym.z;
+        di[1] = t == 0 ? pyp.y - pym.y : pyp.w - pym.w;
+        dr[2] = t == 0 ? pzp.x - pzm.x : pzp.z - pzm.z;
+        di[2] = t == 0 ? pzp.y - pzm.y : pzp.w - pzm.w;
+        int c = 0;
 #pragma unroll
-        for (int j = 0; j <= i; ++j, ++c) S[t][c] = scale * (dr[i] * dr[j] + di[i] * di[j]);
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j <= i; ++j, ++c) S[t][c] = scale * (dr[i] * dr[j] + di[i] * di[j]);
+      }
+#pragma unroll
+      for (int c = 0; c < 6; ++c) s[(c * kSrcRows + r) * LP + fswz(m)] = make_float2(S[0][c], S[1][c]);
     }
-#pragma unroll
-    for (int c = 0; c < 6; ++c) s[(c * kSrcRows + r) * LP + fswz(m)] = make_float2(S[0][c], S[1][c]);
   }
   __syncthreads();
   {
@@ -619,7 +640,7 @@ __global__ void __launch_bounds__(6 * kSrcRows * M / 8) k_gws_rows(const float2 
     f_stockham<M, 1, false, true, true>(v, j, line, 1, twc, 1, [&](int i, float2 x) { line[fswz(i)] = x; });
   }
   __syncthreads();
-  split_pairs<M>(s, NL, tws, [&](int b, int k, float2 x) {
+  split_pairs<M, NL>(s, tws, [&](int b, int k, float2 x) {
     out[(b / kSrcRows) * nspec + (row0 + b % kSrcRows) * sp + k] = x;
   });
 }
@@ -663,7 +684,7 @@ __global__ void __launch_bounds__(12 * M / 8) k_uij_rows(const float *__restrict
     f_stockham<M, 1, false, true, true>(v, j, line, 1, twc, 1, [&](int i, float2 x) { line[fswz(i)] = x; });
   }
   __syncthreads();
-  split_pairs<M>(s, 12, tws, [&](int b, int k, float2 x) { out[b * nspec + row * sp + k] = x; });
+  split_pairs<M, 12>(s, tws, [&](int b, int k, float2 x) { out[b * nspec + row * sp + k] = x; });
 }
 
 // The same twelve fields in FP64 (tau u_c and u_c + tau u'_c), split into
