@@ -517,8 +517,8 @@ int axg_destroy(axg_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (void **q : {&ctx->phi[0], &ctx->phi[1], &ctx->phid, &ctx->cphi, &ctx->u[0], &ctx->u[1],
                    &ctx->ud, &ctx->cu, (void **)&ctx->acc, (void **)&ctx->gsrc, (void **)&ctx->gw_omega,
-                   (void **)&ctx->gw_pol, (void **)&ctx->ff_tw, (void **)&ctx->gsrcF, (void **)&ctx->flags, (void **)&ctx->phase,
-                   (void **)&ctx->d_strings, (void **)&ctx->d_walls, (void **)&ctx->spec_mat,
+                   (void **)&ctx->gw_pol, (void **)&ctx->ff_tw, (void **)&ctx->gsrcF, (void **)&ctx->flags,
+                   (void **)&ctx->phase, (void **)&ctx->phase64, (void **)&ctx->d_strings, (void **)&ctx->d_walls, (void **)&ctx->spec_mat,
                    (void **)&ctx->spec_largeq0, (void **)&ctx->spec_dq, (void **)&ctx->spec_buf,
                    &ctx->ubuf, (void **)&ctx->d_red, (void **)&ctx->d_cnt, (void **)&ctx->d_err})
     axg_free(ctx, q);

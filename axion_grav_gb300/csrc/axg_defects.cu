@@ -204,6 +204,18 @@ __device__ __forceinline__ double phase64(const V *phi, const V *comp, int64_t s
   return axd_atan2(im, re);
 }
 
+// The deterministic FP64 phase of every site, for the fits: each fitted cell
+// reads its eight corners here instead of forming them (a string or wall
+// cell's corners are shared with its neighbours, and the fits ran them as
+// divergent FP64 chains at the start of every cell).
+template <typename V>
+__global__ void k_phase64_all(const V *__restrict__ phi, const V *__restrict__ cphi, int64_t n3,
+                              double *__restrict__ ph) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n3; s += stride)
+    ph[s] = phase64(phi, cphi, s);
+}
+
 template <typename V>
 __global__ void k_classify(const float *__restrict__ ph, const V *__restrict__ phi, const V *__restrict__ cphi, int n,
                            int which,
@@ -1089,7 +1101,7 @@ constexpr int kScreenPerPass = 8;
 // instead of 3 (128^3: 237 -> 158 ms; 4, 6 and 8 CTAs measured slower).
 template <typename V>
 __global__ void __launch_bounds__(128, 5) k_string_fit(const V *__restrict__ phi, const V *__restrict__ cphi,
-                                                    const V *__restrict__ phid, int n,
+                                                    const double *__restrict__ ph64, const V *__restrict__ phid, int n,
                                                     double dspa, uint64_t seed, const int64_t *__restrict__ cells,
                                                     int64_t ncell, double *__restrict__ out,
                                                     unsigned long long *__restrict__ next) {
@@ -1106,7 +1118,7 @@ __global__ void __launch_bounds__(128, 5) k_string_fit(const V *__restrict__ phi
     s = cells[k];
     const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
     for (int c = 0; c < 8; ++c) {
-      const double pc = phase64(phi, cphi, corner(n, ix, iy, iz, c));
+      const double pc = ph64[corner(n, ix, iy, iz, c)];
       pcf[c] = axd_ff_from(pc);
       phf[c] = (float)pc;
     }
@@ -1143,8 +1155,7 @@ __global__ void __launch_bounds__(128, 5) k_string_fit(const V *__restrict__ phi
   }
 }
 
-template <typename V>
-__global__ void __launch_bounds__(128) k_wall_fit(const V *__restrict__ phi, const V *__restrict__ cphi, int n,
+__global__ void __launch_bounds__(128) k_wall_fit(const double *__restrict__ ph64, int n,
                                                   const int64_t *__restrict__ cells,
                                                   int64_t ncell, double *__restrict__ out) {
   __shared__ WallGrid grid;
@@ -1155,7 +1166,7 @@ __global__ void __launch_bounds__(128) k_wall_fit(const V *__restrict__ phi, con
   const int64_t s = cells[k];
   const int ix = (int)(s % n), iy = (int)((s / n) % n), iz = (int)(s / ((int64_t)n * n));
   double pc[8];
-  for (int c = 0; c < 8; ++c) pc[c] = phase64(phi, cphi, corner(n, ix, iy, iz, c));
+  for (int c = 0; c < 8; ++c) pc[c] = ph64[corner(n, ix, iy, iz, c)];
   double pos[3], dir[3], gof, a;
   position_wall(pc, grid, pos, dir, &gof, &a);
   double *r = out + 10 * k;
@@ -1494,9 +1505,18 @@ int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], dou
     AXG_LAUNCH(ctx, "defect_compact", k_compact, nb, kCThreads, 0, ctx->flags, ctx->n3, bc, bc + nb,
                cells, cells + ns);
     const int n = (int)ctx->n;
+    const bool f32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
+    if (ns + nw > 0) {
+      if (!ctx->phase64) AXG_TRY(axg_alloc(ctx, (void **)&ctx->phase64, (size_t)ctx->n3 * 8, "FP64 phases"));
+      if (f32)
+        AXG_LAUNCH(ctx, "fit_phases_fp64", k_phase64_all<float2>, grid_for(ctx->n3), 256, 0,
+                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, ctx->n3, ctx->phase64);
+      else
+        AXG_LAUNCH(ctx, "fit_phases_fp64", k_phase64_all<double2>, grid_for(ctx->n3), 256, 0,
+                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, ctx->n3, ctx->phase64);
+    }
     if (ns > 0) {
       // resident CTAs only: lanes take cells from a counter (d_cnt[8])
-      const bool f32 = ctx->p.precision == AXG_PREC_FP32_MIXED;
       int per_sm = 0, sms = 0;
       AXG_CUDA_TRY(ctx, f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_string_fit<float2>, 128, 0)
                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_string_fit<double2>, 128, 0));
@@ -1507,20 +1527,18 @@ int axg_def_id_defects(axg_ctx *ctx, double tau, double sl[3], double wa[3], dou
       AXG_CUDA_TRY(ctx, cudaMemsetAsync(next, 0, sizeof(unsigned long long), ctx->stream));
       if (f32)
         AXG_LAUNCH(ctx, "string_fit_fp32", k_string_fit<float2>, (unsigned)grid, 128, 0,
-                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, (const float2 *)ctx->phid, n,
-                   ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
+                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, ctx->phase64,
+                   (const float2 *)ctx->phid, n, ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings,
+                   next);
       else
         AXG_LAUNCH(ctx, "string_fit_fp64", k_string_fit<double2>, (unsigned)grid, 128, 0,
-                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, (const double2 *)ctx->phid, n,
-                   ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings, next);
+                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, ctx->phase64,
+                   (const double2 *)ctx->phid, n, ctx->p.dspa, (uint64_t)ctx->p.seed, cells, ns, ctx->d_strings,
+                   next);
     }
     if (nw > 0) {
-      if (ctx->p.precision == AXG_PREC_FP32_MIXED)
-        AXG_LAUNCH(ctx, "wall_fit", k_wall_fit<float2>, (unsigned)((nw + 127) / 128), 128, 0,
-                   (const float2 *)ctx->phi[ctx->cur], (const float2 *)ctx->cphi, n, cells + ns, nw, ctx->d_walls);
-      else
-        AXG_LAUNCH(ctx, "wall_fit", k_wall_fit<double2>, (unsigned)((nw + 127) / 128), 128, 0,
-                   (const double2 *)ctx->phi[ctx->cur], (const double2 *)nullptr, n, cells + ns, nw, ctx->d_walls);
+      AXG_LAUNCH(ctx, "wall_fit", k_wall_fit, (unsigned)((nw + 127) / 128), 128, 0, ctx->phase64, n, cells + ns,
+                 nw, ctx->d_walls);
     }
     AXG_LAUNCH(ctx, "defect_sums", k_defect_sums, 1, 256, 0, ctx->d_strings, ns, ctx->d_walls, nw,
                ctx->d_red);

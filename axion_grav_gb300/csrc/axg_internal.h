@@ -115,6 +115,7 @@ struct axg_ctx {
   // defects
   int8_t *flags = nullptr;  // per cell, bits 1/2/4
   float *phase = nullptr;  // per site FP32 phase (filtered classification)
+  double *phase64 = nullptr;  // per site FP64 deterministic phase (the fits of id_defects)
   bool flags_valid = false;
   // fit results of the last id_defects
   double *d_strings = nullptr;
