@@ -612,7 +612,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--e2e-interval", type=int, default=20)
-    ap.add_argument("--e2e-reps", type=int, default=7)
+    ap.add_argument("--e2e-reps", type=int, default=15,
+                    help="timed upload + steps + download intervals (median; robust to a burst of host-link traffic)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy block")
     ap.add_argument("--accuracy-steps", type=int, default=100)
