@@ -103,6 +103,8 @@ EXPORTED_SYMBOLS = (
     "axg_ensemble_launch_count", "axg_adjoint_gw_band", "axg_spectrum_covariance", "axg_compute_crho_cov",
     "axg_epsilon", "axg_ensemble_set_tile", "axg_ensemble_set_launch_mode", "axg_ensemble_launch_mode",
     "axg_selftest_wait_timeout", "axg_ensemble_grav_spec_mean", "axg_ensemble_defect_mean",
+    "axg_write_spectrum", "axg_write_covariance", "axg_write_gravspec", "axg_append_string_wall_line",
+    "axg_append_crho_line", "axg_append_eps_line",
 )
 
 _lib = None
@@ -193,6 +195,16 @@ def load_library():
         "axg_ensemble_grav_spec_mean": ([ctypes.c_void_p, ctypes.c_double, dp, dp, dp, dp], ctypes.c_int),
         "axg_ensemble_defect_mean": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, dp, dp, dp, dp],
                                      ctypes.c_int),
+        "axg_write_spectrum": ([ctypes.c_char_p, ctypes.c_int32, dp, dp, dp, dp, ctypes.c_int32], ctypes.c_int),
+        "axg_write_covariance": ([ctypes.c_char_p, ctypes.c_int32, dp, ctypes.c_int32], ctypes.c_int),
+        "axg_write_gravspec": ([ctypes.c_char_p, ctypes.c_int32, ctypes.c_double, dp, dp, dp, ctypes.c_int32,
+                                ctypes.c_double, ctypes.c_double], ctypes.c_int),
+        "axg_append_string_wall_line": ([ctypes.c_char_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double, dp, dp,
+                                         dp], ctypes.c_int),
+        "axg_append_crho_line": ([ctypes.c_char_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_double], ctypes.c_int),
+        "axg_append_eps_line": ([ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_double, dp, dp], ctypes.c_int),
         "axg_spectrum_covariance": ([c_ctx, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, P(ctypes.c_int)],
                                     ctypes.c_int),
         "axg_compute_crho_cov": ([c_ctx, dp, dp], ctypes.c_int),

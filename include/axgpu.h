@@ -388,14 +388,45 @@ int axg_ensemble_defect_mean(axg_ensemble *e, int64_t idx, double tau, double xi
  * (one partial sum per z-plane, so p->ngrid <= 2048; larger lattices are
  * rejected with AXG_ERR_ARG), held by every GPU that loads the library until
  * the process exits.  The first call on a device looks up that array's device
- * address (once per device, with the device current); make that first call
- * before any stream capture.  A cudaDeviceReset of a device ends the life of
- * everything this library set up on it, that address included: after one,
- * the process makes no further call into the library on that device.  All calls share the array, so calls that
- * overlap on the GPU race; serialise them (one stream, or synchronise).
- * Errors are reported through axg_last_error(NULL). */
+ * address (once per device, with the device current).  The call synchronises
+ * its stream (it returns the moments on the host), so it cannot be part of a
+ * captured graph.  A cudaDeviceReset of a device ends the life of everything
+ * this library set up on it, that address included: after one, the process
+ * makes no further call into the library on that device.  All calls share
+ * the array, so calls that overlap on the GPU race; serialise them (one
+ * stream, or synchronise).  Errors are reported through axg_last_error(NULL). */
 int axg_field_moments_noalloc(const axg_params *p, const double *d_phi, const double *d_phidot,
                               double tau, double out[4], void *stream);
+
+/* ------------------------------------------------------------------ */
+/* text outputs in the reference's formats, for C hosts                 */
+/* ------------------------------------------------------------------ */
+/* A Fortran host keeps the reference's own writers; these write the same
+ * files from host arrays, with the reference's edit descriptors (integers
+ * I12, reals E20.10e3, ten significant digits correctly rounded).  No GPU
+ * work.  AXG_OK, AXG_ERR_ARG or AXG_ERR_IO (axg_last_error(NULL)).
+ *  - axg_write_spectrum: <root>_spectrum_<idx>.dat, rows (q, P, conv/count,
+ *    count) (spectrum.f90:278-285);
+ *  - axg_write_covariance: <root>_covariance_<idx>.dat, rows (i, j, cov_ij)
+ *    of the packed upper covariance, i = 1..nb, j = 1..i (spectrum.f90:294-302);
+ *  - axg_write_gravspec: <root>_gravspec_<idx>.dat, rows (tau, q, q f_cr, P_GW,
+ *    modes), f_cr in Hz from tau_cr and a_now (grav_waves.f90:266,308-316);
+ *  - axg_append_string_wall_line: one (idx, tau, tau^2 zeta, xi(3), A(3), v(3))
+ *    line of _string_wall_parameters.txt (evolve.f90:90,127,202);
+ *  - axg_append_crho_line: one (idx, crho(3)) line of _crho.txt (evolve.f90:128);
+ *  - axg_append_eps_line: one line of _eps.txt from two output times
+ *    (idx, idx2, tau1, tau2, their mean, eps, deps, delta rho, its error;
+ *    crho = (rho, drho) at each time) (spectrum.f90:1034-1035). */
+int axg_write_spectrum(const char *root, int32_t idx, const double *wave, const double *power,
+                       const double *conv_per_mode, const double *count, int32_t nb);
+int axg_write_covariance(const char *root, int32_t idx, const double *cov, int32_t nb);
+int axg_write_gravspec(const char *root, int32_t idx, double tau, const double *wave, const double *power,
+                       const double *denom, int32_t nb, double tau_cr, double a_now);
+int axg_append_string_wall_line(const char *path, int32_t idx, double tau, double zeta_tau2, const double xi[3],
+                                const double area[3], const double vel[3]);
+int axg_append_crho_line(const char *path, int32_t idx, double crho0, double crho1, double crho2);
+int axg_append_eps_line(const char *path, int32_t idx, int32_t idx2, double tau1, double tau2, double eps,
+                        double deps, const double crho1[2], const double crho2[2]);
 
 #ifdef __cplusplus
 }
